@@ -1,0 +1,642 @@
+// C ABI of libcambgpu: host tables, device residency, kernel orchestration.
+// Declarations and the reference interfaces they replace: include/cambgpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/cambgpu.h"
+#include "device_tables.cuh"
+#include "host/cosmo_host.hpp"
+
+namespace cgdev {
+int ode_blocks_per_sm(int team, int threads);
+cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
+                              const WorkItem* items, int nitems, int* counter);
+__global__ void source_spline_kernel(const DevCosmo*, const double* const*);
+__global__ void los_flat_kernel(const DevCosmo*);
+__global__ void scal_cls_kernel(const DevCosmo*);
+}  // namespace cgdev
+
+using namespace cgdev;
+
+namespace {
+
+std::string g_err;
+std::atomic<long long> g_launches{0};
+double g_timings[6] = {0, 0, 0, 0, 0, 0};
+int g_team = 0;
+
+int set_err(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                       \
+  do {                                                                                    \
+    cudaError_t e_ = (x);                                                                 \
+    if (e_ != cudaSuccess) return set_err(CAMBGPU_ERROR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// grow-only device arena, reset per call
+struct Arena {
+  char* base = nullptr;
+  size_t cap = 0, used = 0;
+  int reserve(size_t bytes) {
+    used = 0;
+    if (bytes <= cap) return 0;
+    if (base) cudaFree(base);
+    base = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 4 + (1 << 20);
+    if (cudaMalloc(&base, want) != cudaSuccess) return CAMBGPU_ERROR_ALLOCATION;
+    cap = want;
+    return 0;
+  }
+  template <class T>
+  T* take(size_t n) {
+    size_t bytes = (n * sizeof(T) + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+struct Runtime {
+  bool init = false;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8];
+  int nsm = 0;
+  Arena arena;
+  // Bessel tables resident on the device, keyed by host table address and shape
+  struct DevBessel { const double* host; size_t n; double* dev; double* devx; int num_xx; };
+  std::vector<DevBessel> bessel;
+  // pinned staging for uploads
+  char* pinned = nullptr;
+  size_t pinned_cap = 0;
+};
+Runtime g_rt;
+std::mutex g_mu;
+
+int rt_init() {
+  if (g_rt.init) return 0;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&g_rt.nsm, cudaDevAttrMultiProcessorCount, dev));
+  CUDA_TRY(cudaStreamCreateWithFlags(&g_rt.stream, cudaStreamNonBlocking));
+  for (auto& e : g_rt.ev) CUDA_TRY(cudaEventCreate(&e));
+  CUDA_TRY(cudaFuncSetAttribute(los_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+  g_rt.init = true;
+  return 0;
+}
+
+int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x) {
+  size_t n = (size_t)t.nl * (t.num_xx - 1) * 4;
+  for (auto& b : g_rt.bessel)
+    if (b.host == t.bessel_horner && b.n == n && b.num_xx == t.num_xx) { *dev_h = b.dev; *dev_x = b.devx; return 0; }
+  Runtime::DevBessel b{t.bessel_horner, n, nullptr, nullptr, t.num_xx};
+  CUDA_TRY(cudaMalloc(&b.dev, n * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&b.devx, (size_t)t.num_xx * sizeof(double)));
+  CUDA_TRY(cudaMemcpy(b.dev, t.bessel_horner, n * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(b.devx, t.bess_x, (size_t)t.num_xx * sizeof(double), cudaMemcpyHostToDevice));
+  if (g_rt.bessel.size() >= 4) {
+    cudaFree(g_rt.bessel.front().dev);
+    cudaFree(g_rt.bessel.front().devx);
+    g_rt.bessel.erase(g_rt.bessel.begin());
+  }
+  g_rt.bessel.push_back(b);
+  *dev_h = b.dev;
+  *dev_x = b.devx;
+  return 0;
+}
+
+// per-cosmology upload plan
+struct Upload {
+  const CambGpuTables* t;
+  std::vector<double> spl;  // [5][nk]
+  DevCosmo d;
+};
+
+size_t bytes_for(const CambGpuTables& t) {
+  auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
+  size_t s = 0;
+  s += r((size_t)t.nthermo * 16 * 8) + 4 * r((size_t)t.nthermo * 8);
+  s += 2 * r((size_t)t.ntau * 8) + r((size_t)t.nk * sizeof(CambGpuModeSpec)) + r((size_t)t.nk * 8);
+  s += 2 * r((size_t)t.ntau * t.nsrc * t.nk * 8);
+  s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
+  s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256);
+  return s;
+}
+
+void spline_factors(const CambGpuTables& t, std::vector<double>& spl) {
+  int n = t.nk;
+  const double* x = t.q_evolve;
+  spl.assign(5 * (size_t)n, 0.0);
+  double *inv_dx = &spl[0], *sig = &spl[n], *pinv = &spl[2 * n], *fac = &spl[3 * n], *c6 = &spl[4 * n];
+  for (int i = 0; i < n - 1; ++i) inv_dx[i] = 1.0 / (x[i + 1] - x[i]);
+  fac[0] = 0;
+  for (int i = 1; i < n - 1; ++i) {
+    sig[i] = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double p = sig[i] * fac[i - 1] + 2.0;
+    pinv[i] = 1.0 / p;
+    fac[i] = (sig[i] - 1.0) / p;
+    c6[i] = 6.0 / (x[i + 1] - x[i - 1]);
+  }
+}
+
+// copy host arrays into the arena and fill the device view; H2D on the runtime stream
+int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<const void*, size_t>>>& copies) {
+  const CambGpuTables& t = *u.t;
+  DevCosmo& d = u.d;
+  std::memset(&d, 0, sizeof(d));
+  auto put = [&](const void* src, size_t bytes) {
+    char* p = g_rt.arena.take<char>(bytes);
+    copies.push_back({p, {src, bytes}});
+    return p;
+  };
+  d.grhog = t.grhog; d.grhornomass = t.grhornomass; d.grhoc = t.grhoc; d.grhob = t.grhob; d.grhov = t.grhov;
+  d.tau0 = t.tau0; d.taurend = t.taurend; d.tau_maxvis = t.tau_maxvis; d.matter_verydom_tau = t.matter_verydom_tau;
+  d.photbar_a = t.grhog / t.grhob;
+  d.thermo_horner = (const double*)put(t.thermo_horner, (size_t)t.nthermo * 16 * 8);
+  d.dddotmu = (const double*)put(t.dddotmu, (size_t)t.nthermo * 8);
+  d.ddddotmu = (const double*)put(t.ddddotmu, (size_t)t.nthermo * 8);
+  d.emmu = (const double*)put(t.emmu, (size_t)t.nthermo * 8);
+  d.demmu = (const double*)put(t.demmu, (size_t)t.nthermo * 8);
+  d.nthermo = t.nthermo;
+  d.tauminn = t.tauminn; d.inv_tauminn = 1.0 / t.tauminn; d.dlntau = t.dlntau; d.dlntau_inv = t.dlntau_inv;
+  int e = t.nthermo - 1;
+  d.cs2_end = t.cs2[e]; d.dotmu_end = t.dotmu[e]; d.ddotmu_end = t.ddotmu[e]; d.dddotmu_end = t.dddotmu[e];
+  d.emmu_end = t.emmu[e];
+  d.tau_points = (const double*)put(t.tau_points, (size_t)t.ntau * 8);
+  d.tau_dpoints = (const double*)put(t.tau_dpoints, (size_t)t.ntau * 8);
+  d.ntau = t.ntau;
+  d.modes = (const CambGpuModeSpec*)put(t.modes, (size_t)t.nk * sizeof(CambGpuModeSpec));
+  d.q_evolve = (const double*)put(t.q_evolve, (size_t)t.nk * 8);
+  d.nk = t.nk;
+  d.linear_src = g_rt.arena.take<double>((size_t)t.ntau * t.nsrc * t.nk);
+  d.dd_src = g_rt.arena.take<double>((size_t)t.ntau * t.nsrc * t.nk);
+  d.delta = g_rt.arena.take<double>((size_t)t.nq * t.nl * t.nsrc);
+  d.icl = g_rt.arena.take<double>((size_t)t.nl * 6);
+  d.status = status_dev;
+  d.q_int = (const double*)put(t.q_int, (size_t)t.nq * 8);
+  d.dq_int = (const double*)put(t.dq_int, (size_t)t.nq * 8);
+  d.nq = t.nq;
+  d.ls = (const int*)put(t.ls, (size_t)t.nl * 4);
+  d.nl = t.nl;
+  spline_factors(t, u.spl);
+  double *bh, *bx;
+  int rc = device_bessel(t, &bh, &bx);
+  if (rc) return rc;
+  d.bessel_horner = bh;
+  d.bess_x = bx;
+  d.num_xx = t.num_xx;
+  d.nsrc = t.nsrc; d.want_late_time = t.want_late_time; d.max_etak_scalar = t.max_etak_scalar; d.tol1 = t.tol1;
+  d.AccuracyBoost = t.AccuracyBoost; d.IntTolBoost = t.IntTolBoost; d.TimeSwitchBoost = t.TimeSwitchBoost;
+  d.BessIntBoost = t.BessIntBoost; d.LimberBoost = t.LimberBoost;
+  d.As = t.As; d.ns = t.ns; d.nrun = t.nrun; d.pivot_scalar = t.pivot_scalar; d.Alens = t.Alens;
+  return 0;
+}
+
+// A batch resident on the device
+struct Batch {
+  std::vector<const CambGpuTables*> views;
+  std::vector<Upload> ups;
+  DevCosmo* d_cosmos = nullptr;
+  const double** d_spl = nullptr;
+  WorkItem* d_items = nullptr;
+  int nitems = 0;
+  int* d_counter = nullptr;
+  int* d_status = nullptr;
+  int max_ntau = 0, max_nq = 0, max_nl = 0, max_rows = 0;
+};
+
+int stage_batch(Batch& B) {
+  int rc = rt_init();
+  if (rc) return rc;
+  int n = (int)B.views.size();
+  size_t total = 0;
+  for (auto* v : B.views) total += bytes_for(*v);
+  size_t nitems = 0;
+  for (auto* v : B.views) nitems += v->nk;
+  total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + (nitems * sizeof(WorkItem) + 255) + 512 +
+           ((size_t)n * 4 + 255);
+  rc = g_rt.arena.reserve(total);
+  if (rc) return set_err(rc, "device allocation failed");
+  B.d_status = g_rt.arena.take<int>(n);
+  B.d_counter = g_rt.arena.take<int>(1);
+  std::vector<std::pair<void*, std::pair<const void*, size_t>>> copies;
+  B.ups.resize(n);
+  for (int c = 0; c < n; ++c) {
+    B.ups[c].t = B.views[c];
+    rc = upload(B.ups[c], B.d_status + c, copies);
+    if (rc) return rc;
+    B.max_ntau = std::max(B.max_ntau, B.views[c]->ntau);
+    B.max_nq = std::max(B.max_nq, B.views[c]->nq);
+    B.max_nl = std::max(B.max_nl, B.views[c]->nl);
+    B.max_rows = std::max(B.max_rows, B.views[c]->ntau * B.views[c]->nsrc);
+  }
+  std::vector<DevCosmo> hc(n);
+  std::vector<const double*> hspl(n);
+  for (int c = 0; c < n; ++c) {
+    hc[c] = B.ups[c].d;
+    double* p = g_rt.arena.take<double>(B.ups[c].spl.size());
+    copies.push_back({p, {B.ups[c].spl.data(), B.ups[c].spl.size() * 8}});
+    hspl[c] = p;
+  }
+  B.d_cosmos = g_rt.arena.take<DevCosmo>(n);
+  copies.push_back({B.d_cosmos, {hc.data(), (size_t)n * sizeof(DevCosmo)}});
+  B.d_spl = g_rt.arena.take<const double*>(n);
+  copies.push_back({(void*)B.d_spl, {hspl.data(), (size_t)n * 8}});
+  // work items: all (cosmology, mode) pairs, highest q first (most expensive first)
+  std::vector<WorkItem> items;
+  items.reserve(nitems);
+  for (int c = 0; c < n; ++c)
+    for (int m = 0; m < B.views[c]->nk; ++m) items.push_back({c, m});
+  std::stable_sort(items.begin(), items.end(), [&](const WorkItem& a, const WorkItem& b) {
+    return B.views[a.cosmo]->q_evolve[a.mode] > B.views[b.cosmo]->q_evolve[b.mode];
+  });
+  B.nitems = (int)items.size();
+  B.d_items = g_rt.arena.take<WorkItem>(items.size());
+  copies.push_back({B.d_items, {items.data(), items.size() * sizeof(WorkItem)}});
+  // single pinned staging buffer for all uploads
+  size_t stage = 0;
+  for (auto& cp : copies) stage += (cp.second.second + 255) & ~size_t(255);
+  if (stage > g_rt.pinned_cap) {
+    if (g_rt.pinned) cudaFreeHost(g_rt.pinned);
+    g_rt.pinned = nullptr;
+    g_rt.pinned_cap = 0;
+    CUDA_TRY(cudaMallocHost(&g_rt.pinned, stage + (1 << 20)));
+    g_rt.pinned_cap = stage + (1 << 20);
+  }
+  CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+  size_t off = 0;
+  for (auto& cp : copies) {
+    std::memcpy(g_rt.pinned + off, cp.second.first, cp.second.second);
+    CUDA_TRY(cudaMemcpyAsync(cp.first, g_rt.pinned + off, cp.second.second, cudaMemcpyHostToDevice, g_rt.stream));
+    off += (cp.second.second + 255) & ~size_t(255);
+  }
+  CUDA_TRY(cudaMemsetAsync(B.d_status, 0, (size_t)n * 4, g_rt.stream));
+  for (int c = 0; c < n; ++c) {
+    const auto& v = *B.views[c];
+    CUDA_TRY(cudaMemsetAsync(B.ups[c].d.linear_src, 0, (size_t)v.ntau * v.nsrc * v.nk * 8, g_rt.stream));
+  }
+  return 0;
+}
+
+int pick_team(const Batch& B) {
+  if (g_team) return g_team;
+  // autotuned default: 32 lanes per mode unless a batch has many modes
+  (void)B;
+  return 32;
+}
+
+int run_ode(Batch& B) {
+  CUDA_TRY(cudaMemsetAsync(B.d_counter, 0, sizeof(int), g_rt.stream));
+  int team = pick_team(B);
+  int per_sm = std::max(1, ode_blocks_per_sm(team, 128));
+  int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * team + 127) / 128);
+  if (blocks < 1) blocks = 1;
+  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, B.d_items, B.nitems, B.d_counter));
+  g_launches++;
+  return 0;
+}
+
+int run_los(Batch& B) {
+  int n = (int)B.views.size();
+  dim3 g1((B.max_rows + 127) / 128, n);
+  source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
+  g_launches++;
+  for (int c = 0; c < n; ++c) {
+    const auto& v = *B.views[c];
+    CUDA_TRY(cudaMemsetAsync(B.ups[c].d.delta, 0, (size_t)v.nq * v.nl * v.nsrc * 8, g_rt.stream));
+  }
+  size_t smem = (size_t)B.max_ntau * (3 + 1 + 1) * 8 + (size_t)B.max_ntau * 4 + 64;
+  dim3 g2(B.max_nq, n);
+  los_flat_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
+  g_launches++;
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int run_cls(Batch& B) {
+  int n = (int)B.views.size();
+  dim3 g(B.max_nl, n);
+  scal_cls_kernel<<<g, 256, 0, g_rt.stream>>>(B.d_cosmos);
+  g_launches++;
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+// runs every stage on a staged batch, with events between stages
+int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
+  cudaStream_t s = g_rt.stream;
+  CUDA_TRY(cudaEventRecord(g_rt.ev[0], s));
+  if (do_ode) { int rc = run_ode(B); if (rc) return rc; }
+  CUDA_TRY(cudaEventRecord(g_rt.ev[1], s));
+  if (do_los) { int rc = run_los(B); if (rc) return rc; }
+  CUDA_TRY(cudaEventRecord(g_rt.ev[2], s));
+  if (do_cls) { int rc = run_cls(B); if (rc) return rc; }
+  CUDA_TRY(cudaEventRecord(g_rt.ev[3], s));
+  CUDA_TRY(cudaEventSynchronize(g_rt.ev[3]));
+  g_timings[0] = elapsed(g_rt.ev[0], g_rt.ev[1]);
+  g_timings[1] = 0;
+  g_timings[2] = elapsed(g_rt.ev[1], g_rt.ev[2]);
+  g_timings[3] = elapsed(g_rt.ev[2], g_rt.ev[3]);
+  std::vector<int> st(B.views.size());
+  CUDA_TRY(cudaMemcpy(st.data(), B.d_status, st.size() * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int check_status(const Batch& B, int* status_out) {
+  std::vector<int> st(B.views.size());
+  CUDA_TRY(cudaMemcpy(st.data(), B.d_status, st.size() * 4, cudaMemcpyDeviceToHost));
+  int worst = 0;
+  for (size_t i = 0; i < st.size(); ++i) {
+    if (status_out) status_out[i] = st[i];
+    if (st[i]) worst = st[i];
+  }
+  if (worst) set_err(worst, "evolution failed for at least one k-mode");
+  return worst;
+}
+
+struct Handle {
+  cg::Cosmology c;
+  std::shared_ptr<const cg::BesselTable> bt;
+  CambGpuTables view;
+};
+
+int make_handle(const CambGpuParams* p, Handle*& h) {
+  h = new Handle();
+  std::string err;
+  int rc;
+  try {
+    rc = cg::build_cosmology(*p, h->c, err);
+  } catch (const std::exception& e) {
+    rc = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+    err = e.what();
+  }
+  if (rc) {
+    delete h;
+    h = nullptr;
+    return set_err(rc, err);
+  }
+  h->bt = cg::get_bessel_table(h->c.ls, h->c.maximum_qeta, p->BesselBoost, p->AccuracyBoost);
+  cg::fill_view(h->c, *h->bt, h->view);
+  return 0;
+}
+
+// resident batch for the bench path
+struct Resident {
+  std::vector<Handle*> handles;
+  Batch B;
+  ~Resident() {
+    for (auto* h : handles) delete h;
+  }
+};
+std::unique_ptr<Resident> g_res;
+
+int build_handles(const CambGpuParams* p, int n, std::vector<Handle*>& hs, int* status) {
+  hs.assign(n, nullptr);
+  std::vector<int> rcs(n, 0);
+  std::vector<std::string> errs(n);
+  unsigned nth = std::max(1u, std::min((unsigned)n, std::thread::hardware_concurrency()));
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nth; ++t)
+    th.emplace_back([&]() {
+      for (;;) {
+        int i = next++;
+        if (i >= n) break;
+        Handle* h = new Handle();
+        std::string err;
+        int rc;
+        try {
+          rc = cg::build_cosmology(p[i], h->c, err);
+        } catch (const std::exception& e) {
+          rc = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+          err = e.what();
+        }
+        if (rc) { delete h; h = nullptr; }
+        hs[i] = h;
+        rcs[i] = rc;
+        errs[i] = err;
+      }
+    });
+  for (auto& t : th) t.join();
+  int worst = 0;
+  for (int i = 0; i < n; ++i) {
+    if (status) status[i] = rcs[i];
+    if (rcs[i]) { worst = rcs[i]; g_err = errs[i]; }
+  }
+  for (int i = 0; i < n; ++i) {
+    if (!hs[i]) continue;
+    hs[i]->bt = cg::get_bessel_table(hs[i]->c.ls, hs[i]->c.maximum_qeta, p[i].BesselBoost, p[i].AccuracyBoost);
+    cg::fill_view(hs[i]->c, *hs[i]->bt, hs[i]->view);
+  }
+  return worst;
+}
+
+void finish_cls(const Handle& h, const double* icl, int lmax_out, double* cl_out) {
+  // InterpolateCls (cmbmain.f90:3523-3570) without the high-l template: plain spline
+  for (int l = 0; l <= lmax_out; ++l)
+    for (int c = 0; c < 4; ++c) cl_out[(size_t)l * 4 + c] = 0;
+  const std::vector<int>& ls = h.c.ls;
+  int lmax = std::min(lmax_out, ls.back());
+  // columns: TT(0) EE(1) TE(2) -> output TT EE BB TE
+  cg::interpolate_cls(ls, icl + 0, 6, ls[0], lmax, cl_out + 0, 4);
+  cg::interpolate_cls(ls, icl + 1, 6, ls[0], lmax, cl_out + 1, 4);
+  cg::interpolate_cls(ls, icl + 2, 6, ls[0], lmax, cl_out + 3, 4);
+}
+
+}  // namespace
+
+extern "C" {
+
+void cambgpu_default_params(CambGpuParams* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->H0 = 67.5; p->ombh2 = 0.022; p->omch2 = 0.122; p->omk = 0; p->TCMB = 2.7255; p->YHe = 0.2454;
+  p->num_nu_massless = 3.044; p->optical_depth = 0.06; p->reion_delta_redshift = 0.5;
+  p->As = 2.1e-9; p->ns = 0.965; p->nrun = 0; p->pivot_scalar = 0.05; p->Alens = 1;
+  p->max_l = 2500; p->max_eta_k = 6250; p->do_lensing = 0;
+  p->AccuracyBoost = p->lAccuracyBoost = p->lSampleBoost = p->IntTolBoost = p->TimeStepBoost = 1;
+  p->SourcekAccuracyBoost = p->IntkAccuracyBoost = p->BesselBoost = p->BessIntBoost = 1;
+  p->TimeSwitchBoost = p->LimberBoost = p->BackgroundTimeStepBoost = 1;
+  p->accurate_polarization = 1;
+  p->accurate_reionization = 1;
+}
+
+int cambgpu_tables_create(const CambGpuParams* p, void** handle) {
+  Handle* h = nullptr;
+  int rc = make_handle(p, h);
+  *handle = h;
+  return rc;
+}
+
+int cambgpu_tables_view(void* handle, CambGpuTables* view) {
+  if (!handle) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "null handle");
+  *view = static_cast<Handle*>(handle)->view;
+  return 0;
+}
+
+void cambgpu_tables_destroy(void* handle) { delete static_cast<Handle*>(handle); }
+
+int cambgpu_tables_derived(void* handle, double* o) {
+  if (!handle) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "null handle");
+  const cg::Cosmology& c = static_cast<Handle*>(handle)->c;
+  o[0] = c.tau0; o[1] = c.DMt0; o[2] = c.taurst; o[3] = c.taurend; o[4] = c.tau_maxvis;
+  o[5] = c.reion.redshift; o[6] = c.z_drag; o[7] = c.scale;
+  return 0;
+}
+
+int cambgpu_recfast_xe(void* handle, const double* z, int n, double* xe) {
+  if (!handle) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "null handle");
+  const cg::Cosmology& c = static_cast<Handle*>(handle)->c;
+  for (int i = 0; i < n; ++i) xe[i] = c.recfast.x_e(1 / (1 + z[i]));
+  return 0;
+}
+
+int cambgpu_evolve_scalar_sources(const CambGpuTables* t, double* linear_src) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Batch B;
+  B.views = {t};
+  int rc = stage_batch(B);
+  if (rc) return rc;
+  rc = run_all(B, true, false, false);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy(linear_src, B.ups[0].d.linear_src, (size_t)t->ntau * t->nsrc * t->nk * 8, cudaMemcpyDeviceToHost));
+  return check_status(B, nullptr);
+}
+
+int cambgpu_los_flat(const CambGpuTables* t, const double* linear_src, double* delta) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Batch B;
+  B.views = {t};
+  int rc = stage_batch(B);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(B.ups[0].d.linear_src, linear_src, (size_t)t->ntau * t->nsrc * t->nk * 8,
+                           cudaMemcpyHostToDevice, g_rt.stream));
+  rc = run_all(B, false, true, false);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy(delta, B.ups[0].d.delta, (size_t)t->nq * t->nl * t->nsrc * 8, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int cambgpu_calc_scal_cls(const CambGpuTables* t, const double* delta, double* icl) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Batch B;
+  B.views = {t};
+  int rc = stage_batch(B);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(B.ups[0].d.delta, delta, (size_t)t->nq * t->nl * t->nsrc * 8, cudaMemcpyHostToDevice,
+                           g_rt.stream));
+  rc = run_all(B, false, false, true);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy(icl, B.ups[0].d.icl, (size_t)t->nl * 6 * 8, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, double* cl_out, int* status) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
+  std::vector<Handle*> hs;
+  int rc = build_handles(p, n, hs, status);
+  struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
+  if (rc) return rc;
+  Batch B;
+  for (auto* h : hs) B.views.push_back(&h->view);
+  rc = stage_batch(B);
+  if (rc) return rc;
+  rc = run_all(B, true, true, true);
+  if (rc) return rc;
+  rc = check_status(B, status);
+  if (rc) return rc;
+  std::vector<double> icl;
+  for (int c = 0; c < n; ++c) {
+    icl.resize((size_t)hs[c]->view.nl * 6);
+    CUDA_TRY(cudaMemcpy(icl.data(), B.ups[c].d.icl, icl.size() * 8, cudaMemcpyDeviceToHost));
+    finish_cls(*hs[c], icl.data(), lmax_out, cl_out + (size_t)c * (lmax_out + 1) * 4);
+  }
+  return 0;
+}
+
+int cambgpu_get_results(const CambGpuParams* p, int lmax_out, double* cl_out) {
+  int st = 0;
+  return cambgpu_get_results_batch(p, 1, lmax_out, cl_out, &st);
+}
+
+// ---- resident batch (bench path: inputs staged in HBM before timing) ----
+int cambgpu_batch_prepare(const CambGpuParams* p, int n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_res.reset(new Resident());
+  int rc = build_handles(p, n, g_res->handles, nullptr);
+  if (rc) return rc;
+  for (auto* h : g_res->handles) g_res->B.views.push_back(&h->view);
+  rc = stage_batch(g_res->B);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+  return 0;
+}
+
+int cambgpu_batch_run(double* ms3) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
+  int rc = run_all(g_res->B, true, true, true);
+  if (rc) return rc;
+  if (ms3) { ms3[0] = g_timings[0]; ms3[1] = g_timings[2]; ms3[2] = g_timings[3]; }
+  return check_status(g_res->B, nullptr);
+}
+
+int cambgpu_batch_fetch(int lmax_out, double* cl_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
+  std::vector<double> icl;
+  for (size_t c = 0; c < g_res->handles.size(); ++c) {
+    const Handle& h = *g_res->handles[c];
+    icl.resize((size_t)h.view.nl * 6);
+    CUDA_TRY(cudaMemcpy(icl.data(), g_res->B.ups[c].d.icl, icl.size() * 8, cudaMemcpyDeviceToHost));
+    finish_cls(h, icl.data(), lmax_out, cl_out + c * (size_t)(lmax_out + 1) * 4);
+  }
+  return 0;
+}
+
+void cambgpu_batch_release(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_res.reset();
+}
+
+int cambgpu_set_ode_team(int lanes) {
+  if (lanes != 0 && lanes != 8 && lanes != 16 && lanes != 32)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team size must be 0, 8, 16 or 32");
+  g_team = lanes;
+  return 0;
+}
+
+int cambgpu_last_timings(double* out6) {
+  for (int i = 0; i < 6; ++i) out6[i] = g_timings[i];
+  return 0;
+}
+
+long long cambgpu_kernel_launches(int reset) {
+  long long v = g_launches.load();
+  if (reset) g_launches = 0;
+  return v;
+}
+
+const char* cambgpu_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"

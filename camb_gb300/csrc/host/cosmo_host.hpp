@@ -1,0 +1,128 @@
+// Host-side tables for one cosmology: background, recombination, reionization,
+// thermal-history tables, the source/integration grids, the l sampling and the
+// flat Bessel table.  These are the inputs the GPU hot path consumes; the
+// reference builds them on the host too (results.f90 SetParams / Thermo_Init,
+// recfast.f90, reionization.f90, cmbmain.f90 InitVars and grid setup,
+// bessels.f90 GenerateBessels).
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../../include/cambgpu.h"
+
+namespace cg {
+
+// ---- physical constants (constants.f90:17-60) ----
+namespace K {
+constexpr double pi = 3.1415926535897932384626433832795;
+constexpr double twopi = 2 * pi, fourpi = 4 * pi, eightpi = 8 * pi;
+constexpr double c = 2.99792458e8;
+constexpr double h_P = 6.62607015e-34;
+constexpr double G = 6.67430e-11;
+constexpr double sigma_thomson = 6.6524587321e-29;
+constexpr double sigma_boltz = 5.670374419e-8;
+constexpr double k_B = 1.380649e-23;
+constexpr double m_p = 1.67262192369e-27;
+constexpr double m_e = 9.1093837015e-31;
+constexpr double m_H = 1.673575e-27;
+constexpr double m_He4 = 6.646479073e-27;
+constexpr double mass_ratio_He_H = m_He4 / m_H;
+constexpr double Mpc = 3.085677581e22;
+constexpr double MPC_in_sec = Mpc / c;
+constexpr double barssc0 = k_B / m_p / (c * c);
+constexpr double kappa = 8.0 * pi * G;
+constexpr double COBE_CMBTemp = 2.7255;
+}  // namespace K
+
+// forutils-style ranges of points (RangeUtils TRanges) as used at the call sites
+// cmbmain.f90:918-933, 1284-1345, results.f90:2669-2741, bessels.f90:168-180.
+// The forutils source is not available; semantics inferred from the call sites:
+//  - Add_delta(a,b,d,log): n = max(1, int((b-a)/d + 1 - RangeTol)) equal steps
+//    (in log space if log), RangeTol = 0.1;
+//  - overlapping ranges are merged so that the finer local spacing wins;
+//  - dpoints(i) = (points(i+1)-points(i-1))/2 with half intervals at the ends.
+struct Ranges {
+  struct R { double lo, hi; int n; bool log; };
+  std::vector<R> r;
+  std::vector<double> points, dpoints;
+  void add_delta(double lo, double hi, double delta, bool islog = false);
+  void add(double lo, double hi, int n, bool islog = false);
+  void get_array(bool want_dpoints = true);
+  int npoints() const { return (int)points.size(); }
+  // 0-based index i with points[i] <= x < points[i+1] (clamped to [0, n-2]).
+  int index_of(double x) const;
+};
+
+// natural/clamped cubic spline helpers
+void spline_second_derivs(const double* x, const double* y, int n, double* d2,
+                          bool clamp_start = false, double d1_start = 0,
+                          bool clamp_end = false, double d1_end = 0);
+
+struct Recfast {
+  int nz = 2046;
+  double delta_z = 0, minz = 0, maxz = 0, Tnow = 0, NNow = 0, fHe = 0, HO = 0, z_eq = 0;
+  double OmegaT = 0, OmegaK = 0, fu = 1.125;
+  std::vector<double> xrec, tmrec, xh, th;  // xh/th: [nz-1][4] Horner coefficients
+  double x_e(double a) const;
+  void xe_Tm(double a, double& xe, double& Tm) const;
+};
+
+struct Reion {
+  bool on = true;
+  double redshift = 10, optical_depth = 0.06, delta_redshift = 0.5, fraction = -1;
+  double helium_redshift = 3.5, helium_delta_redshift = 0.4, helium_redshiftstart = 5.5;
+  double fHe = 0, WindowVarMid = 0, WindowVarDelta = 0;
+  void set_zre(double z);
+  double x_e(double z, double xstart = 0) const;
+};
+
+struct Cosmology {
+  CambGpuParams P;
+  // background (CAMBdata)
+  double grhocrit, grhog, grhor, grhornomass, grhoc, grhob, grhov, grhok, adotrad;
+  double Nnow, akthom, fHe, z_eq, Omega_de, tau0, DMt0, scale = 1;
+  // InitVars
+  double qmax, qmin, dtaurec, max_etak_scalar, maximum_qeta;
+  int maximum_l;
+  // thermal history (TThermoData)
+  int nthermo;
+  double tauminn, dlntau, dlntau_inv, tight_tau, matter_verydom_tau, actual_opt_depth;
+  double taurst, taurend, tau_maxvis, reion_tau_start, reion_tau_complete;
+  int reion_n_steps;
+  double z_drag, r_drag0;
+  std::vector<double> thermo_horner;  // [nthermo][16]
+  std::vector<double> dotmu, ddotmu, dddotmu, ddddotmu, emmu, demmu, cs2, xe, tb, adot;
+  Recfast recfast;
+  Reion reion;
+  // grids
+  Ranges timesteps, evolve_q, q_int;
+  std::vector<int> ls;
+  std::vector<CambGpuModeSpec> modes;
+  int nsrc;
+  double tol1;
+
+  double dtauda(double a) const;
+  double delta_time(double a1, double a2, double tol = -1) const;
+  double time_of_z(double z, double tol = -1) const { return delta_time(0, 1 / (z + 1), tol); }
+  double ScalarPower(double k) const;
+};
+
+// Shared flat Bessel table keyed on (l sampling, x_max, BesselBoost*AccuracyBoost).
+struct BesselTable {
+  std::vector<int> ls;
+  double xmax = 0, acc = 0, boost = 0;
+  std::vector<double> x;       // [num_xx]
+  std::vector<double> horner;  // [nl][num_xx-1][4]
+};
+
+int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err);
+std::shared_ptr<const BesselTable> get_bessel_table(const std::vector<int>& ls, double xmax,
+                                                    double bessel_boost, double accuracy_boost);
+void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v);
+// InterpolateClArr (results.f90:1710-1745): spline from the sampled l to every l.
+void interpolate_cls(const std::vector<int>& ls, const double* icl_col, int stride, int lmin,
+                     int lmax_out, double* out, int out_stride);
+
+}  // namespace cg

@@ -1,0 +1,778 @@
+// Persistent per-k-mode Einstein-Boltzmann integrator for sm_103a (FP64).
+//
+// One "team" of T lanes integrates one k-mode (T = 32 is one warp per mode).
+// The mode's state vector uses a fixed per-mode layout
+//     [etak, clxc, clxb, vb | T_0..T_lmaxg | E_0..E_lmaxgpol | N_0..N_lmaxnr]
+// (photon temperature, photon E polarization, massless neutrinos) spread over
+// the team's lanes entry-major: flat index i lives in lane i % T, register
+// entry i / T.  The approximation switches of the reference only change which
+// entries are active (tight coupling, k*tau neutrino truncation, late-time
+// radiation truncation), so no repacking is ever needed.  All Dormand-Prince
+// stage vectors stay in registers; the error norm and max|y| are team
+// shuffle max-reductions.  The scalar part of the right-hand side (thermal
+// history lookup, background, constraints, tight-coupling slip) is computed
+// redundantly by the team's lanes, the multipole recurrences one entry per lane.
+//
+// Follows: RungeKuttaDP45 (RungeKuttaDP45.f90:94-408), GaugeInterface_ScalEv /
+// EvolveScal (equations.f90:212-460), initial (equations.f90:1891-2112),
+// derivs + source output (equations.f90:2273-2949), Thermo_values and
+// IonizationFunctionsAtTime (results.f90:1848-1880, 3069-3108) and the time loop
+// of CalcScalarSources (cmbmain.f90:998-1074).  Every spin of the mode loop is
+// bounded: a mode that exceeds its derivative-evaluation budget or whose step
+// size underflows stores CAMBGPU_ERROR_EVOLUTION in its cosmology's status word.
+#include <cuda_runtime.h>
+
+#include "device_tables.cuh"
+
+namespace cgdev {
+
+constexpr int NVAR_MAX = 128;
+constexpr long long kMaxEvalsPerMode = 40000000LL;
+
+template <int T>
+struct Team {
+  unsigned mask;
+  int t;
+  __device__ __forceinline__ Team() {
+    int lane = threadIdx.x & 31;
+    t = lane & (T - 1);
+    if constexpr (T == 32) mask = 0xffffffffu;
+    else mask = ((1u << T) - 1u) << (lane & ~(T - 1));
+  }
+  __device__ __forceinline__ double bcast(double v, int src) const {
+    if constexpr (T == 1) return v;
+    else return __shfl_sync(mask, v, src, T);
+  }
+  __device__ __forceinline__ int bcast_i(int v, int src) const {
+    if constexpr (T == 1) return v;
+    else return __shfl_sync(mask, v, src, T);
+  }
+  __device__ __forceinline__ double maxr(double v) const {
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(mask, v, o, T));
+    return v;
+  }
+};
+
+// Uniform (team-wide) per-mode control state.
+struct Mode {
+  double k, ik, k2, ik2, q;
+  double denlk1, denlk2_1, denlk_2, denlk2_2, poltruncfac;
+  double pig, pigdot, tight_off;
+  int lmaxg, lmaxgpol, lmaxnr, g_ix, pol_ix, r_ix, nvar;
+  bool tc, hk, nonu, nophot;
+};
+
+// special entries whose derivative comes from the scalar part
+enum { SP_ETAK = 0, SP_CLXC, SP_CLXB, SP_VB, SP_CLXG, SP_QG, SP_PIG, SP_E2, SP_CLXR, SP_QR, SP_PIR, SP_NONE = 15 };
+
+template <int T>
+struct Lanes {
+  static constexpr int E = NVAR_MAX / T;
+  double A[E], B[E], cOp[E], cCo[E];
+  unsigned char sp[E];
+  unsigned act;  // bit e: entry e active
+};
+
+struct Scal {  // scalar outputs of one right-hand-side evaluation
+  double S[11];
+};
+
+struct SrcOut {
+  double s[3];
+};
+
+__device__ __forceinline__ double ldg(const double* p) { return __ldg(p); }
+
+// Thermo_values (results.f90:1848-1880)
+__device__ __forceinline__ void thermo_values(const DevCosmo& C, double tau, double itau, double& a, double& cs2,
+                                              double& opac, double& dopac) {
+  double d = log(tau * C.inv_tauminn) * C.dlntau_inv + 1.0;
+  int i = (int)d;
+  d = d - i;
+  if (i >= C.nthermo) {
+    cs2 = C.cs2_end;
+    opac = C.dotmu_end;
+    a = 1;
+    dopac = C.ddotmu_end * itau * C.dlntau_inv;
+  } else {
+    const double* h = C.thermo_horner + (size_t)(i - 1) * 16;
+    cs2 = ldg(h + 0) + d * (ldg(h + 1) + d * (ldg(h + 2) + d * ldg(h + 3)));
+    opac = ldg(h + 4) + d * (ldg(h + 5) + d * (ldg(h + 6) + d * ldg(h + 7)));
+    a = (ldg(h + 8) + d * (ldg(h + 9) + d * (ldg(h + 10) + d * ldg(h + 11)))) * tau;
+    dopac = (ldg(h + 12) + d * (ldg(h + 13) + d * (ldg(h + 14) + d * ldg(h + 15)))) * itau * C.dlntau_inv;
+  }
+}
+
+// IonizationFunctionsAtTime (results.f90:3069-3108): visibility and derivatives
+__device__ __forceinline__ void ionization(const DevCosmo& C, double tau, double itau, double& opac, double& dopac,
+                                           double& vis, double& dvis, double& ddvis, double& expmmu) {
+  double a, cs2;
+  thermo_values(C, tau, itau, a, cs2, opac, dopac);
+  double d = log(tau * C.inv_tauminn) * C.dlntau_inv + 1.0;
+  int i = (int)d;
+  d = d - i;
+  double ddopac;
+  double tdl = tau * C.dlntau;
+  if (i < C.nthermo) {
+    int j = i - 1;
+    double f3a = ldg(C.dddotmu + j), f3b = ldg(C.dddotmu + j + 1);
+    double f4a = ldg(C.ddddotmu + j), f4b = ldg(C.ddddotmu + j + 1);
+    double ema = ldg(C.emmu + j), emb = ldg(C.emmu + j + 1);
+    double dea = ldg(C.demmu + j), deb = ldg(C.demmu + j + 1);
+    ddopac = (f3a + d * (f4a + d * (3.0 * (f3b - f3a) - 2.0 * f4a - f4b + d * (f4a + f4b + 2.0 * (f3a - f3b)))) -
+              (C.dlntau * C.dlntau) * tau * dopac) /
+             (tdl * tdl);
+    expmmu = ema + d * (dea + d * (3.0 * (emb - ema) - 2.0 * dea - deb + d * (dea + deb + 2.0 * (ema - emb))));
+  } else {
+    ddopac = (C.dddotmu_end - (C.dlntau * C.dlntau) * tau * dopac) / (tdl * tdl);
+    expmmu = C.emmu_end;
+  }
+  vis = opac * expmmu;
+  dvis = expmmu * (opac * opac + dopac);
+  ddvis = expmmu * (opac * opac * opac + 3 * opac * dopac + ddopac);
+}
+
+template <int T>
+__device__ __forceinline__ double sel(const double (&v)[NVAR_MAX / T], int e) {
+  constexpr int E = NVAR_MAX / T;
+  double r = v[0];
+#pragma unroll
+  for (int j = 1; j < E; ++j)
+    if (e == j) r = v[j];
+  return r;
+}
+
+// value of flat variable idx (uniform across the team)
+template <int T>
+__device__ __forceinline__ double getv(const Team<T>& tm, const double (&v)[NVAR_MAX / T], int idx) {
+  return tm.bcast(sel<T>(v, idx / T), idx % T);
+}
+
+// Per-entry recurrence coefficients for the mode layout (denlk, denlk2, polfack of
+// initial(), equations.f90:1911-1916, flat: Kf = 1).
+template <int T>
+__device__ void setup_layout(const Mode& M, const Team<T>& tm, Lanes<T>& L) {
+  constexpr int E = NVAR_MAX / T;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    int i = e * T + tm.t;
+    double A = 0, B = 0, cop = 0, cco = 0;
+    int sp = SP_NONE;
+    double k = M.k;
+    if (i < 4) sp = SP_ETAK + i;
+    else if (i < M.pol_ix) {  // photon temperature l
+      int l = i - M.g_ix;
+      double dl = 1.0 / (2 * l + 1);
+      if (l == 0) sp = SP_CLXG;
+      else if (l == 1) sp = SP_QG;
+      else if (l == 2) sp = SP_PIG;
+      else if (l < M.lmaxg) { A = dl * k * l; B = -(dl * k * (l + 1)); cop = 1; }
+      else { A = k; cop = 1; cco = M.lmaxg + 1; }
+    } else if (i < M.r_ix) {  // photon E polarization l
+      int l = i - M.pol_ix;
+      double dl = 1.0 / (2 * l + 1);
+      if (l == 2) sp = SP_E2;
+      else if (l >= 3 && l < M.lmaxgpol) {
+        double polfac = (double)((l + 3) * (l - 1)) / (l + 1);
+        A = dl * k * l;
+        B = -(polfac * k * dl);
+        cop = 1;
+      } else if (l == M.lmaxgpol) { A = k * M.poltruncfac; cop = 1; cco = M.lmaxgpol + 3; }
+    } else if (i < M.nvar) {  // massless neutrinos l
+      int l = i - M.r_ix;
+      double dl = 1.0 / (2 * l + 1);
+      if (l == 0) sp = SP_CLXR;
+      else if (l == 1) sp = SP_QR;
+      else if (l == 2) sp = SP_PIR;
+      else if (l < M.lmaxnr) { A = dl * k * l; B = -(dl * k * (l + 1)); }
+      else { A = k; cco = M.lmaxnr + 1; }
+    }
+    L.A[e] = A;
+    L.B[e] = B;
+    L.cOp[e] = cop;
+    L.cCo[e] = cco;
+    L.sp[e] = (unsigned char)sp;
+  }
+}
+
+// Which entries are propagated (SetupScalarArrayIndices, equations.f90:585-701)
+template <int T>
+__device__ void update_activity(const Mode& M, const Team<T>& tm, Lanes<T>& L) {
+  constexpr int E = NVAR_MAX / T;
+  unsigned act = 0;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    int i = e * T + tm.t;
+    bool a = false;
+    if (i < 4) a = true;
+    else if (i < M.pol_ix) { int l = i - M.g_ix; a = !M.nophot && (l <= 1 || !M.tc); }
+    else if (i < M.r_ix) { int l = i - M.pol_ix; a = !M.nophot && !M.tc && l >= 2; }
+    else if (i < M.nvar) { int l = i - M.r_ix; a = !M.nonu && (l <= 2 || !M.hk); }
+    if (a) act |= 1u << e;
+  }
+  L.act = act;
+}
+
+// Right-hand side (derivs, equations.f90:2273-2773) for the flat, Lambda,
+// massless-neutrino adiabatic case; with `src` also the CMB sources of
+// equations.f90:2775-2912.
+template <int T, bool WITH_SRC>
+__device__ __forceinline__ void derivs(const DevCosmo& C, Mode& M, const Team<T>& tm, const Lanes<T>& L,
+                                       double tau, const double (&y)[NVAR_MAX / T], double (&dy)[NVAR_MAX / T],
+                                       SrcOut* so) {
+  constexpr int E = NVAR_MAX / T;
+  const double k = M.k, ik = M.ik;
+  double itau = 1.0 / tau;
+  double a, cs2, opac, dopac;
+  thermo_values(C, tau, itau, a, cs2, opac, dopac);
+  double a2 = a * a, ia = 1.0 / a, ia2 = ia * ia;
+  double etak = getv<T>(tm, y, 0), clxc = getv<T>(tm, y, 1), clxb = getv<T>(tm, y, 2), vb = getv<T>(tm, y, 3);
+  double grhob_t = C.grhob * ia, grhoc_t = C.grhoc * ia, grhor_t = C.grhornomass * ia2, grhog_t = C.grhog * ia2;
+  double grhov_t = C.grhov * a2;
+  double dgrho = grhob_t * clxb + grhoc_t * clxc;
+  double dgq = grhob_t * vb;
+  double grho = (grhob_t + grhoc_t) + grhor_t + grhog_t + grhov_t;
+  double gpres_noDE = (grhor_t + grhog_t) / 3;
+  double adotoa = sqrt(grho / 3);
+  double iad = 1.0 / adotoa;
+  double z = 0, dz = 0, clxr, qr, pir, N3 = 0, clxg, qg, pig = 0, T3 = 0, E2 = 0, E3 = 0;
+  if (M.nonu) {
+    z = (0.5 * dgrho * ik + etak) * iad;
+    dz = -adotoa * z - 0.5 * dgrho * ik;
+    clxr = -4 * dz * ik;
+    qr = -4.0 / 3 * z;
+    pir = 0;
+  } else {
+    clxr = getv<T>(tm, y, M.r_ix);
+    qr = getv<T>(tm, y, M.r_ix + 1);
+    pir = getv<T>(tm, y, M.r_ix + 2);
+    if (!M.hk) N3 = getv<T>(tm, y, M.r_ix + 3);
+  }
+  if (M.nophot) {
+    if (!M.nonu) {
+      z = (0.5 * dgrho * ik + etak) * iad;
+      dz = -adotoa * z - 0.5 * dgrho * ik;
+      clxg = -4 * dz * ik - 4 * ik * opac * (vb + z);
+      qg = -4.0 / 3 * z;
+    } else {
+      clxg = clxr - 4 * ik * opac * (vb + z);
+      qg = qr;
+    }
+  } else {
+    clxg = getv<T>(tm, y, M.g_ix);
+    qg = getv<T>(tm, y, M.g_ix + 1);
+    if (!M.tc) {
+      pig = getv<T>(tm, y, M.g_ix + 2);
+      T3 = getv<T>(tm, y, M.g_ix + 3);
+      E2 = getv<T>(tm, y, M.pol_ix + 2);
+      E3 = getv<T>(tm, y, M.pol_ix + 3);
+    }
+  }
+  dgrho = dgrho + grhog_t * clxg + grhor_t * clxr;
+  dgq = dgq + grhog_t * qg + grhor_t * qr;
+  double photbar = C.photbar_a * ia;
+  double pb43 = 4.0 / 3 * photbar;
+  z = (0.5 * dgrho * ik + etak) * iad;
+  double sigma = z + 1.5 * dgq * M.ik2;
+  Scal sc;
+  sc.S[SP_ETAK] = 0.5 * dgq;
+  sc.S[SP_CLXC] = -k * z;
+  double clxbdot = -k * (z + vb);
+  sc.S[SP_CLXB] = clxbdot;
+  double clxgdot = -k * (4.0 / 3.0 * z + qg);
+  double delta_p_b = cs2 * clxb;
+  double vbdot, pigdot = 0;
+  if (M.tc) {
+    double gpres = gpres_noDE - grhov_t;
+    double adotdota = (adotoa * adotoa - gpres) / 2;
+    double iop = 1.0 / opac, iop2 = iop * iop;
+    double i1pb = 1.0 / (1 + pb43);
+    pig = 32.0 / 45 * iop * k * (sigma + vb);
+    double slip = -(2 * adotoa * i1pb + dopac * iop) * (vb - 3.0 / 4 * qg) +
+                  (-adotdota * vb - k / 2 * adotoa * clxg + k * (cs2 * clxbdot - clxgdot / 4)) * iop * i1pb;
+    double dgs = grhog_t * pig + grhor_t * pir;
+    double sigmadot = -2 * adotoa * sigma - dgs * ik + etak;
+    double qgdot_tc = k * (clxg / 4.0 - pig / 2.0) + opac * slip;
+    double f11 = dopac * 11.0 / 6.0 * iop2;
+    pig = 32.0 / 45 * iop * k * (sigma + 3.0 * qg / 4.0) * (1 + f11) +
+          (32.0 / 45.0 * iop2) * k * (sigmadot + 3.0 * qgdot_tc / 4.0) * (-11.0 / 6.0);
+    pigdot = -(32.0 / 45.0) * (dopac * iop2) * k * (sigma + 3.0 * qg / 4.0) * (1 + f11) +
+             (32.0 / 45.0 * iop) * k * (sigmadot + 3.0 * qgdot_tc / 4.0) * (1 + (11.0 / 6.0) * (dopac * iop2));
+    M.pigdot = pigdot;
+    vbdot = (-adotoa * vb + cs2 * k * clxb + k / 4 * pb43 * (clxg - 2 * pig)) * i1pb;
+    vbdot = vbdot + pb43 * i1pb * slip;
+    M.pig = pig;
+  } else {
+    vbdot = -adotoa * vb + k * delta_p_b - photbar * opac * (4.0 / 3 * vb - qg);
+  }
+  sc.S[SP_VB] = vbdot;
+  double qgdot = 0, polter = 0;
+  if (!M.nophot) {
+    sc.S[SP_CLXG] = clxgdot;
+    double inv_pb43 = 0.75 * a / C.photbar_a;
+    qgdot = 4.0 / 3 * (-vbdot - adotoa * vb + delta_p_b * k) * inv_pb43 + M.denlk1 * clxg - M.denlk2_1 * pig;
+    sc.S[SP_QG] = qgdot;
+    if (!M.tc) {
+      polter = pig / 10 + 9.0 / 15 * E2;
+      pigdot = M.denlk_2 * qg - M.denlk2_2 * T3 - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
+      sc.S[SP_PIG] = pigdot;
+      sc.S[SP_E2] = -opac * (E2 - polter) - k / 3.0 * E3;
+    } else {
+      sc.S[SP_PIG] = 0;
+      sc.S[SP_E2] = 0;
+    }
+  } else {
+    sc.S[SP_CLXG] = sc.S[SP_QG] = sc.S[SP_PIG] = sc.S[SP_E2] = 0;
+  }
+  double clxrdot = 0, qrdot = 0, pirdot = 0;
+  if (!M.nonu) {
+    clxrdot = -k * (4.0 / 3.0 * z + qr);
+    qrdot = M.denlk1 * clxr - M.denlk2_1 * pir;
+    if (M.hk) pirdot = -3 * pir * itau - clxrdot;
+    else pirdot = M.denlk_2 * qr - M.denlk2_2 * N3 + 8.0 / 15.0 * k * sigma;
+  }
+  sc.S[SP_CLXR] = clxrdot;
+  sc.S[SP_QR] = qrdot;
+  sc.S[SP_PIR] = pirdot;
+
+  // multipole recurrences: d = A*prev + B*next - (cOp*opacity + cCo/tau)*y
+  // entries beyond the mode's layout are never active (and skipped below)
+  const int eact = (M.nvar + T - 1) / T;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    if (e < eact) {
+      double prev, next;
+      if constexpr (T == 1) {
+        prev = e > 0 ? y[e - 1] : 0.0;
+        next = e + 1 < E ? y[e + 1] : 0.0;
+      } else {
+        double up = __shfl_up_sync(tm.mask, y[e], 1, T);
+        double wrapu = __shfl_sync(tm.mask, e > 0 ? y[e > 0 ? e - 1 : 0] : 0.0, T - 1, T);
+        prev = tm.t == 0 ? wrapu : up;
+        double dn = __shfl_down_sync(tm.mask, y[e], 1, T);
+        double wrapd = __shfl_sync(tm.mask, e + 1 < E ? y[e + 1 < E ? e + 1 : e] : 0.0, 0, T);
+        next = tm.t == T - 1 ? wrapd : dn;
+      }
+      double d = L.A[e] * prev + L.B[e] * next - (L.cOp[e] * opac + L.cCo[e] * itau) * y[e];
+      int sp = L.sp[e];
+      double s = 0;
+#pragma unroll
+      for (int j = 0; j < 11; ++j)
+        if (sp == j) s = sc.S[j];
+      d += s;
+      dy[e] = ((L.act >> e) & 1u) ? d : 0.0;
+    } else {
+      dy[e] = 0.0;
+    }
+  }
+
+  if constexpr (WITH_SRC) {
+    // CMB source functions (equations.f90:2775-2912), flat Kf = 1
+    double Ed2 = 0, Ed3 = 0, octgdot = 0;
+    if (M.nophot) {
+      pigdot = 0;
+      octgdot = 0;
+      qgdot = -4 * dz / 3;
+      E2 = E3 = 0;
+    } else if (M.tc) {
+      double iop = 1.0 / opac;
+      E2 = pig / 4 + pigdot * iop * (-5.0 / 8.0);
+      E3 = (3.0 / 7.0) * (k * iop) * E2;
+      Ed2 = (pigdot / 4.0) * (1 + (5.0 / 2.0) * (dopac * iop * iop));
+      Ed3 = 0;
+      octgdot = 0;
+    } else {
+      Ed2 = sc.S[SP_E2];
+      Ed3 = getv<T>(tm, dy, M.pol_ix + 3);
+      octgdot = getv<T>(tm, dy, M.g_ix + 3);
+    }
+    if (M.nonu) pirdot = 0;
+    double dgpi = grhor_t * pir + grhog_t * pig;
+    double pidot_sum = grhog_t * pigdot + grhor_t * pirdot;
+    double gpres = gpres_noDE - grhov_t;
+    double diff_rhopi = pidot_sum - (4 * dgpi) * adotoa;
+    double phi = -((dgrho + 3 * dgq * adotoa * ik) + dgpi) / (2 * M.k2);
+    double op2, dop2, vis, dvis, ddvis, exptau;
+    ionization(C, tau, itau, op2, dop2, vis, dvis, ddvis, exptau);
+    double k2 = M.k2;
+    double phidot = 0.5 * (adotoa * (-dgpi - 2 * k2 * phi) + dgq * k - diff_rhopi + k * sigma * (gpres + grho)) * M.ik2;
+    double sigmadot = -adotoa * sigma - 0.5 * dgpi * ik + k * phi;
+    polter = pig / 10 + 9.0 / 15 * E2;
+    double polterdot = (1.0 / 10.0) * pigdot + (3.0 / 5.0) * Ed2;
+    double polterddot = -2.0 / 25.0 * adotoa * dgq * ik - 4.0 / 75.0 * adotoa * k * sigma - 4.0 / 75.0 * dgpi -
+                        2.0 / 75.0 * dgrho - 3.0 / 50.0 * k * octgdot + (1.0 / 25.0) * k * qgdot - 1.0 / 5.0 * k * Ed3 +
+                        (-1.0 / 10.0 * pig + (7.0 / 10.0) * polter - 3.0 / 5.0 * E2) * dop2 +
+                        (-1.0 / 10.0 * pigdot + (7.0 / 10.0) * polterdot - 3.0 / 5.0 * Ed2) * op2;
+    double ISW = 2 * phidot * exptau;
+    double monopole_source = (-etak * ik + 2 * phi + clxg / 4) * vis;
+    double doppler = ((sigma + vb) * dvis + (sigmadot + vbdot) * vis) * ik;
+    double quadrupole_source =
+        (5.0 / 8.0) * (3 * polter * ddvis + 6 * polterdot * dvis + (k2 * polter + 3 * polterddot) * vis) * M.ik2;
+    so->s[0] = ISW + doppler + monopole_source + quadrupole_source;
+    double ang = C.tau0 - tau;
+    so->s[1] = tau < C.tau0 ? vis * polter * (15.0 / 8.0) / (ang * ang * k2) : 0.0;
+    so->s[2] = 0;
+    if (C.nsrc > 2 && tau > C.tau_maxvis && ang > 0.1)
+      so->s[2] = -2 * phi * (tau - C.tau_maxvis) / ((C.tau0 - C.tau_maxvis) * ang);
+  }
+}
+
+// Dormand-Prince 5(4) tableau (RungeKuttaDP45.f90:108-133)
+namespace dp {
+constexpr double a21 = 1.0 / 5.0, a31 = 3.0 / 40.0, a32 = 9.0 / 40.0, a41 = 44.0 / 45.0, a42 = -56.0 / 15.0,
+                 a43 = 32.0 / 9.0, a51 = 19372.0 / 6561.0, a52 = -25360.0 / 2187.0, a53 = 64448.0 / 6561.0,
+                 a54 = -212.0 / 729.0, a61 = 9017.0 / 3168.0, a62 = -355.0 / 33.0, a63 = 46732.0 / 5247.0,
+                 a64 = 49.0 / 176.0, a65 = -5103.0 / 18656.0, b1 = 35.0 / 384.0, b3 = 500.0 / 1113.0,
+                 b4 = 125.0 / 192.0, b5 = -2187.0 / 6784.0, b6 = 11.0 / 84.0, e1 = 71.0 / 57600.0,
+                 e3 = -71.0 / 16695.0, e4 = 71.0 / 1920.0, e5 = -17253.0 / 339200.0, e6 = 22.0 / 525.0,
+                 e7 = -1.0 / 40.0;
+constexpr double eps = 2.220446049250313e-16, tiny = 2.2250738585072014e-308;
+}  // namespace dp
+
+// Persistent step-control state (RungeKuttaDP45Settings fields that survive calls)
+struct RK {
+  double h, err, ms_user;
+  int fails;
+  bool fsal;   // first_derivative_valid
+  bool reset;  // ind == 1 on the next call
+  long long evals;
+};
+
+template <int T>
+struct Regs {
+  static constexpr int E = NVAR_MAX / T;
+  double y[E], k1[E], k2[E], k3[E], k4[E], k5[E], k6[E], yt[E];
+};
+
+// one call of RungeKuttaDP45 from x to xend (ind = 1 or 3 on entry)
+template <int T>
+__device__ int dp45(const DevCosmo& C, Mode& M, const Team<T>& tm, const Lanes<T>& L, Regs<T>& R, RK& rk,
+                    double& x, double xend, double tol) {
+  constexpr int E = NVAR_MAX / T;
+  using namespace dp;
+  bool first = rk.reset;
+  double hmax_user = rk.reset ? 0.0 : rk.ms_user;  // settings reset wipes max_step_size
+  if (rk.reset) {
+    rk.fsal = false;
+    rk.fails = 0;
+    rk.reset = false;
+  }
+  SrcOut dummy;
+  bool need_f = true;
+  const double g1 = 2.0 / 0.9, g2 = g1 * g1;
+  const double grow_lim = g2 * g2 * g1;  // (2/0.9)**5
+  for (;;) {
+    if (rk.evals > kMaxEvalsPerMode) return -1;
+    if (need_f) {
+      if (rk.fsal) rk.fsal = false;
+      else {
+        derivs<T, false>(C, M, tm, L, x, R.y, R.k1, &dummy);
+        rk.evals++;
+      }
+    }
+    need_f = false;
+    double ny = 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      if ((L.act >> e) & 1u) ny = fmax(ny, fabs(R.y[e]));
+    ny = fmin(tm.maxr(ny), 1.0);
+    double hmin = 10.0 * fmax(tiny, eps * fmax(ny / tol, fabs(x)));
+    double hmax = hmax_user != 0.0 ? hmax_user : 20.0;
+    if (hmin > hmax) return -2;
+    if (first) {
+      rk.h = hmax * pow(tol, 0.2);
+      first = false;
+    } else if (rk.fails <= 1) {
+      double t2 = 2.0 * rk.h;
+      if (tol < grow_lim * rk.err) t2 = 0.9 * pow(tol / rk.err, 0.2) * rk.h;
+      rk.h = fmax(t2, 0.5 * rk.h);
+    } else {
+      rk.h = 0.5 * rk.h;
+    }
+    rk.h = fmin(rk.h, hmax);
+    rk.h = fmax(rk.h, hmin);
+    double rem = fabs(xend - x), xt;
+    if (rk.h < rem && (rem > 1.2 * rk.h || rem > hmax)) {
+      rk.h = fmin(rk.h, 0.5 * rem);
+      xt = x + copysign(rk.h, xend - x);
+    } else {
+      rk.h = rem;
+      xt = xend;
+    }
+    const double hs = xt - x;
+#pragma unroll
+    for (int e = 0; e < E; ++e) R.yt[e] = R.y[e] + hs * a21 * R.k1[e];
+    derivs<T, false>(C, M, tm, L, x + hs / 5.0, R.yt, R.k2, &dummy);
+#pragma unroll
+    for (int e = 0; e < E; ++e) R.yt[e] = R.y[e] + hs * (a31 * R.k1[e] + a32 * R.k2[e]);
+    derivs<T, false>(C, M, tm, L, x + hs * (3.0 / 10.0), R.yt, R.k3, &dummy);
+#pragma unroll
+    for (int e = 0; e < E; ++e) R.yt[e] = R.y[e] + hs * (a41 * R.k1[e] + a42 * R.k2[e] + a43 * R.k3[e]);
+    derivs<T, false>(C, M, tm, L, x + hs * (4.0 / 5.0), R.yt, R.k4, &dummy);
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      R.yt[e] = R.y[e] + hs * (a51 * R.k1[e] + a52 * R.k2[e] + a53 * R.k3[e] + a54 * R.k4[e]);
+    derivs<T, false>(C, M, tm, L, x + hs * (8.0 / 9.0), R.yt, R.k5, &dummy);
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      R.yt[e] = R.y[e] + hs * (a61 * R.k1[e] + a62 * R.k2[e] + a63 * R.k3[e] + a64 * R.k4[e] + a65 * R.k5[e]);
+    derivs<T, false>(C, M, tm, L, x + hs, R.yt, R.k6, &dummy);
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      R.yt[e] = R.y[e] + hs * (b1 * R.k1[e] + b3 * R.k3[e] + b4 * R.k4[e] + b5 * R.k5[e] + b6 * R.k6[e]);
+    // stage 7 (FSAL) into k2's registers
+    derivs<T, false>(C, M, tm, L, x + hs, R.yt, R.k2, &dummy);
+    rk.evals += 6;
+    double m = 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if ((L.act >> e) & 1u) {
+        double ee = e1 * R.k1[e] + e3 * R.k3[e] + e4 * R.k4[e] + e5 * R.k5[e] + e6 * R.k6[e] + e7 * R.k2[e];
+        m = fmax(m, fabs(ee) / fmax(1.0, fabs(R.y[e])));
+      }
+    }
+    m = tm.maxr(m);
+    rk.err = m * rk.h;
+    if (rk.err <= tol) {
+      x = xt;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        R.y[e] = R.yt[e];
+        R.k1[e] = R.k2[e];
+      }
+      rk.fails = 0;
+      if (x == xend) {
+        rk.fsal = true;  // reuse_first_derivative: stage 7 seeds the next call
+        return 0;
+      }
+    } else {
+      rk.fails++;
+      if (rk.h <= hmin) return -3;
+    }
+  }
+}
+
+// set one flat variable (uniform idx) to v
+template <int T>
+__device__ __forceinline__ void setv(const Team<T>& tm, double (&v)[NVAR_MAX / T], int idx, double val) {
+  constexpr int E = NVAR_MAX / T;
+  int e = idx / T;
+  if (tm.t == idx % T) {
+#pragma unroll
+    for (int j = 0; j < E; ++j)
+      if (j == e) v[j] = val;
+  }
+}
+
+template <int T>
+__device__ __forceinline__ void zero_inactive(const Lanes<T>& L, double (&v)[NVAR_MAX / T]) {
+  constexpr int E = NVAR_MAX / T;
+#pragma unroll
+  for (int e = 0; e < E; ++e)
+    if (!((L.act >> e) & 1u)) v[e] = 0.0;
+}
+
+// GaugeInterface_ScalEv (equations.f90:212-234)
+template <int T>
+__device__ int scal_ev(const DevCosmo& C, Mode& M, const Team<T>& tm, const Lanes<T>& L, Regs<T>& R, RK& rk,
+                       double& tau, double tauend) {
+  if (M.q < 2e-3 && tau <= C.taurend) rk.ms_user = 2.0;
+  else rk.ms_user = 20.0 / C.IntTolBoost;
+  return dp45<T>(C, M, tm, L, R, rk, tau, tauend, C.tol1);
+}
+
+// GaugeInterface_EvolveScal (equations.f90:261-460), switches as a loop
+template <int T>
+__device__ int evolve_scal(const DevCosmo& C, Mode& M, const Team<T>& tm, Lanes<T>& L, Regs<T>& R, RK& rk,
+                           double& tau, double tauend) {
+  for (int guard = 0; guard < 16; ++guard) {
+    double noSwitch = C.tau0 + 1;
+    double smallTime = fmin(tau, M.ik) / 100;
+    double switchBoost = C.AccuracyBoost * C.TimeSwitchBoost;
+    double t_ktau = noSwitch, t_nonu = noSwitch, t_nophot = noSwitch;
+    if (!M.hk && !M.nonu) t_ktau = (double)max(20, M.lmaxnr - 4) / M.k;
+    if (!M.nonu) t_nonu = fmax(15 / M.k * switchBoost, fmin(C.taurend, C.matter_verydom_tau));
+    if (!M.nophot && M.k > 0.03 * switchBoost) t_nophot = fmax(15 / M.k, C.taurend) * switchBoost;
+    double next = fmin(fmin(t_ktau, M.tight_off), fmin(fmin(t_nonu, t_nophot), noSwitch));
+    if (!(next < tauend)) return scal_ev<T>(C, M, tm, L, R, rk, tau, tauend);
+    if (next > tau + smallTime) {
+      int rc = scal_ev<T>(C, M, tm, L, R, rk, tau, next);
+      if (rc) return rc;
+    }
+    if (next == M.tight_off) {
+      // leave tight coupling: seed pi_g, G_3, E_2, E_3 with the 2nd-order TC values
+      M.tc = false;
+      M.tight_off = noSwitch;
+      rk.reset = true;
+      update_activity<T>(M, tm, L);
+      double itau = 1.0 / tau, a, cs2, opac, dopac;
+      thermo_values(C, tau, itau, a, cs2, opac, dopac);
+      double kb = M.k, op2 = opac * opac;
+      double g2 = M.pig;
+      double g3 = (3.0 / 7.0) * g2 * (kb / opac) * (1.0 + dopac / op2) + (3.0 / 7.0) * M.pigdot * (kb / op2) * (-1.0);
+      double p2 = M.pig / 4 + M.pigdot * (1.0 / opac) * (-5.0 / 8.0 - (25.0 / 16.0) * dopac / op2) +
+                  M.pig * (kb / opac) * (kb / opac) * (-5.0 / 56.0);
+      double p3 = (3.0 / 7.0) * (kb / opac) * p2 * (1.0 + dopac / op2) +
+                  (3.0 / 7.0) * (kb / op2) * ((M.pigdot / 4.0) * (1.0 + (5.0 / 2.0) * dopac / op2)) * (-1.0);
+      zero_inactive<T>(L, R.y);
+      setv<T>(tm, R.y, M.g_ix + 2, g2);
+      setv<T>(tm, R.y, M.g_ix + 3, g3);
+      setv<T>(tm, R.y, M.pol_ix + 2, p2);
+      setv<T>(tm, R.y, M.pol_ix + 3, p3);
+    } else if (next == t_ktau) {
+      M.hk = true;
+      update_activity<T>(M, tm, L);
+      zero_inactive<T>(L, R.y);
+    } else if (next == t_nonu) {
+      rk.reset = true;
+      M.nonu = true;
+      update_activity<T>(M, tm, L);
+      zero_inactive<T>(L, R.y);
+    } else if (next == t_nophot) {
+      rk.reset = true;
+      M.nophot = true;
+      update_activity<T>(M, tm, L);
+      zero_inactive<T>(L, R.y);
+    }
+    rk.fsal = false;
+  }
+  return -4;
+}
+
+// initial (equations.f90:1891-2112), adiabatic mode, flat, massless neutrinos
+template <int T>
+__device__ void initial(const DevCosmo& C, const Mode& M, const Team<T>& tm, Regs<T>& R, double tau) {
+  constexpr int E = NVAR_MAX / T;
+#pragma unroll
+  for (int e = 0; e < E; ++e) R.y[e] = 0;
+  double k = M.k;
+  double x = k * tau, x2 = x * x, x3 = x2 * x;
+  double grhonu = C.grhornomass;
+  double om = (C.grhob + C.grhoc) / sqrt(3 * (C.grhog + grhonu));
+  double omtau = om * tau;
+  double Rv = grhonu / (grhonu + C.grhog);
+  double Rp15 = 4 * Rv + 15;
+  double iv_clxg = -1.0 / 3 * x2 * (1 - omtau / 5);
+  double iv_clxb = 0.75 * iv_clxg;
+  double iv_qg = iv_clxg * x / 9.0;
+  double iv_qr = -(4 * Rv + 23) / Rp15 * x3 / 27;
+  double iv_vb = 0.75 * iv_qg;
+  double iv_pir = 4.0 / 3 * x2 / Rp15 * (1 + omtau / 4 * (4 * Rv - 5) / (2 * Rv + 15));
+  double iv_aj3r = 4 / 21.0 / Rp15 * x3;
+  double iv_eta = -2 * (1 - x2 / 12 * (-10.0 / Rp15 + 1));
+  setv<T>(tm, R.y, 0, iv_eta * k / 2);
+  setv<T>(tm, R.y, 1, -iv_clxb);
+  setv<T>(tm, R.y, 2, -iv_clxb);
+  setv<T>(tm, R.y, 3, -iv_vb);
+  setv<T>(tm, R.y, M.g_ix, -iv_clxg);
+  setv<T>(tm, R.y, M.g_ix + 1, -iv_qg);
+  setv<T>(tm, R.y, M.r_ix, -iv_clxg);
+  setv<T>(tm, R.y, M.r_ix + 1, -iv_qr);
+  setv<T>(tm, R.y, M.r_ix + 2, -iv_pir);
+  if (M.lmaxnr > 2) setv<T>(tm, R.y, M.r_ix + 3, -iv_aj3r);
+}
+
+// CalcScalarSources (cmbmain.f90:998-1074) for one mode
+template <int T>
+__device__ void evolve_mode(const DevCosmo& C, int q_ix, const Team<T>& tm) {
+  const CambGpuModeSpec ms = C.modes[q_ix];
+  Mode M;
+  M.q = ms.q;
+  M.k = ms.q;
+  M.ik = 1.0 / M.k;
+  M.k2 = M.k * M.k;
+  M.ik2 = 1.0 / M.k2;
+  M.lmaxg = ms.lmaxg;
+  M.lmaxgpol = ms.lmaxgpol;
+  M.lmaxnr = ms.lmaxnr;
+  M.g_ix = 4;
+  M.pol_ix = M.g_ix + M.lmaxg + 1;
+  M.r_ix = M.pol_ix + M.lmaxgpol + 1;
+  M.nvar = M.r_ix + M.lmaxnr + 1;
+  M.denlk1 = (1.0 / 3) * M.k;
+  M.denlk2_1 = (1.0 / 3) * M.k * 2;
+  M.denlk_2 = (1.0 / 5) * M.k * 2;
+  M.denlk2_2 = (1.0 / 5) * M.k * 3;
+  M.poltruncfac = (double)M.lmaxgpol / max(1, M.lmaxgpol - 2);
+  M.pig = 0;
+  M.pigdot = 0;
+  M.tight_off = ms.tight_switch_tau;
+  M.tc = true;
+  M.hk = false;
+  M.nonu = false;
+  M.nophot = false;
+  const int nsrc = C.nsrc, nk = C.nk;
+  if (M.nvar > NVAR_MAX) {
+    if (tm.t == 0) atomicExch(C.status, (int)CAMBGPU_ERROR_UNSUPPORTED_PARAMS);
+    return;
+  }
+  Lanes<T> L;
+  setup_layout<T>(M, tm, L);
+  update_activity<T>(M, tm, L);
+  Regs<T> R;
+  initial<T>(C, M, tm, R, ms.taustart);
+  double tau = ms.taustart;
+  RK rk;
+  rk.h = 0;
+  rk.err = 0;
+  rk.ms_user = 0;
+  rk.fails = 0;
+  rk.fsal = false;
+  rk.reset = true;
+  rk.evals = 0;
+  double* out = C.linear_src;
+  for (int j = 1; j < C.ntau; ++j) {
+    double tauend = C.tau_points[j];
+    if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time) {
+      // rest of the sources stay zero (buffer cleared before launch)
+      break;
+    }
+    int rc = evolve_scal<T>(C, M, tm, L, R, rk, tau, tauend);
+    if (rc) {
+      if (tm.t == 0) atomicExch(C.status, (int)CAMBGPU_ERROR_EVOLUTION);
+      return;
+    }
+    constexpr int E = NVAR_MAX / T;
+    double dy[E];
+    SrcOut so;
+    derivs<T, true>(C, M, tm, L, tau, R.y, dy, &so);
+    if (tm.t == 0) {
+      for (int s = 0; s < nsrc; ++s) out[((size_t)j * nsrc + s) * nk + q_ix] = so.s[s];
+    }
+  }
+}
+
+template <int T>
+__global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __restrict__ cosmos,
+                                                             const WorkItem* __restrict__ items, int nitems,
+                                                             int* __restrict__ counter) {
+  Team<T> tm;
+  for (;;) {
+    int w = 0;
+    if (tm.t == 0) w = atomicAdd(counter, 1);
+    w = tm.bcast_i(w, 0);
+    if (w >= nitems) break;
+    WorkItem it = items[w];
+    evolve_mode<T>(cosmos[it.cosmo], it.mode, tm);
+  }
+}
+
+// host-side launch helpers (template kernels stay in this translation unit)
+int ode_blocks_per_sm(int team, int threads) {
+  int per_sm = 0;
+  if (team == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<32>, threads, 0);
+  else if (team == 16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<16>, threads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<8>, threads, 0);
+  return per_sm;
+}
+
+cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
+                              const WorkItem* items, int nitems, int* counter) {
+  if (team == 32) ode_persistent_kernel<32><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 16) ode_persistent_kernel<16><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else ode_persistent_kernel<8><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  return cudaGetLastError();
+}
+
+}  // namespace cgdev

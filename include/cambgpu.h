@@ -1,0 +1,178 @@
+/*
+ * cambgpu.h -- C ABI of the GB300 scalar-perturbation library (libcambgpu.so).
+ *
+ * The library replaces three OpenMP call sites of the reference's
+ * fortran/cmbmain.f90 with CUDA kernels for sm_103a:
+ *
+ *   (1) the source loop  `do q_ix ... call DoSourcek`      (cmbmain.f90:205-209)
+ *       -> cambgpu_evolve_scalar_sources
+ *   (2) the transfer loop `do q_ix ... call SourceToTransfers` (cmbmain.f90:287-291),
+ *       with the source k-spline of InitSourceInterpolation (cmbmain.f90:1249-1265)
+ *       -> cambgpu_los_flat
+ *   (3) `call CalcScalCls(State%CLdata%CTransScal)`        (cmbmain.f90:323)
+ *       -> cambgpu_calc_scal_cls
+ *
+ * plus whole-pipeline entry points that mirror CAMB_GetResults
+ * (fortran/camb.f90:60-192) for one cosmology or a batch.
+ *
+ * Conventions (following the reference):
+ *   - every array is caller-allocated host memory (GetSourceMem cmbmain.f90:755-782,
+ *     Init_ClTransfer results.f90:3110-3123, ClTransferToCl cmbmain.f90:310-356);
+ *   - the library owns its device buffers and caches the Bessel table across calls
+ *     (as bessels.f90:64-112 caches it on the host);
+ *   - return 0 on success, else an error code with the meaning of config.f90:66-74
+ *     (4 = error_evolution for ODE failures, 9 = allocation, 2 = unsupported params,
+ *     5 = reionization, 3 = recombination);  the library never exits the process.
+ *   - not thread-safe: one host thread per call, like the reference (cmbmain.f90:7-8).
+ */
+#ifndef CAMBGPU_H
+#define CAMBGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CAMBGPU_OK 0
+#define CAMBGPU_ERROR_UNSUPPORTED_PARAMS 2
+#define CAMBGPU_ERROR_RECOMBINATION 3
+#define CAMBGPU_ERROR_EVOLUTION 4
+#define CAMBGPU_ERROR_REIONIZATION 5
+#define CAMBGPU_ERROR_ALLOCATION 9
+#define CAMBGPU_ERROR_CUDA 10
+
+/* Cosmological and accuracy parameters: the subset of CAMBParams / AccuracyParams
+ * (fortran/model.f90:27-209) that the scalar flat path reads. */
+typedef struct CambGpuParams {
+    double H0, ombh2, omch2, omk, TCMB, YHe;
+    double num_nu_massless;      /* N_eff carried by massless neutrinos */
+    double optical_depth;        /* reionization tau (re_use_optical_depth = T) */
+    double reion_delta_redshift; /* tanh width, default 0.5 */
+    double As, ns, nrun, pivot_scalar, Alens;
+    int max_l;                   /* CP%Max_l */
+    double max_eta_k;            /* CP%Max_eta_k */
+    int do_lensing;              /* lensing-potential source (3 sources) */
+    double AccuracyBoost, lAccuracyBoost, lSampleBoost, IntTolBoost, TimeStepBoost;
+    double SourcekAccuracyBoost, IntkAccuracyBoost, BesselBoost, BessIntBoost;
+    double TimeSwitchBoost, LimberBoost, BackgroundTimeStepBoost;
+    int accurate_polarization, accurate_reionization;
+} CambGpuParams;
+
+/* Per-k-mode setup: the hierarchy sizes of GetNumEqns (equations.f90:860-1070)
+ * and the start/tight-coupling times of GetTauStart (cmbmain.f90:706-729) and
+ * initial (equations.f90:1940-1950). */
+typedef struct CambGpuModeSpec {
+    double q;
+    double taustart;
+    double tight_switch_tau;
+    int lmaxg, lmaxgpol, lmaxnr;
+    int pad;
+} CambGpuModeSpec;
+
+/* Read-only view of everything the hot path consumes for one cosmology: the
+ * background scalars of CAMBdata (results.f90:188-216), the thermal-history tables
+ * of TThermoData (results.f90:75-111), the source time grid (SetTimeSteps), the
+ * source and integration k grids, the l sampling and the flat Bessel table.
+ * All pointers are host pointers owned by the handle that filled the view. */
+typedef struct CambGpuTables {
+    /* background */
+    double grhog, grhor, grhornomass, grhoc, grhob, grhov, grhok;
+    double adotrad, tau0, DMt0, taurst, taurend, tau_maxvis, matter_verydom_tau;
+    double akthom, fHe;
+    /* thermal history */
+    int nthermo;
+    double tauminn, dlntau, dlntau_inv, tight_tau;
+    const double* thermo_horner; /* [nthermo][16]: cs2b(4) opacity(4) a/tau(4) dopacity(4) */
+    const double* dotmu;         /* [nthermo] */
+    const double* ddotmu;        /* [nthermo] */
+    const double* cs2;           /* [nthermo] */
+    const double* dddotmu;       /* [nthermo] */
+    const double* ddddotmu;      /* [nthermo] */
+    const double* emmu;          /* [nthermo] */
+    const double* demmu;         /* [nthermo] */
+    /* source time steps (TimeSteps%points / dpoints) */
+    int ntau;
+    const double* tau_points;
+    const double* tau_dpoints;
+    /* source k grid (Evolve_q) and per-mode setup */
+    int nk;
+    const double* q_evolve;
+    const CambGpuModeSpec* modes;
+    /* integration q grid (ThisCT%q) */
+    int nq;
+    const double* q_int;
+    const double* dq_int;
+    /* sampled l (ThisCT%ls%l) */
+    int nl;
+    const int* ls;
+    /* flat Bessel table: bessel_horner(4, num_xx-1, nl) laid out [l][x][4] */
+    int num_xx;
+    const double* bess_x;
+    const double* bessel_horner;
+    /* settings */
+    int nsrc;                /* 2 unlensed, 3 with lensing potential */
+    int want_late_time;      /* WantLateTime (cmbmain.f90:138) */
+    double max_etak_scalar;  /* InitVars cmbmain.f90:812-813 */
+    double tol1;             /* ODE tolerance, cmbmain.f90:1018 */
+    double max_bessels_etak; /* maximum_qeta */
+    double AccuracyBoost, IntTolBoost, TimeSwitchBoost, BessIntBoost, LimberBoost;
+    double lAccuracyBoost;
+    int accurate_polarization, accurate_reionization;
+    double As, ns, nrun, pivot_scalar, Alens;
+} CambGpuTables;
+
+/* Fills p with the reference's defaults (model.f90:36-209, Python set_params). */
+void cambgpu_default_params(CambGpuParams* p);
+
+/* ---- host-side tables (background, RECFAST, reionization, grids, Bessel table) ---- */
+/* Replaces CAMBdata%SetParams + InitVars (results.f90:332-628, cmbmain.f90:785-862),
+ * SetkValuesForSources (cmbmain.f90:864-936), lSamples_init (results.f90:1505-1704),
+ * SetkValuesForInt (cmbmain.f90:1267-1349) and InitSpherBessels (bessels.f90:64-112). */
+int cambgpu_tables_create(const CambGpuParams* p, void** handle);
+int cambgpu_tables_view(void* handle, CambGpuTables* view);
+void cambgpu_tables_destroy(void* handle);
+/* Background quantities for checks: tau0, DMt0, taurst, taurend, tau_maxvis,
+ * zre (reionization mid redshift), x_e(z) at the requested redshifts. */
+int cambgpu_tables_derived(void* handle, double* out8);
+int cambgpu_recfast_xe(void* handle, const double* z, int n, double* xe);
+
+/* ---- hot path on the GPU (host buffers in and out) ---- */
+/* (1) cmbmain.f90:205-209: LinearSrc laid out [ntau][nsrc][nk] (k fastest, as the
+ *     reference's LinearSrc(nk, nsrc, ntau) in Fortran order). */
+int cambgpu_evolve_scalar_sources(const CambGpuTables* t, double* linear_src);
+/* (2) cmbmain.f90:1249-1265 + 287-291: Delta_p_l_k laid out [nq][nl][nsrc]
+ *     (src fastest, as Delta_p_l_k(nsrc, nl, nq) in Fortran order). */
+int cambgpu_los_flat(const CambGpuTables* t, const double* linear_src, double* delta_p_l_k);
+/* (3) cmbmain.f90:3179-3343: iCl laid out [nl][6] with columns TT EE TE PP PT PE
+ *     (C_Temp..C_PhiE), l(l+1)C_l/2pi at the sampled l. */
+int cambgpu_calc_scal_cls(const CambGpuTables* t, const double* delta_p_l_k, double* icl);
+
+/* ---- whole pipeline (CAMB_GetResults for the scalar flat path) ---- */
+/* cl_out: [lmax_out+1][4] TT EE BB TE of l(l+1)C_l/2pi (dimensionless), BB = 0,
+ * as results.py get_unlensed_scalar_cls. */
+int cambgpu_get_results(const CambGpuParams* p, int lmax_out, double* cl_out);
+/* n cosmologies in one persistent launch per stage; cl_out [n][lmax_out+1][4];
+ * status [n] (per-cosmology error code). */
+int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, double* cl_out, int* status);
+
+/* ---- resident batch: tables staged in device memory once, then timed runs ---- */
+/* Builds and uploads n cosmologies; the batch stays resident until released. */
+int cambgpu_batch_prepare(const CambGpuParams* p, int n);
+/* Runs ODE, source spline + LOS, C_l on the resident batch; ms3 = device ms per stage. */
+int cambgpu_batch_run(double* ms3);
+/* C_l of the last run, [n][lmax_out+1][4] as cambgpu_get_results. */
+int cambgpu_batch_fetch(int lmax_out, double* cl_out);
+void cambgpu_batch_release(void);
+
+/* ---- runtime ---- */
+/* Team size for the ODE kernel (lanes per k-mode: 1,2,4,8,16,32); 0 = autotuned. */
+int cambgpu_set_ode_team(int lanes_per_mode);
+/* Kernel timing of the last GPU call, in ms: [ode, spline, los, cls, h2d, d2h]. */
+int cambgpu_last_timings(double* out6);
+/* Number of kernels the library launched since the counter was reset. */
+long long cambgpu_kernel_launches(int reset);
+const char* cambgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
