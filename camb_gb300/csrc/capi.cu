@@ -22,6 +22,7 @@ namespace cgdev {
 int ode_blocks_per_sm(int team, int threads);
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
                               const WorkItem* items, int nitems, int* counter);
+cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
 __global__ void los_flat_kernel(const DevCosmo*);
 __global__ void scal_cls_kernel(const DevCosmo*);
@@ -35,6 +36,8 @@ std::string g_err;
 std::atomic<long long> g_launches{0};
 double g_timings[6] = {0, 0, 0, 0, 0, 0};
 int g_team = 0;
+long long g_last_evals = 0;
+long long g_h2d = 0, g_d2h = 0;
 
 int set_err(int code, const std::string& msg) {
   g_err = msg;
@@ -216,6 +219,7 @@ struct Batch {
   int nitems = 0;
   int* d_counter = nullptr;
   int* d_status = nullptr;
+  unsigned long long* d_evals = nullptr;
   int max_ntau = 0, max_nq = 0, max_nl = 0, max_rows = 0;
 };
 
@@ -233,12 +237,14 @@ int stage_batch(Batch& B) {
   if (rc) return set_err(rc, "device allocation failed");
   B.d_status = g_rt.arena.take<int>(n);
   B.d_counter = g_rt.arena.take<int>(1);
+  B.d_evals = g_rt.arena.take<unsigned long long>(1);
   std::vector<std::pair<void*, std::pair<const void*, size_t>>> copies;
   B.ups.resize(n);
   for (int c = 0; c < n; ++c) {
     B.ups[c].t = B.views[c];
     rc = upload(B.ups[c], B.d_status + c, copies);
     if (rc) return rc;
+    B.ups[c].d.evals = B.d_evals;
     B.max_ntau = std::max(B.max_ntau, B.views[c]->ntau);
     B.max_nq = std::max(B.max_nq, B.views[c]->nq);
     B.max_nl = std::max(B.max_nl, B.views[c]->nl);
@@ -279,7 +285,10 @@ int stage_batch(Batch& B) {
   }
   CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
   size_t off = 0;
+  g_h2d = 0;
+  g_d2h = 0;
   for (auto& cp : copies) {
+    g_h2d += (long long)cp.second.second;
     std::memcpy(g_rt.pinned + off, cp.second.first, cp.second.second);
     CUDA_TRY(cudaMemcpyAsync(cp.first, g_rt.pinned + off, cp.second.second, cudaMemcpyHostToDevice, g_rt.stream));
     off += (cp.second.second + 255) & ~size_t(255);
@@ -301,6 +310,7 @@ int pick_team(const Batch& B) {
 
 int run_ode(Batch& B) {
   CUDA_TRY(cudaMemsetAsync(B.d_counter, 0, sizeof(int), g_rt.stream));
+  CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
   int team = pick_team(B);
   int per_sm = std::max(1, ode_blocks_per_sm(team, 128));
   int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * team + 127) / 128);
@@ -357,8 +367,11 @@ int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
   g_timings[1] = 0;
   g_timings[2] = elapsed(g_rt.ev[1], g_rt.ev[2]);
   g_timings[3] = elapsed(g_rt.ev[2], g_rt.ev[3]);
-  std::vector<int> st(B.views.size());
-  CUDA_TRY(cudaMemcpy(st.data(), B.d_status, st.size() * 4, cudaMemcpyDeviceToHost));
+  if (do_ode) {
+    unsigned long long ev = 0;
+    CUDA_TRY(cudaMemcpy(&ev, B.d_evals, sizeof(ev), cudaMemcpyDeviceToHost));
+    g_last_evals = (long long)ev;
+  }
   return 0;
 }
 
@@ -569,6 +582,7 @@ int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, doubl
   for (int c = 0; c < n; ++c) {
     icl.resize((size_t)hs[c]->view.nl * 6);
     CUDA_TRY(cudaMemcpy(icl.data(), B.ups[c].d.icl, icl.size() * 8, cudaMemcpyDeviceToHost));
+    g_d2h += (long long)icl.size() * 8;
     finish_cls(*hs[c], icl.data(), lmax_out, cl_out + (size_t)c * (lmax_out + 1) * 4);
   }
   return 0;
@@ -628,6 +642,34 @@ int cambgpu_set_ode_team(int lanes) {
 
 int cambgpu_last_timings(double* out6) {
   for (int i = 0; i < 6; ++i) out6[i] = g_timings[i];
+  return 0;
+}
+
+long long cambgpu_last_ode_evals(void) { return g_last_evals; }
+
+int cambgpu_last_transfer_bytes(long long* out2) {
+  out2[0] = g_h2d;
+  out2[1] = g_d2h;
+  return 0;
+}
+
+int cambgpu_probe_fp64_tflops(double* tflops) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int rc = rt_init();
+  if (rc) return rc;
+  double* d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, 8));
+  const int threads = 256, iters = 4096;
+  const int blocks = g_rt.nsm * 8;
+  CUDA_TRY(launch_fp64_probe(blocks, threads, 64, d, g_rt.stream));  // warm-up
+  CUDA_TRY(cudaEventRecord(g_rt.ev[4], g_rt.stream));
+  CUDA_TRY(launch_fp64_probe(blocks, threads, iters, d, g_rt.stream));
+  CUDA_TRY(cudaEventRecord(g_rt.ev[5], g_rt.stream));
+  CUDA_TRY(cudaEventSynchronize(g_rt.ev[5]));
+  g_launches += 2;
+  double ms = elapsed(g_rt.ev[4], g_rt.ev[5]);
+  cudaFree(d);
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
   return 0;
 }
 

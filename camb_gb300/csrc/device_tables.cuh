@@ -34,6 +34,7 @@ struct DevCosmo {
   double* delta;       // [nq][nl][nsrc]
   double* icl;         // [nl][6]
   int* status;         // per-cosmology status word
+  unsigned long long* evals;  // derivative evaluations (shared counter)
   // integration grid and l sampling
   const double* q_int;
   const double* dq_int;

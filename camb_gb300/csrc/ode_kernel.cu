@@ -27,7 +27,7 @@
 namespace cgdev {
 
 constexpr int NVAR_MAX = 128;
-constexpr long long kMaxEvalsPerMode = 40000000LL;
+constexpr long long kMaxEvalsPerMode = 2000000LL;
 
 template <int T>
 struct Team {
@@ -90,6 +90,10 @@ __device__ __forceinline__ void thermo_values(const DevCosmo& C, double tau, dou
   double d = log(tau * C.inv_tauminn) * C.dlntau_inv + 1.0;
   int i = (int)d;
   d = d - i;
+  if (i < 1) {  // before the table start (never reached: every mode starts after tauminn)
+    i = 1;
+    d = 0;
+  }
   if (i >= C.nthermo) {
     cs2 = C.cs2_end;
     opac = C.dotmu_end;
@@ -112,6 +116,10 @@ __device__ __forceinline__ void ionization(const DevCosmo& C, double tau, double
   double d = log(tau * C.inv_tauminn) * C.dlntau_inv + 1.0;
   int i = (int)d;
   d = d - i;
+  if (i < 1) {
+    i = 1;
+    d = 0;
+  }
   double ddopac;
   double tdl = tau * C.dlntau;
   if (i < C.nthermo) {
@@ -737,10 +745,12 @@ __device__ void evolve_mode(const DevCosmo& C, int q_ix, const Team<T>& tm) {
     double dy[E];
     SrcOut so;
     derivs<T, true>(C, M, tm, L, tau, R.y, dy, &so);
+    rk.evals++;
     if (tm.t == 0) {
       for (int s = 0; s < nsrc; ++s) out[((size_t)j * nsrc + s) * nk + q_ix] = so.s[s];
     }
   }
+  if (tm.t == 0) atomicAdd(C.evals, (unsigned long long)rk.evals);
 }
 
 template <int T>
@@ -756,6 +766,27 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
     WorkItem it = items[w];
     evolve_mode<T>(cosmos[it.cosmo], it.mode, tm);
   }
+}
+
+// DFMA throughput probe: 8 independent FMA chains per thread
+__global__ void fp64_probe_kernel(double* out, int iters) {
+  double a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = 1.0 + 1e-7 * (threadIdx.x + j);
+  const double m = 0.999999, c = 1e-9;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fma(a[j], m, c);
+  }
+  double s = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  if (s == 12345.0) out[0] = s;  // keeps the chains live
+}
+
+cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s) {
+  fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, iters);
+  return cudaGetLastError();
 }
 
 // host-side launch helpers (template kernels stay in this translation unit)

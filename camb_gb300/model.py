@@ -1,0 +1,129 @@
+"""Parameters, mirroring the reference's camb/model.py CAMBparams for the scalar flat path.
+
+Only what the GPU path reads is kept: cosmology (set_cosmology, model.py:641),
+l range and k range (set_for_lmax, model.py:1018-1063), the power-law primordial
+spectrum (initialpower.py InitialPowerLaw.set_params) and the accuracy knobs of
+AccuracyParams (model.py:164; fortran/model.f90:36-104).
+"""
+import ctypes as C
+import math
+
+from . import _lib
+from ._lib import CAMBError
+
+
+class AccuracyParams:
+    """Accuracy knobs (fortran/model.f90:36-104), all default 1 / True."""
+
+    _names = ["AccuracyBoost", "lAccuracyBoost", "lSampleBoost", "IntTolBoost", "TimeStepBoost",
+              "SourcekAccuracyBoost", "IntkAccuracyBoost", "BesselBoost", "BessIntBoost", "TimeSwitchBoost",
+              "LimberBoost", "BackgroundTimeStepBoost"]
+
+    def __init__(self):
+        for n in self._names:
+            setattr(self, n, 1.0)
+        self.AccuratePolarization = True
+        self.AccurateReionization = True
+
+
+class InitialPowerLaw:
+    """Power-law primordial spectrum (InitialPower.f90:121-144)."""
+
+    def __init__(self):
+        self.As, self.ns, self.nrun, self.pivot_scalar = 2.1e-9, 0.965, 0.0, 0.05
+
+    def set_params(self, As=2e-9, ns=0.96, nrun=0, pivot_scalar=0.05, **kwargs):
+        if kwargs.get("r"):
+            raise CAMBError("tensor modes are not part of the GPU scalar path")
+        self.As, self.ns, self.nrun, self.pivot_scalar = As, ns, nrun, pivot_scalar
+        return self
+
+
+class TanhReionization:
+    """tanh reionization set from the optical depth (reionization.f90:97-360)."""
+
+    def __init__(self):
+        self.optical_depth = 0.06
+        self.delta_redshift = 0.5
+
+
+class CAMBparams:
+    def __init__(self, **kwargs):
+        self.H0, self.ombh2, self.omch2, self.omk = 67.5, 0.022, 0.122, 0.0
+        self.TCMB, self.YHe, self.num_nu_massless = 2.7255, 0.2454, 3.044
+        self.Alens = 1.0
+        self.max_l, self.max_eta_k = 2500, 6250.0
+        self.DoLensing = False
+        self.WantCls, self.WantScalars = True, True
+        self.InitPower = InitialPowerLaw()
+        self.Reion = TanhReionization()
+        self.Accuracy = AccuracyParams()
+        for k, v in kwargs.items():
+            setattr(self, k, v)
+
+    def set_cosmology(self, H0=67.5, ombh2=0.022, omch2=0.12, omk=0.0, mnu=0.0, nnu=3.044, YHe=None,
+                      TCMB=2.7255, tau=None, Alens=1.0, **kwargs):
+        """Sets the background cosmology (model.py:641).  Massive neutrinos are not part of
+        this path yet: mnu must be 0 (all of nnu is massless).  YHe=None keeps 0.2454
+        (the BBN value at the fiducial ombh2) rather than recomputing BBN consistency."""
+        if mnu:
+            raise CAMBError("massive neutrinos are not supported by the GPU path yet (set mnu=0)")
+        if abs(omk) > 5e-7:
+            raise CAMBError("only flat models are supported")
+        self.H0, self.ombh2, self.omch2, self.omk = H0, ombh2, omch2, omk
+        self.num_nu_massless = nnu
+        if YHe is not None:
+            self.YHe = YHe
+        self.TCMB, self.Alens = TCMB, Alens
+        if tau is not None:
+            self.Reion.optical_depth = tau
+        return self
+
+    def set_for_lmax(self, lmax, max_eta_k=None, lens_potential_accuracy=0, lens_output_margin=200,
+                     k_eta_fac=2.5, lens_k_eta_reference=18000.0):
+        """model.py:1018-1063 (the non-linear lensing switch is out of scope)."""
+        self.max_l = lmax + lens_output_margin if self.DoLensing else lmax
+        self.max_eta_k = max_eta_k or self.max_l * k_eta_fac
+        if lens_potential_accuracy:
+            self.max_eta_k = max(self.max_eta_k, lens_k_eta_reference * lens_potential_accuracy)
+        return self
+
+    def scalar_power(self, k):
+        p = self.InitPower
+        lnrat = math.log(k / p.pivot_scalar)
+        return p.As * math.exp(lnrat * (p.ns - 1 + lnrat * (p.nrun / 2)))
+
+    def to_struct(self):
+        s = _lib.default_params()
+        for n in ["H0", "ombh2", "omch2", "omk", "TCMB", "YHe", "num_nu_massless", "Alens", "max_l", "max_eta_k"]:
+            setattr(s, n, getattr(self, n))
+        s.max_l = int(self.max_l)
+        s.optical_depth = self.Reion.optical_depth
+        s.reion_delta_redshift = self.Reion.delta_redshift
+        s.As, s.ns, s.nrun, s.pivot_scalar = (self.InitPower.As, self.InitPower.ns, self.InitPower.nrun,
+                                              self.InitPower.pivot_scalar)
+        s.do_lensing = 1 if self.DoLensing else 0
+        for n in AccuracyParams._names:
+            setattr(s, n, getattr(self.Accuracy, n))
+        s.accurate_polarization = int(bool(self.Accuracy.AccuratePolarization))
+        s.accurate_reionization = int(bool(self.Accuracy.AccurateReionization))
+        return s
+
+
+def set_params(cp=None, lmax=None, H0=None, ombh2=0.022, omch2=0.12, omk=0.0, mnu=0.0, nnu=3.044, YHe=None,
+               tau=None, As=2e-9, ns=0.96, nrun=0, pivot_scalar=0.05, lens_potential_accuracy=0, max_eta_k=None,
+               DoLensing=False, **kwargs):
+    """camb.set_params (camb.py:135) restricted to the parameters of the GPU scalar path."""
+    cp = cp or CAMBparams()
+    cp.DoLensing = DoLensing
+    cp.set_cosmology(H0=H0 if H0 is not None else 67.5, ombh2=ombh2, omch2=omch2, omk=omk, mnu=mnu, nnu=nnu,
+                     YHe=YHe, tau=tau)
+    cp.InitPower.set_params(As=As, ns=ns, nrun=nrun, pivot_scalar=pivot_scalar)
+    if lmax is not None:
+        cp.set_for_lmax(lmax, max_eta_k=max_eta_k, lens_potential_accuracy=lens_potential_accuracy)
+    for k, v in kwargs.items():
+        if hasattr(cp.Accuracy, k):
+            setattr(cp.Accuracy, k, v)
+        else:
+            setattr(cp, k, v)
+    return cp

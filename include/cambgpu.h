@@ -168,6 +168,12 @@ void cambgpu_batch_release(void);
 int cambgpu_set_ode_team(int lanes_per_mode);
 /* Kernel timing of the last GPU call, in ms: [ode, spline, los, cls, h2d, d2h]. */
 int cambgpu_last_timings(double* out6);
+/* Derivative evaluations of the last ODE launch (all modes of all cosmologies). */
+long long cambgpu_last_ode_evals(void);
+/* Host<->device bytes moved by the last pipeline call: out2 = [h2d, d2h]. */
+int cambgpu_last_transfer_bytes(long long* out2);
+/* Measures the device's FP64 FMA throughput (TFLOP/s) with a DFMA-chain kernel. */
+int cambgpu_probe_fp64_tflops(double* tflops);
 /* Number of kernels the library launched since the counter was reset. */
 long long cambgpu_kernel_launches(int reset);
 const char* cambgpu_last_error(void);

@@ -1,0 +1,61 @@
+"""Parameter sets shared by the tests (the reference's test configurations)."""
+import json
+import os
+
+import numpy as np
+
+from camb_gb300 import _lib
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def fiducial(lmax=1000, lensing=False, **over):
+    """Plain flat LCDM of the scalar-path benchmark: H0=67.5, ombh2=0.022, omch2=0.122,
+    massless N_eff, tau=0.06, As=2.1e-9, ns=0.965."""
+    p = _lib.default_params()
+    p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
+    p.num_nu_massless = 3.046
+    p.max_l = lmax
+    p.do_lensing = 1 if lensing else 0
+    p.max_eta_k = (lmax + (200 if lensing else 0)) * 2.5
+    if lensing:
+        p.max_l = lmax + 200
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p
+
+
+def planck2018(lmax=1000):
+    """inifiles/planck_2018.ini cosmology with its massive neutrino folded into
+    massless N_eff (radiation era) and CDM (late times)."""
+    g = json.load(open(os.path.join(HERE, "golden", "template_cls.json")))["cosmology"]
+    p = _lib.default_params()
+    p.ombh2 = g["ombh2"]
+    p.omch2 = g["omch2"] + g["omnuh2"]
+    p.H0 = g["hubble"]
+    p.YHe = g["helium_fraction"]
+    p.num_nu_massless = g["massless_neutrinos"] + g["massive_neutrinos"]
+    p.optical_depth = g["re_optical_depth"]
+    p.As = g["scalar_amp"]
+    p.ns = g["scalar_spectral_index"]
+    p.TCMB = g["temp_cmb"]
+    p.max_l = lmax
+    p.max_eta_k = lmax * 2.5
+    return p
+
+
+def draws(n, seed=1234, lmax=1000, frac=0.05):
+    """Seeded draws, each parameter uniform in fiducial +-5% (the batch configuration)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        p = fiducial(lmax)
+        for name in ["ombh2", "omch2", "H0", "optical_depth", "As", "ns"]:
+            setattr(p, name, getattr(p, name) * (1 + frac * (2 * rng.random() - 1)))
+        out.append(p)
+    return out
+
+
+def template():
+    g = json.load(open(os.path.join(HERE, "golden", "template_cls.json")))
+    return {int(k): np.array(v) for k, v in g["cls"].items()}
