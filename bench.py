@@ -1,0 +1,251 @@
+"""Benchmark: cosmologies/s of the GB300 scalar-perturbation path.
+
+One step = one batch of B seeded cosmology draws (each of ombh2, omch2, H0, tau,
+As, ns uniform in fiducial +-5%, massless neutrinos, unlensed scalar C_l to
+lmax=2500) through the hot path: per-k ODE sources, source k-spline + flat
+line-of-sight projection, C_l.  `value` times the device pipeline on tables already
+resident in HBM (CUDA events on the library's stream); `e2e` times the C ABI call a
+user makes (cambgpu_get_results_batch: host parameters in, host C_l out, host table
+build and host<->device copies inside the timed region).
+
+--impl reference times the reference's CPU path for the same workload on this
+machine's host cores: the C++ restatement of the reference (oracle/) with OpenMP
+over k-modes, as the reference parallelises it (cmbmain.f90:205-209, 287-291).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--lmax", type=int, default=2500)
+    ap.add_argument("--team", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=4)
+    return ap.parse_args()
+
+
+def workload(n, lmax, seed):
+    from camb_gb300 import _lib
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        p = _lib.default_params()
+        p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
+        p.num_nu_massless = 3.046
+        for name in ["ombh2", "omch2", "H0", "optical_depth", "As", "ns"]:
+            setattr(p, name, getattr(p, name) * (1 + 0.05 * (2 * rng.random() - 1)))
+        p.max_l = lmax
+        p.max_eta_k = 2.5 * lmax
+        out.append(p)
+    return out
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples, self.index, self.proc = [], index, None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(s[0]) for s in self.samples if len(s) >= 6 and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) >= 6 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) >= 6 for i in range(4)
+                          if s[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def cpu_reference(params, nthreads):
+    """Reference CPU path on the host cores: host tables + restated ODE/LOS/C_l."""
+    from camb_gb300 import _lib
+    from oracle import oracle as orc
+    t0 = time.perf_counter()
+    for p in params:
+        T = _lib.Tables(p)
+        src = orc.evolve_sources(T, nthreads)
+        d = orc.los(T, src, nthreads)
+        orc.cls(T, d)
+    return time.perf_counter() - t0
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def barrier_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    nth = os.cpu_count() or 1
+    ps = workload(args.cpu_sample, args.lmax, seed=2024)
+    for _ in range(max(1, min(args.warmup, 1))):
+        cpu_reference(ps[:1], nth)
+    times = [cpu_reference(ps, nth) for _ in range(args.steps)]
+    t = statistics.mean(times)
+    v = len(ps) / t
+    line = {"impl": "reference", "metric": "cosmologies/s (unlensed scalar C_l to l=2500, FP64)", "value": v,
+            "unit": "cosmologies/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic seeded draws",
+            "config": {"workload": f"{len(ps)} seeded draws (+-5% LCDM, massless nu) lmax={args.lmax}, CPU sample"},
+            "cpu_baseline": {"value": v, "unit": "cosmologies/s", "cores": nth, "kind": "port",
+                             "sample": f"{len(ps)} cosmologies per step, host tables + ODE + LOS + C_l"},
+            "e2e": {"value": v, "unit": "cosmologies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    from camb_gb300 import _lib
+    lib = _lib.load()
+    torch.cuda.init()
+    if args.team:
+        _lib.check(lib.cambgpu_set_ode_team(args.team))
+    B = args.batch
+    ps = workload(B, args.lmax, seed=1000 + rank)
+    arr = (_lib.CambGpuParams * B)(*ps)
+    # ---- device-resident pipeline ----
+    _lib.check(lib.cambgpu_batch_prepare(arr, B))
+    ms = np.zeros(3)
+    for _ in range(args.warmup):
+        _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
+    stage = np.zeros(3)
+    evals = 0
+    lib.cambgpu_kernel_launches(1)
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
+            stage += ms
+            evals += lib.cambgpu_last_ode_evals()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = lib.cambgpu_kernel_launches(1)
+    barrier(world)
+    dev_ms = stage.sum() / args.steps
+    step_ms = barrier_max(dev_ms, world)
+    value = world * B / (step_ms * 1e-3)
+    lib.cambgpu_batch_release()
+    # ---- end to end through the C ABI (host params -> host C_l) ----
+    cls = np.zeros((B, args.lmax + 1, 4))
+    st = np.zeros(B, dtype=np.int32)
+    _lib.check(lib.cambgpu_get_results_batch(arr, B, args.lmax, _lib.dptr(cls), _lib.iptr(st)))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _lib.check(lib.cambgpu_get_results_batch(arr, B, args.lmax, _lib.dptr(cls), _lib.iptr(st)))
+    e2e_s = barrier_max((time.perf_counter() - t0) / args.steps, world)
+    xfer = (C.c_longlong * 2)()
+    lib.cambgpu_last_transfer_bytes(xfer)
+    # ---- roofline of the dominant kernel (ODE, FP64 pipe) ----
+    tf = C.c_double()
+    _lib.check(lib.cambgpu_probe_fp64_tflops(C.byref(tf)))
+    ode_ms = stage[0] / args.steps
+    evals_step = evals / args.steps
+    flops_per_eval = float(os.environ.get("CAMBGPU_FLOPS_PER_EVAL", "640"))
+    achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
+    line = {"metric": "cosmologies/s (unlensed scalar C_l to l=2500, FP64)", "value": value,
+            "unit": "cosmologies/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic seeded draws",
+            "config": {"workload": f"batch of {B} seeded draws (fiducial LCDM +-5%, massless nu), "
+                                   f"unlensed TT/EE/TE to lmax={args.lmax}, max_eta_k={2.5 * args.lmax:g}",
+                       "global_batch": B * world, "per_gpu_batch": B, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (per-cosmology tables ~3 MB x batch)",
+                       "stage_ms": {"ode": stage[0] / args.steps, "spline_los": stage[1] / args.steps,
+                                    "cls": stage[2] / args.steps}},
+            "e2e": {"value": world * B / e2e_s, "unit": "cosmologies/s", "h2d_bytes_per_step": int(xfer[0]),
+                    "d2h_bytes_per_step": int(xfer[1])},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "fp64", "kernel": "ode_thread_kernel", "achieved": achieved, "peak": tf.value,
+                         "unit": "TFLOP/s", "frac": achieved / tf.value, "traffic": None,
+                         "peak_source": "DFMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64)",
+                         "flops_per_eval": flops_per_eval, "evals_per_step": evals_step},
+            "clocks": clk.summary(), "wall_s_timed": wall}
+    if rank == 0:
+        nth = os.cpu_count() or 1
+        cps = workload(args.cpu_sample, args.lmax, seed=2024)
+        cpu_reference(cps[:1], nth)
+        t = cpu_reference(cps, nth)
+        line["cpu_baseline"] = {"value": len(cps) / t, "unit": "cosmologies/s", "cores": nth, "kind": "port",
+                                "sample": f"{len(cps)} draws of the same workload, host tables + ODE + LOS + C_l"}
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -301,11 +301,12 @@ int stage_batch(Batch& B) {
   return 0;
 }
 
+// Lanes per k-mode for the ODE kernel.  The FP64 pipe binds: one thread per mode
+// does no redundant scalar work and wins once there are enough modes to fill the
+// GPU; a warp per mode has the shortest per-mode latency for small batches.
 int pick_team(const Batch& B) {
   if (g_team) return g_team;
-  // autotuned default: 32 lanes per mode unless a batch has many modes
-  (void)B;
-  return 32;
+  return B.nitems >= 24 * g_rt.nsm ? 1 : 32;
 }
 
 int run_ode(Batch& B) {
@@ -634,8 +635,8 @@ void cambgpu_batch_release(void) {
 }
 
 int cambgpu_set_ode_team(int lanes) {
-  if (lanes != 0 && lanes != 8 && lanes != 16 && lanes != 32)
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team size must be 0, 8, 16 or 32");
+  if (lanes != 0 && lanes != 1 && lanes != 8 && lanes != 16 && lanes != 32)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team size must be 0, 1, 8, 16 or 32");
   g_team = lanes;
   return 0;
 }

@@ -768,6 +768,544 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
   }
 }
 
+// ---------------------------------------------------------------------------
+// Thread-per-mode variant (team size 1).  On GB300 the FP64 pipe is the binding
+// resource; the warp-per-mode kernel above evaluates the scalar part of every
+// right-hand side on all 32 lanes.  Here one thread owns one k-mode: the state and
+// Dormand-Prince stage vectors live in the thread's local memory (interleaved per
+// warp, L1/L2 resident), and the per-thread loop is a flat state machine in which
+// every iteration performs exactly one trial step, so threads of a warp never wait
+// for one another's integration intervals.  Work items are handed out in order of
+// decreasing q, so a warp integrates neighbouring k-modes whose switch times and
+// step-size histories are close.
+// ---------------------------------------------------------------------------
+namespace tpm {
+
+constexpr int NV = 104;  // 4 + (64+1) + (16+1) + (14+1) at lAccuracyBoost = 1
+constexpr int NL = 66;
+
+struct St {
+  double k, ik, k2, ik2, q;
+  double pig, pigdot, tight_off, poltruncfac;
+  int lmaxg, lmaxgpol, lmaxnr, g_ix, pol_ix, r_ix, nvar;
+  bool tc, hk, nonu, nophot;
+};
+
+// active index ranges of the flat state vector (SetupScalarArrayIndices)
+struct Ranges4 {
+  int lo[4], hi[4];
+};
+
+__device__ __forceinline__ Ranges4 active_ranges(const St& M) {
+  Ranges4 r;
+  r.lo[0] = 0;
+  r.hi[0] = 4;
+  r.lo[1] = M.g_ix;
+  r.hi[1] = M.nophot ? M.g_ix : (M.tc ? M.g_ix + 2 : M.g_ix + M.lmaxg + 1);
+  r.lo[2] = M.pol_ix + 2;
+  r.hi[2] = (M.nophot || M.tc) ? M.pol_ix + 2 : M.pol_ix + M.lmaxgpol + 1;
+  r.lo[3] = M.r_ix;
+  r.hi[3] = M.nonu ? M.r_ix : (M.hk ? M.r_ix + 3 : M.r_ix + M.lmaxnr + 1);
+  return r;
+}
+
+#define TPM_FOR_ACTIVE(R, i, body)                                   \
+  _Pragma("unroll") for (int rr_ = 0; rr_ < 4; ++rr_) {              \
+    for (int i = (R).lo[rr_]; i < (R).hi[rr_]; ++i) { body }         \
+  }
+
+// derivs (equations.f90:2273-2773) + sources (2775-2912) for one thread's mode
+template <bool WITH_SRC>
+__device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* __restrict__ dl,
+                                        const double* __restrict__ dl2, const double* __restrict__ pf, double tau,
+                                        const double* __restrict__ y, double* __restrict__ dy, double* src) {
+  const double k = M.k, ik = M.ik;
+  const double itau = 1.0 / tau;
+  double a, cs2, opac, dopac;
+  thermo_values(C, tau, itau, a, cs2, opac, dopac);
+  const double a2 = a * a, ia = 1.0 / a, ia2 = ia * ia;
+  const double etak = y[0], clxc = y[1], clxb = y[2], vb = y[3];
+  const double grhob_t = C.grhob * ia, grhoc_t = C.grhoc * ia, grhor_t = C.grhornomass * ia2,
+               grhog_t = C.grhog * ia2, grhov_t = C.grhov * a2;
+  double dgrho = grhob_t * clxb + grhoc_t * clxc;
+  double dgq = grhob_t * vb;
+  const double grho = (grhob_t + grhoc_t) + grhor_t + grhog_t + grhov_t;
+  const double gpres_noDE = (grhor_t + grhog_t) / 3;
+  const double g3 = grho / 3;
+  const double iad = rsqrt(g3);
+  const double adotoa = g3 * iad;
+  double z = 0, dz = 0, clxr, qr, pir, clxg, qg, pig = 0;
+  const int g = M.g_ix, pol = M.pol_ix, r = M.r_ix;
+  if (M.nonu) {
+    z = (0.5 * dgrho * ik + etak) * iad;
+    dz = -adotoa * z - 0.5 * dgrho * ik;
+    clxr = -4 * dz * ik;
+    qr = -4.0 / 3 * z;
+    pir = 0;
+  } else {
+    clxr = y[r];
+    qr = y[r + 1];
+    pir = y[r + 2];
+  }
+  if (M.nophot) {
+    if (!M.nonu) {
+      z = (0.5 * dgrho * ik + etak) * iad;
+      dz = -adotoa * z - 0.5 * dgrho * ik;
+      clxg = -4 * dz * ik - 4 * ik * opac * (vb + z);
+      qg = -4.0 / 3 * z;
+    } else {
+      clxg = clxr - 4 * ik * opac * (vb + z);
+      qg = qr;
+    }
+  } else {
+    clxg = y[g];
+    qg = y[g + 1];
+    if (!M.tc) pig = y[g + 2];
+  }
+  dgrho = dgrho + grhog_t * clxg + grhor_t * clxr;
+  dgq = dgq + grhog_t * qg + grhor_t * qr;
+  const double photbar = C.photbar_a * ia;
+  const double pb43 = 4.0 / 3 * photbar;
+  z = (0.5 * dgrho * ik + etak) * iad;
+  const double sigma = z + 1.5 * dgq * M.ik2;
+  dy[0] = 0.5 * dgq;
+  dy[1] = -k * z;
+  const double clxbdot = -k * (z + vb);
+  dy[2] = clxbdot;
+  const double clxgdot = -k * (4.0 / 3.0 * z + qg);
+  const double delta_p_b = cs2 * clxb;
+  double vbdot, pigdot = 0;
+  if (M.tc) {
+    const double gpres = gpres_noDE - grhov_t;
+    const double adotdota = (adotoa * adotoa - gpres) / 2;
+    const double iop = 1.0 / opac, iop2 = iop * iop;
+    const double i1pb = 1.0 / (1 + pb43);
+    pig = 32.0 / 45 * iop * k * (sigma + vb);
+    const double slip = -(2 * adotoa * i1pb + dopac * iop) * (vb - 3.0 / 4 * qg) +
+                        (-adotdota * vb - k / 2 * adotoa * clxg + k * (cs2 * clxbdot - clxgdot / 4)) * iop * i1pb;
+    const double dgs = grhog_t * pig + grhor_t * pir;
+    const double sigmadot = -2 * adotoa * sigma - dgs * ik + etak;
+    const double qgdot_tc = k * (clxg / 4.0 - pig / 2.0) + opac * slip;
+    const double f11 = dopac * 11.0 / 6.0 * iop2;
+    pig = 32.0 / 45 * iop * k * (sigma + 3.0 * qg / 4.0) * (1 + f11) +
+          (32.0 / 45.0 * iop2) * k * (sigmadot + 3.0 * qgdot_tc / 4.0) * (-11.0 / 6.0);
+    pigdot = -(32.0 / 45.0) * (dopac * iop2) * k * (sigma + 3.0 * qg / 4.0) * (1 + f11) +
+             (32.0 / 45.0 * iop) * k * (sigmadot + 3.0 * qgdot_tc / 4.0) * (1 + (11.0 / 6.0) * (dopac * iop2));
+    M.pigdot = pigdot;
+    vbdot = (-adotoa * vb + cs2 * k * clxb + k / 4 * pb43 * (clxg - 2 * pig)) * i1pb;
+    vbdot = vbdot + pb43 * i1pb * slip;
+    M.pig = pig;
+  } else {
+    vbdot = -adotoa * vb + k * delta_p_b - photbar * opac * (4.0 / 3 * vb - qg);
+  }
+  dy[3] = vbdot;
+  double qgdot = 0, polter = 0, E2 = 0;
+  if (!M.nophot) {
+    dy[g] = clxgdot;
+    const double inv_pb43 = 0.75 * a / C.photbar_a;
+    qgdot = 4.0 / 3 * (-vbdot - adotoa * vb + delta_p_b * k) * inv_pb43 + dl[1] * clxg - dl2[1] * pig;
+    dy[g + 1] = qgdot;
+    if (!M.tc) {
+      E2 = y[pol + 2];
+      polter = pig / 10 + 9.0 / 15 * E2;
+      pigdot = dl[2] * qg - dl2[2] * y[g + 3] - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
+      dy[g + 2] = pigdot;
+      const int lg = M.lmaxg;
+      for (int l = 3; l < lg; ++l)
+        dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
+      dy[g + lg] = k * y[g + lg - 1] - (lg + 1) * itau * y[g + lg] - opac * y[g + lg];
+      dy[pol + 2] = -opac * (E2 - polter) - k / 3.0 * y[pol + 3];
+      const int lp = M.lmaxgpol;
+      for (int l = 3; l < lp; ++l)
+        dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
+      dy[pol + lp] = -opac * y[pol + lp] + k * M.poltruncfac * y[pol + lp - 1] - (lp + 3) * itau * y[pol + lp];
+    }
+  }
+  double clxrdot = 0, pirdot = 0;
+  if (!M.nonu) {
+    clxrdot = -k * (4.0 / 3.0 * z + qr);
+    dy[r] = clxrdot;
+    dy[r + 1] = dl[1] * clxr - dl2[1] * pir;
+    if (M.hk) {
+      pirdot = -3 * pir * itau - clxrdot;
+      dy[r + 2] = pirdot;
+    } else {
+      pirdot = dl[2] * qr - dl2[2] * y[r + 3] + 8.0 / 15.0 * k * sigma;
+      dy[r + 2] = pirdot;
+      const int ln = M.lmaxnr;
+      for (int l = 3; l < ln; ++l) dy[r + l] = dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1];
+      dy[r + ln] = k * y[r + ln - 1] - (ln + 1) * itau * y[r + ln];
+    }
+  }
+  if constexpr (WITH_SRC) {
+    double Ed2 = 0, Ed3 = 0, octgdot = 0, E2s = 0;
+    if (M.nophot) {
+      pigdot = 0;
+      qgdot = -4 * dz / 3;
+    } else if (M.tc) {
+      const double iop = 1.0 / opac;
+      E2s = pig / 4 + pigdot * iop * (-5.0 / 8.0);
+      Ed2 = (pigdot / 4.0) * (1 + (5.0 / 2.0) * (dopac * iop * iop));
+    } else {
+      E2s = E2;
+      Ed2 = dy[pol + 2];
+      Ed3 = dy[pol + 3];
+      octgdot = dy[g + 3];
+    }
+    if (M.nonu) pirdot = 0;
+    const double dgpi = grhor_t * pir + grhog_t * pig;
+    const double pidot_sum = grhog_t * pigdot + grhor_t * pirdot;
+    const double gpres = gpres_noDE - grhov_t;
+    const double diff_rhopi = pidot_sum - (4 * dgpi) * adotoa;
+    const double phi = -((dgrho + 3 * dgq * adotoa * ik) + dgpi) / (2 * M.k2);
+    double op2, dop2, vis, dvis, ddvis, exptau;
+    ionization(C, tau, itau, op2, dop2, vis, dvis, ddvis, exptau);
+    const double k2 = M.k2;
+    const double phidot =
+        0.5 * (adotoa * (-dgpi - 2 * k2 * phi) + dgq * k - diff_rhopi + k * sigma * (gpres + grho)) * M.ik2;
+    const double sigmadot = -adotoa * sigma - 0.5 * dgpi * ik + k * phi;
+    polter = pig / 10 + 9.0 / 15 * E2s;
+    const double polterdot = (1.0 / 10.0) * pigdot + (3.0 / 5.0) * Ed2;
+    const double polterddot = -2.0 / 25.0 * adotoa * dgq * ik - 4.0 / 75.0 * adotoa * k * sigma - 4.0 / 75.0 * dgpi -
+                              2.0 / 75.0 * dgrho - 3.0 / 50.0 * k * octgdot + (1.0 / 25.0) * k * qgdot -
+                              1.0 / 5.0 * k * Ed3 + (-1.0 / 10.0 * pig + (7.0 / 10.0) * polter - 3.0 / 5.0 * E2s) * dop2 +
+                              (-1.0 / 10.0 * pigdot + (7.0 / 10.0) * polterdot - 3.0 / 5.0 * Ed2) * op2;
+    const double ISW = 2 * phidot * exptau;
+    const double monopole_source = (-etak * ik + 2 * phi + clxg / 4) * vis;
+    const double doppler = ((sigma + vb) * dvis + (sigmadot + vbdot) * vis) * ik;
+    const double quadrupole_source =
+        (5.0 / 8.0) * (3 * polter * ddvis + 6 * polterdot * dvis + (k2 * polter + 3 * polterddot) * vis) * M.ik2;
+    src[0] = ISW + doppler + monopole_source + quadrupole_source;
+    const double ang = C.tau0 - tau;
+    src[1] = tau < C.tau0 ? vis * polter * (15.0 / 8.0) / (ang * ang * k2) : 0.0;
+    src[2] = 0;
+    if (C.nsrc > 2 && tau > C.tau_maxvis && ang > 0.1)
+      src[2] = -2 * phi * (tau - C.tau_maxvis) / ((C.tau0 - C.tau_maxvis) * ang);
+  }
+}
+
+struct Work {
+  double y[NV], k1[NV], k2[NV], k3[NV], k4[NV], k5[NV], k6[NV], yt[NV];
+  double dl[NL], dl2[NL], pf[20];
+};
+
+// state of one mode's integration, advanced one trial step per loop iteration
+struct Run {
+  double tau, target, sw_time, h, err, call_hmax;
+  long long evals;
+  int j, fails, status;
+  bool active, target_is_switch, need_f, first, fsal, reset;
+};
+
+__device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
+  const CambGpuModeSpec ms = C.modes[q_ix];
+  M.q = ms.q;
+  M.k = ms.q;
+  M.ik = 1.0 / M.k;
+  M.k2 = M.k * M.k;
+  M.ik2 = 1.0 / M.k2;
+  M.lmaxg = ms.lmaxg;
+  M.lmaxgpol = ms.lmaxgpol;
+  M.lmaxnr = ms.lmaxnr;
+  M.g_ix = 4;
+  M.pol_ix = M.g_ix + M.lmaxg + 1;
+  M.r_ix = M.pol_ix + M.lmaxgpol + 1;
+  M.nvar = M.r_ix + M.lmaxnr + 1;
+  M.poltruncfac = (double)M.lmaxgpol / max(1, M.lmaxgpol - 2);
+  M.pig = M.pigdot = 0;
+  M.tight_off = ms.tight_switch_tau;
+  M.tc = true;
+  M.hk = M.nonu = M.nophot = false;
+  R.active = true;
+  R.status = 0;
+  if (M.nvar > NV || M.lmaxg >= NL || M.lmaxgpol >= 20) {
+    R.active = false;
+    R.status = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+    return;
+  }
+  const int lm = max(M.lmaxg, max(M.lmaxgpol, M.lmaxnr));
+  for (int l = 1; l <= lm && l < NL; ++l) {
+    double dn = 1.0 / (2 * l + 1);
+    W.dl[l] = dn * M.k * l;
+    W.dl2[l] = dn * M.k * (l + 1);
+    if (l < 20) W.pf[l] = ((double)((l + 3) * (l - 1)) / (l + 1)) * M.k * dn;
+  }
+  for (int i = 0; i < M.nvar; ++i) W.y[i] = 0;
+  // initial (equations.f90:1891-2112), adiabatic
+  const double tau = ms.taustart, k = M.k;
+  const double x = k * tau, x2 = x * x, x3 = x2 * x;
+  const double grhonu = C.grhornomass;
+  const double om = (C.grhob + C.grhoc) / sqrt(3 * (C.grhog + grhonu));
+  const double omtau = om * tau;
+  const double Rv = grhonu / (grhonu + C.grhog);
+  const double Rp15 = 4 * Rv + 15;
+  const double iv_clxg = -1.0 / 3 * x2 * (1 - omtau / 5);
+  const double iv_clxb = 0.75 * iv_clxg;
+  const double iv_qg = iv_clxg * x / 9.0;
+  const double iv_qr = -(4 * Rv + 23) / Rp15 * x3 / 27;
+  const double iv_vb = 0.75 * iv_qg;
+  const double iv_pir = 4.0 / 3 * x2 / Rp15 * (1 + omtau / 4 * (4 * Rv - 5) / (2 * Rv + 15));
+  const double iv_aj3r = 4 / 21.0 / Rp15 * x3;
+  const double iv_eta = -2 * (1 - x2 / 12 * (-10.0 / Rp15 + 1));
+  W.y[0] = iv_eta * k / 2;
+  W.y[1] = -iv_clxb;
+  W.y[2] = -iv_clxb;
+  W.y[3] = -iv_vb;
+  W.y[M.g_ix] = -iv_clxg;
+  W.y[M.g_ix + 1] = -iv_qg;
+  W.y[M.r_ix] = -iv_clxg;
+  W.y[M.r_ix + 1] = -iv_qr;
+  W.y[M.r_ix + 2] = -iv_pir;
+  if (M.lmaxnr > 2) W.y[M.r_ix + 3] = -iv_aj3r;
+  R.tau = tau;
+  R.j = 1;
+  R.h = R.err = 0;
+  R.fails = 0;
+  R.fsal = false;
+  R.reset = true;
+  R.need_f = false;
+  R.first = false;
+  R.evals = 0;
+  R.target = tau;
+  R.target_is_switch = false;
+  R.call_hmax = 0;
+}
+
+// Picks the next integration target (EvolveScal switch logic) and performs
+// switches that fall within smallTime of the current time.  Returns false when
+// the mode is finished.
+__device__ bool next_target(const DevCosmo& C, St& M, Work& W, Run& R) {
+  for (int guard = 0; guard < 16; ++guard) {
+    if (R.j >= C.ntau) return false;
+    const double tauend = C.tau_points[R.j];
+    if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time) return false;
+    const double noSwitch = C.tau0 + 1;
+    const double smallTime = fmin(R.tau, M.ik) / 100;
+    const double switchBoost = C.AccuracyBoost * C.TimeSwitchBoost;
+    double t_ktau = noSwitch, t_nonu = noSwitch, t_nophot = noSwitch;
+    if (!M.hk && !M.nonu) t_ktau = (double)max(20, M.lmaxnr - 4) / M.k;
+    if (!M.nonu) t_nonu = fmax(15 / M.k * switchBoost, fmin(C.taurend, C.matter_verydom_tau));
+    if (!M.nophot && M.k > 0.03 * switchBoost) t_nophot = fmax(15 / M.k, C.taurend) * switchBoost;
+    const double next = fmin(fmin(t_ktau, M.tight_off), fmin(fmin(t_nonu, t_nophot), noSwitch));
+    double tgt;
+    bool is_switch;
+    if (next < tauend) {
+      if (!(next > R.tau + smallTime)) {
+        // switch at the current time without integrating
+        R.target = R.tau;
+        R.sw_time = next;
+        R.target_is_switch = true;
+        return true;
+      }
+      tgt = next;
+      is_switch = true;
+    } else {
+      tgt = tauend;
+      is_switch = false;
+    }
+    // start of a GaugeInterface_ScalEv / RungeKuttaDP45 call
+    const double ms_user = (M.q < 2e-3 && R.tau <= C.taurend) ? 2.0 : 20.0 / C.IntTolBoost;
+    R.call_hmax = R.reset ? 0.0 : ms_user;
+    R.first = R.reset;
+    if (R.reset) {
+      R.fsal = false;
+      R.fails = 0;
+      R.reset = false;
+    }
+    R.need_f = true;
+    R.target = tgt;
+    R.sw_time = tgt;
+    R.target_is_switch = is_switch;
+    return true;
+  }
+  R.status = CAMBGPU_ERROR_EVOLUTION;
+  return false;
+}
+
+__device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
+  const double noSwitch = C.tau0 + 1;
+  const double switchBoost = C.AccuracyBoost * C.TimeSwitchBoost;
+  double t_ktau = noSwitch, t_nonu = noSwitch, t_nophot = noSwitch;
+  if (!M.hk && !M.nonu) t_ktau = (double)max(20, M.lmaxnr - 4) / M.k;
+  if (!M.nonu) t_nonu = fmax(15 / M.k * switchBoost, fmin(C.taurend, C.matter_verydom_tau));
+  if (!M.nophot && M.k > 0.03 * switchBoost) t_nophot = fmax(15 / M.k, C.taurend) * switchBoost;
+  const double next = R.sw_time;
+  if (next == M.tight_off) {
+    M.tc = false;
+    M.tight_off = noSwitch;
+    R.reset = true;
+    const double tau = R.tau, itau = 1.0 / tau;
+    double a, cs2, opac, dopac;
+    thermo_values(C, tau, itau, a, cs2, opac, dopac);
+    const double kb = M.k, op2 = opac * opac;
+    const double g2 = M.pig;
+    W.y[M.g_ix + 2] = g2;
+    W.y[M.g_ix + 3] = (3.0 / 7.0) * g2 * (kb / opac) * (1.0 + dopac / op2) + (3.0 / 7.0) * M.pigdot * (kb / op2) * (-1.0);
+    const double p2 = M.pig / 4 + M.pigdot * (1.0 / opac) * (-5.0 / 8.0 - (25.0 / 16.0) * dopac / op2) +
+                      M.pig * (kb / opac) * (kb / opac) * (-5.0 / 56.0);
+    W.y[M.pol_ix + 2] = p2;
+    W.y[M.pol_ix + 3] = (3.0 / 7.0) * (kb / opac) * p2 * (1.0 + dopac / op2) +
+                        (3.0 / 7.0) * (kb / op2) * ((M.pigdot / 4.0) * (1.0 + (5.0 / 2.0) * dopac / op2)) * (-1.0);
+    for (int l = 4; l <= M.lmaxg; ++l) W.y[M.g_ix + l] = 0;
+    for (int l = 4; l <= M.lmaxgpol; ++l) W.y[M.pol_ix + l] = 0;
+  } else if (next == t_ktau) {
+    M.hk = true;
+    for (int l = 3; l <= M.lmaxnr; ++l) W.y[M.r_ix + l] = 0;
+  } else if (next == t_nonu) {
+    R.reset = true;
+    M.nonu = true;
+  } else if (next == t_nophot) {
+    R.reset = true;
+    M.nophot = true;
+  }
+  R.fsal = false;
+}
+
+// one trial step of RungeKuttaDP45 toward R.target; returns <0 on failure
+__device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
+  using namespace dp;
+  const Ranges4 A = active_ranges(M);
+  const double tol = C.tol1;
+  if (R.need_f) {
+    if (R.fsal) R.fsal = false;
+    else {
+      derivs1<false>(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, W.k1, nullptr);
+      R.evals++;
+    }
+    R.need_f = false;
+  }
+  if (R.evals > kMaxEvalsPerMode) return -1;
+  double ny = 0;
+  TPM_FOR_ACTIVE(A, i, ny = fmax(ny, fabs(W.y[i]));)
+  ny = fmin(ny, 1.0);
+  const double x = R.tau;
+  const double hmin = 10.0 * fmax(tiny, eps * fmax(ny / tol, fabs(x)));
+  const double hmax = R.call_hmax != 0.0 ? R.call_hmax : 20.0;
+  if (hmin > hmax) return -2;
+  if (R.first) {
+    R.h = hmax * pow(tol, 0.2);
+    R.first = false;
+  } else if (R.fails <= 1) {
+    const double g1 = 2.0 / 0.9, g2 = g1 * g1;
+    double t2 = 2.0 * R.h;
+    if (tol < g2 * g2 * g1 * R.err) t2 = 0.9 * pow(tol / R.err, 0.2) * R.h;
+    R.h = fmax(t2, 0.5 * R.h);
+  } else {
+    R.h = 0.5 * R.h;
+  }
+  R.h = fmin(R.h, hmax);
+  R.h = fmax(R.h, hmin);
+  const double xend = R.target;
+  const double rem = fabs(xend - x);
+  double xt;
+  if (R.h < rem && (rem > 1.2 * R.h || rem > hmax)) {
+    R.h = fmin(R.h, 0.5 * rem);
+    xt = x + copysign(R.h, xend - x);
+  } else {
+    R.h = rem;
+    xt = xend;
+  }
+  const double hs = xt - x;
+  TPM_FOR_ACTIVE(A, i, W.yt[i] = W.y[i] + hs * a21 * W.k1[i];)
+  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, W.yt, W.k2, nullptr);
+  TPM_FOR_ACTIVE(A, i, W.yt[i] = W.y[i] + hs * (a31 * W.k1[i] + a32 * W.k2[i]);)
+  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), W.yt, W.k3, nullptr);
+  TPM_FOR_ACTIVE(A, i, W.yt[i] = W.y[i] + hs * (a41 * W.k1[i] + a42 * W.k2[i] + a43 * W.k3[i]);)
+  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), W.yt, W.k4, nullptr);
+  TPM_FOR_ACTIVE(A, i,
+                 W.yt[i] = W.y[i] + hs * (a51 * W.k1[i] + a52 * W.k2[i] + a53 * W.k3[i] + a54 * W.k4[i]);)
+  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), W.yt, W.k5, nullptr);
+  TPM_FOR_ACTIVE(A, i,
+                 W.yt[i] = W.y[i] + hs * (a61 * W.k1[i] + a62 * W.k2[i] + a63 * W.k3[i] + a64 * W.k4[i] +
+                                          a65 * W.k5[i]);)
+  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k6, nullptr);
+  TPM_FOR_ACTIVE(A, i,
+                 W.yt[i] = W.y[i] + hs * (b1 * W.k1[i] + b3 * W.k3[i] + b4 * W.k4[i] + b5 * W.k5[i] +
+                                          b6 * W.k6[i]);)
+  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k2, nullptr);  // stage 7 (FSAL) into k2
+  R.evals += 6;
+  double m = 0;
+  TPM_FOR_ACTIVE(A, i, {
+    const double ee = e1 * W.k1[i] + e3 * W.k3[i] + e4 * W.k4[i] + e5 * W.k5[i] + e6 * W.k6[i] + e7 * W.k2[i];
+    m = fmax(m, fabs(ee) / fmax(1.0, fabs(W.y[i])));
+  })
+  R.err = m * R.h;
+  if (R.err <= tol) {
+    R.tau = xt;
+    TPM_FOR_ACTIVE(A, i, {
+      W.y[i] = W.yt[i];
+      W.k1[i] = W.k2[i];
+    })
+    R.fails = 0;
+    if (xt == xend) R.fsal = true;
+  } else {
+    R.fails++;
+    if (R.h <= hmin) return -3;
+  }
+  return 0;
+}
+
+__global__ void __launch_bounds__(128) ode_thread_kernel(const DevCosmo* __restrict__ cosmos,
+                                                         const WorkItem* __restrict__ items, int nitems,
+                                                         int* __restrict__ counter) {
+  St M;
+  Work W;
+  Run R;
+  int cosmo = -1, q_ix = 0;
+  R.active = false;
+  for (int iter = 0;; ++iter) {
+    if (!R.active) {
+      int w = atomicAdd(counter, 1);
+      if (w >= nitems) break;
+      WorkItem it = items[w];
+      cosmo = it.cosmo;
+      q_ix = it.mode;
+      mode_init(cosmos[cosmo], q_ix, M, W, R);
+      if (!R.active) {
+        atomicExch(cosmos[cosmo].status, R.status);
+        continue;
+      }
+      if (!next_target(cosmos[cosmo], M, W, R)) {
+        R.active = false;
+        atomicAdd(cosmos[cosmo].evals, (unsigned long long)R.evals);
+        continue;
+      }
+    }
+    const DevCosmo& C = cosmos[cosmo];
+    int rc = 0;
+    if (R.target != R.tau) rc = trial_step(C, M, W, R);
+    if (rc) {
+      atomicExch(C.status, (int)CAMBGPU_ERROR_EVOLUTION);
+      atomicAdd(C.evals, (unsigned long long)R.evals);
+      R.active = false;
+      continue;
+    }
+    if (R.tau == R.target) {
+      bool more;
+      if (R.target_is_switch) {
+        apply_switch(C, M, W, R);
+        more = next_target(C, M, W, R);
+      } else {
+        double dyv[NV];
+        double src[3];
+        derivs1<true>(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, dyv, src);
+        R.evals++;
+        const int nsrc = C.nsrc, nk = C.nk;
+        for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = src[s];
+        R.j++;
+        more = next_target(C, M, W, R);
+      }
+      if (!more) {
+        if (R.status) atomicExch(C.status, R.status);
+        atomicAdd(C.evals, (unsigned long long)R.evals);
+        R.active = false;
+      }
+    }
+  }
+}
+
+}  // namespace tpm
+
 // DFMA throughput probe: 8 independent FMA chains per thread
 __global__ void fp64_probe_kernel(double* out, int iters) {
   double a[8];
@@ -792,7 +1330,8 @@ cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, c
 // host-side launch helpers (template kernels stay in this translation unit)
 int ode_blocks_per_sm(int team, int threads) {
   int per_sm = 0;
-  if (team == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<32>, threads, 0);
+  if (team == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel, threads, 0);
+  else if (team == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<32>, threads, 0);
   else if (team == 16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<16>, threads, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<8>, threads, 0);
   return per_sm;
@@ -800,7 +1339,8 @@ int ode_blocks_per_sm(int team, int threads) {
 
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
                               const WorkItem* items, int nitems, int* counter) {
-  if (team == 32) ode_persistent_kernel<32><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  if (team == 1) tpm::ode_thread_kernel<<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 32) ode_persistent_kernel<32><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 16) ode_persistent_kernel<16><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else ode_persistent_kernel<8><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   return cudaGetLastError();
