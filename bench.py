@@ -37,6 +37,7 @@ def parse():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--lmax", type=int, default=2500)
     ap.add_argument("--team", type=int, default=0)
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=4)
     return ap.parse_args()
 
@@ -177,6 +178,12 @@ def main():
     B = args.batch
     ps = workload(B, args.lmax, seed=1000 + rank)
     arr = (_lib.CambGpuParams * B)(*ps)
+    tuned = None
+    if not args.team and not args.no_autotune:
+        best = (C.c_int * 3)()
+        times = np.zeros(8)
+        _lib.check(lib.cambgpu_autotune_ode(arr, B, best, _lib.dptr(times)))
+        tuned = {"team": best[0], "queue_order": best[1], "candidate_ode_ms": [round(x, 2) for x in times[:5]]}
     # ---- device-resident pipeline ----
     _lib.check(lib.cambgpu_batch_prepare(arr, B))
     ms = np.zeros(3)
@@ -227,6 +234,7 @@ def main():
                                    f"unlensed TT/EE/TE to lmax={args.lmax}, max_eta_k={2.5 * args.lmax:g}",
                        "global_batch": B * world, "per_gpu_batch": B, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (per-cosmology tables ~3 MB x batch)",
+                       "ode_autotune": tuned,
                        "stage_ms": {"ode": stage[0] / args.steps, "spline_los": stage[1] / args.steps,
                                     "cls": stage[2] / args.steps}},
             "e2e": {"value": world * B / e2e_s, "unit": "cosmologies/s", "h2d_bytes_per_step": int(xfer[0]),

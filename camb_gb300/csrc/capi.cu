@@ -36,6 +36,10 @@ std::string g_err;
 std::atomic<long long> g_launches{0};
 double g_timings[6] = {0, 0, 0, 0, 0, 0};
 int g_team = 0;
+// autotuned ODE configuration per batch-size class: [0] small (< 24 modes/SM), [1] large
+struct OdeCfg { int team; int order; };
+OdeCfg g_tuned[2] = {{32, 0}, {1, 0}};
+int g_order = -1;  // forced queue order (-1: use the tuned one)
 long long g_last_evals = 0;
 long long g_h2d = 0, g_d2h = 0;
 
@@ -216,6 +220,8 @@ struct Batch {
   DevCosmo* d_cosmos = nullptr;
   const double** d_spl = nullptr;
   WorkItem* d_items = nullptr;
+  WorkItem* d_items_rev = nullptr;
+  std::vector<WorkItem> h_items_rev;
   int nitems = 0;
   int* d_counter = nullptr;
   int* d_status = nullptr;
@@ -231,8 +237,8 @@ int stage_batch(Batch& B) {
   for (auto* v : B.views) total += bytes_for(*v);
   size_t nitems = 0;
   for (auto* v : B.views) nitems += v->nk;
-  total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + (nitems * sizeof(WorkItem) + 255) + 512 +
-           ((size_t)n * 4 + 255);
+  total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + 2 * (nitems * sizeof(WorkItem) + 255) +
+           1024 + ((size_t)n * 4 + 255);
   rc = g_rt.arena.reserve(total);
   if (rc) return set_err(rc, "device allocation failed");
   B.d_status = g_rt.arena.take<int>(n);
@@ -273,6 +279,10 @@ int stage_batch(Batch& B) {
   B.nitems = (int)items.size();
   B.d_items = g_rt.arena.take<WorkItem>(items.size());
   copies.push_back({B.d_items, {items.data(), items.size() * sizeof(WorkItem)}});
+  // the same items in increasing q (second queue order the autotuner tries)
+  B.h_items_rev.assign(items.rbegin(), items.rend());
+  B.d_items_rev = g_rt.arena.take<WorkItem>(items.size());
+  copies.push_back({B.d_items_rev, {B.h_items_rev.data(), items.size() * sizeof(WorkItem)}});
   // single pinned staging buffer for all uploads
   size_t stage = 0;
   for (auto& cp : copies) stage += (cp.second.second + 255) & ~size_t(255);
@@ -304,19 +314,24 @@ int stage_batch(Batch& B) {
 // Lanes per k-mode for the ODE kernel.  The FP64 pipe binds: one thread per mode
 // does no redundant scalar work and wins once there are enough modes to fill the
 // GPU; a warp per mode has the shortest per-mode latency for small batches.
+int size_class(const Batch& B) { return B.nitems >= 24 * g_rt.nsm ? 1 : 0; }
+
 int pick_team(const Batch& B) {
   if (g_team) return g_team;
-  return B.nitems >= 24 * g_rt.nsm ? 1 : 32;
+  return g_tuned[size_class(B)].team;
 }
 
 int run_ode(Batch& B) {
   CUDA_TRY(cudaMemsetAsync(B.d_counter, 0, sizeof(int), g_rt.stream));
   CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
   int team = pick_team(B);
+  int order = g_order >= 0 ? g_order : g_tuned[size_class(B)].order;
+  int lanes = team <= 3 ? 1 : team;
   int per_sm = std::max(1, ode_blocks_per_sm(team, 128));
-  int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * team + 127) / 128);
+  int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * lanes + 127) / 128);
   if (blocks < 1) blocks = 1;
-  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, B.d_items, B.nitems, B.d_counter));
+  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, order ? B.d_items_rev : B.d_items, B.nitems,
+                             B.d_counter));
   g_launches++;
   return 0;
 }
@@ -635,8 +650,8 @@ void cambgpu_batch_release(void) {
 }
 
 int cambgpu_set_ode_team(int lanes) {
-  if (lanes != 0 && lanes != 1 && lanes != 8 && lanes != 16 && lanes != 32)
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team size must be 0, 1, 8, 16 or 32");
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 3 && lanes != 8 && lanes != 16 && lanes != 32)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team code must be 0, 1, 2, 3, 8, 16 or 32");
   g_team = lanes;
   return 0;
 }
@@ -647,6 +662,36 @@ int cambgpu_last_timings(double* out6) {
 }
 
 long long cambgpu_last_ode_evals(void) { return g_last_evals; }
+
+int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times) {
+  // candidates: (team code, queue order); team 32 = warp per mode, 1/2/3 = thread per mode
+  // with 3/4/5 resident blocks per SM
+  static const int cand[][2] = {{32, 0}, {1, 0}, {2, 0}, {3, 0}, {2, 1}};
+  const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
+  int rc = cambgpu_batch_prepare(p, n);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Batch& B = g_res->B;
+  int saved_team = g_team, saved_order = g_order;
+  double best_ms = 1e30;
+  int bi = 0;
+  for (int c = 0; c < nc; ++c) {
+    g_team = cand[c][0];
+    g_order = cand[c][1];
+    rc = run_all(B, true, false, false);  // warm-up
+    if (rc) break;
+    rc = run_all(B, true, false, false);
+    if (rc) break;
+    if (times) times[c] = g_timings[0];
+    if (g_timings[0] < best_ms) { best_ms = g_timings[0]; bi = c; }
+  }
+  g_team = saved_team;
+  g_order = saved_order;
+  if (rc) return rc;
+  g_tuned[size_class(B)] = {cand[bi][0], cand[bi][1]};
+  if (best) { best[0] = cand[bi][0]; best[1] = cand[bi][1]; best[2] = size_class(B); }
+  return 0;
+}
 
 int cambgpu_last_transfer_bytes(long long* out2) {
   out2[0] = g_h2d;

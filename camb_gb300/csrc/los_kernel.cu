@@ -81,9 +81,9 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
   extern __shared__ double smem[];
   const int ntau = C.ntau, nsrc = C.nsrc, nk = C.nk;
   double* s_src = smem;                          // [ntau][3]
-  double* s_w = s_src + (size_t)ntau * 3;        // [ntau] left weight * 1 (Horner variable)
-  double* s_dt = s_w + ntau;                     // [ntau] dpoints
-  int* s_bix = (int*)(s_dt + ntau);              // [ntau] 0-based Bessel interval
+  double* s_w = s_src + (size_t)ntau * 3;        // [ntau] Horner variable (left weight)
+  double* s_raw3 = s_w + ntau;                   // [ntau] lensing source without dtau (Limber)
+  int* s_bix = (int*)(s_raw3 + ntau);            // [ntau] 0-based Bessel interval
   const double q = C.q_int[q_ix];
   const double tau0 = C.tau0;
   const double max_etak = C.want_late_time ? 0.0 : C.max_etak_scalar;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
     double x_hi = ldgd(C.bess_x + bi + 1), dx = x_hi - ldgd(C.bess_x + bi);
     s_bix[i] = bi;
     s_w[i] = (x_hi - xx) / dx;
-    s_dt[i] = C.tau_dpoints[i];
+    const double dt = C.tau_dpoints[i];
     for (int s = 0; s < 3; ++s) {
       double v = 0;
       if (s < nsrc && i >= 1 && i < 1 + s_cnt) {
@@ -127,7 +127,9 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
         v = a0 * C.linear_src[b + klo] + b0 * C.linear_src[b + khi] +
             (a03 * C.dd_src[b + klo] + b03 * C.dd_src[b + khi]) * ho2o6;
       }
-      s_src[i * 3 + s] = v;
+      // the time weight dtau_n is folded into the staged source
+      s_src[i * 3 + s] = v * dt;
+      if (s == 2) s_raw3[i] = v;
     }
   }
   __syncthreads();
@@ -159,8 +161,7 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
         const double a2 = s_w[i];
         const double2* hp = reinterpret_cast<const double2*>(H + (size_t)s_bix[i] * 4);
         const double2 c01 = __ldg(hp), c23 = __ldg(hp + 1);
-        double J = c01.x + a2 * (c01.y + a2 * (c23.x + a2 * c23.y));
-        J = J * s_dt[i];
+        const double J = c01.x + a2 * (c01.y + a2 * (c23.x + a2 * c23.y));
         acc0 += s_src[i * 3 + 0] * J;
         acc1 += s_src[i * 3 + 1] * J;
         acc2 += s_src[i * 3 + 2] * J;
@@ -178,8 +179,8 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
       if (xf < tp[ntau - 1] && xf > tp[0]) {
         int n = time_index_of(tp, ntau, xf);  // 1-based
         double f = (xf - tp[n - 1]) / (tp[n] - tp[n - 1]);
-        double s_lo = (n - 1 < source_steps) ? s_src[(n - 1) * 3 + 2] : 0.0;
-        double s_hi = (n < source_steps) ? s_src[n * 3 + 2] : 0.0;
+        double s_lo = (n - 1 < source_steps) ? s_raw3[n - 1] : 0.0;
+        double s_hi = (n < source_steps) ? s_raw3[n] : 0.0;
         acc2 = (s_lo * (1 - f) + f * s_hi) * sqrt(3.14159265358979323846 / 2 / (l + 0.5)) / q;
       } else acc2 = 0;
     }

@@ -86,7 +86,7 @@ __device__ __forceinline__ double ldg(const double* p) { return __ldg(p); }
 
 // Thermo_values (results.f90:1848-1880)
 __device__ __forceinline__ void thermo_values(const DevCosmo& C, double tau, double itau, double& a, double& cs2,
-                                              double& opac, double& dopac) {
+                                              double& opac, double& dopac, bool want_dop = true) {
   double d = log(tau * C.inv_tauminn) * C.dlntau_inv + 1.0;
   int i = (int)d;
   d = d - i;
@@ -104,7 +104,7 @@ __device__ __forceinline__ void thermo_values(const DevCosmo& C, double tau, dou
     cs2 = ldg(h + 0) + d * (ldg(h + 1) + d * (ldg(h + 2) + d * ldg(h + 3)));
     opac = ldg(h + 4) + d * (ldg(h + 5) + d * (ldg(h + 6) + d * ldg(h + 7)));
     a = (ldg(h + 8) + d * (ldg(h + 9) + d * (ldg(h + 10) + d * ldg(h + 11)))) * tau;
-    dopac = (ldg(h + 12) + d * (ldg(h + 13) + d * (ldg(h + 14) + d * ldg(h + 15)))) * itau * C.dlntau_inv;
+    if (want_dop) dopac = (ldg(h + 12) + d * (ldg(h + 13) + d * (ldg(h + 14) + d * ldg(h + 15)))) * itau * C.dlntau_inv;
   }
 }
 
@@ -782,11 +782,22 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
 namespace tpm {
 
 constexpr int NV = 104;  // 4 + (64+1) + (16+1) + (14+1) at lAccuracyBoost = 1
+
+// x**(1/5) for the step-size update: FP32 seed, two Newton steps on y^5 = x in FP64
+__device__ __forceinline__ double fifth_root(double x) {
+  if (!(x > 1e-300) || !(x < 1e300)) return pow(x, 0.2);
+  double y = (double)exp2f(0.2f * log2f((float)x));
+  double y4 = (y * y) * (y * y);
+  y = 0.8 * y + 0.2 * x / y4;
+  y4 = (y * y) * (y * y);
+  y = 0.8 * y + 0.2 * x / y4;
+  return y;
+}
 constexpr int NL = 66;
 
 struct St {
   double k, ik, k2, ik2, q;
-  double pig, pigdot, tight_off, poltruncfac;
+  double pig, pigdot, tight_off, poltruncfac, kptf, tr_g, tr_p, tr_n;
   int lmaxg, lmaxgpol, lmaxnr, g_ix, pol_ix, r_ix, nvar;
   bool tc, hk, nonu, nophot;
 };
@@ -815,14 +826,13 @@ __device__ __forceinline__ Ranges4 active_ranges(const St& M) {
   }
 
 // derivs (equations.f90:2273-2773) + sources (2775-2912) for one thread's mode
-template <bool WITH_SRC>
 __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* __restrict__ dl,
                                         const double* __restrict__ dl2, const double* __restrict__ pf, double tau,
                                         const double* __restrict__ y, double* __restrict__ dy, double* src) {
   const double k = M.k, ik = M.ik;
   const double itau = 1.0 / tau;
-  double a, cs2, opac, dopac;
-  thermo_values(C, tau, itau, a, cs2, opac, dopac);
+  double a, cs2, opac, dopac = 0;
+  thermo_values(C, tau, itau, a, cs2, opac, dopac, M.tc || src != nullptr);
   const double a2 = a * a, ia = 1.0 / a, ia2 = ia * ia;
   const double etak = y[0], clxc = y[1], clxb = y[2], vb = y[3];
   const double grhob_t = C.grhob * ia, grhoc_t = C.grhoc * ia, grhor_t = C.grhornomass * ia2,
@@ -830,8 +840,8 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   double dgrho = grhob_t * clxb + grhoc_t * clxc;
   double dgq = grhob_t * vb;
   const double grho = (grhob_t + grhoc_t) + grhor_t + grhog_t + grhov_t;
-  const double gpres_noDE = (grhor_t + grhog_t) / 3;
-  const double g3 = grho / 3;
+  const double gpres_noDE = (grhor_t + grhog_t) * (1.0 / 3);
+  const double g3 = grho * (1.0 / 3);
   const double iad = rsqrt(g3);
   const double adotoa = g3 * iad;
   double z = 0, dz = 0, clxr, qr, pir, clxg, qg, pig = 0;
@@ -907,18 +917,18 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
     dy[g + 1] = qgdot;
     if (!M.tc) {
       E2 = y[pol + 2];
-      polter = pig / 10 + 9.0 / 15 * E2;
+      polter = pig * 0.1 + 9.0 / 15 * E2;
       pigdot = dl[2] * qg - dl2[2] * y[g + 3] - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
       dy[g + 2] = pigdot;
       const int lg = M.lmaxg;
       for (int l = 3; l < lg; ++l)
         dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
-      dy[g + lg] = k * y[g + lg - 1] - (lg + 1) * itau * y[g + lg] - opac * y[g + lg];
-      dy[pol + 2] = -opac * (E2 - polter) - k / 3.0 * y[pol + 3];
+      dy[g + lg] = k * y[g + lg - 1] - M.tr_g * itau * y[g + lg] - opac * y[g + lg];
+      dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * y[pol + 3];
       const int lp = M.lmaxgpol;
       for (int l = 3; l < lp; ++l)
         dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
-      dy[pol + lp] = -opac * y[pol + lp] + k * M.poltruncfac * y[pol + lp - 1] - (lp + 3) * itau * y[pol + lp];
+      dy[pol + lp] = -opac * y[pol + lp] + M.kptf * y[pol + lp - 1] - M.tr_p * itau * y[pol + lp];
     }
   }
   double clxrdot = 0, pirdot = 0;
@@ -934,10 +944,10 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       dy[r + 2] = pirdot;
       const int ln = M.lmaxnr;
       for (int l = 3; l < ln; ++l) dy[r + l] = dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1];
-      dy[r + ln] = k * y[r + ln - 1] - (ln + 1) * itau * y[r + ln];
+      dy[r + ln] = k * y[r + ln - 1] - M.tr_n * itau * y[r + ln];
     }
   }
-  if constexpr (WITH_SRC) {
+  if (src) {
     double Ed2 = 0, Ed3 = 0, octgdot = 0, E2s = 0;
     if (M.nophot) {
       pigdot = 0;
@@ -991,7 +1001,9 @@ struct Work {
 
 // state of one mode's integration, advanced one trial step per loop iteration
 struct Run {
+  double src[3];
   double tau, target, sw_time, h, err, call_hmax;
+  bool src_valid;
   long long evals;
   int j, fails, status;
   bool active, target_is_switch, need_f, first, fsal, reset;
@@ -1012,6 +1024,10 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   M.r_ix = M.pol_ix + M.lmaxgpol + 1;
   M.nvar = M.r_ix + M.lmaxnr + 1;
   M.poltruncfac = (double)M.lmaxgpol / max(1, M.lmaxgpol - 2);
+  M.kptf = M.k * M.poltruncfac;
+  M.tr_g = M.lmaxg + 1;
+  M.tr_p = M.lmaxgpol + 3;
+  M.tr_n = M.lmaxnr + 1;
   M.pig = M.pigdot = 0;
   M.tight_off = ms.tight_switch_tau;
   M.tc = true;
@@ -1068,6 +1084,7 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   R.evals = 0;
   R.target = tau;
   R.target_is_switch = false;
+  R.src_valid = false;
   R.call_hmax = 0;
 }
 
@@ -1169,15 +1186,16 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
-      derivs1<false>(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, W.k1, nullptr);
+      derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, W.k1, nullptr);
       R.evals++;
     }
     R.need_f = false;
   }
   if (R.evals > kMaxEvalsPerMode) return -1;
-  double ny = 0;
-  TPM_FOR_ACTIVE(A, i, ny = fmax(ny, fabs(W.y[i]));)
-  ny = fmin(ny, 1.0);
+  unsigned long long nb = 0;
+  TPM_FOR_ACTIVE(A, i, nb = max(nb, (unsigned long long)__double_as_longlong(W.y[i]) & 0x7fffffffffffffffULL);)
+  double ny = __longlong_as_double((long long)nb);
+  ny = ny < 1.0 ? ny : 1.0;
   const double x = R.tau;
   const double hmin = 10.0 * fmax(tiny, eps * fmax(ny / tol, fabs(x)));
   const double hmax = R.call_hmax != 0.0 ? R.call_hmax : 20.0;
@@ -1188,7 +1206,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   } else if (R.fails <= 1) {
     const double g1 = 2.0 / 0.9, g2 = g1 * g1;
     double t2 = 2.0 * R.h;
-    if (tol < g2 * g2 * g1 * R.err) t2 = 0.9 * pow(tol / R.err, 0.2) * R.h;
+    if (tol < g2 * g2 * g1 * R.err) t2 = 0.9 * fifth_root(tol / R.err) * R.h;
     R.h = fmax(t2, 0.5 * R.h);
   } else {
     R.h = 0.5 * R.h;
@@ -1206,29 +1224,44 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
     xt = xend;
   }
   const double hs = xt - x;
-  TPM_FOR_ACTIVE(A, i, W.yt[i] = W.y[i] + hs * a21 * W.k1[i];)
-  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, W.yt, W.k2, nullptr);
-  TPM_FOR_ACTIVE(A, i, W.yt[i] = W.y[i] + hs * (a31 * W.k1[i] + a32 * W.k2[i]);)
-  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), W.yt, W.k3, nullptr);
-  TPM_FOR_ACTIVE(A, i, W.yt[i] = W.y[i] + hs * (a41 * W.k1[i] + a42 * W.k2[i] + a43 * W.k3[i]);)
-  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), W.yt, W.k4, nullptr);
+  const double c21 = hs * a21, c31 = hs * a31, c32 = hs * a32, c41 = hs * a41, c42 = hs * a42, c43 = hs * a43;
+  const double c51 = hs * a51, c52 = hs * a52, c53 = hs * a53, c54 = hs * a54;
+  const double c61 = hs * a61, c62 = hs * a62, c63 = hs * a63, c64 = hs * a64, c65 = hs * a65;
+  const double cb1 = hs * b1, cb3 = hs * b3, cb4 = hs * b4, cb5 = hs * b5, cb6 = hs * b6;
+  TPM_FOR_ACTIVE(A, i, W.yt[i] = fma(c21, W.k1[i], W.y[i]);)
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, W.yt, W.k2, nullptr);
+  TPM_FOR_ACTIVE(A, i, W.yt[i] = fma(c32, W.k2[i], fma(c31, W.k1[i], W.y[i]));)
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), W.yt, W.k3, nullptr);
+  TPM_FOR_ACTIVE(A, i, W.yt[i] = fma(c43, W.k3[i], fma(c42, W.k2[i], fma(c41, W.k1[i], W.y[i])));)
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), W.yt, W.k4, nullptr);
   TPM_FOR_ACTIVE(A, i,
-                 W.yt[i] = W.y[i] + hs * (a51 * W.k1[i] + a52 * W.k2[i] + a53 * W.k3[i] + a54 * W.k4[i]);)
-  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), W.yt, W.k5, nullptr);
+                 W.yt[i] = fma(c54, W.k4[i], fma(c53, W.k3[i], fma(c52, W.k2[i], fma(c51, W.k1[i], W.y[i]))));)
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), W.yt, W.k5, nullptr);
   TPM_FOR_ACTIVE(A, i,
-                 W.yt[i] = W.y[i] + hs * (a61 * W.k1[i] + a62 * W.k2[i] + a63 * W.k3[i] + a64 * W.k4[i] +
-                                          a65 * W.k5[i]);)
-  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k6, nullptr);
+                 W.yt[i] = fma(c65, W.k5[i],
+                               fma(c64, W.k4[i], fma(c63, W.k3[i], fma(c62, W.k2[i], fma(c61, W.k1[i], W.y[i])))));)
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k6, nullptr);
   TPM_FOR_ACTIVE(A, i,
-                 W.yt[i] = W.y[i] + hs * (b1 * W.k1[i] + b3 * W.k3[i] + b4 * W.k4[i] + b5 * W.k5[i] +
-                                          b6 * W.k6[i]);)
-  derivs1<false>(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k2, nullptr);  // stage 7 (FSAL) into k2
+                 W.yt[i] = fma(cb6, W.k6[i],
+                               fma(cb5, W.k5[i], fma(cb4, W.k4[i], fma(cb3, W.k3[i], fma(cb1, W.k1[i], W.y[i])))));)
+  // stage 7 (FSAL) into k2; at an output time it is the output() evaluation too
+  const bool want_src = (xt == xend) && !R.target_is_switch;
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k2, want_src ? R.src : nullptr);
+  R.src_valid = want_src;
   R.evals += 6;
-  double m = 0;
+  // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry
+  double num = 0, den = 1;
   TPM_FOR_ACTIVE(A, i, {
-    const double ee = e1 * W.k1[i] + e3 * W.k3[i] + e4 * W.k4[i] + e5 * W.k5[i] + e6 * W.k6[i] + e7 * W.k2[i];
-    m = fmax(m, fabs(ee) / fmax(1.0, fabs(W.y[i])));
+    const double ee = fma(e7, W.k2[i], fma(e6, W.k6[i], fma(e5, W.k5[i], fma(e4, W.k4[i], fma(e3, W.k3[i], e1 * W.k1[i])))));
+    const double ae = fabs(ee);
+    const double ay = fabs(W.y[i]);
+    const double sc = ay > 1.0 ? ay : 1.0;
+    if (ae * den > num * sc) {
+      num = ae;
+      den = sc;
+    }
   })
+  const double m = num / den;
   R.err = m * R.h;
   if (R.err <= tol) {
     R.tau = xt;
@@ -1245,9 +1278,10 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   return 0;
 }
 
-__global__ void __launch_bounds__(128) ode_thread_kernel(const DevCosmo* __restrict__ cosmos,
-                                                         const WorkItem* __restrict__ items, int nitems,
-                                                         int* __restrict__ counter) {
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* __restrict__ cosmos,
+                                                               const WorkItem* __restrict__ items, int nitems,
+                                                               int* __restrict__ counter) {
   St M;
   Work W;
   Run R;
@@ -1286,12 +1320,13 @@ __global__ void __launch_bounds__(128) ode_thread_kernel(const DevCosmo* __restr
         apply_switch(C, M, W, R);
         more = next_target(C, M, W, R);
       } else {
-        double dyv[NV];
-        double src[3];
-        derivs1<true>(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, dyv, src);
-        R.evals++;
+        if (!R.src_valid) {
+          double dyv[NV];
+          derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, dyv, R.src);
+        }
+        R.evals++;  // the output() evaluation of the reference
         const int nsrc = C.nsrc, nk = C.nk;
-        for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = src[s];
+        for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = R.src[s];
         R.j++;
         more = next_target(C, M, W, R);
       }
@@ -1328,9 +1363,12 @@ cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, c
 }
 
 // host-side launch helpers (template kernels stay in this translation unit)
+// team 1 = thread per mode with 3 resident blocks per SM, 2 = 4 blocks, 3 = 5 blocks
 int ode_blocks_per_sm(int team, int threads) {
   int per_sm = 0;
-  if (team == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel, threads, 0);
+  if (team == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<3>, threads, 0);
+  else if (team == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<4>, threads, 0);
+  else if (team == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<5>, threads, 0);
   else if (team == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<32>, threads, 0);
   else if (team == 16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<16>, threads, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<8>, threads, 0);
@@ -1339,7 +1377,9 @@ int ode_blocks_per_sm(int team, int threads) {
 
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
                               const WorkItem* items, int nitems, int* counter) {
-  if (team == 1) tpm::ode_thread_kernel<<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  if (team == 1) tpm::ode_thread_kernel<3><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 2) tpm::ode_thread_kernel<4><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 3) tpm::ode_thread_kernel<5><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 32) ode_persistent_kernel<32><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 16) ode_persistent_kernel<16><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else ode_persistent_kernel<8><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);

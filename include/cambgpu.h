@@ -164,8 +164,13 @@ int cambgpu_batch_fetch(int lmax_out, double* cl_out);
 void cambgpu_batch_release(void);
 
 /* ---- runtime ---- */
-/* Team size for the ODE kernel (lanes per k-mode: 1,2,4,8,16,32); 0 = autotuned. */
+/* ODE kernel variant: 32/16/8 = lanes per k-mode (warp teams); 1/2/3 = one thread per
+ * k-mode with 3/4/5 resident blocks per SM; 0 = the autotuned choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
+/* In-library autotuner: times every ODE variant and work-queue order on n cosmologies
+ * and keeps the fastest for that batch-size class.  best = [team, order, class];
+ * times (optional, >= 5 entries) receives ms per candidate. */
+int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Kernel timing of the last GPU call, in ms: [ode, spline, los, cls, h2d, d2h]. */
 int cambgpu_last_timings(double* out6);
 /* Derivative evaluations of the last ODE launch (all modes of all cosmologies). */
