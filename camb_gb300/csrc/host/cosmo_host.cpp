@@ -1032,6 +1032,23 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
   if (rc) return rc;
   rc = thermo_init(c, taumin, err);
   if (rc) return rc;
+  // The logarithmic part of the source k grid ends at min(dkn1/dlnk0, q_switch),
+  // which exceeds qmax when max_eta_k is small (lmax below ~220): its modes would start
+  // before the thermal tables (the reference stops with 'thermo out of bounds' there).
+  // Extend the tables back to the start time of the largest grid wavenumber.
+  {
+    double SAB = P.AccuracyBoost * P.SourcekAccuracyBoost;
+    double dlnk0 = (c.reion.on && P.accurate_polarization) ? 2.0 / 10 / SAB : 5.0 / 10 / SAB;
+    if (P.accurate_reionization) dlnk0 /= 2;
+    if (c.reion.on && P.accurate_polarization && P.accurate_reionization) dlnk0 = std::min(dlnk0, 0.075);
+    double qlog_end = std::min(0.6 / c.taurst / SAB / dlnk0, 2 * 6.3 / c.taurst);
+    if (qlog_end > c.qmax * 1.0001) {
+      double dtaurec0 = 4 / c.qmax / initAccuracyBoost;
+      c.dtaurec = dtaurec0;
+      rc = thermo_init(c, get_tau_start(c, 1.2 * qlog_end), err);
+      if (rc) return rc;
+    }
+  }
   // SetTimeSteps (results.f90:2658-2779)
   {
     double TimeSampleBoost = P.AccuracyBoost * P.TimeStepBoost;

@@ -127,3 +127,16 @@ def test_invalid_parameters_raise():
     p.H0 = -1
     with pytest.raises(_lib.CAMBError):
         _lib.Tables(p)
+
+
+def test_small_lmax_modes_start_inside_thermal_tables():
+    """For lmax below ~220 the log part of the source k grid reaches past qmax; every
+    mode must still start after the first thermal-table time."""
+    from tests.cosmologies import draws
+    for lmax in (30, 100, 200):
+        for p in draws(2, seed=11, lmax=lmax):
+            T = _lib.Tables(p)
+            starts = [m[1] for m in T.modes()]
+            assert min(starts) >= T.view.tauminn
+            src = orc.evolve_sources(T, 2)
+            assert np.all(np.isfinite(src))
