@@ -424,7 +424,13 @@ int make_handle(const CambGpuParams* p, Handle*& h) {
     h = nullptr;
     return set_err(rc, err);
   }
-  h->bt = cg::get_bessel_table(h->c.ls, h->c.maximum_qeta, p->BesselBoost, p->AccuracyBoost);
+  try {
+    h->bt = cg::get_bessel_table(h->c.ls, h->c.maximum_qeta, p->BesselBoost, p->AccuracyBoost);
+  } catch (const std::exception& e) {
+    delete h;
+    h = nullptr;
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, e.what());
+  }
   cg::fill_view(h->c, *h->bt, h->view);
   return 0;
 }
@@ -474,7 +480,16 @@ int build_handles(const CambGpuParams* p, int n, std::vector<Handle*>& hs, int* 
   }
   for (int i = 0; i < n; ++i) {
     if (!hs[i]) continue;
-    hs[i]->bt = cg::get_bessel_table(hs[i]->c.ls, hs[i]->c.maximum_qeta, p[i].BesselBoost, p[i].AccuracyBoost);
+    try {
+      hs[i]->bt = cg::get_bessel_table(hs[i]->c.ls, hs[i]->c.maximum_qeta, p[i].BesselBoost, p[i].AccuracyBoost);
+    } catch (const std::exception& e) {
+      g_err = e.what();
+      if (status) status[i] = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+      worst = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+      delete hs[i];
+      hs[i] = nullptr;
+      continue;
+    }
     cg::fill_view(hs[i]->c, *hs[i]->bt, hs[i]->view);
   }
   return worst;

@@ -1188,11 +1188,11 @@ std::shared_ptr<const BesselTable> get_bessel_table(const std::vector<int>& ls, 
   tab->acc = acc;
   tab->boost = bessel_boost;
   Ranges br;
-  br.add_delta(0.0, 1.0, 0.01 / bessel_boost);
-  br.add_delta(1.0, 5.0, 0.1 / bessel_boost);
-  br.add_delta(5.0, 25.0, 0.2 / bessel_boost);
-  br.add_delta(25.0, 150.0, 0.5 / acc);
-  br.add_delta(150.0, requested_xmax, 0.7 / acc);
+  // bessels.f90:170-178; ranges are clipped at x_max for small max_eta_k
+  const double edges[6] = {0.0, 1.0, 5.0, 25.0, 150.0, 1e300};
+  const double steps[5] = {0.01 / bessel_boost, 0.1 / bessel_boost, 0.2 / bessel_boost, 0.5 / acc, 0.7 / acc};
+  for (int r = 0; r < 5 && edges[r] < requested_xmax; ++r)
+    br.add_delta(edges[r], std::min(edges[r + 1], requested_xmax), steps[r]);
   br.get_array(false);
   tab->x = br.points;
   int num_xx = (int)tab->x.size(), nl = (int)ls.size();
