@@ -78,6 +78,7 @@ SIGNATURES = {
     "cambgpu_evolve_scalar_sources": (C.c_int, [C.POINTER(CambGpuTables), _c_double_p]),
     "cambgpu_los_flat": (C.c_int, [C.POINTER(CambGpuTables), _c_double_p, _c_double_p]),
     "cambgpu_calc_scal_cls": (C.c_int, [C.POINTER(CambGpuTables), _c_double_p, _c_double_p]),
+    "cambgpu_los_flat_noalloc": (C.c_int, [C.POINTER(CambGpuTables), C.c_void_p, C.c_void_p, C.c_void_p]),
     "cambgpu_get_results": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, _c_double_p]),
     "cambgpu_get_results_batch": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, _c_double_p, _c_int_p]),
     "cambgpu_batch_prepare": (C.c_int, [C.POINTER(CambGpuParams), C.c_int]),

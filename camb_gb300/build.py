@@ -15,7 +15,7 @@ LIB = os.path.join(BUILD, "libcambgpu.so")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["ode_kernel.cu", "los_kernel.cu", "capi.cu"]
+CU_SOURCES = ["ode_kernel.cu", "los_kernel.cu", "capi.cu", "noalloc.cu"]
 CXX_SOURCES = ["host/cosmo_host.cpp"]
 
 

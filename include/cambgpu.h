@@ -146,6 +146,18 @@ int cambgpu_los_flat(const CambGpuTables* t, const double* linear_src, double* d
  *     (C_Temp..C_PhiE), l(l+1)C_l/2pi at the sampled l. */
 int cambgpu_calc_scal_cls(const CambGpuTables* t, const double* delta_p_l_k, double* icl);
 
+/* Allocation-free variant of cambgpu_los_flat (no counterpart in the reference): for
+ * callers that cannot call cudaMalloc -- code inside a framework that owns all device
+ * memory, or a service that must not allocate after start-up.  Every array pointer in
+ * `t` (q_evolve, tau_points, tau_dpoints, q_int, ls, bess_x, bessel_horner) and both
+ * buffers are DEVICE pointers owned by the caller; the spline scratch lives in a 16 MiB
+ * static device array inside the library (problems with 5*nk + ntau*nsrc*nk beyond it
+ * are rejected with code 2).  Work is enqueued on `stream` (a cudaStream_t, NULL = the
+ * default stream) and the stream is synchronised before returning.  All calls share the
+ * scratch: calls that overlap on the GPU race.  The first call on a device sets up the
+ * scratch address; make it before any stream capture. */
+int cambgpu_los_flat_noalloc(const CambGpuTables* t, const double* linear_src_dev, double* delta_dev, void* stream);
+
 /* ---- whole pipeline (CAMB_GetResults for the scalar flat path) ---- */
 /* cl_out: [lmax_out+1][4] TT EE BB TE of l(l+1)C_l/2pi (dimensionless), BB = 0,
  * as results.py get_unlensed_scalar_cls. */
