@@ -49,7 +49,7 @@ def workload(n, lmax, seed):
     for _ in range(n):
         p = _lib.default_params()
         p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
-        p.num_nu_massless = 3.046
+        p.nnu = 3.046
         for name in ["ombh2", "omch2", "H0", "optical_depth", "As", "ns"]:
             setattr(p, name, getattr(p, name) * (1 + 0.05 * (2 * rng.random() - 1)))
         p.max_l = lmax

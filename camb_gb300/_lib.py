@@ -18,7 +18,9 @@ class CambGpuParams(C.Structure):
     _fields_ = [
         ("H0", C.c_double), ("ombh2", C.c_double), ("omch2", C.c_double), ("omk", C.c_double),
         ("TCMB", C.c_double), ("YHe", C.c_double),
-        ("num_nu_massless", C.c_double),
+        ("nnu", C.c_double),
+        ("mnu", C.c_double),
+        ("num_massive_neutrinos", C.c_int),
         ("optical_depth", C.c_double),
         ("reion_delta_redshift", C.c_double),
         ("As", C.c_double), ("ns", C.c_double), ("nrun", C.c_double), ("pivot_scalar", C.c_double),
@@ -37,7 +39,9 @@ class CambGpuParams(C.Structure):
 
 class CambGpuModeSpec(C.Structure):
     _fields_ = [("q", C.c_double), ("taustart", C.c_double), ("tight_switch_tau", C.c_double),
-                ("lmaxg", C.c_int), ("lmaxgpol", C.c_int), ("lmaxnr", C.c_int), ("pad", C.c_int)]
+                ("lmaxg", C.c_int), ("lmaxgpol", C.c_int), ("lmaxnr", C.c_int), ("lmaxnu", C.c_int),
+                ("nq0", C.c_int * 3), ("pad", C.c_int),
+                ("nu_l_boost", C.c_double * 3), ("nu_approx_time", C.c_double * 3)]
 
 
 class CambGpuTables(C.Structure):
@@ -47,6 +51,9 @@ class CambGpuTables(C.Structure):
         ("adotrad", C.c_double), ("tau0", C.c_double), ("DMt0", C.c_double), ("taurst", C.c_double),
         ("taurend", C.c_double), ("tau_maxvis", C.c_double), ("matter_verydom_tau", C.c_double),
         ("akthom", C.c_double), ("fHe", C.c_double),
+        ("nu_eig", C.c_int), ("nqmax", C.c_int),
+        ("nu_masses", C.c_double * 3), ("grhormass", C.c_double * 3), ("nu_tau_nonrel", C.c_double * 3),
+        ("nu_q", _c_double_p), ("nu_int_kernel", _c_double_p), ("nu_tau_notmassless", _c_double_p),
         ("nthermo", C.c_int),
         ("tauminn", C.c_double), ("dlntau", C.c_double), ("dlntau_inv", C.c_double), ("tight_tau", C.c_double),
         ("thermo_horner", _c_double_p), ("dotmu", _c_double_p), ("ddotmu", _c_double_p), ("cs2", _c_double_p),

@@ -514,7 +514,7 @@ extern "C" {
 void cambgpu_default_params(CambGpuParams* p) {
   std::memset(p, 0, sizeof(*p));
   p->H0 = 67.5; p->ombh2 = 0.022; p->omch2 = 0.122; p->omk = 0; p->TCMB = 2.7255; p->YHe = 0.2454;
-  p->num_nu_massless = 3.044; p->optical_depth = 0.06; p->reion_delta_redshift = 0.5;
+  p->nnu = 3.044; p->mnu = 0; p->num_massive_neutrinos = 1; p->optical_depth = 0.06; p->reion_delta_redshift = 0.5;
   p->As = 2.1e-9; p->ns = 0.965; p->nrun = 0; p->pivot_scalar = 0.05; p->Alens = 1;
   p->max_l = 2500; p->max_eta_k = 6250; p->do_lensing = 0;
   p->AccuracyBoost = p->lAccuracyBoost = p->lSampleBoost = p->IntTolBoost = p->TimeStepBoost = 1;

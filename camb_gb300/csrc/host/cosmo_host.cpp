@@ -148,12 +148,77 @@ static void spline_integral_array(const std::vector<double>& x, const std::vecto
   }
 }
 
+
+// ------------------------------------------------------------------------
+// thermal massive-neutrino background (massive_neutrinos.f90): density and
+// pressure in units of one massless eigenstate, as functions of a*m/(k_B T_nu)
+// ------------------------------------------------------------------------
+namespace nu {
+const double zeta3 = 1.2020569031595942853997, zeta5 = 1.0369277551433699263313, zeta7 = 1.0083492773819228268397;
+const double fermi_dirac_const = 7.0 / 120 * K::pi * K::pi * K::pi * K::pi;
+const double const2 = 5.0 / 7.0 / (K::pi * K::pi);
+const double rhop_am_min = 0.42, rhop_am_max = 70.0, am_min = 0.3, am_max = 70.0;
+const double rhop_fit_c = std::sqrt(rhop_am_min * rhop_am_max);
+const double rhop_fit_inv_zmax = (rhop_am_max + rhop_fit_c) / (rhop_am_max - rhop_fit_c);
+const double fit_c = std::sqrt(am_min * am_max);
+const double fit_inv_zmax = (am_max + fit_c) / (am_max - fit_c);
+const double fit_rho_scale = 3.0 * zeta3 / (2.0 * fermi_dirac_const);
+const double fit_p_denom_scale = fermi_dirac_const / ((900.0 / 120.0) * zeta5);
+const double rho_c[6] = {7.499710425926954249e-01, 1.188066888581748443e-01, 1.545077526625578401e-01,
+                         -8.378996019212282820e-02, 2.123075360029347963e-02, -2.544964203886362908e-03};
+const double p_c[7] = {9.283417043601330798e-01, 3.156134695375645838e-01, -2.435843189264263742e-01,
+                       -2.509793530357270000e-02, 4.067958090718486880e-02, 2.378742143669706002e-03,
+                       -1.965863329520473827e-03};
+const double low_rho_c[2] = {-1.872929199948838302e-02, 1.831728681837861694e-02};
+const double low_p_c[2] = {1.667044572156534468e-02, -2.277471498716537868e-02};
+const double D_c[6] = {5.800497880734221123e-01, 1.801974470841860576e-01, -1.602709049602861757e-01,
+                       3.167230341650149189e-02, 1.056591590995091534e-02, -3.877662402660121861e-03};
+
+void rho_P(double am, double& rhonu, double& pnu) {
+  if (am <= rhop_am_min) {
+    double am2 = am * am, am4 = am2 * am2;
+    rhonu = 1.0 + const2 * am2 + am4 * (low_rho_c[0] + am2 * low_rho_c[1]);
+    pnu = (1.0 - const2 * am2) / 3.0 + am4 * (low_p_c[0] + am2 * low_p_c[1]);
+    return;
+  } else if (am >= rhop_am_max) {
+    rhonu = 3 / (2 * fermi_dirac_const) * (zeta3 * am + ((15 * zeta5) / 2 - 945.0 / 16 * zeta7 / (am * am)) / am);
+    pnu = 900.0 / 120.0 / fermi_dirac_const * (zeta5 - 63.0 / 4 * zeta7 / (am * am)) / am;
+    return;
+  }
+  double z = ((am - rhop_fit_c) / (am + rhop_fit_c)) * rhop_fit_inv_zmax;
+  double rfit = (((((rho_c[5] * z + rho_c[4]) * z + rho_c[3]) * z + rho_c[2]) * z + rho_c[1]) * z + rho_c[0]);
+  double pfit = ((((((p_c[6] * z + p_c[5]) * z + p_c[4]) * z + p_c[3]) * z + p_c[2]) * z + p_c[1]) * z + p_c[0]);
+  rhonu = (1.0 + fit_rho_scale * am) * rfit;
+  pnu = pfit / (1.0 + fit_p_denom_scale * am);
+}
+
+double rho(double am) {
+  double r, p;
+  rho_P(am, r, p);
+  return r;
+}
+
+double drho(double am, double adotoa) {
+  if (am <= am_min) {
+    double am2 = am * am;
+    return am2 * (2 * const2 + am2 * (.4399706676e-1 * std::log(am) - .2970400378e-2 - .29331377855e-1 * am)) * adotoa;
+  } else if (am >= am_max) {
+    return 3 / (2 * fermi_dirac_const) * (zeta3 * am + (-(15 * zeta5) / 2 + 2835.0 / 16 * zeta7 / (am * am)) / am) *
+           adotoa;
+  }
+  double z = ((am - fit_c) / (am + fit_c)) * fit_inv_zmax;
+  double Dfit = (((((D_c[5] * z + D_c[4]) * z + D_c[3]) * z + D_c[2]) * z + D_c[1]) * z + D_c[0]);
+  return am * am / (1.0 + 2.0 * am) * Dfit * adotoa;
+}
+}  // namespace nu
+
 // ------------------------------------------------------------------------
 // background (results.f90:332-628, equations.f90:5-24)
 // ------------------------------------------------------------------------
 double Cosmology::dtauda(double a) const {
   // grho_no_de (results.f90:1393-1410) + cosmological-constant dark energy
   double grhoa2 = grhok * a * a + (grhoc + grhob) * a + grhog + grhornomass;
+  for (int i = 0; i < nu_eig; ++i) grhoa2 += nu::rho(a * nu_masses[i]) * grhormass[i];
   grhoa2 += grhov * a * a * a * a;
   if (grhoa2 <= 0) return 0;
   return std::sqrt(3.0 / grhoa2);
@@ -636,8 +701,24 @@ static void pade_derivative(const std::vector<double>& y, std::vector<double>& d
 }
 
 static double get_tau_start(const Cosmology& c, double q) {
-  // GetTauStart (cmbmain.f90:706-729), massless neutrinos
-  return std::min(0.001 / q, 0.1);
+  // GetTauStart (cmbmain.f90:706-729)
+  double t = std::min(0.001 / q, 0.1);
+  double mmax = 0;
+  for (int i = 0; i < c.nu_eig; ++i) mmax = std::max(mmax, c.nu_masses[i]);
+  if (c.nu_eig > 0 && mmax != 0) t = std::min(t, 1e-3 / mmax / c.adotrad);
+  return t;
+}
+
+// MassiveNuTransferSwitchBoost / MassiveNuTransferLAccuracyBoost (equations.f90:484-510)
+static double nu_switch_boost(const Cosmology& c, double nu_mass) {
+  double b = c.P.AccuracyBoost * c.P.TimeSwitchBoost;
+  if (nu_mass > 600) b *= 2;  // AccuracyTarget > 0 and WantCls
+  return b;
+}
+static double nu_l_boost(const Cosmology& c, double nu_mass, double q, double tau_nonrel_phys) {
+  double b = c.P.lAccuracyBoost;
+  if (nu_mass > 600 && q * tau_nonrel_phys < 500) b *= 2.0;
+  return b;
 }
 
 static int thermo_init(Cosmology& c, double taumin, std::string& err) {
@@ -652,7 +733,9 @@ static int thermo_init(Cosmology& c, double taumin, std::string& err) {
   g[0] = 0;
   for (int i = 1; i < nthermo; ++i) g[i] = 1 / (4.0 - g[i - 1]);
 
-  double om = (c.grhob + c.grhoc) / std::sqrt(3 * (c.grhog + c.grhornomass));
+  double grhomass = 0;
+  for (int i = 0; i < c.nu_eig; ++i) grhomass += c.grhormass[i];
+  double om = (c.grhob + c.grhoc) / std::sqrt(3 * (c.grhog + grhomass + c.grhornomass));
   double a0 = c.tauminn * c.adotrad * (1 + om * c.tauminn / 4);
   int ninverse = nint(background_boost * std::log(1 / a0) / std::log(1 / 2e-10) * 4000);
   int nlin = ninverse / 2;
@@ -935,8 +1018,30 @@ static CambGpuModeSpec mode_setup(const Cosmology& c, double q) {
   m.q = q;
   double lab = P.lAccuracyBoost;
   int min_lmaxnr = std::max(3, nint(3 * lab));
+  double max_nu_mass = 0;
+  int lmaxnu = 0;
+  if (c.nu_eig > 0) {
+    for (int i = 0; i < c.nu_eig; ++i) max_nu_mass = std::max(max_nu_mass, c.nu_masses[i]);
+    for (int i = 0; i < c.nu_eig; ++i) {
+      int q_rel = 0;
+      for (int j = 0; j < c.nqmax; ++j) {
+        if (c.nu_q[j] > c.nu_masses[i] * c.adotrad / q) break;
+        ++q_rel;
+      }
+      m.nq0[i] = (q_rel >= c.nqmax - 2) ? c.nqmax : q_rel;
+      m.nu_l_boost[i] = nu_l_boost(c, c.nu_masses[i], q, c.nu_tau_nonrel_phys[i]);
+    }
+    lmaxnu = std::max(3, nint(10 * lab));
+    if (max_nu_mass > 700) lmaxnu = std::max(3, nint(15 * lab));
+    for (int i = 0; i < c.nu_eig; ++i) {
+      lmaxnu = std::max(lmaxnu, nint(10 * m.nu_l_boost[i]));
+      if (c.nu_masses[i] > 700) lmaxnu = std::max(lmaxnu, nint(15 * m.nu_l_boost[i]));
+    }
+  }
+  m.lmaxnu = lmaxnu;
   int lmaxg = P.accurate_polarization ? std::max(nint(11 * lab), 3) : std::max(nint(8 * lab), 3);
   int lmaxnr = std::max(nint(14 * lab), min_lmaxnr);
+  if (max_nu_mass > 700) lmaxnr = std::max(nint(32 * lab), min_lmaxnr);
   int lmaxgpol = lmaxg;
   if (!P.accurate_polarization) lmaxgpol = std::max(nint(4 * lab), 3);
   else if (q > 0.15) {  // AccuracyTarget > 0 and Want_CMB
@@ -953,10 +1058,20 @@ static CambGpuModeSpec mode_setup(const Cosmology& c, double q) {
       lmaxgpol = lmaxgpol * 2;
     }
   }
+  if (lmaxnr < lmaxnu) lmaxnr = lmaxnu;
   m.lmaxg = lmaxg;
   m.lmaxgpol = lmaxgpol;
   m.lmaxnr = lmaxnr;
   m.taustart = get_tau_start(c, q);
+  // MassiveNuApproxTime (initial, equations.f90:2091-2102)
+  for (int i = 0; i < c.nu_eig; ++i) {
+    double sb = nu_switch_boost(c, c.nu_masses[i]);
+    m.nu_approx_time[i] = c.nu_tau_massive[i];
+    double a_massive = 20000 * q / c.nu_masses[i] * sb * m.nu_l_boost[i];
+    if (a_massive >= 0.99) m.nu_approx_time[i] = c.tau0 + 1;
+    else if (a_massive > 17.0 / c.nu_masses[i] * sb)
+      m.nu_approx_time[i] = std::max(m.nu_approx_time[i], c.delta_time(0, a_massive, 0.01));
+  }
   // tight-coupling switch time
   double epsw = 100 / c.tau0, ep0 = 1e-2, ep;
   if (q > epsw) ep = (q > epsw * 5) ? ep0 * 5 / P.AccuracyBoost * 0.65 : ep0;
@@ -986,20 +1101,135 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
   c.grhocrit = 3 * P.H0 * P.H0 / (c_si * c_si) * 1000 * 1000;
   c.grhog = K::kappa / (c_si * c_si) * 4 * K::sigma_boltz / (c_si * c_si * c_si) * std::pow(P.TCMB, 4) * K::Mpc * K::Mpc;
   c.grhor = 7.0 / 8 * std::pow(4.0 / 11, 4.0 / 3) * c.grhog;
-  c.grhornomass = c.grhor * P.num_nu_massless;
+  // neutrinos: CAMBparams_SetNeutrinoMasses, degenerate hierarchy (model.f90:260-405), then
+  // the massive-neutrino part of SetParams (results.f90:405-433, 497-525)
   double h2 = (P.H0 / 100) * (P.H0 / 100);
+  double nu_massless_degeneracy = P.nnu;
+  c.nu_eig = 0;
+  c.omnuh2 = 0;
+  if (P.mnu > 0) {
+    const double default_nnu = 3.044;
+    const double eV = 1.602176634e-19, hbar = K::h_P / K::twopi;
+    const double kB_T = K::k_B * K::COBE_CMBTemp / hbar / K::c;
+    const double inv_neutrino_mass_fac = nu::zeta3 * 3.0 / 2 / (K::pi * K::pi) * 4.0 / 11 *
+                                         (kB_T * kB_T * kB_T * K::kappa / 3 /
+                                          ((100 * 1000 / K::Mpc) * (100 * 1000 / K::Mpc)) / (K::c * K::c / eV));
+    const double neutrino_mass_fac = 1 / inv_neutrino_mass_fac;
+    int nmass = std::max(1, P.num_massive_neutrinos);
+    double neff_massive_standard = nmass * default_nnu / 3;
+    if (P.nnu > neff_massive_standard) nu_massless_degeneracy = P.nnu - neff_massive_standard;
+    else {
+      nu_massless_degeneracy = 0;
+      neff_massive_standard = P.nnu;
+    }
+    c.nu_eig = 1;
+    c.nu_degeneracy[0] = neff_massive_standard;
+    double mass = P.mnu / nmass;
+    double T_nu = K::k_B * P.TCMB / eV * std::pow(4.0 / 11, 1.0 / 3);
+    double rhonu = nu::rho(mass / (T_nu * std::pow(neff_massive_standard / nmass, 0.25)));
+    c.omnuh2 = neff_massive_standard * T_nu * std::pow(P.TCMB / K::COBE_CMBTemp, 3) * rhonu /
+               (neutrino_mass_fac * nu::fit_rho_scale);
+  }
+  c.grhornomass = c.grhor * nu_massless_degeneracy;
+  for (int i = 0; i < c.nu_eig; ++i) c.grhormass[i] = c.grhor * c.nu_degeneracy[i];
   c.grhoc = c.grhocrit * P.omch2 / h2;
   c.grhob = c.grhocrit * P.ombh2 / h2;
   c.grhok = 0;
-  c.Omega_de = 1 - (P.omch2 + P.ombh2) / h2 - P.omk - (c.grhornomass + c.grhog) / c.grhocrit;
+  c.Omega_de = 1 - (P.omch2 + P.ombh2 + c.omnuh2) / h2 - P.omk - (c.grhornomass + c.grhog) / c.grhocrit;
   c.grhov = c.grhocrit * c.Omega_de;
-  c.adotrad = std::sqrt((c.grhog + c.grhornomass) / 3);
+  double grhomass = 0;
+  for (int i = 0; i < c.nu_eig; ++i) grhomass += c.grhormass[i];
+  c.adotrad = std::sqrt((c.grhog + c.grhornomass + grhomass) / 3);
+  if (c.nu_eig > 0) {
+    // nu_masses = m c^2/(k_B T_nu0) from the density (find_nu_mass_for_rho, massive_neutrinos.f90:271-322)
+    for (int i = 0; i < c.nu_eig; ++i) {
+      double rho = c.omnuh2 / h2 * 1.0 * c.grhocrit / c.grhormass[i];
+      double m;
+      if (rho <= 1) m = 0;
+      else if (rho <= 1.005) {
+        double delta = rho - 1;
+        double y = delta / nu::const2 - nu::low_rho_c[0] * delta * delta / (nu::const2 * nu::const2 * nu::const2);
+        m = std::sqrt(std::max(0.0, y));
+      } else {
+        m = nu::fermi_dirac_const / (1.5 * nu::zeta3) * rho;
+        if (m > 4) {
+          double B = 15.0 * nu::zeta5 / (2.0 * nu::zeta3);
+          m = m - B / m;
+          double rn = nu::rho(m), rnd = nu::drho(m, 1.0);
+          m = m - m * (rn - rho) / rnd;
+        } else {
+          int iflag = 0;
+          double fa = nu::rho(0.0) - rho, fb = nu::rho(m) - rho;
+          m = brent_zero([&](double x) { return nu::rho(x) - rho; }, 0.0, m, fa, fb, 0.01, iflag);
+          if (iflag) { err = "find_nu_mass_for_rho failed"; return CAMBGPU_ERROR_UNSUPPORTED_PARAMS; }
+        }
+      }
+      c.nu_masses[i] = std::max(m, 1e-3);
+    }
+    // TNuPerturbations_init (massive_neutrinos.f90:122-171)
+    double acc = P.AccuracyBoost;
+    double max_nu_mass = c.nu_masses[0];
+    if (max_nu_mass > 4300) acc = std::max(acc, 2.001);
+    else if (max_nu_mass > 600) acc = std::max(acc, 1.001);
+    if (acc > 3) c.nqmax = nint(acc * 10);
+    else if (acc > 2) c.nqmax = 5;
+    else if (acc > 1) c.nqmax = 4;
+    else c.nqmax = 3;
+    if (c.nqmax == 3) {
+      c.nu_q = {0.913201, 3.37517, 7.79184};
+      c.nu_int_kernel = {0.0687359, 3.31435, 2.29911};
+    } else if (c.nqmax == 4) {
+      c.nu_q = {0.5802007037903776, 2.2150938570691223, 4.948032138986023, 9.65253759848097};
+      c.nu_int_kernel = {0.0082119845039711, 1.1143258498419168, 3.6819104154615907, 0.8777790167504481};
+    } else if (c.nqmax == 5) {
+      c.nu_q = {0.4620995950854295, 1.7331898360630928, 3.7956972681313816, 7.2113928588584990,
+                13.2665914595911080};
+      c.nu_int_kernel = {0.0026946402277849193, 0.46041071394952310, 2.9207114780286405, 2.1821643017186352,
+                         0.11621584305889110};
+    } else {
+      c.nu_q.assign(c.nqmax, 0);
+      c.nu_int_kernel.assign(c.nqmax, 0);
+      double dq = (12 + c.nqmax / 5) / (double)c.nqmax;
+      for (int i = 0; i < c.nqmax; ++i) {
+        double qq = (i + 0.5) * dq, dlfdlq = -qq / (1.0 + std::exp(-qq));
+        c.nu_q[i] = qq;
+        c.nu_int_kernel[i] = dq * qq * qq * qq / (std::exp(qq) + 1.0) * (-0.25 * dlfdlq);
+      }
+    }
+    for (auto& w : c.nu_int_kernel) w /= nu::fermi_dirac_const;
+  }
   c.Nnow = P.ombh2 / h2 * (1 - P.YHe) * c.grhocrit * c_si * c_si / K::kappa / K::m_H / (K::Mpc * K::Mpc);
   c.akthom = K::sigma_thomson * c.Nnow * K::Mpc;
   c.fHe = P.YHe / (K::mass_ratio_He_H * (1 - P.YHe));
-  c.z_eq = (c.grhob + c.grhoc) / (c.grhog + c.grhornomass) - 1;
+  c.z_eq = (c.grhob + c.grhoc) / (c.grhog + c.grhornomass + grhomass) - 1;
   c.tau0 = c.time_of_z(0);
   c.DMt0 = c.tau0;
+  // GaugeInterface_Init (equations.f90:512-583): times at which the momentum bins and the
+  // eigenstates become non-relativistic
+  if (c.nu_eig > 0) {
+    auto dtm = [&](double a1, double a2, double tol) {  // DeltaTimeMaxed
+      if (a1 > 1) return 0.0;
+      if (a2 > 1) return c.delta_time(a1, 1.01, tol);
+      return c.delta_time(a1, a2, tol);
+    };
+    c.nu_tau_notmassless.assign((size_t)c.nu_eig * c.nqmax, 0.0);
+    for (int i = 0; i < c.nu_eig; ++i) {
+      double nu_mass = std::max(0.1, c.nu_masses[i]);
+      double a_mass = 1e-1 / nu_mass / P.lAccuracyBoost;
+      double time = c.delta_time(0, c.nu_q[0] * a_mass);
+      c.nu_tau_notmassless[(size_t)i * c.nqmax] = time;
+      for (int j = 1; j < c.nqmax; ++j) {
+        time += dtm(c.nu_q[j - 1] * a_mass, c.nu_q[j] * a_mass, 0.01);
+        c.nu_tau_notmassless[(size_t)i * c.nqmax + j] = time;
+      }
+      double a_nonrel = 2.5 / nu_mass;
+      c.nu_tau_nonrel_phys[i] = dtm(0, a_nonrel, -1);
+      a_nonrel = a_nonrel * nu_switch_boost(c, nu_mass);
+      c.nu_tau_nonrel[i] = dtm(0, a_nonrel, -1);
+      double a_massive = 17.0 / nu_mass * nu_switch_boost(c, nu_mass);
+      c.nu_tau_massive[i] = c.nu_tau_nonrel[i] + dtm(a_nonrel, a_massive, -1);
+    }
+  }
   // reionization (TBaseTauWithHeReionization_Init, zreFromOptDepth)
   Reion& R = c.reion;
   R.fHe = c.fHe;
@@ -1257,6 +1487,13 @@ void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   v.grhob = c.grhob; v.grhov = c.grhov; v.grhok = c.grhok; v.adotrad = c.adotrad; v.tau0 = c.tau0;
   v.DMt0 = c.DMt0; v.taurst = c.taurst; v.taurend = c.taurend; v.tau_maxvis = c.tau_maxvis;
   v.matter_verydom_tau = c.matter_verydom_tau; v.akthom = c.akthom; v.fHe = c.fHe;
+  v.nu_eig = c.nu_eig; v.nqmax = c.nqmax;
+  for (int i = 0; i < 3; ++i) {
+    v.nu_masses[i] = c.nu_masses[i]; v.grhormass[i] = c.grhormass[i]; v.nu_tau_nonrel[i] = c.nu_tau_nonrel[i];
+  }
+  v.nu_q = c.nu_q.empty() ? nullptr : c.nu_q.data();
+  v.nu_int_kernel = c.nu_int_kernel.empty() ? nullptr : c.nu_int_kernel.data();
+  v.nu_tau_notmassless = c.nu_tau_notmassless.empty() ? nullptr : c.nu_tau_notmassless.data();
   v.nthermo = c.nthermo; v.tauminn = c.tauminn; v.dlntau = c.dlntau; v.dlntau_inv = c.dlntau_inv;
   v.tight_tau = c.tight_tau;
   v.thermo_horner = c.thermo_horner.data();

@@ -82,6 +82,11 @@ struct Cosmology {
   CambGpuParams P;
   // background (CAMBdata)
   double grhocrit, grhog, grhor, grhornomass, grhoc, grhob, grhov, grhok, adotrad;
+  // massive neutrinos (MassiveNu / GaugeInterface_Init)
+  int nu_eig = 0, nqmax = 0;
+  double omnuh2 = 0, nu_masses[3] = {0, 0, 0}, grhormass[3] = {0, 0, 0}, nu_degeneracy[3] = {0, 0, 0};
+  double nu_tau_nonrel[3] = {0, 0, 0}, nu_tau_nonrel_phys[3] = {0, 0, 0}, nu_tau_massive[3] = {0, 0, 0};
+  std::vector<double> nu_q, nu_int_kernel, nu_tau_notmassless;  // notmassless [eig][nqmax]
   double Nnow, akthom, fHe, z_eq, Omega_de, tau0, DMt0, scale = 1;
   // InitVars
   double qmax, qmin, dtaurec, max_etak_scalar, maximum_qeta;

@@ -50,7 +50,7 @@ class TanhReionization:
 class CAMBparams:
     def __init__(self, **kwargs):
         self.H0, self.ombh2, self.omch2, self.omk = 67.5, 0.022, 0.122, 0.0
-        self.TCMB, self.YHe, self.num_nu_massless = 2.7255, 0.2454, 3.044
+        self.TCMB, self.YHe, self.nnu = 2.7255, 0.2454, 3.044
         self.Alens = 1.0
         self.max_l, self.max_eta_k = 2500, 6250.0
         self.DoLensing = False
@@ -71,7 +71,7 @@ class CAMBparams:
         if abs(omk) > 5e-7:
             raise CAMBError("only flat models are supported")
         self.H0, self.ombh2, self.omch2, self.omk = H0, ombh2, omch2, omk
-        self.num_nu_massless = nnu
+        self.nnu = nnu
         if YHe is not None:
             self.YHe = YHe
         self.TCMB, self.Alens = TCMB, Alens
@@ -95,7 +95,7 @@ class CAMBparams:
 
     def to_struct(self):
         s = _lib.default_params()
-        for n in ["H0", "ombh2", "omch2", "omk", "TCMB", "YHe", "num_nu_massless", "Alens", "max_l", "max_eta_k"]:
+        for n in ["H0", "ombh2", "omch2", "omk", "TCMB", "YHe", "nnu", "Alens", "max_l", "max_eta_k"]:
             setattr(s, n, getattr(self, n))
         s.max_l = int(self.max_l)
         s.optical_depth = self.Reion.optical_depth

@@ -44,7 +44,9 @@ extern "C" {
  * (fortran/model.f90:27-209) that the scalar flat path reads. */
 typedef struct CambGpuParams {
     double H0, ombh2, omch2, omk, TCMB, YHe;
-    double num_nu_massless;      /* N_eff carried by massless neutrinos */
+    double nnu;                  /* total effective number of neutrinos N_eff */
+    double mnu;                  /* sum of the massive neutrino masses in eV (0: all massless) */
+    int num_massive_neutrinos;   /* degenerate massive eigenstate holds this many neutrinos */
     double optical_depth;        /* reionization tau (re_use_optical_depth = T) */
     double reion_delta_redshift; /* tanh width, default 0.5 */
     double As, ns, nrun, pivot_scalar, Alens;
@@ -65,7 +67,11 @@ typedef struct CambGpuModeSpec {
     double taustart;
     double tight_switch_tau;
     int lmaxg, lmaxgpol, lmaxnr;
+    int lmaxnu;                /* massive-neutrino hierarchy lmax (0 without massive neutrinos) */
+    int nq0[3];                /* momentum bins evolved from the start, per mass eigenstate */
     int pad;
+    double nu_l_boost[3];      /* MassiveNuTransferLAccuracyBoost (equations.f90:484-500) */
+    double nu_approx_time[3];  /* MassiveNuApproxTime set in initial (equations.f90:2091-2102) */
 } CambGpuModeSpec;
 
 /* Read-only view of everything the hot path consumes for one cosmology: the
@@ -78,6 +84,12 @@ typedef struct CambGpuTables {
     double grhog, grhor, grhornomass, grhoc, grhob, grhov, grhok;
     double adotrad, tau0, DMt0, taurst, taurend, tau_maxvis, matter_verydom_tau;
     double akthom, fHe;
+    /* massive neutrinos (one or two mass eigenstates; MassiveNu module) */
+    int nu_eig, nqmax;
+    double nu_masses[3], grhormass[3], nu_tau_nonrel[3];
+    const double* nu_q;               /* [nqmax] momenta */
+    const double* nu_int_kernel;      /* [nqmax] quadrature weights */
+    const double* nu_tau_notmassless; /* [nu_eig][nqmax] */
     /* thermal history */
     int nthermo;
     double tauminn, dlntau, dlntau_inv, tight_tau;

@@ -38,12 +38,19 @@ inline int nint(double x) { return (int)std::lround(x); }
 const int max_l_evolve = 256;
 const double ep0 = 1.0e-2;
 
+const int max_nu = 3;
+const int lmaxnu_high_ktau = 4;
+
 struct EvolutionVars {
   double q, q2, k_buf, k2_buf;
   int lmaxg, lmaxnr, lmaxgpol, MaxlNeeded;
   int g_ix, r_ix, polind, nvar, ScalEqsToPropagate;
   bool TightCoupling, high_ktau_neutrino_approx, no_nu_multpoles, no_phot_multpoles;
   double TightSwitchoffTime, pig, pigdot, poltruncfac;
+  // massive neutrinos (EvolutionVars, equations.f90:66-151)
+  int lmaxnu, nq[max_nu], lmaxnu_tau[max_nu], nu_ix[max_nu], nu_pert_ix, lmaxnu_pert;
+  bool has_nu_relativistic, MassiveNuApprox[max_nu], nu_nonrelativistic[max_nu];
+  double MassiveNuApproxTime[max_nu], G11[max_nu], G30[max_nu], nu_l_boost[max_nu];
   double denlk[max_l_evolve + 1], denlk2[max_l_evolve + 1], polfack[max_l_evolve + 1];
   double* OutputSources;  // non-null inside output()
 };
@@ -63,6 +70,56 @@ struct Ctx {
   double polfac[max_l_evolve + 1], denl[max_l_evolve + 1];
   double epsw;
 };
+
+// ---- massive neutrino background in units of one massless eigenstate
+// (massive_neutrinos.f90: rho_P 186-216, drho 325-347) ----
+namespace nufit {
+const double zeta3 = 1.2020569031595942853997, zeta5 = 1.0369277551433699263313, zeta7 = 1.0083492773819228268397;
+const double pi = 3.1415926535897932384626433832795;
+const double fdc = 7.0 / 120 * pi * pi * pi * pi;
+const double const2 = 5.0 / 7.0 / (pi * pi);
+const double rc[6] = {7.499710425926954249e-01, 1.188066888581748443e-01, 1.545077526625578401e-01,
+                      -8.378996019212282820e-02, 2.123075360029347963e-02, -2.544964203886362908e-03};
+const double pc[7] = {9.283417043601330798e-01, 3.156134695375645838e-01, -2.435843189264263742e-01,
+                      -2.509793530357270000e-02, 4.067958090718486880e-02, 2.378742143669706002e-03,
+                      -1.965863329520473827e-03};
+const double lrc[2] = {-1.872929199948838302e-02, 1.831728681837861694e-02};
+const double lpc[2] = {1.667044572156534468e-02, -2.277471498716537868e-02};
+const double dc[6] = {5.800497880734221123e-01, 1.801974470841860576e-01, -1.602709049602861757e-01,
+                      3.167230341650149189e-02, 1.056591590995091534e-02, -3.877662402660121861e-03};
+void rho_P(double am, double& rhonu, double& pnu) {
+  const double amin = 0.42, amax = 70.0;
+  if (am <= amin) {
+    double am2 = am * am, am4 = am2 * am2;
+    rhonu = 1.0 + const2 * am2 + am4 * (lrc[0] + am2 * lrc[1]);
+    pnu = (1.0 - const2 * am2) / 3.0 + am4 * (lpc[0] + am2 * lpc[1]);
+    return;
+  }
+  if (am >= amax) {
+    rhonu = 3 / (2 * fdc) * (zeta3 * am + ((15 * zeta5) / 2 - 945.0 / 16 * zeta7 / (am * am)) / am);
+    pnu = 900.0 / 120.0 / fdc * (zeta5 - 63.0 / 4 * zeta7 / (am * am)) / am;
+    return;
+  }
+  double fc = std::sqrt(amin * amax), izm = (amax + fc) / (amax - fc);
+  double z = ((am - fc) / (am + fc)) * izm;
+  double rfit = (((((rc[5] * z + rc[4]) * z + rc[3]) * z + rc[2]) * z + rc[1]) * z + rc[0]);
+  double pfit = ((((((pc[6] * z + pc[5]) * z + pc[4]) * z + pc[3]) * z + pc[2]) * z + pc[1]) * z + pc[0]);
+  rhonu = (1.0 + 3.0 * zeta3 / (2.0 * fdc) * am) * rfit;
+  pnu = pfit / (1.0 + fdc / ((900.0 / 120.0) * zeta5) * am);
+}
+double drho(double am, double adotoa) {
+  const double amin = 0.3, amax = 70.0;
+  if (am <= amin) {
+    double am2 = am * am;
+    return am2 * (2 * const2 + am2 * (.4399706676e-1 * std::log(am) - .2970400378e-2 - .29331377855e-1 * am)) * adotoa;
+  }
+  if (am >= amax) return 3 / (2 * fdc) * (zeta3 * am + (-(15 * zeta5) / 2 + 2835.0 / 16 * zeta7 / (am * am)) / am) * adotoa;
+  double fc = std::sqrt(amin * amax), izm = (amax + fc) / (amax - fc);
+  double z = ((am - fc) / (am + fc)) * izm;
+  double D = (((((dc[5] * z + dc[4]) * z + dc[3]) * z + dc[2]) * z + dc[1]) * z + dc[0]);
+  return am * am / (1.0 + 2.0 * am) * D * adotoa;
+}
+}  // namespace nufit
 
 // ---- thermal history lookups (results.f90:1826-1880, 3069-3108) ----
 void thermo_values(const Ctx& C, double tau, double& a, double& cs2b, double& opacity, double* dopacity) {
@@ -118,17 +175,40 @@ double opacity_to_time(const Ctx& C, double opacity) {
 }
 
 // ---- GetNumEqns (massless neutrinos) ----
-void get_num_eqns(const Ctx& C, EvolutionVars& EV) {
+void get_num_eqns(const Ctx& C, EvolutionVars& EV, const CambGpuModeSpec& ms) {
   const CambGpuTables* T = C.T;
   double lab = T->lAccuracyBoost;
   int min_lmaxnr = std::max(3, nint(3 * lab));
+  double max_nu_mass = 0;
+  EV.lmaxnu = 0;
+  if (T->nu_eig > 0) {
+    for (int i = 0; i < T->nu_eig; ++i) max_nu_mass = std::max(max_nu_mass, T->nu_masses[i]);
+    for (int i = 0; i < T->nu_eig; ++i) {
+      int q_rel = 0;
+      for (int j = 1; j <= T->nqmax; ++j) {
+        if (T->nu_q[j - 1] > T->nu_masses[i] * T->adotrad / EV.q) break;
+        q_rel++;
+      }
+      EV.nq[i] = (q_rel >= T->nqmax - 2) ? T->nqmax : q_rel;
+      EV.nu_nonrelativistic[i] = false;
+      EV.nu_l_boost[i] = ms.nu_l_boost[i];  // MassiveNuTransferLAccuracyBoost, a host input
+    }
+    EV.lmaxnu = std::max(3, nint(10 * lab));
+    if (max_nu_mass > 700) EV.lmaxnu = std::max(3, nint(15 * lab));
+    for (int i = 0; i < T->nu_eig; ++i) {
+      EV.lmaxnu = std::max(EV.lmaxnu, nint(10 * EV.nu_l_boost[i]));
+      if (T->nu_masses[i] > 700) EV.lmaxnu = std::max(EV.lmaxnu, nint(15 * EV.nu_l_boost[i]));
+    }
+  }
   EV.high_ktau_neutrino_approx = false;
+  for (int i = 0; i < max_nu; ++i) EV.MassiveNuApprox[i] = false;
   EV.TightCoupling = true;
   EV.no_phot_multpoles = false;
   EV.no_nu_multpoles = false;
   if (T->accurate_polarization) EV.lmaxg = std::max(nint(11 * lab), 3);
   else EV.lmaxg = std::max(nint(8 * lab), 3);
   EV.lmaxnr = std::max(nint(14 * lab), min_lmaxnr);
+  if (max_nu_mass > 700) EV.lmaxnr = std::max(nint(32 * lab), min_lmaxnr);
   EV.lmaxgpol = EV.lmaxg;
   if (!T->accurate_polarization) EV.lmaxgpol = std::max(nint(4 * lab), 3);
   else if (EV.q > 0.15) {
@@ -145,12 +225,14 @@ void get_num_eqns(const Ctx& C, EvolutionVars& EV) {
       EV.lmaxgpol = EV.lmaxgpol * 2;
     }
   }
+  if (EV.lmaxnr < EV.lmaxnu) EV.lmaxnr = EV.lmaxnu;
   EV.poltruncfac = (double)EV.lmaxgpol / std::max(1, EV.lmaxgpol - 2);
-  EV.MaxlNeeded = std::max(EV.lmaxg, std::max(EV.lmaxnr, EV.lmaxgpol));
-  EV.nvar = 4 + (EV.lmaxg + 1) + (EV.lmaxnr + 1) + EV.lmaxgpol - 1;
+  EV.MaxlNeeded = std::max(std::max(EV.lmaxg, EV.lmaxnu), std::max(EV.lmaxnr, EV.lmaxgpol));
 }
 
-void setup_indices(EvolutionVars& EV) {
+thread_local const Ctx* C_ = nullptr;  // the context of the mode being evolved
+
+void setup_indices(EvolutionVars& EV, bool want_maxeq = false) {
   int neq = 4;
   if (!EV.no_phot_multpoles) {
     EV.g_ix = 5;
@@ -166,7 +248,33 @@ void setup_indices(EvolutionVars& EV) {
     if (EV.high_ktau_neutrino_approx) neq += 3;
     else neq += EV.lmaxnr + 1;
   }
+  int maxeq = 4 + (EV.lmaxg + 1) + (EV.lmaxnr + 1) + EV.lmaxgpol - 1;
+  EV.has_nu_relativistic = false;
+  if (C_->T->nu_eig > 0) {
+    const CambGpuTables* T = C_->T;
+    for (int i = 0; i < T->nu_eig; ++i) EV.has_nu_relativistic |= EV.nq[i] != T->nqmax;
+    if (EV.has_nu_relativistic) {
+      EV.lmaxnu_pert = EV.lmaxnu;
+      EV.nu_pert_ix = neq + 1;
+      neq += EV.lmaxnu_pert + 1;
+      maxeq += EV.lmaxnu_pert + 1;
+    } else EV.lmaxnu_pert = 0;
+    for (int i = 0; i < T->nu_eig; ++i) {
+      double b = EV.nu_l_boost[i];
+      if (EV.high_ktau_neutrino_approx) EV.lmaxnu_tau[i] = (int)(lmaxnu_high_ktau * b);
+      else {
+        EV.lmaxnu_tau[i] = std::max(std::min(nint(0.8 * EV.q * T->nu_tau_nonrel[i] * b), EV.lmaxnu), 3);
+        if (EV.nu_nonrelativistic[i]) EV.lmaxnu_tau[i] = std::min(EV.lmaxnu_tau[i], nint(4 * b));
+      }
+      EV.lmaxnu_tau[i] = std::min(EV.lmaxnu, EV.lmaxnu_tau[i]);
+      EV.nu_ix[i] = neq + 1;
+      if (EV.MassiveNuApprox[i]) neq += 4;
+      else neq += EV.nq[i] * (EV.lmaxnu_tau[i] + 1);
+      maxeq += T->nqmax * (EV.lmaxnu + 1);
+    }
+  }
   EV.ScalEqsToPropagate = neq;
+  if (want_maxeq) EV.nvar = maxeq;
 }
 
 void copy_vars(const double* y, double* yout, const EvolutionVars& EV, const EvolutionVars& EVo) {
@@ -184,6 +292,115 @@ void copy_vars(const double* y, double* yout, const EvolutionVars& EV, const Evo
     int lmax = (EV.high_ktau_neutrino_approx || EVo.high_ktau_neutrino_approx) ? 2 : std::min(EV.lmaxnr, EVo.lmaxnr);
     for (int l = 0; l <= lmax; ++l) yout[EVo.r_ix + l] = y[EV.r_ix + l];
   }
+  const CambGpuTables* T = C_->T;
+  if (T->nu_eig > 0) {
+    for (int i = 0; i < T->nu_eig; ++i) {
+      int off = EV.nu_ix[i], off2 = EVo.nu_ix[i];
+      if (EV.MassiveNuApprox[i] && EVo.MassiveNuApprox[i]) {
+        for (int j = 0; j < 4; ++j) yout[off2 + j] = y[off + j];
+      } else if (!EV.MassiveNuApprox[i] && !EVo.MassiveNuApprox[i]) {
+        int lmax = std::min(EV.lmaxnu_tau[i], EVo.lmaxnu_tau[i]);
+        int nq = std::min(EV.nq[i], EVo.nq[i]);
+        for (int iq = 1; iq <= nq; ++iq) {
+          int ind = off + (iq - 1) * (EV.lmaxnu_tau[i] + 1), ind2 = off2 + (iq - 1) * (EVo.lmaxnu_tau[i] + 1);
+          for (int l = 0; l <= lmax; ++l) yout[ind2 + l] = y[ind + l];
+        }
+        for (int iq = nq + 1; iq <= EVo.nq[i]; ++iq) {
+          int lm = std::min(EVo.lmaxnu_tau[i], EV.lmaxnr);
+          int ind2 = off2 + (iq - 1) * (EVo.lmaxnu_tau[i] + 1);
+          for (int l = 0; l <= lm; ++l) yout[ind2 + l] = y[EV.r_ix + l];
+          double qq = T->nu_q[iq - 1];
+          double pert_scale = (T->nu_masses[i] / qq) * (T->nu_masses[i] / qq) / 2;
+          lm = std::min(lm, EV.lmaxnu_pert);
+          for (int l = 0; l <= lm; ++l) yout[ind2 + l] = yout[ind2 + l] + y[EV.nu_pert_ix + l] * pert_scale;
+        }
+      }
+    }
+    if (EVo.has_nu_relativistic && EV.has_nu_relativistic) {
+      int lmax = std::min(EVo.lmaxnu_pert, EV.lmaxnu_pert);
+      for (int l = 0; l <= lmax; ++l) yout[EVo.nu_pert_ix + l] = y[EV.nu_pert_ix + l];
+    }
+  }
+}
+
+// Nu_Integrate_L01 / L012 / Nu_pinudot / Nu_Intvsq (equations.f90:1178-1356)
+void nu_integrate_l012(const EvolutionVars& EV, const double* y, double a, int i, double& drhonu, double& fnu,
+                       double& dpnu, double& pinu, bool want_l2) {
+  const CambGpuTables* T = C_->T;
+  drhonu = fnu = dpnu = pinu = 0;
+  double am = a * T->nu_masses[i];
+  int ind = EV.nu_ix[i];
+  for (int iq = 1; iq <= EV.nq[i]; ++iq) {
+    double aq = am / T->nu_q[iq - 1];
+    double w = T->nu_int_kernel[iq - 1];
+    if (want_l2) {
+      double v = 1.0 / std::sqrt(1.0 + aq * aq);
+      drhonu += w * y[ind] / v;
+      fnu += w * y[ind + 1];
+      dpnu += w * y[ind] * v;
+      pinu += w * y[ind + 2] * v;
+    } else {
+      drhonu += w * y[ind] * std::sqrt(1.0 + aq * aq);
+      fnu += w * y[ind + 1];
+    }
+    ind += EV.lmaxnu_tau[i] + 1;
+  }
+  ind = EV.nu_pert_ix;
+  for (int iq = EV.nq[i] + 1; iq <= T->nqmax; ++iq) {
+    double qq = T->nu_q[iq - 1], aq = am / qq, w = T->nu_int_kernel[iq - 1];
+    double pert_scale = (T->nu_masses[i] / qq) * (T->nu_masses[i] / qq) / 2;
+    double tmp = w * (y[EV.r_ix] + pert_scale * y[ind]);
+    if (want_l2) {
+      double v = 1.0 / std::sqrt(1.0 + aq * aq);
+      drhonu += tmp / v;
+      fnu += w * (y[EV.r_ix + 1] + pert_scale * y[ind + 1]);
+      dpnu += tmp * v;
+      pinu += w * (y[EV.r_ix + 2] + pert_scale * y[ind + 2]) * v;
+    } else {
+      drhonu += tmp * std::sqrt(1.0 + aq * aq);
+      fnu += w * (y[EV.r_ix + 1] + pert_scale * y[ind + 1]);
+    }
+  }
+  if (want_l2) dpnu = dpnu / 3;
+}
+
+double nu_pinudot(const EvolutionVars& EV, const double* y, const double* ydot, double a, double adotoa, int i) {
+  const CambGpuTables* T = C_->T;
+  double pinudot = 0;
+  int ind = EV.nu_ix[i] + 2;
+  double am = a * T->nu_masses[i];
+  for (int iq = 1; iq <= EV.nq[i]; ++iq) {
+    double qq = T->nu_q[iq - 1], aq = am / qq, aqdot = aq * adotoa;
+    double v = 1.0 / std::sqrt(1.0 + aq * aq);
+    double vdot = -aq * aqdot / std::pow(1.0 + aq * aq, 1.5);
+    pinudot += T->nu_int_kernel[iq - 1] * (ydot[ind] * v + y[ind] * vdot);
+    ind += EV.lmaxnu_tau[i] + 1;
+  }
+  ind = EV.nu_pert_ix + 2;
+  for (int iq = EV.nq[i] + 1; iq <= T->nqmax; ++iq) {
+    double qq = T->nu_q[iq - 1], aq = am / qq, aqdot = aq * adotoa;
+    double pert_scale = (T->nu_masses[i] / qq) * (T->nu_masses[i] / qq) / 2;
+    double v = 1.0 / std::sqrt(1.0 + aq * aq);
+    double vdot = -aq * aqdot / std::pow(1.0 + aq * aq, 1.5);
+    double psi2dot = ydot[EV.r_ix + 2] + pert_scale * ydot[ind];
+    double psi2 = y[EV.r_ix + 2] + pert_scale * y[ind];
+    pinudot += T->nu_int_kernel[iq - 1] * (psi2dot * v + psi2 * vdot);
+  }
+  return pinudot;
+}
+
+void nu_intvsq(const EvolutionVars& EV, const double* y, double a, int i, double& G11, double& G30) {
+  const CambGpuTables* T = C_->T;
+  double am = a * T->nu_masses[i];
+  int ind = EV.nu_ix[i];
+  G11 = G30 = 0;
+  for (int iq = 1; iq <= EV.nq[i]; ++iq) {
+    double aq = am / T->nu_q[iq - 1];
+    double v = 1.0 / std::sqrt(1.0 + aq * aq);
+    G11 += T->nu_int_kernel[iq - 1] * y[ind + 1] * v * v;
+    if (EV.lmaxnu_tau[i] > 2) G30 += T->nu_int_kernel[iq - 1] * y[ind + 3] * v * v;
+    ind += EV.lmaxnu_tau[i] + 1;
+  }
 }
 
 // ---- derivs (equations.f90:2273-2949), flat, Lambda, massless neutrinos ----
@@ -199,7 +416,26 @@ void derivs(const Ctx& C, EvolutionVars& EV, int n, double tau, const double* ay
   double grhov_t = T->grhov * a2, w_dark_energy_t = -1;
   double dgrho_matter = grhob_t * clxb + grhoc_t * clxc;
   double dgq = grhob_t * vb;
-  double gpres_nu = 0, grhonu_t = 0;
+  double gpres_nu = 0, grhonu_t = 0, wnu_arr[max_nu] = {0, 0, 0};
+  for (int i = 0; i < T->nu_eig; ++i) {  // MassiveNuVars (equations.f90:1358-1401)
+    double grhormass_t = T->grhormass[i] / (a * a), rhonu, pnu, clxnu, qnu;
+    nufit::rho_P(a * T->nu_masses[i], rhonu, pnu);
+    if (EV.MassiveNuApprox[i]) {
+      clxnu = ay[EV.nu_ix[i]];
+      qnu = ay[EV.nu_ix[i] + 2];
+    } else {
+      double dp, pn;
+      nu_integrate_l012(EV, ay, a, i, clxnu, qnu, dp, pn, false);
+      qnu = qnu / rhonu;
+      clxnu = clxnu / rhonu;
+    }
+    double g_t = grhormass_t * rhonu, gp_t = grhormass_t * pnu;
+    grhonu_t += g_t;
+    gpres_nu += gp_t;
+    dgrho_matter += g_t * clxnu;
+    dgq += g_t * qnu;
+    wnu_arr[i] = pnu / rhonu;
+  }
   double grho_matter = grhonu_t + grhob_t + grhoc_t;
   double grho = grho_matter + grhor_t + grhog_t + grhov_t;
   double gpres_noDE = gpres_nu + (grhor_t + grhog_t) / 3;
@@ -319,6 +555,54 @@ void derivs(const Ctx& C, EvolutionVars& EV, int n, double tau, const double* ay
       ayprime[ix] = k * ay[ix - 1] - (EV.lmaxnr + 1) * cothxor * ay[ix];
     }
   }
+  // massive neutrino equations of motion (equations.f90:2710-2773)
+  for (int i = 0; i < T->nu_eig; ++i) {
+    if (EV.MassiveNuApprox[i]) {
+      double G11_t = EV.G11[i] / a / a2, G30_t = EV.G30[i] / a / a2;
+      int off = EV.nu_ix[i];
+      double w = wnu_arr[i];
+      ayprime[off] = -k * z * (w + 1) + 3 * adotoa * (w * ay[off] - ay[off + 1]) - k * ay[off + 2];
+      ayprime[off + 1] = (3 * w - 2) * adotoa * ay[off + 1] - 5.0 / 3 * k * z * w - k / 3 * G11_t;
+      ayprime[off + 2] = (3 * w - 1) * adotoa * ay[off + 2] - k * (2.0 / 3 * ay[off + 3] - ay[off + 1]);
+      ayprime[off + 3] = (3 * w - 2) * adotoa * ay[off + 3] + 2 * w * k * sigma - k / 5 * (3 * G30_t - 2 * G11_t);
+    } else {
+      int ind = EV.nu_ix[i];
+      for (int iq = 1; iq <= EV.nq[i]; ++iq) {
+        double qq = T->nu_q[iq - 1], aq = a * T->nu_masses[i] / qq;
+        double v = 1.0 / std::sqrt(1.0 + aq * aq);
+        ayprime[ind] = -k * (4.0 / 3.0 * z + v * ay[ind + 1]);
+        ind++;
+        ayprime[ind] = v * (EV.denlk[1] * ay[ind - 1] - EV.denlk2[1] * ay[ind + 1]);
+        ind++;
+        if (EV.lmaxnu_tau[i] == 2) {
+          ayprime[ind] = -ayprime[ind - 2] - 3 * cothxor * ay[ind];
+        } else {
+          ayprime[ind] = v * (EV.denlk[2] * ay[ind - 1] - EV.denlk2[2] * ay[ind + 1]) + k * 8.0 / 15.0 * sigma;
+          for (int l = 3; l <= EV.lmaxnu_tau[i] - 1; ++l) {
+            ind++;
+            ayprime[ind] = v * (EV.denlk[l] * ay[ind - 1] - EV.denlk2[l] * ay[ind + 1]);
+          }
+          ind++;
+          ayprime[ind] = k * v * ay[ind - 1] - (EV.lmaxnu_tau[i] + 1) * cothxor * ay[ind];
+        }
+        ind++;
+      }
+    }
+  }
+  if (EV.has_nu_relativistic) {
+    int ind = EV.nu_pert_ix;
+    ayprime[ind] = +k * a2 * qr - k * ay[ind + 1];
+    int ind2 = EV.r_ix;
+    for (int l = 1; l <= EV.lmaxnu_pert - 1; ++l) {
+      ind++;
+      ind2++;
+      ayprime[ind] = -a2 * (EV.denlk[l] * ay[ind2 - 1] - EV.denlk2[l] * ay[ind2 + 1]) +
+                     (EV.denlk[l] * ay[ind - 1] - EV.denlk2[l] * ay[ind + 1]);
+    }
+    ind++;
+    ind2++;
+    ayprime[ind] = k * (ay[ind - 1] - a2 * ay[ind2 - 1]) - (EV.lmaxnu_pert + 1) * cothxor * ay[ind];
+  }
   if (!EV.OutputSources) return;
   // ---- source output (equations.f90:2775-2912) ----
   double E[4] = {0, 0, 0, 0}, Edot[4] = {0, 0, 0, 0}, octg, octgdot;
@@ -353,6 +637,31 @@ void derivs(const Ctx& C, EvolutionVars& EV, int n, double tau, const double* ay
   double dgpi = grhor_t * pir + grhog_t * pig;
   double dgpi_diff = 0;
   double pidot_sum = grhog_t * pigdot + grhor_t * pirdot;
+  for (int i = 0; i < T->nu_eig; ++i) {  // MassiveNuVarsOut (equations.f90:1113-1176)
+    double grhormass_t = T->grhormass[i] / (a * a), rhonu, pnu, clxnu, qnu, pinu, pinudot;
+    nufit::rho_P(a * T->nu_masses[i], rhonu, pnu);
+    if (EV.MassiveNuApprox[i]) {
+      clxnu = ay[EV.nu_ix[i]];
+      qnu = ay[EV.nu_ix[i] + 2];
+      pinu = ay[EV.nu_ix[i] + 3];
+      pinudot = ayprime[EV.nu_ix[i] + 3];
+    } else {
+      double dpnu;
+      nu_integrate_l012(EV, ay, a, i, clxnu, qnu, dpnu, pinu, true);
+      qnu = qnu / rhonu;
+      clxnu = clxnu / rhonu;
+      pinu = pinu / rhonu;
+      double rhonudot = nufit::drho(a * T->nu_masses[i], adotoa);
+      pinudot = nu_pinudot(EV, ay, ayprime, a, adotoa, i);
+      pinudot = pinudot / rhonu - rhonudot / rhonu * pinu;
+    }
+    (void)clxnu;
+    (void)qnu;
+    double g_t = grhormass_t * rhonu, gp_t = grhormass_t * pnu;
+    dgpi += g_t * pinu;
+    dgpi_diff += pinu * (3 * gp_t - g_t);
+    pidot_sum += g_t * pinudot;
+  }
   gpres = gpres_noDE + w_dark_energy_t * grhov_t;
   double diff_rhopi = pidot_sum - (4 * dgpi + dgpi_diff) * adotoa;
   double phi = -((dgrho + 3 * dgq * adotoa / k) + dgpi) / (2 * k2);
@@ -499,6 +808,41 @@ void runge_kutta_dp45(const Ctx& C, EvolutionVars& EV, int n, double& x, double*
 
 struct ModeStats { long evals = 0; int status = 0; };
 
+// next_nu_nq (equations.f90:242-258)
+int next_nu_nq(const CambGpuTables* T, int nq) {
+  if (nq == 0) return 1;
+  int qq = (int)T->nu_q[nq - 1];
+  return qq >= 10 ? T->nqmax : nq + 1;
+}
+
+// SwitchToMassiveNuApprox (equations.f90:1072-1111)
+void switch_to_massive_nu_approx(EvolutionVars& EV, double a, std::vector<double>& y, int i) {
+  const CambGpuTables* T = C_->T;
+  double a2 = a * a;
+  EvolutionVars EVout = EV;
+  EVout.MassiveNuApprox[i] = true;
+  setup_indices(EVout);
+  std::vector<double> yout(EV.nvar + 2, 0.0);
+  copy_vars(y.data(), yout.data(), EV, EVout);
+  double rhonu, pnu;
+  nufit::rho_P(a * T->nu_masses[i], rhonu, pnu);
+  double clxnu, qnu, dpnu, pinu;
+  nu_integrate_l012(EV, y.data(), a, i, clxnu, qnu, dpnu, pinu, true);
+  dpnu = dpnu / rhonu;
+  qnu = qnu / rhonu;
+  clxnu = clxnu / rhonu;
+  pinu = pinu / rhonu;
+  yout[EVout.nu_ix[i]] = clxnu;
+  yout[EVout.nu_ix[i] + 1] = dpnu;
+  yout[EVout.nu_ix[i] + 2] = qnu;
+  yout[EVout.nu_ix[i] + 3] = pinu;
+  nu_intvsq(EV, y.data(), a, i, EVout.G11[i], EVout.G30[i]);
+  EVout.G11[i] = EVout.G11[i] * a2 * a / rhonu;
+  EVout.G30[i] = EVout.G30[i] * a2 * a / rhonu;
+  EV = EVout;
+  y = yout;
+}
+
 bool scal_ev(const Ctx& C, EvolutionVars& EV, double* y, double& tau, double tauend, double tol1, int& ind,
              RKSettings& s, std::vector<double>* w, ModeStats& st) {
   if (EV.q < 2e-3 && tau <= C.T->taurend) s.max_step_size = 2.0;  // WantCls
@@ -520,8 +864,16 @@ bool evolve_scal(const Ctx& C, EvolutionVars& EV, double& tau, std::vector<doubl
     double smallTime = std::min(tau, 1 / EV.k_buf) / 100;
     double switchBoost = T->AccuracyBoost * T->TimeSwitchBoost;
     double tau_switch_ktau = noSwitch, tau_switch_no_nu_multpoles = noSwitch, tau_switch_no_phot_multpoles = noSwitch;
+    double tau_switch_nu_massless = noSwitch, tau_switch_nu_nonrel = noSwitch, tau_switch_nu_massive = noSwitch;
     if (!EV.high_ktau_neutrino_approx && !EV.no_nu_multpoles)
       tau_switch_ktau = std::max(20, EV.lmaxnr - 4) / EV.k_buf;
+    for (int i = 0; i < T->nu_eig; ++i) {
+      if (EV.nq[i] != T->nqmax)
+        tau_switch_nu_massless =
+            std::min(tau_switch_nu_massless, T->nu_tau_notmassless[(size_t)i * T->nqmax + next_nu_nq(T, EV.nq[i]) - 1]);
+      else if (!EV.nu_nonrelativistic[i]) tau_switch_nu_nonrel = std::min(T->nu_tau_nonrel[i], tau_switch_nu_nonrel);
+      else if (!EV.MassiveNuApprox[i]) tau_switch_nu_massive = std::min(tau_switch_nu_massive, EV.MassiveNuApproxTime[i]);
+    }
     // DoLateRadTruncation
     if (!EV.no_nu_multpoles)
       tau_switch_no_nu_multpoles = std::max(15 / EV.k_buf * switchBoost, std::min(T->taurend, T->matter_verydom_tau));
@@ -530,8 +882,9 @@ bool evolve_scal(const Ctx& C, EvolutionVars& EV, double& tau, std::vector<doubl
       if (EV.k_buf > 0.03 * latePhotSwitchBoost)  // WantCls
         tau_switch_no_phot_multpoles = std::max(15 / EV.k_buf, T->taurend) * latePhotSwitchBoost;
     }
-    double next_switch = std::min(std::min(tau_switch_ktau, EV.TightSwitchoffTime),
-                                  std::min(std::min(tau_switch_no_nu_multpoles, tau_switch_no_phot_multpoles), noSwitch));
+    double next_switch = std::min(std::min(std::min(tau_switch_ktau, tau_switch_nu_massless), EV.TightSwitchoffTime),
+                                  std::min(std::min(tau_switch_nu_massive, tau_switch_no_nu_multpoles),
+                                           std::min(std::min(tau_switch_no_phot_multpoles, tau_switch_nu_nonrel), noSwitch)));
     if (next_switch < tauend) {
       if (next_switch > tau + smallTime) {
         if (!scal_ev(C, EV, y.data(), tau, next_switch, tol1, ind, s, w, st)) return false;
@@ -559,13 +912,47 @@ bool evolve_scal(const Ctx& C, EvolutionVars& EV, double& tau, std::vector<doubl
                                ((EV.pigdot / 4.0) * (1.0 + (5.0 / 2.0) * dopacity / (opacity * opacity))) * (-1.0);
       } else if (next_switch == tau_switch_ktau) {
         EVout.high_ktau_neutrino_approx = true;
+        for (int i = 0; i < T->nu_eig; ++i) EVout.nq[i] = T->nqmax;
         setup_indices(EVout);
         copy_vars(y.data(), yout.data(), EV, EVout);
         y = yout;
         EV = EVout;
+      } else if (next_switch == tau_switch_nu_massless) {
+        for (int i = 0; i < T->nu_eig; ++i) {
+          if (EV.nq[i] != T->nqmax &&
+              next_switch == T->nu_tau_notmassless[(size_t)i * T->nqmax + next_nu_nq(T, EV.nq[i]) - 1]) {
+            EVout.nq[i] = next_nu_nq(T, EV.nq[i]);
+            setup_indices(EVout);
+            copy_vars(y.data(), yout.data(), EV, EVout);
+            EV = EVout;
+            y = yout;
+            break;
+          }
+        }
+      } else if (next_switch == tau_switch_nu_nonrel) {
+        for (int i = 0; i < T->nu_eig; ++i) {
+          if (!EV.nu_nonrelativistic[i] && next_switch == T->nu_tau_nonrel[i]) {
+            EVout.nu_nonrelativistic[i] = true;
+            setup_indices(EVout);
+            copy_vars(y.data(), yout.data(), EV, EVout);
+            EV = EVout;
+            y = yout;
+            break;
+          }
+        }
+      } else if (next_switch == tau_switch_nu_massive) {
+        double a, cs2, opacity;
+        thermo_values(C, tau, a, cs2, opacity, nullptr);
+        for (int i = 0; i < T->nu_eig; ++i) {
+          if (!EV.MassiveNuApprox[i] && next_switch == EV.MassiveNuApproxTime[i]) {
+            switch_to_massive_nu_approx(EV, a, y, i);
+            break;
+          }
+        }
       } else if (next_switch == tau_switch_no_nu_multpoles) {
         ind = 1;
         EVout.no_nu_multpoles = true;
+        for (int i = 0; i < T->nu_eig; ++i) EVout.nq[i] = T->nqmax;
         setup_indices(EVout);
         copy_vars(y.data(), yout.data(), EV, EVout);
         y = yout;
@@ -603,7 +990,9 @@ void initial(const Ctx& C, EvolutionVars& EV, std::vector<double>& y, double tau
   EV.TightSwitchoffTime = std::min(T->tight_tau, opacity_to_time(C, EV.k_buf / ep));
   std::fill(y.begin(), y.end(), 0.0);
   double x = k * tau, x2 = x * x, x3 = x2 * x;
-  double grhonu = T->grhornomass;
+  double rhomass = 0;
+  for (int i = 0; i < T->nu_eig; ++i) rhomass += T->grhormass[i];
+  double grhonu = rhomass + T->grhornomass;
   double om = (T->grhob + T->grhoc) / std::sqrt(3 * (T->grhog + grhonu));
   double omtau = om * tau;
   double Rv = grhonu / (grhonu + T->grhog);
@@ -627,18 +1016,38 @@ void initial(const Ctx& C, EvolutionVars& EV, std::vector<double>& y, double tau
   y[EV.r_ix + 1] = -iv_qr;
   y[EV.r_ix + 2] = -iv_pir;
   if (EV.lmaxnr > 2) y[EV.r_ix + 3] = -iv_aj3r;
+  for (int i = 0; i < T->nu_eig; ++i) {
+    int ind = EV.nu_ix[i];
+    for (int iq = 1; iq <= EV.nq[i]; ++iq) {
+      for (int j = 0; j < 3; ++j) y[ind + j] = y[EV.r_ix + j];
+      if (EV.lmaxnu_tau[i] > 2) y[ind + 3] = -iv_aj3r;
+      ind += EV.lmaxnu_tau[i] + 1;
+    }
+  }
 }
 
 // CalcScalarSources (cmbmain.f90:998-1074)
+// GetTauStart (cmbmain.f90:706-729)
+double tau_start(const CambGpuTables* T, double q) {
+  double t = std::min(0.001 / q, 0.1);
+  double mmax = 0;
+  for (int i = 0; i < T->nu_eig; ++i) mmax = std::max(mmax, T->nu_masses[i]);
+  if (T->nu_eig > 0 && mmax != 0) t = std::min(t, 1e-3 / mmax / T->adotrad);
+  return t;
+}
+
 void calc_scalar_sources(const Ctx& C, int q_ix, double* LinearSrc, ModeStats& st) {
   const CambGpuTables* T = C.T;
+  C_ = &C;
   EvolutionVars EV{};
   EV.q = T->q_evolve[q_ix];
   EV.q2 = EV.q * EV.q;
   EV.OutputSources = nullptr;
-  double taustart = std::min(0.001 / EV.q, 0.1);
-  get_num_eqns(C, EV);
-  setup_indices(EV);
+  double taustart = tau_start(T, EV.q);
+  const CambGpuModeSpec& ms = T->modes[q_ix];
+  get_num_eqns(C, EV, ms);
+  setup_indices(EV, true);
+  for (int i = 0; i < T->nu_eig; ++i) EV.MassiveNuApproxTime[i] = ms.nu_approx_time[i];
   std::vector<double> w[10];
   for (int j = 1; j <= 9; ++j) w[j].assign(EV.nvar + 2, 0.0);
   std::vector<double> y(EV.nvar + 2, 0.0);
@@ -708,13 +1117,17 @@ extern "C" {
 int oracle_mode_setup(const CambGpuTables* T, double q, int* lmax3, double* tight_switch) {
   Ctx C;
   init_ctx(C, T);
+  C_ = &C;
   EvolutionVars EV{};
   EV.q = q;
   EV.q2 = q * q;
-  get_num_eqns(C, EV);
-  setup_indices(EV);
+  int q_ix = 0;
+  for (int i = 0; i < T->nk; ++i)
+    if (T->q_evolve[i] == q) q_ix = i;
+  get_num_eqns(C, EV, T->modes[q_ix]);
+  setup_indices(EV, true);
   std::vector<double> y(EV.nvar + 2);
-  initial(C, EV, y, std::min(0.001 / q, 0.1));
+  initial(C, EV, y, tau_start(T, q));
   lmax3[0] = EV.lmaxg;
   lmax3[1] = EV.lmaxgpol;
   lmax3[2] = EV.lmaxnr;

@@ -14,7 +14,7 @@ def fiducial(lmax=1000, lensing=False, **over):
     massless N_eff, tau=0.06, As=2.1e-9, ns=0.965."""
     p = _lib.default_params()
     p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
-    p.num_nu_massless = 3.046
+    p.nnu = 3.046
     p.max_l = lmax
     p.do_lensing = 1 if lensing else 0
     p.max_eta_k = (lmax + (200 if lensing else 0)) * 2.5
@@ -26,15 +26,17 @@ def fiducial(lmax=1000, lensing=False, **over):
 
 
 def planck2018(lmax=1000):
-    """inifiles/planck_2018.ini cosmology with its massive neutrino folded into
-    massless N_eff (radiation era) and CDM (late times)."""
+    """inifiles/planck_2018.ini cosmology: one massive neutrino of 0.06 eV (the ini's
+    omnuh2), N_eff = 3.046."""
     g = json.load(open(os.path.join(HERE, "golden", "template_cls.json")))["cosmology"]
     p = _lib.default_params()
     p.ombh2 = g["ombh2"]
-    p.omch2 = g["omch2"] + g["omnuh2"]
+    p.omch2 = g["omch2"]
+    p.mnu = 0.06
+    p.num_massive_neutrinos = 1
     p.H0 = g["hubble"]
     p.YHe = g["helium_fraction"]
-    p.num_nu_massless = g["massless_neutrinos"] + g["massive_neutrinos"]
+    p.nnu = g["massless_neutrinos"] + g["massive_neutrinos"]
     p.optical_depth = g["re_optical_depth"]
     p.As = g["scalar_amp"]
     p.ns = g["scalar_spectral_index"]

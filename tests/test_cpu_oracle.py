@@ -32,18 +32,19 @@ def test_library_exports_every_header_symbol(lib):
 
 def test_oracle_pinned_to_reference_template():
     """Known answer: fortran/HighLExtrapTemplate_lenspotentialCls.dat is the reference's
-    high-accuracy unlensed C_l for inifiles/planck_2018.ini.  Our cosmology folds its
-    0.06 eV neutrino into massless N_eff + CDM, so the pin is at the 1% level."""
+    high-accuracy unlensed C_l for inifiles/planck_2018.ini (one 0.06 eV neutrino).  At
+    default accuracy the oracle agrees to 4e-3 (the reference's own check_accuracy
+    tolerance for unlensed TT/EE is 3e-3, 1e-3 above l=600)."""
     T = _lib.Tables(planck2018(1000))
+    assert T.view.nu_eig == 1
     icl = oracle_cls(T)
     ref = template()
     ls = T.ls
     for j, l in enumerate(ls):
         r = ref[int(l)]
-        assert abs(icl[j, 0] / r[0] - 1) < 1e-2, (l, icl[j, 0], r[0])
-        if l >= 20:
-            assert abs(icl[j, 1] / r[1] - 1) < 2e-2, (l, icl[j, 1], r[1])
-        assert abs(icl[j, 2] - r[3]) / np.sqrt(r[0] * r[1]) < 1e-2, (l, icl[j, 2], r[3])
+        assert abs(icl[j, 0] / r[0] - 1) < 4e-3, (l, icl[j, 0], r[0])
+        assert abs(icl[j, 1] / r[1] - 1) < 4e-3, (l, icl[j, 1], r[1])
+        assert abs(icl[j, 2] - r[3]) / np.sqrt(r[0] * r[1]) < 4e-3, (l, icl[j, 2], r[3])
 
 
 def test_scalar_power_known_answer():
