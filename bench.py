@@ -1,8 +1,8 @@
 """Benchmark: cosmologies/s of the GB300 scalar-perturbation path.
 
 One step = one batch of B seeded cosmology draws (each of ombh2, omch2, H0, tau,
-As, ns uniform in fiducial +-5%, massless neutrinos, unlensed scalar C_l to
-lmax=2500) through the hot path: per-k ODE sources, source k-spline + flat
+As, ns uniform in fiducial +-5%, one massive neutrino eigenstate with mnu uniform in
+0-0.2 eV, unlensed scalar C_l to lmax=2500) through the hot path: per-k ODE sources, source k-spline + flat
 line-of-sight projection, C_l.  `value` times the device pipeline on tables already
 resident in HBM (CUDA events on the library's stream); `e2e` times the C ABI call a
 user makes (cambgpu_get_results_batch: host parameters in, host C_l out, host table
@@ -39,10 +39,11 @@ def parse():
     ap.add_argument("--team", type=int, default=0)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=4)
+    ap.add_argument("--mnu-max", type=float, default=0.2)
     return ap.parse_args()
 
 
-def workload(n, lmax, seed):
+def workload(n, lmax, seed, mnu_max=0.2):
     from camb_gb300 import _lib
     rng = np.random.default_rng(seed)
     out = []
@@ -52,6 +53,9 @@ def workload(n, lmax, seed):
         p.nnu = 3.046
         for name in ["ombh2", "omch2", "H0", "optical_depth", "As", "ns"]:
             setattr(p, name, getattr(p, name) * (1 + 0.05 * (2 * rng.random() - 1)))
+        if mnu_max > 0:
+            p.mnu = mnu_max * rng.random()
+            p.num_massive_neutrinos = 1
         p.max_l = lmax
         p.max_eta_k = 2.5 * lmax
         out.append(p)
@@ -146,7 +150,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     nth = os.cpu_count() or 1
-    ps = workload(args.cpu_sample, args.lmax, seed=2024)
+    ps = workload(args.cpu_sample, args.lmax, seed=2024, mnu_max=args.mnu_max)
     for _ in range(max(1, min(args.warmup, 1))):
         cpu_reference(ps[:1], nth)
     times = [cpu_reference(ps, nth) for _ in range(args.steps)]
@@ -156,7 +160,8 @@ def run_reference(args, rank, world):
             "unit": "cosmologies/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic seeded draws",
-            "config": {"workload": f"{len(ps)} seeded draws (+-5% LCDM, massless nu) lmax={args.lmax}, CPU sample"},
+            "config": {"workload": f"{len(ps)} seeded draws (+-5% LCDM, mnu 0-{args.mnu_max:g} eV) lmax={args.lmax}, "
+                                   "CPU sample"},
             "cpu_baseline": {"value": v, "unit": "cosmologies/s", "cores": nth, "kind": "port",
                              "sample": f"{len(ps)} cosmologies per step, host tables + ODE + LOS + C_l"},
             "e2e": {"value": v, "unit": "cosmologies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -176,7 +181,7 @@ def main():
     if args.team:
         _lib.check(lib.cambgpu_set_ode_team(args.team))
     B = args.batch
-    ps = workload(B, args.lmax, seed=1000 + rank)
+    ps = workload(B, args.lmax, seed=1000 + rank, mnu_max=args.mnu_max)
     arr = (_lib.CambGpuParams * B)(*ps)
     tuned = None
     if not args.team and not args.no_autotune:
@@ -230,7 +235,7 @@ def main():
             "unit": "cosmologies/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic seeded draws",
-            "config": {"workload": f"batch of {B} seeded draws (fiducial LCDM +-5%, massless nu), "
+            "config": {"workload": f"batch of {B} seeded draws (fiducial LCDM +-5%, mnu 0-{args.mnu_max:g} eV), "
                                    f"unlensed TT/EE/TE to lmax={args.lmax}, max_eta_k={2.5 * args.lmax:g}",
                        "global_batch": B * world, "per_gpu_batch": B, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (per-cosmology tables ~3 MB x batch)",
@@ -247,7 +252,7 @@ def main():
             "clocks": clk.summary(), "wall_s_timed": wall}
     if rank == 0:
         nth = os.cpu_count() or 1
-        cps = workload(args.cpu_sample, args.lmax, seed=2024)
+        cps = workload(args.cpu_sample, args.lmax, seed=2024, mnu_max=args.mnu_max)
         cpu_reference(cps[:1], nth)
         t = cpu_reference(cps, nth)
         line["cpu_baseline"] = {"value": len(cps) / t, "unit": "cosmologies/s", "cores": nth, "kind": "port",

@@ -141,6 +141,7 @@ size_t bytes_for(const CambGpuTables& t) {
   s += 2 * r((size_t)t.ntau * t.nsrc * t.nk * 8);
   s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
   s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256);
+  s += 2 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
   return s;
 }
 
@@ -173,6 +174,18 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.grhog = t.grhog; d.grhornomass = t.grhornomass; d.grhoc = t.grhoc; d.grhob = t.grhob; d.grhov = t.grhov;
   d.tau0 = t.tau0; d.taurend = t.taurend; d.tau_maxvis = t.tau_maxvis; d.matter_verydom_tau = t.matter_verydom_tau;
   d.photbar_a = t.grhog / t.grhob;
+  d.nu_eig = t.nu_eig;
+  d.nqmax = t.nqmax;
+  for (int i = 0; i < 3; ++i) {
+    d.nu_masses[i] = t.nu_masses[i];
+    d.grhormass[i] = t.grhormass[i];
+    d.nu_tau_nonrel[i] = t.nu_tau_nonrel[i];
+  }
+  if (t.nu_eig > 0) {
+    d.nu_q = (const double*)put(t.nu_q, (size_t)t.nqmax * 8);
+    d.nu_int_kernel = (const double*)put(t.nu_int_kernel, (size_t)t.nqmax * 8);
+    d.nu_tau_notmassless = (const double*)put(t.nu_tau_notmassless, (size_t)t.nu_eig * t.nqmax * 8);
+  }
   d.thermo_horner = (const double*)put(t.thermo_horner, (size_t)t.nthermo * 16 * 8);
   d.dddotmu = (const double*)put(t.dddotmu, (size_t)t.nthermo * 8);
   d.ddddotmu = (const double*)put(t.ddddotmu, (size_t)t.nthermo * 8);
@@ -227,6 +240,7 @@ struct Batch {
   int* d_status = nullptr;
   unsigned long long* d_evals = nullptr;
   int max_ntau = 0, max_nq = 0, max_nl = 0, max_rows = 0;
+  bool massive_nu = false;  // some cosmology has massive neutrinos (thread-per-mode kernel only)
 };
 
 int stage_batch(Batch& B) {
@@ -255,6 +269,7 @@ int stage_batch(Batch& B) {
     B.max_nq = std::max(B.max_nq, B.views[c]->nq);
     B.max_nl = std::max(B.max_nl, B.views[c]->nl);
     B.max_rows = std::max(B.max_rows, B.views[c]->ntau * B.views[c]->nsrc);
+    B.massive_nu |= B.views[c]->nu_eig > 0;
   }
   std::vector<DevCosmo> hc(n);
   std::vector<const double*> hspl(n);
@@ -317,8 +332,10 @@ int stage_batch(Batch& B) {
 int size_class(const Batch& B) { return B.nitems >= 24 * g_rt.nsm ? 1 : 0; }
 
 int pick_team(const Batch& B) {
-  if (g_team) return g_team;
-  return g_tuned[size_class(B)].team;
+  int t = g_team ? g_team : g_tuned[size_class(B)].team;
+  // the warp-per-mode kernel evolves the massless-neutrino equation layout only
+  if (B.massive_nu && t >= 8) t = 2;
+  return t;
 }
 
 int run_ode(Batch& B) {
@@ -691,6 +708,8 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   double best_ms = 1e30;
   int bi = 0;
   for (int c = 0; c < nc; ++c) {
+    if (times) times[c] = 0;
+    if (B.massive_nu && cand[c][0] >= 8) continue;  // massless-only warp kernel
     g_team = cand[c][0];
     g_order = cand[c][1];
     rc = run_all(B, true, false, false);  // warm-up

@@ -11,6 +11,12 @@ struct DevCosmo {
   // background
   double grhog, grhornomass, grhoc, grhob, grhov, tau0, taurend, tau_maxvis, matter_verydom_tau;
   double photbar_a;  // grhog/grhob: photon/baryon density ratio times a
+  // massive neutrinos
+  int nu_eig, nqmax;
+  double nu_masses[3], grhormass[3], nu_tau_nonrel[3];
+  const double* nu_q;
+  const double* nu_int_kernel;
+  const double* nu_tau_notmassless;  // [nu_eig][nqmax]
   // thermal history
   const double* thermo_horner;  // [nthermo][16]
   const double* dddotmu;

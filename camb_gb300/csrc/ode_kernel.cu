@@ -764,6 +764,10 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
     w = tm.bcast_i(w, 0);
     if (w >= nitems) break;
     WorkItem it = items[w];
+    if (cosmos[it.cosmo].nu_eig > 0) {  // this kernel carries the massless-neutrino layout only
+      if (tm.t == 0) atomicExch(cosmos[it.cosmo].status, (int)CAMBGPU_ERROR_UNSUPPORTED_PARAMS);
+      continue;
+    }
     evolve_mode<T>(cosmos[it.cosmo], it.mode, tm);
   }
 }
@@ -781,7 +785,9 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
 // ---------------------------------------------------------------------------
 namespace tpm {
 
-constexpr int NV = 104;  // 4 + (64+1) + (16+1) + (14+1) at lAccuracyBoost = 1
+constexpr int NV = 320;  // largest packed scalar system handled (mode_init rejects larger ones)
+constexpr int NL = 66;
+constexpr int NUE = 3;
 
 // x**(1/5) for the step-size update: FP32 seed, two Newton steps on y^5 = x in FP64
 __device__ __forceinline__ double fifth_root(double x) {
@@ -793,39 +799,221 @@ __device__ __forceinline__ double fifth_root(double x) {
   y = 0.8 * y + 0.2 * x / y4;
   return y;
 }
-constexpr int NL = 66;
 
+// Massive-neutrino background in units of one massless eigenstate, as a function of
+// a*m/(k_B T_nu) (fits of massive_neutrinos.f90:186-216 and 325-347).
+namespace nuf {
+constexpr double zeta3 = 1.2020569031595942853997, zeta5 = 1.0369277551433699263313, zeta7 = 1.0083492773819228268397;
+constexpr double pi = 3.1415926535897932384626433832795;
+constexpr double fdc = 7.0 / 120 * pi * pi * pi * pi;
+constexpr double const2 = 5.0 / 7.0 / (pi * pi);
+__device__ __forceinline__ void rho_P(double am, double& rhonu, double& pnu) {
+  const double amin = 0.42, amax = 70.0;
+  if (am <= amin) {
+    const double am2 = am * am, am4 = am2 * am2;
+    rhonu = 1.0 + const2 * am2 + am4 * (-1.872929199948838302e-02 + am2 * 1.831728681837861694e-02);
+    pnu = (1.0 - const2 * am2) / 3.0 + am4 * (1.667044572156534468e-02 + am2 * -2.277471498716537868e-02);
+    return;
+  }
+  if (am >= amax) {
+    rhonu = 3 / (2 * fdc) * (zeta3 * am + ((15 * zeta5) / 2 - 945.0 / 16 * zeta7 / (am * am)) / am);
+    pnu = 900.0 / 120.0 / fdc * (zeta5 - 63.0 / 4 * zeta7 / (am * am)) / am;
+    return;
+  }
+  const double fc = 5.422176684690383;   // sqrt(0.42 * 70)
+  const double izm = (amax + fc) / (amax - fc);
+  const double z = ((am - fc) / (am + fc)) * izm;
+  const double rfit = (((((-2.544964203886362908e-03 * z + 2.123075360029347963e-02) * z - 8.378996019212282820e-02) * z +
+                         1.545077526625578401e-01) * z + 1.188066888581748443e-01) * z + 7.499710425926954249e-01);
+  const double pfit = ((((((-1.965863329520473827e-03 * z + 2.378742143669706002e-03) * z + 4.067958090718486880e-02) * z -
+                          2.509793530357270000e-02) * z - 2.435843189264263742e-01) * z + 3.156134695375645838e-01) * z +
+                       9.283417043601330798e-01);
+  rhonu = (1.0 + 3.0 * zeta3 / (2.0 * fdc) * am) * rfit;
+  pnu = pfit / (1.0 + fdc / ((900.0 / 120.0) * zeta5) * am);
+}
+__device__ __forceinline__ double drho(double am, double adotoa) {
+  const double amin = 0.3, amax = 70.0;
+  if (am <= amin) {
+    const double am2 = am * am;
+    return am2 * (2 * const2 + am2 * (.4399706676e-1 * log(am) - .2970400378e-2 - .29331377855e-1 * am)) * adotoa;
+  }
+  if (am >= amax) return 3 / (2 * fdc) * (zeta3 * am + (-(15 * zeta5) / 2 + 2835.0 / 16 * zeta7 / (am * am)) / am) * adotoa;
+  const double fc = 4.58257569495584;  // sqrt(0.3 * 70)
+  const double izm = (amax + fc) / (amax - fc);
+  const double z = ((am - fc) / (am + fc)) * izm;
+  const double D = (((((-3.877662402660121861e-03 * z + 1.056591590995091534e-02) * z + 3.167230341650149189e-02) * z -
+                       1.602709049602861757e-01) * z + 1.801974470841860576e-01) * z + 5.800497880734221123e-01);
+  return am * am / (1.0 + 2.0 * am) * D * adotoa;
+}
+}  // namespace nuf
+
+// per-mode control state (EvolutionVars, equations.f90:66-151), indices 0-based
 struct St {
-  double k, ik, k2, ik2, q;
-  double pig, pigdot, tight_off, poltruncfac, kptf, tr_g, tr_p, tr_n;
-  int lmaxg, lmaxgpol, lmaxnr, g_ix, pol_ix, r_ix, nvar;
-  bool tc, hk, nonu, nophot;
+  double q, k, ik, k2, ik2;
+  double pig, pigdot, tight_off, poltruncfac, kptf;
+  int lmaxg, lmaxgpol, lmaxnr, lmaxnu, nvar, n;
+  int g_ix, pol0, r_ix, nu_pert_ix, lmaxnu_pert;
+  int nu_ix[NUE], nq[NUE], lmaxnu_tau[NUE];
+  bool tc, hk, nonu, nophot, has_nu_rel;
+  bool approx[NUE], nonrel[NUE];
+  double approx_time[NUE], G11[NUE], G30[NUE], lboost[NUE];
 };
 
-// active index ranges of the flat state vector (SetupScalarArrayIndices)
-struct Ranges4 {
-  int lo[4], hi[4];
-};
-
-__device__ __forceinline__ Ranges4 active_ranges(const St& M) {
-  Ranges4 r;
-  r.lo[0] = 0;
-  r.hi[0] = 4;
-  r.lo[1] = M.g_ix;
-  r.hi[1] = M.nophot ? M.g_ix : (M.tc ? M.g_ix + 2 : M.g_ix + M.lmaxg + 1);
-  r.lo[2] = M.pol_ix + 2;
-  r.hi[2] = (M.nophot || M.tc) ? M.pol_ix + 2 : M.pol_ix + M.lmaxgpol + 1;
-  r.lo[3] = M.r_ix;
-  r.hi[3] = M.nonu ? M.r_ix : (M.hk ? M.r_ix + 3 : M.r_ix + M.lmaxnr + 1);
-  return r;
+// SetupScalarArrayIndices (equations.f90:585-701): the propagated variables are packed
+// [etak clxc clxb vb | photon T | photon E (l>=2) | massless nu | nu perturbation | massive nu]
+__device__ void setup_indices(const DevCosmo& C, St& M, bool want_max) {
+  int neq = 4;
+  if (!M.nophot) {
+    M.g_ix = 4;
+    if (M.tc) neq += 2;
+    else {
+      neq += M.lmaxg + 1;
+      M.pol0 = neq - 2;
+      neq += M.lmaxgpol - 1;
+    }
+  }
+  if (!M.nonu) {
+    M.r_ix = neq;
+    neq += M.hk ? 3 : M.lmaxnr + 1;
+  }
+  int maxeq = 4 + (M.lmaxg + 1) + (M.lmaxnr + 1) + M.lmaxgpol - 1;
+  M.has_nu_rel = false;
+  if (C.nu_eig > 0) {
+    for (int i = 0; i < C.nu_eig; ++i) M.has_nu_rel |= M.nq[i] != C.nqmax;
+    if (M.has_nu_rel) {
+      M.lmaxnu_pert = M.lmaxnu;
+      M.nu_pert_ix = neq;
+      neq += M.lmaxnu_pert + 1;
+      maxeq += M.lmaxnu_pert + 1;
+    } else {
+      M.lmaxnu_pert = 0;
+    }
+    for (int i = 0; i < C.nu_eig; ++i) {
+      const double b = M.lboost[i];
+      int lt;
+      if (M.hk) lt = (int)(4 * b);
+      else {
+        lt = max(min((int)llrint(0.8 * M.q * C.nu_tau_nonrel[i] * b), M.lmaxnu), 3);
+        if (M.nonrel[i]) lt = min(lt, (int)llrint(4 * b));
+      }
+      M.lmaxnu_tau[i] = min(M.lmaxnu, lt);
+      M.nu_ix[i] = neq;
+      neq += M.approx[i] ? 4 : M.nq[i] * (M.lmaxnu_tau[i] + 1);
+      maxeq += C.nqmax * (M.lmaxnu + 1);
+    }
+  }
+  M.n = neq;
+  if (want_max) M.nvar = maxeq;
 }
 
-#define TPM_FOR_ACTIVE(R, i, body)                                   \
-  _Pragma("unroll") for (int rr_ = 0; rr_ < 4; ++rr_) {              \
-    for (int i = (R).lo[rr_]; i < (R).hi[rr_]; ++i) { body }         \
+// CopyScalarVariableArray (equations.f90:703-791) from layout O to layout N
+__device__ void copy_vars(const DevCosmo& C, const St& O, const St& N, const double* __restrict__ y,
+                          double* __restrict__ yo) {
+  for (int i = 0; i < N.nvar; ++i) yo[i] = 0;
+  for (int i = 0; i < 4; ++i) yo[i] = y[i];
+  if (!O.nophot && !N.nophot) {
+    int lmax = (O.tc || N.tc) ? 1 : min(O.lmaxg, N.lmaxg);
+    for (int l = 0; l <= lmax; ++l) yo[N.g_ix + l] = y[O.g_ix + l];
+    if (!O.tc && !N.tc) {
+      lmax = min(O.lmaxgpol, N.lmaxgpol);
+      for (int l = 2; l <= lmax; ++l) yo[N.pol0 + l] = y[O.pol0 + l];
+    }
   }
+  if (!O.nonu && !N.nonu) {
+    const int lmax = (O.hk || N.hk) ? 2 : min(O.lmaxnr, N.lmaxnr);
+    for (int l = 0; l <= lmax; ++l) yo[N.r_ix + l] = y[O.r_ix + l];
+  }
+  for (int i = 0; i < C.nu_eig; ++i) {
+    const int off = O.nu_ix[i], off2 = N.nu_ix[i];
+    if (O.approx[i] && N.approx[i]) {
+      for (int j = 0; j < 4; ++j) yo[off2 + j] = y[off + j];
+    } else if (!O.approx[i] && !N.approx[i]) {
+      const int lmax = min(O.lmaxnu_tau[i], N.lmaxnu_tau[i]);
+      const int nq = min(O.nq[i], N.nq[i]);
+      for (int iq = 0; iq < nq; ++iq) {
+        const int a = off + iq * (O.lmaxnu_tau[i] + 1), b = off2 + iq * (N.lmaxnu_tau[i] + 1);
+        for (int l = 0; l <= lmax; ++l) yo[b + l] = y[a + l];
+      }
+      for (int iq = nq; iq < N.nq[i]; ++iq) {
+        int lm = min(N.lmaxnu_tau[i], O.lmaxnr);
+        const int b = off2 + iq * (N.lmaxnu_tau[i] + 1);
+        for (int l = 0; l <= lm; ++l) yo[b + l] = y[O.r_ix + l];
+        const double qq = C.nu_q[iq];
+        const double ps = (C.nu_masses[i] / qq) * (C.nu_masses[i] / qq) / 2;
+        lm = min(lm, O.lmaxnu_pert);
+        for (int l = 0; l <= lm; ++l) yo[b + l] = yo[b + l] + y[O.nu_pert_ix + l] * ps;
+      }
+    }
+  }
+  if (N.has_nu_rel && O.has_nu_rel) {
+    const int lmax = min(N.lmaxnu_pert, O.lmaxnu_pert);
+    for (int l = 0; l <= lmax; ++l) yo[N.nu_pert_ix + l] = y[O.nu_pert_ix + l];
+  }
+}
 
-// derivs (equations.f90:2273-2773) + sources (2775-2912) for one thread's mode
+// Nu_Integrate_L01/L012 (equations.f90:1178-1270): momentum integrals of one eigenstate
+template <bool L2>
+__device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, const double* __restrict__ y, double a,
+                                             int i, double& drhonu, double& fnu, double& dpnu, double& pinu) {
+  drhonu = fnu = dpnu = pinu = 0;
+  const double am = a * C.nu_masses[i];
+  int ind = M.nu_ix[i];
+  for (int iq = 0; iq < M.nq[i]; ++iq) {
+    const double aq = am / C.nu_q[iq], w = C.nu_int_kernel[iq];
+    const double s1 = sqrt(1.0 + aq * aq);
+    drhonu += w * y[ind] * s1;
+    fnu += w * y[ind + 1];
+    if (L2) {
+      const double v = 1.0 / s1;
+      dpnu += w * y[ind] * v;
+      pinu += w * y[ind + 2] * v;
+    }
+    ind += M.lmaxnu_tau[i] + 1;
+  }
+  ind = M.nu_pert_ix;
+  for (int iq = M.nq[i]; iq < C.nqmax; ++iq) {
+    const double qq = C.nu_q[iq], aq = am / qq, w = C.nu_int_kernel[iq];
+    const double ps = (C.nu_masses[i] / qq) * (C.nu_masses[i] / qq) / 2;
+    const double tmp = w * (y[M.r_ix] + ps * y[ind]);
+    const double s1 = sqrt(1.0 + aq * aq);
+    drhonu += tmp * s1;
+    fnu += w * (y[M.r_ix + 1] + ps * y[ind + 1]);
+    if (L2) {
+      const double v = 1.0 / s1;
+      dpnu += tmp * v;
+      pinu += w * (y[M.r_ix + 2] + ps * y[ind + 2]) * v;
+    }
+  }
+  if (L2) dpnu = dpnu / 3;
+}
+
+// Nu_pinudot (equations.f90:1272-1313)
+__device__ double nu_pinudot(const DevCosmo& C, const St& M, const double* __restrict__ y,
+                             const double* __restrict__ ydot, double a, double adotoa, int i) {
+  double pinudot = 0;
+  int ind = M.nu_ix[i] + 2;
+  const double am = a * C.nu_masses[i];
+  for (int iq = 0; iq < M.nq[i]; ++iq) {
+    const double aq = am / C.nu_q[iq], aqdot = aq * adotoa;
+    const double v = 1.0 / sqrt(1.0 + aq * aq);
+    const double vdot = -aq * aqdot * (v * v * v);
+    pinudot += C.nu_int_kernel[iq] * (ydot[ind] * v + y[ind] * vdot);
+    ind += M.lmaxnu_tau[i] + 1;
+  }
+  ind = M.nu_pert_ix + 2;
+  for (int iq = M.nq[i]; iq < C.nqmax; ++iq) {
+    const double qq = C.nu_q[iq], aq = am / qq, aqdot = aq * adotoa;
+    const double ps = (C.nu_masses[i] / qq) * (C.nu_masses[i] / qq) / 2;
+    const double v = 1.0 / sqrt(1.0 + aq * aq);
+    const double vdot = -aq * aqdot * (v * v * v);
+    const double psi2dot = ydot[M.r_ix + 2] + ps * ydot[ind];
+    const double psi2 = y[M.r_ix + 2] + ps * y[ind];
+    pinudot += C.nu_int_kernel[iq] * (psi2dot * v + psi2 * vdot);
+  }
+  return pinudot;
+}
+
+// derivs (equations.f90:2273-2773) + sources (2775-2912), one thread per mode
 __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* __restrict__ dl,
                                         const double* __restrict__ dl2, const double* __restrict__ pf, double tau,
                                         const double* __restrict__ y, double* __restrict__ dy, double* src) {
@@ -839,13 +1027,35 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
                grhog_t = C.grhog * ia2, grhov_t = C.grhov * a2;
   double dgrho = grhob_t * clxb + grhoc_t * clxc;
   double dgq = grhob_t * vb;
-  const double grho = (grhob_t + grhoc_t) + grhor_t + grhog_t + grhov_t;
-  const double gpres_noDE = (grhor_t + grhog_t) * (1.0 / 3);
+  double grhonu_t = 0, gpres_nu = 0, wnu[NUE] = {0, 0, 0};
+  for (int i = 0; i < C.nu_eig; ++i) {  // MassiveNuVars (equations.f90:1358-1401)
+    const double gm_t = C.grhormass[i] * ia2;
+    double rhonu, pnu, clxnu, qnu;
+    nuf::rho_P(a * C.nu_masses[i], rhonu, pnu);
+    if (M.approx[i]) {
+      clxnu = y[M.nu_ix[i]];
+      qnu = y[M.nu_ix[i] + 2];
+    } else {
+      double dp, pn;
+      nu_integrate<false>(C, M, y, a, i, clxnu, qnu, dp, pn);
+      const double ir = 1.0 / rhonu;
+      qnu = qnu * ir;
+      clxnu = clxnu * ir;
+    }
+    const double g_t = gm_t * rhonu;
+    grhonu_t += g_t;
+    gpres_nu += gm_t * pnu;
+    dgrho += g_t * clxnu;
+    dgq += g_t * qnu;
+    wnu[i] = pnu / rhonu;
+  }
+  const double grho = (grhonu_t + grhob_t + grhoc_t) + grhor_t + grhog_t + grhov_t;
+  const double gpres_noDE = gpres_nu + (grhor_t + grhog_t) * (1.0 / 3);
   const double g3 = grho * (1.0 / 3);
   const double iad = rsqrt(g3);
   const double adotoa = g3 * iad;
   double z = 0, dz = 0, clxr, qr, pir, clxg, qg, pig = 0;
-  const int g = M.g_ix, pol = M.pol_ix, r = M.r_ix;
+  const int g = M.g_ix, pol = M.pol0, r = M.r_ix;
   if (M.nonu) {
     z = (0.5 * dgrho * ik + etak) * iad;
     dz = -adotoa * z - 0.5 * dgrho * ik;
@@ -921,14 +1131,12 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       pigdot = dl[2] * qg - dl2[2] * y[g + 3] - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
       dy[g + 2] = pigdot;
       const int lg = M.lmaxg;
-      for (int l = 3; l < lg; ++l)
-        dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
-      dy[g + lg] = k * y[g + lg - 1] - M.tr_g * itau * y[g + lg] - opac * y[g + lg];
+      for (int l = 3; l < lg; ++l) dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
+      dy[g + lg] = k * y[g + lg - 1] - (lg + 1) * itau * y[g + lg] - opac * y[g + lg];
       dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * y[pol + 3];
       const int lp = M.lmaxgpol;
-      for (int l = 3; l < lp; ++l)
-        dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
-      dy[pol + lp] = -opac * y[pol + lp] + M.kptf * y[pol + lp - 1] - M.tr_p * itau * y[pol + lp];
+      for (int l = 3; l < lp; ++l) dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
+      dy[pol + lp] = -opac * y[pol + lp] + M.kptf * y[pol + lp - 1] - (lp + 3) * itau * y[pol + lp];
     }
   }
   double clxrdot = 0, pirdot = 0;
@@ -944,8 +1152,44 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       dy[r + 2] = pirdot;
       const int ln = M.lmaxnr;
       for (int l = 3; l < ln; ++l) dy[r + l] = dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1];
-      dy[r + ln] = k * y[r + ln - 1] - M.tr_n * itau * y[r + ln];
+      dy[r + ln] = k * y[r + ln - 1] - (ln + 1) * itau * y[r + ln];
     }
+  }
+  // massive neutrinos (equations.f90:2710-2773)
+  for (int i = 0; i < C.nu_eig; ++i) {
+    if (M.approx[i]) {
+      const double G11_t = M.G11[i] * ia * ia2, G30_t = M.G30[i] * ia * ia2;
+      const int off = M.nu_ix[i];
+      const double w = wnu[i];
+      dy[off] = -k * z * (w + 1) + 3 * adotoa * (w * y[off] - y[off + 1]) - k * y[off + 2];
+      dy[off + 1] = (3 * w - 2) * adotoa * y[off + 1] - 5.0 / 3 * k * z * w - k / 3 * G11_t;
+      dy[off + 2] = (3 * w - 1) * adotoa * y[off + 2] - k * (2.0 / 3 * y[off + 3] - y[off + 1]);
+      dy[off + 3] = (3 * w - 2) * adotoa * y[off + 3] + 2 * w * k * sigma - k / 5 * (3 * G30_t - 2 * G11_t);
+    } else {
+      int ind = M.nu_ix[i];
+      const int lt = M.lmaxnu_tau[i];
+      for (int iq = 0; iq < M.nq[i]; ++iq) {
+        const double aq = a * C.nu_masses[i] / C.nu_q[iq];
+        const double v = rsqrt(1.0 + aq * aq);
+        dy[ind] = -k * (4.0 / 3.0 * z + v * y[ind + 1]);
+        dy[ind + 1] = v * (dl[1] * y[ind] - dl2[1] * y[ind + 2]);
+        if (lt == 2) {
+          dy[ind + 2] = -dy[ind] - 3 * itau * y[ind + 2];
+        } else {
+          dy[ind + 2] = v * (dl[2] * y[ind + 1] - dl2[2] * y[ind + 3]) + k * 8.0 / 15.0 * sigma;
+          for (int l = 3; l < lt; ++l) dy[ind + l] = v * (dl[l] * y[ind + l - 1] - dl2[l] * y[ind + l + 1]);
+          dy[ind + lt] = k * v * y[ind + lt - 1] - (lt + 1) * itau * y[ind + lt];
+        }
+        ind += lt + 1;
+      }
+    }
+  }
+  if (M.has_nu_rel) {
+    const int p0 = M.nu_pert_ix, lp = M.lmaxnu_pert;
+    dy[p0] = k * a2 * qr - k * y[p0 + 1];
+    for (int l = 1; l < lp; ++l)
+      dy[p0 + l] = -a2 * (dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1]) + (dl[l] * y[p0 + l - 1] - dl2[l] * y[p0 + l + 1]);
+    dy[p0 + lp] = k * (y[p0 + lp - 1] - a2 * y[r + lp - 1]) - (lp + 1) * itau * y[p0 + lp];
   }
   if (src) {
     double Ed2 = 0, Ed3 = 0, octgdot = 0, E2s = 0;
@@ -963,10 +1207,31 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       octgdot = dy[g + 3];
     }
     if (M.nonu) pirdot = 0;
-    const double dgpi = grhor_t * pir + grhog_t * pig;
-    const double pidot_sum = grhog_t * pigdot + grhor_t * pirdot;
+    double dgpi = grhor_t * pir + grhog_t * pig;
+    double dgpi_diff = 0;
+    double pidot_sum = grhog_t * pigdot + grhor_t * pirdot;
+    for (int i = 0; i < C.nu_eig; ++i) {  // MassiveNuVarsOut (equations.f90:1113-1176)
+      const double gm_t = C.grhormass[i] * ia2;
+      double rhonu, pnu, pinu, pinudot;
+      nuf::rho_P(a * C.nu_masses[i], rhonu, pnu);
+      if (M.approx[i]) {
+        pinu = y[M.nu_ix[i] + 3];
+        pinudot = dy[M.nu_ix[i] + 3];
+      } else {
+        double clxnu, qnu, dpnu;
+        nu_integrate<true>(C, M, y, a, i, clxnu, qnu, dpnu, pinu);
+        pinu = pinu / rhonu;
+        const double rhonudot = nuf::drho(a * C.nu_masses[i], adotoa);
+        pinudot = nu_pinudot(C, M, y, dy, a, adotoa, i);
+        pinudot = pinudot / rhonu - rhonudot / rhonu * pinu;
+      }
+      const double g_t = gm_t * rhonu, gp_t = gm_t * pnu;
+      dgpi += g_t * pinu;
+      dgpi_diff += pinu * (3 * gp_t - g_t);
+      pidot_sum += g_t * pinudot;
+    }
     const double gpres = gpres_noDE - grhov_t;
-    const double diff_rhopi = pidot_sum - (4 * dgpi) * adotoa;
+    const double diff_rhopi = pidot_sum - (4 * dgpi + dgpi_diff) * adotoa;
     const double phi = -((dgrho + 3 * dgq * adotoa * ik) + dgpi) / (2 * M.k2);
     double op2, dop2, vis, dvis, ddvis, exptau;
     ionization(C, tau, itau, op2, dop2, vis, dvis, ddvis, exptau);
@@ -1003,11 +1268,18 @@ struct Work {
 struct Run {
   double src[3];
   double tau, target, sw_time, h, err, call_hmax;
-  bool src_valid;
   long long evals;
-  int j, fails, status;
-  bool active, target_is_switch, need_f, first, fsal, reset;
+  int j, fails, status, sw_kind, sw_eig;
+  bool active, target_is_switch, need_f, first, fsal, reset, src_valid;
 };
+
+enum { SW_TC = 1, SW_KTAU, SW_NU_MASSLESS, SW_NU_NONREL, SW_NU_MASSIVE, SW_NONU, SW_NOPHOT };
+
+__device__ __forceinline__ int next_nu_nq(const DevCosmo& C, int nq) {
+  if (nq == 0) return 1;
+  const int qq = (int)C.nu_q[nq - 1];
+  return qq >= 10 ? C.nqmax : nq + 1;
+}
 
 __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   const CambGpuModeSpec ms = C.modes[q_ix];
@@ -1019,29 +1291,34 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   M.lmaxg = ms.lmaxg;
   M.lmaxgpol = ms.lmaxgpol;
   M.lmaxnr = ms.lmaxnr;
-  M.g_ix = 4;
-  M.pol_ix = M.g_ix + M.lmaxg + 1;
-  M.r_ix = M.pol_ix + M.lmaxgpol + 1;
-  M.nvar = M.r_ix + M.lmaxnr + 1;
+  M.lmaxnu = ms.lmaxnu;
   M.poltruncfac = (double)M.lmaxgpol / max(1, M.lmaxgpol - 2);
   M.kptf = M.k * M.poltruncfac;
-  M.tr_g = M.lmaxg + 1;
-  M.tr_p = M.lmaxgpol + 3;
-  M.tr_n = M.lmaxnr + 1;
   M.pig = M.pigdot = 0;
   M.tight_off = ms.tight_switch_tau;
   M.tc = true;
   M.hk = M.nonu = M.nophot = false;
+  for (int i = 0; i < NUE; ++i) {
+    M.nq[i] = ms.nq0[i];
+    M.approx[i] = false;
+    M.nonrel[i] = false;
+    M.lboost[i] = ms.nu_l_boost[i];
+    M.approx_time[i] = ms.nu_approx_time[i];
+    M.G11[i] = M.G30[i] = 0;
+  }
+  M.nu_pert_ix = 0;
+  M.pol0 = 0;
+  setup_indices(C, M, true);
   R.active = true;
   R.status = 0;
-  if (M.nvar > NV || M.lmaxg >= NL || M.lmaxgpol >= 20) {
+  const int lm = max(max(M.lmaxg, M.lmaxgpol), max(M.lmaxnr, M.lmaxnu));
+  if (M.nvar > NV || lm >= NL || M.lmaxgpol >= 20 || C.nu_eig > NUE) {
     R.active = false;
     R.status = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
     return;
   }
-  const int lm = max(M.lmaxg, max(M.lmaxgpol, M.lmaxnr));
-  for (int l = 1; l <= lm && l < NL; ++l) {
-    double dn = 1.0 / (2 * l + 1);
+  for (int l = 1; l <= lm; ++l) {
+    const double dn = 1.0 / (2 * l + 1);
     W.dl[l] = dn * M.k * l;
     W.dl2[l] = dn * M.k * (l + 1);
     if (l < 20) W.pf[l] = ((double)((l + 3) * (l - 1)) / (l + 1)) * M.k * dn;
@@ -1050,7 +1327,9 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   // initial (equations.f90:1891-2112), adiabatic
   const double tau = ms.taustart, k = M.k;
   const double x = k * tau, x2 = x * x, x3 = x2 * x;
-  const double grhonu = C.grhornomass;
+  double rhomass = 0;
+  for (int i = 0; i < C.nu_eig; ++i) rhomass += C.grhormass[i];
+  const double grhonu = rhomass + C.grhornomass;
   const double om = (C.grhob + C.grhoc) / sqrt(3 * (C.grhog + grhonu));
   const double omtau = om * tau;
   const double Rv = grhonu / (grhonu + C.grhog);
@@ -1073,6 +1352,14 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   W.y[M.r_ix + 1] = -iv_qr;
   W.y[M.r_ix + 2] = -iv_pir;
   if (M.lmaxnr > 2) W.y[M.r_ix + 3] = -iv_aj3r;
+  for (int i = 0; i < C.nu_eig; ++i) {
+    int ind = M.nu_ix[i];
+    for (int iq = 0; iq < M.nq[i]; ++iq) {
+      for (int jj = 0; jj < 3; ++jj) W.y[ind + jj] = W.y[M.r_ix + jj];
+      if (M.lmaxnu_tau[i] > 2) W.y[ind + 3] = -iv_aj3r;
+      ind += M.lmaxnu_tau[i] + 1;
+    }
+  }
   R.tau = tau;
   R.j = 1;
   R.h = R.err = 0;
@@ -1086,94 +1373,154 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   R.target_is_switch = false;
   R.src_valid = false;
   R.call_hmax = 0;
+  R.sw_kind = 0;
+  R.sw_eig = 0;
 }
 
-// Picks the next integration target (EvolveScal switch logic) and performs
-// switches that fall within smallTime of the current time.  Returns false when
-// the mode is finished.
-__device__ bool next_target(const DevCosmo& C, St& M, Work& W, Run& R) {
-  for (int guard = 0; guard < 16; ++guard) {
-    if (R.j >= C.ntau) return false;
-    const double tauend = C.tau_points[R.j];
-    if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time) return false;
-    const double noSwitch = C.tau0 + 1;
-    const double smallTime = fmin(R.tau, M.ik) / 100;
-    const double switchBoost = C.AccuracyBoost * C.TimeSwitchBoost;
-    double t_ktau = noSwitch, t_nonu = noSwitch, t_nophot = noSwitch;
-    if (!M.hk && !M.nonu) t_ktau = (double)max(20, M.lmaxnr - 4) / M.k;
-    if (!M.nonu) t_nonu = fmax(15 / M.k * switchBoost, fmin(C.taurend, C.matter_verydom_tau));
-    if (!M.nophot && M.k > 0.03 * switchBoost) t_nophot = fmax(15 / M.k, C.taurend) * switchBoost;
-    const double next = fmin(fmin(t_ktau, M.tight_off), fmin(fmin(t_nonu, t_nophot), noSwitch));
-    double tgt;
-    bool is_switch;
-    if (next < tauend) {
-      if (!(next > R.tau + smallTime)) {
-        // switch at the current time without integrating
-        R.target = R.tau;
-        R.sw_time = next;
-        R.target_is_switch = true;
-        return true;
-      }
-      tgt = next;
-      is_switch = true;
-    } else {
-      tgt = tauend;
-      is_switch = false;
-    }
-    // start of a GaugeInterface_ScalEv / RungeKuttaDP45 call
-    const double ms_user = (M.q < 2e-3 && R.tau <= C.taurend) ? 2.0 : 20.0 / C.IntTolBoost;
-    R.call_hmax = R.reset ? 0.0 : ms_user;
-    R.first = R.reset;
-    if (R.reset) {
-      R.fsal = false;
-      R.fails = 0;
-      R.reset = false;
-    }
-    R.need_f = true;
-    R.target = tgt;
-    R.sw_time = tgt;
-    R.target_is_switch = is_switch;
-    return true;
-  }
-  R.status = CAMBGPU_ERROR_EVOLUTION;
-  return false;
-}
-
-__device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
+// Picks the next integration target with the switch logic of EvolveScal
+// (equations.f90:261-331) and records which switch the target is.  Returns false
+// when the mode is finished.
+__device__ bool next_target(const DevCosmo& C, St& M, Run& R) {
+  if (R.j >= C.ntau) return false;
+  const double tauend = C.tau_points[R.j];
+  if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time) return false;
   const double noSwitch = C.tau0 + 1;
+  const double smallTime = fmin(R.tau, M.ik) / 100;
   const double switchBoost = C.AccuracyBoost * C.TimeSwitchBoost;
   double t_ktau = noSwitch, t_nonu = noSwitch, t_nophot = noSwitch;
+  double t_massless = noSwitch, t_nonrel = noSwitch, t_massive = noSwitch;
+  int e_massless = 0, e_nonrel = 0, e_massive = 0;
   if (!M.hk && !M.nonu) t_ktau = (double)max(20, M.lmaxnr - 4) / M.k;
+  for (int i = 0; i < C.nu_eig; ++i) {
+    if (M.nq[i] != C.nqmax) {
+      const double t = C.nu_tau_notmassless[i * C.nqmax + next_nu_nq(C, M.nq[i]) - 1];
+      if (t < t_massless) { t_massless = t; e_massless = i; }
+    } else if (!M.nonrel[i]) {
+      if (C.nu_tau_nonrel[i] < t_nonrel) { t_nonrel = C.nu_tau_nonrel[i]; e_nonrel = i; }
+    } else if (!M.approx[i]) {
+      if (M.approx_time[i] < t_massive) { t_massive = M.approx_time[i]; e_massive = i; }
+    }
+  }
   if (!M.nonu) t_nonu = fmax(15 / M.k * switchBoost, fmin(C.taurend, C.matter_verydom_tau));
   if (!M.nophot && M.k > 0.03 * switchBoost) t_nophot = fmax(15 / M.k, C.taurend) * switchBoost;
-  const double next = R.sw_time;
-  if (next == M.tight_off) {
-    M.tc = false;
-    M.tight_off = noSwitch;
+  const double next = fmin(fmin(fmin(t_ktau, t_massless), M.tight_off),
+                           fmin(fmin(t_massive, t_nonu), fmin(fmin(t_nophot, t_nonrel), noSwitch)));
+  // the order of the reference's if-chain decides ties
+  int kind = 0, eig = 0;
+  if (next == M.tight_off) kind = SW_TC;
+  else if (next == t_ktau) kind = SW_KTAU;
+  else if (next == t_massless) { kind = SW_NU_MASSLESS; eig = e_massless; }
+  else if (next == t_nonrel) { kind = SW_NU_NONREL; eig = e_nonrel; }
+  else if (next == t_massive) { kind = SW_NU_MASSIVE; eig = e_massive; }
+  else if (next == t_nonu) kind = SW_NONU;
+  else if (next == t_nophot) kind = SW_NOPHOT;
+  double tgt;
+  bool is_switch;
+  if (next < tauend) {
+    R.sw_kind = kind;
+    R.sw_eig = eig;
+    R.sw_time = next;
+    if (!(next > R.tau + smallTime)) {  // switch at the current time without integrating
+      R.target = R.tau;
+      R.target_is_switch = true;
+      return true;
+    }
+    tgt = next;
+    is_switch = true;
+  } else {
+    tgt = tauend;
+    is_switch = false;
+  }
+  // start of a GaugeInterface_ScalEv / RungeKuttaDP45 call
+  const double ms_user = (M.q < 2e-3 && R.tau <= C.taurend) ? 2.0 : 20.0 / C.IntTolBoost;
+  R.call_hmax = R.reset ? 0.0 : ms_user;
+  R.first = R.reset;
+  if (R.reset) {
+    R.fsal = false;
+    R.fails = 0;
+    R.reset = false;
+  }
+  R.need_f = true;
+  R.target = tgt;
+  R.target_is_switch = is_switch;
+  return true;
+}
+
+// the switch branches of EvolveScal (equations.f90:333-451); layout changes repack y via yt
+__device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
+  const double noSwitch = C.tau0 + 1;
+  St N = M;
+  const int kind = R.sw_kind, e = R.sw_eig;
+  if (kind == SW_TC) {
+    N.tc = false;
+    N.tight_off = noSwitch;
+    setup_indices(C, N, false);
+    copy_vars(C, M, N, W.y, W.yt);
+    M = N;
+    for (int i = 0; i < M.nvar; ++i) W.y[i] = W.yt[i];
     R.reset = true;
     const double tau = R.tau, itau = 1.0 / tau;
     double a, cs2, opac, dopac;
     thermo_values(C, tau, itau, a, cs2, opac, dopac);
     const double kb = M.k, op2 = opac * opac;
-    const double g2 = M.pig;
-    W.y[M.g_ix + 2] = g2;
-    W.y[M.g_ix + 3] = (3.0 / 7.0) * g2 * (kb / opac) * (1.0 + dopac / op2) + (3.0 / 7.0) * M.pigdot * (kb / op2) * (-1.0);
+    W.y[M.g_ix + 2] = M.pig;
+    W.y[M.g_ix + 3] = (3.0 / 7.0) * M.pig * (kb / opac) * (1.0 + dopac / op2) + (3.0 / 7.0) * M.pigdot * (kb / op2) * (-1.0);
     const double p2 = M.pig / 4 + M.pigdot * (1.0 / opac) * (-5.0 / 8.0 - (25.0 / 16.0) * dopac / op2) +
                       M.pig * (kb / opac) * (kb / opac) * (-5.0 / 56.0);
-    W.y[M.pol_ix + 2] = p2;
-    W.y[M.pol_ix + 3] = (3.0 / 7.0) * (kb / opac) * p2 * (1.0 + dopac / op2) +
-                        (3.0 / 7.0) * (kb / op2) * ((M.pigdot / 4.0) * (1.0 + (5.0 / 2.0) * dopac / op2)) * (-1.0);
-    for (int l = 4; l <= M.lmaxg; ++l) W.y[M.g_ix + l] = 0;
-    for (int l = 4; l <= M.lmaxgpol; ++l) W.y[M.pol_ix + l] = 0;
-  } else if (next == t_ktau) {
-    M.hk = true;
-    for (int l = 3; l <= M.lmaxnr; ++l) W.y[M.r_ix + l] = 0;
-  } else if (next == t_nonu) {
-    R.reset = true;
-    M.nonu = true;
-  } else if (next == t_nophot) {
-    R.reset = true;
-    M.nophot = true;
+    W.y[M.pol0 + 2] = p2;
+    W.y[M.pol0 + 3] = (3.0 / 7.0) * (kb / opac) * p2 * (1.0 + dopac / op2) +
+                      (3.0 / 7.0) * (kb / op2) * ((M.pigdot / 4.0) * (1.0 + (5.0 / 2.0) * dopac / op2)) * (-1.0);
+  } else if (kind == SW_NU_MASSIVE) {
+    // SwitchToMassiveNuApprox (equations.f90:1072-1111)
+    const double tau = R.tau, itau = 1.0 / tau;
+    double a, cs2, opac, dopac;
+    thermo_values(C, tau, itau, a, cs2, opac, dopac, false);
+    const double a2 = a * a;
+    N.approx[e] = true;
+    setup_indices(C, N, false);
+    copy_vars(C, M, N, W.y, W.yt);
+    double rhonu, pnu, clxnu, qnu, dpnu, pinu;
+    nuf::rho_P(a * C.nu_masses[e], rhonu, pnu);
+    nu_integrate<true>(C, M, W.y, a, e, clxnu, qnu, dpnu, pinu);
+    W.yt[N.nu_ix[e]] = clxnu / rhonu;
+    W.yt[N.nu_ix[e] + 1] = dpnu / rhonu;
+    W.yt[N.nu_ix[e] + 2] = qnu / rhonu;
+    W.yt[N.nu_ix[e] + 3] = pinu / rhonu;
+    // Nu_Intvsq (equations.f90:1331-1356) on the old layout
+    double G11 = 0, G30 = 0;
+    const double am = a * C.nu_masses[e];
+    int ind = M.nu_ix[e];
+    for (int iq = 0; iq < M.nq[e]; ++iq) {
+      const double aq = am / C.nu_q[iq];
+      const double v = 1.0 / sqrt(1.0 + aq * aq);
+      G11 += C.nu_int_kernel[iq] * W.y[ind + 1] * v * v;
+      if (M.lmaxnu_tau[e] > 2) G30 += C.nu_int_kernel[iq] * W.y[ind + 3] * v * v;
+      ind += M.lmaxnu_tau[e] + 1;
+    }
+    N.G11[e] = G11 * a2 * a / rhonu;
+    N.G30[e] = G30 * a2 * a / rhonu;
+    M = N;
+    for (int i = 0; i < M.nvar; ++i) W.y[i] = W.yt[i];
+  } else {
+    if (kind == SW_KTAU) {
+      N.hk = true;
+      for (int i = 0; i < C.nu_eig; ++i) N.nq[i] = C.nqmax;
+    } else if (kind == SW_NU_MASSLESS) {
+      N.nq[e] = next_nu_nq(C, M.nq[e]);
+    } else if (kind == SW_NU_NONREL) {
+      N.nonrel[e] = true;
+    } else if (kind == SW_NONU) {
+      R.reset = true;
+      N.nonu = true;
+      for (int i = 0; i < C.nu_eig; ++i) N.nq[i] = C.nqmax;
+    } else if (kind == SW_NOPHOT) {
+      R.reset = true;
+      N.nophot = true;
+    }
+    setup_indices(C, N, false);
+    copy_vars(C, M, N, W.y, W.yt);
+    M = N;
+    for (int i = 0; i < M.nvar; ++i) W.y[i] = W.yt[i];
   }
   R.fsal = false;
 }
@@ -1181,8 +1528,8 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
 // one trial step of RungeKuttaDP45 toward R.target; returns <0 on failure
 __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   using namespace dp;
-  const Ranges4 A = active_ranges(M);
   const double tol = C.tol1;
+  const int n = M.n;
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
@@ -1193,7 +1540,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   }
   if (R.evals > kMaxEvalsPerMode) return -1;
   unsigned long long nb = 0;
-  TPM_FOR_ACTIVE(A, i, nb = max(nb, (unsigned long long)__double_as_longlong(W.y[i]) & 0x7fffffffffffffffULL);)
+  for (int i = 0; i < n; ++i) nb = max(nb, (unsigned long long)__double_as_longlong(W.y[i]) & 0x7fffffffffffffffULL);
   double ny = __longlong_as_double((long long)nb);
   ny = ny < 1.0 ? ny : 1.0;
   const double x = R.tau;
@@ -1228,22 +1575,20 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   const double c51 = hs * a51, c52 = hs * a52, c53 = hs * a53, c54 = hs * a54;
   const double c61 = hs * a61, c62 = hs * a62, c63 = hs * a63, c64 = hs * a64, c65 = hs * a65;
   const double cb1 = hs * b1, cb3 = hs * b3, cb4 = hs * b4, cb5 = hs * b5, cb6 = hs * b6;
-  TPM_FOR_ACTIVE(A, i, W.yt[i] = fma(c21, W.k1[i], W.y[i]);)
+  for (int i = 0; i < n; ++i) W.yt[i] = fma(c21, W.k1[i], W.y[i]);
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, W.yt, W.k2, nullptr);
-  TPM_FOR_ACTIVE(A, i, W.yt[i] = fma(c32, W.k2[i], fma(c31, W.k1[i], W.y[i]));)
+  for (int i = 0; i < n; ++i) W.yt[i] = fma(c32, W.k2[i], fma(c31, W.k1[i], W.y[i]));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), W.yt, W.k3, nullptr);
-  TPM_FOR_ACTIVE(A, i, W.yt[i] = fma(c43, W.k3[i], fma(c42, W.k2[i], fma(c41, W.k1[i], W.y[i])));)
+  for (int i = 0; i < n; ++i) W.yt[i] = fma(c43, W.k3[i], fma(c42, W.k2[i], fma(c41, W.k1[i], W.y[i])));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), W.yt, W.k4, nullptr);
-  TPM_FOR_ACTIVE(A, i,
-                 W.yt[i] = fma(c54, W.k4[i], fma(c53, W.k3[i], fma(c52, W.k2[i], fma(c51, W.k1[i], W.y[i]))));)
+  for (int i = 0; i < n; ++i)
+    W.yt[i] = fma(c54, W.k4[i], fma(c53, W.k3[i], fma(c52, W.k2[i], fma(c51, W.k1[i], W.y[i]))));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), W.yt, W.k5, nullptr);
-  TPM_FOR_ACTIVE(A, i,
-                 W.yt[i] = fma(c65, W.k5[i],
-                               fma(c64, W.k4[i], fma(c63, W.k3[i], fma(c62, W.k2[i], fma(c61, W.k1[i], W.y[i])))));)
+  for (int i = 0; i < n; ++i)
+    W.yt[i] = fma(c65, W.k5[i], fma(c64, W.k4[i], fma(c63, W.k3[i], fma(c62, W.k2[i], fma(c61, W.k1[i], W.y[i])))));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k6, nullptr);
-  TPM_FOR_ACTIVE(A, i,
-                 W.yt[i] = fma(cb6, W.k6[i],
-                               fma(cb5, W.k5[i], fma(cb4, W.k4[i], fma(cb3, W.k3[i], fma(cb1, W.k1[i], W.y[i])))));)
+  for (int i = 0; i < n; ++i)
+    W.yt[i] = fma(cb6, W.k6[i], fma(cb5, W.k5[i], fma(cb4, W.k4[i], fma(cb3, W.k3[i], fma(cb1, W.k1[i], W.y[i])))));
   // stage 7 (FSAL) into k2; at an output time it is the output() evaluation too
   const bool want_src = (xt == xend) && !R.target_is_switch;
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k2, want_src ? R.src : nullptr);
@@ -1251,24 +1596,22 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   R.evals += 6;
   // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry
   double num = 0, den = 1;
-  TPM_FOR_ACTIVE(A, i, {
+  for (int i = 0; i < n; ++i) {
     const double ee = fma(e7, W.k2[i], fma(e6, W.k6[i], fma(e5, W.k5[i], fma(e4, W.k4[i], fma(e3, W.k3[i], e1 * W.k1[i])))));
-    const double ae = fabs(ee);
-    const double ay = fabs(W.y[i]);
+    const double ae = fabs(ee), ay = fabs(W.y[i]);
     const double sc = ay > 1.0 ? ay : 1.0;
     if (ae * den > num * sc) {
       num = ae;
       den = sc;
     }
-  })
-  const double m = num / den;
-  R.err = m * R.h;
+  }
+  R.err = (num / den) * R.h;
   if (R.err <= tol) {
     R.tau = xt;
-    TPM_FOR_ACTIVE(A, i, {
+    for (int i = 0; i < n; ++i) {
       W.y[i] = W.yt[i];
       W.k1[i] = W.k2[i];
-    })
+    }
     R.fails = 0;
     if (xt == xend) R.fsal = true;
   } else {
@@ -1287,11 +1630,11 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
   Run R;
   int cosmo = -1, q_ix = 0;
   R.active = false;
-  for (int iter = 0;; ++iter) {
+  for (;;) {
     if (!R.active) {
-      int w = atomicAdd(counter, 1);
+      const int w = atomicAdd(counter, 1);
       if (w >= nitems) break;
-      WorkItem it = items[w];
+      const WorkItem it = items[w];
       cosmo = it.cosmo;
       q_ix = it.mode;
       mode_init(cosmos[cosmo], q_ix, M, W, R);
@@ -1299,7 +1642,7 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
         atomicExch(cosmos[cosmo].status, R.status);
         continue;
       }
-      if (!next_target(cosmos[cosmo], M, W, R)) {
+      if (!next_target(cosmos[cosmo], M, R)) {
         R.active = false;
         atomicAdd(cosmos[cosmo].evals, (unsigned long long)R.evals);
         continue;
@@ -1315,21 +1658,25 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
       continue;
     }
     if (R.tau == R.target) {
-      bool more;
+      bool more = true;
       if (R.target_is_switch) {
         apply_switch(C, M, W, R);
-        more = next_target(C, M, W, R);
       } else {
         if (!R.src_valid) {
-          double dyv[NV];
-          derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, dyv, R.src);
+          derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, W.yt, R.src);
         }
         R.evals++;  // the output() evaluation of the reference
         const int nsrc = C.nsrc, nk = C.nk;
         for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = R.src[s];
         R.j++;
-        more = next_target(C, M, W, R);
       }
+      int guard = 0;
+      for (;;) {
+        more = next_target(C, M, R);
+        if (!more || !(R.target_is_switch && R.target == R.tau) || ++guard > 16) break;
+        apply_switch(C, M, W, R);  // switches due at the current time
+      }
+      if (guard > 16) R.status = CAMBGPU_ERROR_EVOLUTION, more = false;
       if (!more) {
         if (R.status) atomicExch(C.status, R.status);
         atomicAdd(C.evals, (unsigned long long)R.evals);

@@ -51,6 +51,7 @@ class CAMBparams:
     def __init__(self, **kwargs):
         self.H0, self.ombh2, self.omch2, self.omk = 67.5, 0.022, 0.122, 0.0
         self.TCMB, self.YHe, self.nnu = 2.7255, 0.2454, 3.044
+        self.mnu, self.num_massive_neutrinos = 0.0, 1
         self.Alens = 1.0
         self.max_l, self.max_eta_k = 2500, 6250.0
         self.DoLensing = False
@@ -61,17 +62,23 @@ class CAMBparams:
         for k, v in kwargs.items():
             setattr(self, k, v)
 
-    def set_cosmology(self, H0=67.5, ombh2=0.022, omch2=0.12, omk=0.0, mnu=0.0, nnu=3.044, YHe=None,
-                      TCMB=2.7255, tau=None, Alens=1.0, **kwargs):
-        """Sets the background cosmology (model.py:641).  Massive neutrinos are not part of
-        this path yet: mnu must be 0 (all of nnu is massless).  YHe=None keeps 0.2454
-        (the BBN value at the fiducial ombh2) rather than recomputing BBN consistency."""
-        if mnu:
-            raise CAMBError("massive neutrinos are not supported by the GPU path yet (set mnu=0)")
+    def set_cosmology(self, H0=67.5, ombh2=0.022, omch2=0.12, omk=0.0, mnu=0.06, nnu=3.044, YHe=None,
+                      TCMB=2.7255, tau=None, Alens=1.0, num_massive_neutrinos=1, neutrino_hierarchy="degenerate",
+                      **kwargs):
+        """Sets the background cosmology (model.py:641).  Massive neutrinos follow the
+        degenerate hierarchy (num_massive_neutrinos eigenstates of mass mnu /
+        num_massive_neutrinos, model.py:700-745 and SetNeutrinoMasses); the normal and
+        inverted hierarchies are not part of this path.  YHe=None keeps 0.2454 (the BBN
+        value at the fiducial ombh2) rather than recomputing BBN consistency."""
         if abs(omk) > 5e-7:
             raise CAMBError("only flat models are supported")
+        if neutrino_hierarchy != "degenerate":
+            raise CAMBError("only the degenerate neutrino hierarchy is supported")
+        if mnu < 0 or (mnu > 0 and not 1 <= num_massive_neutrinos <= 3):
+            raise CAMBError("mnu must be >= 0 with 1 to 3 massive eigenstates")
         self.H0, self.ombh2, self.omch2, self.omk = H0, ombh2, omch2, omk
         self.nnu = nnu
+        self.mnu, self.num_massive_neutrinos = mnu, num_massive_neutrinos
         if YHe is not None:
             self.YHe = YHe
         self.TCMB, self.Alens = TCMB, Alens
@@ -95,7 +102,8 @@ class CAMBparams:
 
     def to_struct(self):
         s = _lib.default_params()
-        for n in ["H0", "ombh2", "omch2", "omk", "TCMB", "YHe", "nnu", "Alens", "max_l", "max_eta_k"]:
+        for n in ["H0", "ombh2", "omch2", "omk", "TCMB", "YHe", "nnu", "mnu", "num_massive_neutrinos", "Alens",
+                  "max_l", "max_eta_k"]:
             setattr(s, n, getattr(self, n))
         s.max_l = int(self.max_l)
         s.optical_depth = self.Reion.optical_depth
@@ -110,14 +118,14 @@ class CAMBparams:
         return s
 
 
-def set_params(cp=None, lmax=None, H0=None, ombh2=0.022, omch2=0.12, omk=0.0, mnu=0.0, nnu=3.044, YHe=None,
+def set_params(cp=None, lmax=None, H0=None, ombh2=0.022, omch2=0.12, omk=0.0, mnu=0.06, nnu=3.044, YHe=None,
                tau=None, As=2e-9, ns=0.96, nrun=0, pivot_scalar=0.05, lens_potential_accuracy=0, max_eta_k=None,
-               DoLensing=False, **kwargs):
+               DoLensing=False, num_massive_neutrinos=1, **kwargs):
     """camb.set_params (camb.py:135) restricted to the parameters of the GPU scalar path."""
     cp = cp or CAMBparams()
     cp.DoLensing = DoLensing
     cp.set_cosmology(H0=H0 if H0 is not None else 67.5, ombh2=ombh2, omch2=omch2, omk=omk, mnu=mnu, nnu=nnu,
-                     YHe=YHe, tau=tau)
+                     YHe=YHe, tau=tau, num_massive_neutrinos=num_massive_neutrinos)
     cp.InitPower.set_params(As=As, ns=ns, nrun=nrun, pivot_scalar=pivot_scalar)
     if lmax is not None:
         cp.set_for_lmax(lmax, max_eta_k=max_eta_k, lens_potential_accuracy=lens_potential_accuracy)

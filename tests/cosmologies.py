@@ -46,14 +46,18 @@ def planck2018(lmax=1000):
     return p
 
 
-def draws(n, seed=1234, lmax=1000, frac=0.05):
-    """Seeded draws, each parameter uniform in fiducial +-5% (the batch configuration)."""
+def draws(n, seed=1234, lmax=1000, frac=0.05, mnu_max=0.0):
+    """Seeded draws, each parameter uniform in fiducial +-5% (the batch configuration);
+    with mnu_max > 0 one massive eigenstate of mass uniform in [0, mnu_max] eV."""
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(n):
         p = fiducial(lmax)
         for name in ["ombh2", "omch2", "H0", "optical_depth", "As", "ns"]:
             setattr(p, name, getattr(p, name) * (1 + frac * (2 * rng.random() - 1)))
+        if mnu_max > 0:
+            p.mnu = mnu_max * rng.random()
+            p.num_massive_neutrinos = 1
         out.append(p)
     return out
 
