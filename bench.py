@@ -103,8 +103,9 @@ class Clocks:
                 "reasons": reasons, "samples": len(sm)}
 
 
-def cpu_reference(params, nthreads):
-    """Reference CPU path on the host cores: host tables + restated ODE/LOS/C_l."""
+def cpu_reference(params, nthreads, keep=None):
+    """Reference CPU path on the host cores: host tables + restated ODE/LOS/C_l.  With
+    keep=list, appends (sampled ls, C_l at those ls) of each cosmology."""
     from camb_gb300 import _lib
     from oracle import oracle as orc
     t0 = time.perf_counter()
@@ -112,8 +113,31 @@ def cpu_reference(params, nthreads):
         T = _lib.Tables(p)
         src = orc.evolve_sources(T, nthreads)
         d = orc.los(T, src, nthreads)
-        orc.cls(T, d)
+        icl = orc.cls(T, d)
+        if keep is not None:
+            keep.append((T.ls, icl))
     return time.perf_counter() - t0
+
+
+def accuracy_vs_fp64(params, ref, lmax):
+    """max |dC_l/C_l| (TT, EE) and max |dTE|/sqrt(TT EE) over the sampled l of the GPU
+    C_l (through cambgpu_get_results_batch) against the FP64 CPU restatement."""
+    from camb_gb300 import _lib
+    lib = _lib.load()
+    n = len(params)
+    arr = (_lib.CambGpuParams * n)(*params)
+    cls = np.zeros((n, lmax + 1, 4))
+    st = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.cambgpu_get_results_batch(arr, n, lmax, _lib.dptr(cls), _lib.iptr(st)))
+    tt = ee = te = 0.0
+    for i, (ls, icl) in enumerate(ref):
+        m = (ls >= 2) & (ls <= lmax)
+        g, r = cls[i][ls[m]], icl[m]
+        tt = max(tt, float(np.max(np.abs(g[:, 0] / r[:, 0] - 1))))
+        ee = max(ee, float(np.max(np.abs(g[:, 1] / r[:, 1] - 1))))
+        te = max(te, float(np.max(np.abs(g[:, 3] - r[:, 2]) / np.sqrt(r[:, 0] * r[:, 1]))))
+    return {"vs": "FP64 CPU restatement, same draws as cpu_baseline", "max_rel_TT": tt, "max_rel_EE": ee,
+            "max_TE_over_sqrt_TTEE": te}
 
 
 def dist_setup(args):
@@ -229,7 +253,10 @@ def main():
     _lib.check(lib.cambgpu_probe_fp64_tflops(C.byref(tf)))
     ode_ms = stage[0] / args.steps
     evals_step = evals / args.steps
-    flops_per_eval = float(os.environ.get("CAMBGPU_FLOPS_PER_EVAL", "640"))
+    # FP64 flops per right-hand-side evaluation, stage combinations and error norm
+    # included: 2*DFMA + DMUL + DADD thread instructions per evaluation counted by ncu on
+    # this workload (mnu 0-0.2 eV, lmax 2500), profiles/ode_thread_kernel_batch32_lmax2500.md
+    flops_per_eval = float(os.environ.get("CAMBGPU_FLOPS_PER_EVAL", "1315"))
     achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
     line = {"metric": "cosmologies/s (unlensed scalar C_l to l=2500, FP64)", "value": value,
             "unit": "cosmologies/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -254,7 +281,9 @@ def main():
         nth = os.cpu_count() or 1
         cps = workload(args.cpu_sample, args.lmax, seed=2024, mnu_max=args.mnu_max)
         cpu_reference(cps[:1], nth)
-        t = cpu_reference(cps, nth)
+        ref = []
+        t = cpu_reference(cps, nth, keep=ref)
+        line["accuracy"] = accuracy_vs_fp64(cps, ref, args.lmax)
         line["cpu_baseline"] = {"value": len(cps) / t, "unit": "cosmologies/s", "cores": nth, "kind": "port",
                                 "sample": f"{len(cps)} draws of the same workload, host tables + ODE + LOS + C_l"}
         print(json.dumps(line))
