@@ -34,6 +34,7 @@ class CambGpuParams(C.Structure):
         ("BessIntBoost", C.c_double),
         ("TimeSwitchBoost", C.c_double), ("LimberBoost", C.c_double), ("BackgroundTimeStepBoost", C.c_double),
         ("accurate_polarization", C.c_int), ("accurate_reionization", C.c_int),
+        ("LensingBoost", C.c_double),
     ]
 
 
@@ -71,6 +72,8 @@ class CambGpuTables(C.Structure):
         ("accurate_polarization", C.c_int), ("accurate_reionization", C.c_int),
         ("As", C.c_double), ("ns", C.c_double), ("nrun", C.c_double), ("pivot_scalar", C.c_double),
         ("Alens", C.c_double),
+        ("max_l", C.c_int), ("do_lensing", C.c_int), ("cl_template_scale", C.c_double),
+        ("lens_accuracy_boost", C.c_double),
     ]
 
 
@@ -88,6 +91,9 @@ SIGNATURES = {
     "cambgpu_los_flat_noalloc": (C.c_int, [C.POINTER(CambGpuTables), C.c_void_p, C.c_void_p, C.c_void_p]),
     "cambgpu_get_results": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, _c_double_p]),
     "cambgpu_get_results_batch": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, _c_double_p, _c_int_p]),
+    "cambgpu_get_spectra_batch": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, _c_double_p, _c_double_p,
+                                              _c_double_p, _c_int_p, _c_int_p]),
+    "cambgpu_lensing_range": (C.c_int, [C.POINTER(CambGpuTables), _c_int_p]),
     "cambgpu_batch_prepare": (C.c_int, [C.POINTER(CambGpuParams), C.c_int]),
     "cambgpu_batch_run": (C.c_int, [_c_double_p]),
     "cambgpu_batch_fetch": (C.c_int, [C.c_int, _c_double_p]),

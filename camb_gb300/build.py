@@ -15,7 +15,8 @@ LIB = os.path.join(BUILD, "libcambgpu.so")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["ode_kernel.cu", "los_kernel.cu", "capi.cu", "noalloc.cu"]
+CU_SOURCES = ["ode_kernel.cu", "los_kernel.cu", "cl_lensing.cu", "capi.cu", "noalloc.cu"]
+TEMPLATE = os.path.join(HERE, "data", "highl_template.f64")
 CXX_SOURCES = ["host/cosmo_host.cpp"]
 
 
@@ -26,6 +27,18 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+def _template_source(path):
+    """C++ source holding the high-L template table (data/highl_template.f64) as hex floats."""
+    import struct
+    raw = open(TEMPLATE, "rb").read()
+    vals = struct.unpack("<%dd" % (len(raw) // 8), raw)
+    assert len(vals) == 8001 * 4
+    body = ",\n".join(", ".join(float(v).hex() for v in vals[i:i + 8]) for i in range(0, len(vals), 8))
+    with open(path, "w") as f:
+        f.write("namespace cgdev {\nextern const double kHighLTemplate[8001 * 4];\n"
+                "const double kHighLTemplate[8001 * 4] = {\n" + body + "};\n}\n")
+
+
 def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in CU_SOURCES + CXX_SOURCES]
@@ -33,6 +46,7 @@ def build(verbose=False, force=False):
     for root, _, files in os.walk(CSRC):
         hdrs += [os.path.join(root, f) for f in files if f.endswith((".cuh", ".hpp", ".h"))]
     hdrs.append(os.path.join(HERE, "..", "include", "cambgpu.h"))
+    hdrs.append(TEMPLATE)
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(f) < t for f in srcs + hdrs):
@@ -49,6 +63,10 @@ def build(verbose=False, force=False):
         objs.append(o)
         cmds.append(["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c",
                      os.path.join(CSRC, s), "-o", o])
+    tsrc = os.path.join(BUILD, "highl_template.cpp")
+    _template_source(tsrc)
+    objs.append(os.path.join(BUILD, "highl_template.o"))
+    cmds.append(["g++", "-O1", "-std=c++17", "-fPIC", "-c", tsrc, "-o", objs[-1]])
     with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
         outs = list(ex.map(_run, cmds))
     if verbose:

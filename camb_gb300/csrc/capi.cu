@@ -90,6 +90,19 @@ struct Runtime {
   // pinned staging for uploads
   char* pinned = nullptr;
   size_t pinned_cap = 0;
+  // high-L template on the device (uploaded once)
+  double* d_tmpl = nullptr;
+  // lensing theta-grid tables, keyed by their geometry
+  struct DevLensGeom {
+    int lmin, lmax, npoints, apw, interp_fac;
+    double dtheta;
+    double* tab;
+    double* roots;
+    double* sinth;
+    int* lsj;
+    int nj;
+  };
+  std::vector<DevLensGeom> lens;
 };
 Runtime g_rt;
 std::mutex g_mu;
@@ -126,6 +139,108 @@ int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x) {
   return 0;
 }
 
+int device_template(double** out) {
+  if (!g_rt.d_tmpl) {
+    CUDA_TRY(cudaMalloc(&g_rt.d_tmpl, sizeof(double) * 8001 * 4));
+    CUDA_TRY(cudaMemcpy(g_rt.d_tmpl, kHighLTemplate, sizeof(double) * 8001 * 4, cudaMemcpyHostToDevice));
+  }
+  *out = g_rt.d_tmpl;
+  return 0;
+}
+
+// Lensing l range and theta grid of one cosmology: LensingExtrapLmax (lensing.f90:161-177),
+// InitLensedClArrays (:230-247) and the sampling set-up of CorrFuncFullSkyApodized
+// (:378-429) with AccurateBB off and the targeted-accuracy theta boost on.
+struct HostLensGeom {
+  int lmin = 2, lmax = 0, lmax_lensed = 0, npoints = 0, apw = 0, interp_fac = 1;
+  double dtheta = 0;
+  std::vector<int> lsj;
+  bool same(const Runtime::DevLensGeom& g) const {
+    return g.lmin == lmin && g.lmax == lmax && g.npoints == npoints && g.apw == apw && g.interp_fac == interp_fac &&
+           g.dtheta == dtheta;
+  }
+};
+
+int lens_geometry(const CambGpuTables& t, HostLensGeom& g) {
+  const int margin = 200, gap = 50;  // lens_output_margin, lens_convolution_gap
+  const double pi = 3.1415926535897932384626433832795;
+  const int max_l = t.max_l;
+  const double boost = t.lens_accuracy_boost;
+  const int output_lmax = max_l - margin;
+  const int extrap = std::max(750, (int)std::ceil((0.45 * output_lmax + 400.0) * boost));
+  g.lmax = std::max(std::min(8000, output_lmax + gap + extrap), max_l);
+  int ix = t.nl - 2;
+  while (ix > 0 && t.ls[ix] > max_l - (margin - gap)) --ix;
+  g.lmax_lensed = std::max(t.ls[ix], max_l - margin);
+  double ramp = std::min(1.0, std::max(0.0, ((double)output_lmax - 2500.0) / 1000.0));
+  ramp = ramp * ramp * (3.0 - 2.0 * ramp);
+  const double theta_boost = boost * (1.6 + 0.6 * ramp);
+  int npoints = (int)(max_l * 2 * theta_boost);
+  if (npoints < 2) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lensing theta grid too small");
+  g.dtheta = pi / npoints;
+  g.apw = (int)std::lround(0.012 / g.dtheta);
+  npoints = (int)(pi / g.dtheta);
+  const double range_fac = std::max(1.0, 32 / boost);
+  g.npoints = (int)(npoints / range_fac);
+  g.interp_fac = std::max(1, std::min((int)std::lround(10 / boost), (int)(range_fac * 2) - 1));
+  g.lsj.clear();
+  for (int l = g.lmin; l <= g.lmax; ++l)
+    if (l <= 15 || (l - 15) % g.interp_fac == g.interp_fac / 2) g.lsj.push_back(l);
+  if (g.npoints < 2 || g.lmax_lensed < g.lmin || max_l < 10)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lensing needs max_l >= 10");
+  return 0;
+}
+
+// device d-table of a lensing geometry, built on first use and cached
+int device_lens_geom(const HostLensGeom& h, LensGeomDev& G) {
+  Runtime::DevLensGeom* found = nullptr;
+  for (auto& g : g_rt.lens)
+    if (h.same(g)) found = &g;
+  if (!found) {
+    if (g_rt.lens.size() >= 2) {
+      auto& o = g_rt.lens.front();
+      cudaFree(o.tab);
+      cudaFree(o.roots);
+      cudaFree(o.sinth);
+      cudaFree(o.lsj);
+      g_rt.lens.erase(g_rt.lens.begin());
+    }
+    Runtime::DevLensGeom g{h.lmin, h.lmax, h.npoints, h.apw, h.interp_fac, h.dtheta,
+                           nullptr, nullptr, nullptr, nullptr, (int)h.lsj.size()};
+    const int npts = h.npoints - 1;
+    const size_t ntab = (size_t)7 * (h.lmax + 1) * npts;
+    CUDA_TRY(cudaMalloc(&g.tab, ntab * 8));
+    CUDA_TRY(cudaMalloc(&g.roots, (size_t)(h.lmax + 6) * 8));
+    CUDA_TRY(cudaMalloc(&g.sinth, (size_t)npts * 8));
+    CUDA_TRY(cudaMalloc(&g.lsj, h.lsj.size() * 4));
+    std::vector<double> roots(h.lmax + 6), sinth(npts);
+    roots[0] = 0;
+    for (int l = 0; l <= h.lmax + 4; ++l) roots[l + 1] = std::sqrt((double)l);
+    for (int ii = 0; ii < npts; ++ii) sinth[ii] = std::sin((ii + 1) * h.dtheta);
+    CUDA_TRY(cudaMemcpy(g.roots, roots.data(), roots.size() * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(g.sinth, sinth.data(), sinth.size() * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(g.lsj, h.lsj.data(), h.lsj.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemsetAsync(g.tab, 0, ntab * 8, g_rt.stream));
+    CUDA_TRY(launch_lens_geom(g.tab, h.lmin, h.lmax, npts, h.dtheta, g_rt.stream));
+    g_launches++;
+    g_rt.lens.push_back(g);
+    found = &g_rt.lens.back();
+  }
+  G.tab = found->tab;
+  G.roots = found->roots;
+  G.sinth = found->sinth;
+  G.lsj = found->lsj;
+  G.nj = found->nj;
+  G.lmin = h.lmin;
+  G.lmax = h.lmax;
+  G.npts = h.npoints - 1;
+  G.npoints = h.npoints;
+  G.apodize_point_width = h.apw;
+  G.interp_fac = h.interp_fac;
+  G.dtheta = h.dtheta;
+  return 0;
+}
+
 // per-cosmology upload plan
 struct Upload {
   const CambGpuTables* t;
@@ -142,6 +257,7 @@ size_t bytes_for(const CambGpuTables& t) {
   s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
   s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256);
   s += 2 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
+  s += r((size_t)(t.max_l + 1) * 6 * 8) + r((size_t)(t.max_l + 1) * 4 * 8);  // all-l C_l, lensed C_l
   return s;
 }
 
@@ -212,6 +328,11 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.nq = t.nq;
   d.ls = (const int*)put(t.ls, (size_t)t.nl * 4);
   d.nl = t.nl;
+  d.max_l = t.max_l;
+  d.cl_template_scale = t.cl_template_scale;
+  d.all_cl = g_rt.arena.take<double>((size_t)(t.max_l + 1) * 6);
+  d.lensed = nullptr;
+  d.lmax_lensed = 0;
   spline_factors(t, u.spl);
   double *bh, *bx;
   int rc = device_bessel(t, &bh, &bx);
@@ -241,14 +362,58 @@ struct Batch {
   unsigned long long* d_evals = nullptr;
   int max_ntau = 0, max_nq = 0, max_nl = 0, max_rows = 0;
   bool massive_nu = false;  // some cosmology has massive neutrinos (thread-per-mode kernel only)
+  // cosmologies to lens, grouped by lensing geometry
+  struct LensGroup {
+    HostLensGeom h;
+    std::vector<int> cidx;
+    int* d_cidx = nullptr;
+    double *prep = nullptr, *sg = nullptr, *corr = nullptr;
+    int lmax_lensed_max = 0;
+  };
+  std::vector<LensGroup> lens_groups;
+  // packed outputs [n][out_lmax+1][4 | 4 | 3]
+  int out_lmax = 0;
+  double *d_unl = nullptr, *d_len = nullptr, *d_pot = nullptr;
 };
 
-int stage_batch(Batch& B) {
+int stage_batch(Batch& B, int lmax_out = 0) {
   int rc = rt_init();
   if (rc) return rc;
   int n = (int)B.views.size();
   size_t total = 0;
   for (auto* v : B.views) total += bytes_for(*v);
+  // lensing groups and their scratch
+  B.lens_groups.clear();
+  std::vector<int> lens_lmax_lensed(n, 0);
+  for (int c = 0; c < n; ++c) {
+    const CambGpuTables& v = *B.views[c];
+    if (v.nl > 512) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "too many sampled l");
+    if (!v.do_lensing) continue;
+    HostLensGeom h;
+    rc = lens_geometry(v, h);
+    if (rc) return rc;
+    lens_lmax_lensed[c] = h.lmax_lensed;
+    Batch::LensGroup* grp = nullptr;
+    for (auto& g : B.lens_groups)
+      if (g.h.lmax == h.lmax && g.h.npoints == h.npoints && g.h.apw == h.apw && g.h.interp_fac == h.interp_fac &&
+          g.h.dtheta == h.dtheta)
+        grp = &g;
+    if (!grp) {
+      B.lens_groups.push_back(Batch::LensGroup{});
+      grp = &B.lens_groups.back();
+      grp->h = h;
+    }
+    grp->cidx.push_back(c);
+    grp->lmax_lensed_max = std::max(grp->lmax_lensed_max, h.lmax_lensed);
+  }
+  auto rr = [](size_t b) { return (b + 255) & ~size_t(255); };
+  for (auto& g : B.lens_groups) {
+    size_t nc = g.cidx.size(), npts = (size_t)g.h.npoints - 1, L = (size_t)g.h.lmax + 1;
+    total += rr(nc * 4) + rr(nc * 4 * L * 8) + rr(nc * npts * 2 * 8) + rr(4 * npts * nc * 8);
+  }
+  B.out_lmax = lmax_out;
+  for (auto* v : B.views) B.out_lmax = std::max(B.out_lmax, v->max_l);
+  total += 2 * rr((size_t)n * (B.out_lmax + 1) * 4 * 8) + rr((size_t)n * (B.out_lmax + 1) * 3 * 8);
   size_t nitems = 0;
   for (auto* v : B.views) nitems += v->nk;
   total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + 2 * (nitems * sizeof(WorkItem) + 255) +
@@ -279,6 +444,23 @@ int stage_batch(Batch& B) {
     copies.push_back({p, {B.ups[c].spl.data(), B.ups[c].spl.size() * 8}});
     hspl[c] = p;
   }
+  for (int c = 0; c < n; ++c) {
+    if (!B.views[c]->do_lensing) continue;
+    B.ups[c].d.lmax_lensed = lens_lmax_lensed[c];
+    B.ups[c].d.lensed = g_rt.arena.take<double>((size_t)(B.views[c]->max_l + 1) * 4);
+    hc[c] = B.ups[c].d;
+  }
+  for (auto& g : B.lens_groups) {
+    size_t nc = g.cidx.size(), npts = (size_t)g.h.npoints - 1, L = (size_t)g.h.lmax + 1;
+    g.d_cidx = g_rt.arena.take<int>(nc);
+    copies.push_back({g.d_cidx, {g.cidx.data(), nc * 4}});
+    g.prep = g_rt.arena.take<double>(nc * 4 * L);
+    g.sg = g_rt.arena.take<double>(nc * npts * 2);
+    g.corr = g_rt.arena.take<double>(4 * npts * nc);
+  }
+  B.d_unl = g_rt.arena.take<double>((size_t)n * (B.out_lmax + 1) * 4);
+  B.d_len = g_rt.arena.take<double>((size_t)n * (B.out_lmax + 1) * 4);
+  B.d_pot = g_rt.arena.take<double>((size_t)n * (B.out_lmax + 1) * 3);
   B.d_cosmos = g_rt.arena.take<DevCosmo>(n);
   copies.push_back({B.d_cosmos, {hc.data(), (size_t)n * sizeof(DevCosmo)}});
   B.d_spl = g_rt.arena.take<const double*>(n);
@@ -376,6 +558,36 @@ int run_cls(Batch& B) {
   scal_cls_kernel<<<g, 256, 0, g_rt.stream>>>(B.d_cosmos);
   g_launches++;
   CUDA_TRY(cudaGetLastError());
+  // InterpolateCls to every l, then lens_Cls for the cosmologies that want lensing
+  double* tmpl = nullptr;
+  int rc = device_template(&tmpl);
+  if (rc) return rc;
+  CUDA_TRY(launch_interp_cls(B.d_cosmos, n, tmpl, g_rt.stream));
+  g_launches++;
+  for (auto& grp : B.lens_groups) {
+    LensGeomDev G;
+    rc = device_lens_geom(grp.h, G);
+    if (rc) return rc;
+    CUDA_TRY(launch_lensing(B.d_cosmos, grp.d_cidx, (int)grp.cidx.size(), tmpl, G, grp.lmax_lensed_max, grp.prep,
+                            grp.sg, grp.corr, g_rt.stream));
+    g_launches += 4;
+  }
+  return 0;
+}
+
+// packs the requested outputs on the device and copies them to the host
+int fetch_spectra(Batch& B, int lmax_out, double* unl, double* len, double* pot) {
+  int n = (int)B.views.size();
+  if (lmax_out > B.out_lmax) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lmax_out above the staged outputs");
+  CUDA_TRY(launch_pack_spectra(B.d_cosmos, n, lmax_out, unl ? B.d_unl : nullptr, len ? B.d_len : nullptr,
+                               pot ? B.d_pot : nullptr, g_rt.stream));
+  g_launches++;
+  size_t m = (size_t)n * (lmax_out + 1);
+  if (unl) CUDA_TRY(cudaMemcpyAsync(unl, B.d_unl, m * 4 * 8, cudaMemcpyDeviceToHost, g_rt.stream));
+  if (len) CUDA_TRY(cudaMemcpyAsync(len, B.d_len, m * 4 * 8, cudaMemcpyDeviceToHost, g_rt.stream));
+  if (pot) CUDA_TRY(cudaMemcpyAsync(pot, B.d_pot, m * 3 * 8, cudaMemcpyDeviceToHost, g_rt.stream));
+  CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+  g_d2h += (long long)m * 8 * ((unl ? 4 : 0) + (len ? 4 : 0) + (pot ? 3 : 0));
   return 0;
 }
 
@@ -512,17 +724,6 @@ int build_handles(const CambGpuParams* p, int n, std::vector<Handle*>& hs, int* 
   return worst;
 }
 
-void finish_cls(const Handle& h, const double* icl, int lmax_out, double* cl_out) {
-  // InterpolateCls (cmbmain.f90:3523-3570) without the high-l template: plain spline
-  for (int l = 0; l <= lmax_out; ++l)
-    for (int c = 0; c < 4; ++c) cl_out[(size_t)l * 4 + c] = 0;
-  const std::vector<int>& ls = h.c.ls;
-  int lmax = std::min(lmax_out, ls.back());
-  // columns: TT(0) EE(1) TE(2) -> output TT EE BB TE
-  cg::interpolate_cls(ls, icl + 0, 6, ls[0], lmax, cl_out + 0, 4);
-  cg::interpolate_cls(ls, icl + 1, 6, ls[0], lmax, cl_out + 1, 4);
-  cg::interpolate_cls(ls, icl + 2, 6, ls[0], lmax, cl_out + 3, 4);
-}
 
 }  // namespace
 
@@ -539,6 +740,7 @@ void cambgpu_default_params(CambGpuParams* p) {
   p->TimeSwitchBoost = p->LimberBoost = p->BackgroundTimeStepBoost = 1;
   p->accurate_polarization = 1;
   p->accurate_reionization = 1;
+  p->LensingBoost = 1;
 }
 
 int cambgpu_tables_create(const CambGpuParams* p, void** handle) {
@@ -611,28 +813,39 @@ int cambgpu_calc_scal_cls(const CambGpuTables* t, const double* delta, double* i
   return 0;
 }
 
-int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, double* cl_out, int* status) {
+int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
+                              double* lens_potential, int* lmax_lensed, int* status) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
+  if (lmax_out < 0 || lmax_out > 8000) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lmax_out out of range");
   std::vector<Handle*> hs;
   int rc = build_handles(p, n, hs, status);
   struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
   if (rc) return rc;
   Batch B;
   for (auto* h : hs) B.views.push_back(&h->view);
-  rc = stage_batch(B);
+  rc = stage_batch(B, lmax_out);
   if (rc) return rc;
   rc = run_all(B, true, true, true);
   if (rc) return rc;
   rc = check_status(B, status);
   if (rc) return rc;
-  std::vector<double> icl;
-  for (int c = 0; c < n; ++c) {
-    icl.resize((size_t)hs[c]->view.nl * 6);
-    CUDA_TRY(cudaMemcpy(icl.data(), B.ups[c].d.icl, icl.size() * 8, cudaMemcpyDeviceToHost));
-    g_d2h += (long long)icl.size() * 8;
-    finish_cls(*hs[c], icl.data(), lmax_out, cl_out + (size_t)c * (lmax_out + 1) * 4);
-  }
+  if (lmax_lensed)
+    for (int c = 0; c < n; ++c) lmax_lensed[c] = B.ups[c].d.lensed ? B.ups[c].d.lmax_lensed : 0;
+  return fetch_spectra(B, lmax_out, unlensed, lensed, lens_potential);
+}
+
+int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, double* cl_out, int* status) {
+  return cambgpu_get_spectra_batch(p, n, lmax_out, cl_out, nullptr, nullptr, nullptr, status);
+}
+
+int cambgpu_lensing_range(const CambGpuTables* t, int* out3) {
+  HostLensGeom h;
+  int rc = lens_geometry(*t, h);
+  if (rc) return rc;
+  out3[0] = h.lmax;
+  out3[1] = h.lmax_lensed;
+  out3[2] = h.npoints - 1;
   return 0;
 }
 
@@ -666,14 +879,7 @@ int cambgpu_batch_run(double* ms3) {
 int cambgpu_batch_fetch(int lmax_out, double* cl_out) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
-  std::vector<double> icl;
-  for (size_t c = 0; c < g_res->handles.size(); ++c) {
-    const Handle& h = *g_res->handles[c];
-    icl.resize((size_t)h.view.nl * 6);
-    CUDA_TRY(cudaMemcpy(icl.data(), g_res->B.ups[c].d.icl, icl.size() * 8, cudaMemcpyDeviceToHost));
-    finish_cls(h, icl.data(), lmax_out, cl_out + c * (size_t)(lmax_out + 1) * 4);
-  }
-  return 0;
+  return fetch_spectra(g_res->B, lmax_out, cl_out, nullptr, nullptr);
 }
 
 void cambgpu_batch_release(void) {

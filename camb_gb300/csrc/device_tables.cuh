@@ -3,6 +3,8 @@
 #pragma once
 #include <cstdint>
 
+#include <cuda_runtime.h>
+
 #include "../../include/cambgpu.h"
 
 namespace cgdev {
@@ -39,6 +41,10 @@ struct DevCosmo {
   double* dd_src;      // [ntau][nsrc][nk] spline second derivatives in k
   double* delta;       // [nq][nl][nsrc]
   double* icl;         // [nl][6]
+  double* all_cl;      // [max_l+1][6] InterpolateCls output, TT EE TE PP PT PE
+  double* lensed;      // [lmax_lensed+1][4] TT EE BB TE (lensed cosmologies only)
+  int max_l, lmax_lensed;
+  double cl_template_scale;
   int* status;         // per-cosmology status word
   unsigned long long* evals;  // derivative evaluations (shared counter)
   // integration grid and l sampling
@@ -61,5 +67,25 @@ struct WorkItem {
   int cosmo;
   int mode;
 };
+
+// theta grid and Legendre / Wigner-d table of the lensing correlation sums
+struct LensGeomDev {
+  const double* tab;     // [7][lmax+1][npts]: P, dP, d11, d-11, d22, d2-2, d20
+  const double* roots;   // sqrt(l) at [l+1], l in [-1, lmax+4]
+  const double* sinth;   // [npts]
+  const int* lsj;        // sub-sampled l of the correlation sums
+  int nj, lmin, lmax, npts, npoints, apodize_point_width, interp_fac;
+  double dtheta;
+};
+
+extern const double kHighLTemplate[8001 * 4];  // TT EE TE PP by l (generated at build time)
+
+cudaError_t launch_interp_cls(const DevCosmo* cosmos, int n, const double* tmpl, cudaStream_t s);
+cudaError_t launch_lens_geom(double* tab, int lmin, int lmax, int npts, double dtheta, cudaStream_t s);
+cudaError_t launch_lensing(const DevCosmo* cosmos, const int* cidx, int nc, const double* tmpl,
+                           const LensGeomDev& G, int lmax_lensed_max, double* prep, double* sg, double* corr,
+                           cudaStream_t s);
+cudaError_t launch_pack_spectra(const DevCosmo* cosmos, int n, int lmax_out, double* unl, double* len, double* pot,
+                                cudaStream_t s);
 
 }  // namespace cgdev

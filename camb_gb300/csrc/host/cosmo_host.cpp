@@ -1512,22 +1512,13 @@ void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   v.lAccuracyBoost = c.P.lAccuracyBoost; v.accurate_polarization = c.P.accurate_polarization;
   v.accurate_reionization = c.P.accurate_reionization;
   v.As = c.P.As; v.ns = c.P.ns; v.nrun = c.P.nrun; v.pivot_scalar = c.P.pivot_scalar; v.Alens = c.P.Alens;
+  v.max_l = c.P.max_l;
+  v.do_lensing = c.P.do_lensing;
+  // lSamples%template_l_scale: the drag-angle scale when it differs from 1 by more than
+  // template_shift_scale_tol (results.f90:49, 1517-1520)
+  v.cl_template_scale = std::fabs(c.scale - 1.0) > 0.01 ? c.scale : 1.0;
+  v.lens_accuracy_boost = c.P.AccuracyBoost * (c.P.LensingBoost > 0 ? c.P.LensingBoost : 1.0);
 }
 
-void interpolate_cls(const std::vector<int>& ls, const double* icl, int stride, int lmin, int lmax_out,
-                     double* out, int out_stride) {
-  int nl = (int)ls.size();
-  std::vector<double> xl(nl), y(nl), d2(nl);
-  for (int i = 0; i < nl; ++i) { xl[i] = ls[i]; y[i] = icl[(size_t)i * stride]; }
-  spline_second_derivs(xl.data(), y.data(), nl, d2.data());
-  int llo = 0;
-  for (int il = lmin; il <= std::min(lmax_out, ls[nl - 1]); ++il) {
-    if (il > ls[llo + 1] && llo < nl - 2) ++llo;
-    int lhi = llo + 1;
-    double ho = ls[lhi] - ls[llo];
-    double a0 = (ls[lhi] - il) / ho, b0 = 1 - a0;
-    out[(size_t)il * out_stride] = a0 * y[llo] + b0 * y[lhi] - a0 * b0 * ((1 + a0) * d2[llo] + (1 + b0) * d2[lhi]) * ho * ho / 6;
-  }
-}
 
 }  // namespace cg

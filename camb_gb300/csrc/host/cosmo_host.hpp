@@ -126,8 +126,5 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err);
 std::shared_ptr<const BesselTable> get_bessel_table(const std::vector<int>& ls, double xmax,
                                                     double bessel_boost, double accuracy_boost);
 void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v);
-// InterpolateClArr (results.f90:1710-1745): spline from the sampled l to every l.
-void interpolate_cls(const std::vector<int>& ls, const double* icl_col, int stride, int lmin,
-                     int lmax_out, double* out, int out_stride);
 
 }  // namespace cg

@@ -17,7 +17,7 @@ class AccuracyParams:
 
     _names = ["AccuracyBoost", "lAccuracyBoost", "lSampleBoost", "IntTolBoost", "TimeStepBoost",
               "SourcekAccuracyBoost", "IntkAccuracyBoost", "BesselBoost", "BessIntBoost", "TimeSwitchBoost",
-              "LimberBoost", "BackgroundTimeStepBoost"]
+              "LimberBoost", "BackgroundTimeStepBoost", "LensingBoost"]
 
     def __init__(self):
         for n in self._names:
@@ -54,7 +54,7 @@ class CAMBparams:
         self.mnu, self.num_massive_neutrinos = 0.0, 1
         self.Alens = 1.0
         self.max_l, self.max_eta_k = 2500, 6250.0
-        self.DoLensing = False
+        self.DoLensing = True  # model.f90:122
         self.WantCls, self.WantScalars = True, True
         self.InitPower = InitialPowerLaw()
         self.Reion = TanhReionization()
@@ -120,7 +120,7 @@ class CAMBparams:
 
 def set_params(cp=None, lmax=None, H0=None, ombh2=0.022, omch2=0.12, omk=0.0, mnu=0.06, nnu=3.044, YHe=None,
                tau=None, As=2e-9, ns=0.96, nrun=0, pivot_scalar=0.05, lens_potential_accuracy=0, max_eta_k=None,
-               DoLensing=False, num_massive_neutrinos=1, **kwargs):
+               DoLensing=True, num_massive_neutrinos=1, **kwargs):
     """camb.set_params (camb.py:135) restricted to the parameters of the GPU scalar path."""
     cp = cp or CAMBparams()
     cp.DoLensing = DoLensing

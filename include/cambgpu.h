@@ -57,6 +57,7 @@ typedef struct CambGpuParams {
     double SourcekAccuracyBoost, IntkAccuracyBoost, BesselBoost, BessIntBoost;
     double TimeSwitchBoost, LimberBoost, BackgroundTimeStepBoost;
     int accurate_polarization, accurate_reionization;
+    double LensingBoost;         /* AccuracyParams%LensingBoost (lensing theta sampling and range) */
 } CambGpuParams;
 
 /* Per-k-mode setup: the hierarchy sizes of GetNumEqns (equations.f90:860-1070)
@@ -130,6 +131,11 @@ typedef struct CambGpuTables {
     double lAccuracyBoost;
     int accurate_polarization, accurate_reionization;
     double As, ns, nrun, pivot_scalar, Alens;
+    /* C_l interpolation and lensing */
+    int max_l;                  /* CP%Max_l (last sampled l) */
+    int do_lensing;             /* lens the C_l (CP%DoLensing) */
+    double cl_template_scale;   /* lSamples%template_l_scale (results.f90:1517-1520) */
+    double lens_accuracy_boost; /* AccuracyBoost * LensingBoost */
 } CambGpuTables;
 
 /* Fills p with the reference's defaults (model.f90:36-209, Python set_params). */
@@ -177,6 +183,23 @@ int cambgpu_get_results(const CambGpuParams* p, int lmax_out, double* cl_out);
 /* n cosmologies in one persistent launch per stage; cl_out [n][lmax_out+1][4];
  * status [n] (per-cosmology error code). */
 int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, double* cl_out, int* status);
+
+/* Spectra of n cosmologies: camb.get_results followed by the CAMBdata getters
+ * get_unlensed_scalar_cls, get_lensed_scalar_cls and get_lens_potential_cls
+ * (camb_python.f90:585-632).  Any output pointer may be NULL to skip it.
+ *   unlensed, lensed: [n][lmax_out+1][4] TT EE BB TE of l(l+1)C_l/2pi;
+ *   lens_potential:   [n][lmax_out+1][3] PP PT PE ([L(L+1)]^2 C_L/2pi and crosses).
+ * C_l at every l come from the sampled l by InterpolateCls (cmbmain.f90:3523-3540,
+ * spline on the difference from the high-L template); lensing is CorrFuncFullSkyApodized
+ * (lensing.f90:338-678, the reference default with AccurateBB off) and needs
+ * do_lensing = 1; lensed spectra are zero above each cosmology's lmax_lensed, written to
+ * lmax_lensed[n] (0 for cosmologies without lensing) when that pointer is not NULL. */
+int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
+                              double* lens_potential, int* lmax_lensed, int* status);
+/* Lensing l range of a cosmology's tables: out3 = {lmax of the lensing sums
+ * (LensingExtrapLmax, lensing.f90:161-177), lmax_lensed (InitLensedClArrays,
+ * lensing.f90:230-247), number of theta points}. */
+int cambgpu_lensing_range(const CambGpuTables* t, int* out3);
 
 /* ---- resident batch: tables staged in device memory once, then timed runs ---- */
 /* Builds and uploads n cosmologies; the batch stays resident until released. */

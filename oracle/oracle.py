@@ -25,6 +25,13 @@ def load():
         lib.oracle_los_flat.argtypes = [C.c_void_p, dp, dp, C.c_int]
         lib.oracle_calc_scal_cls.restype = C.c_int
         lib.oracle_calc_scal_cls.argtypes = [C.c_void_p, dp, dp]
+        ip = C.POINTER(C.c_int)
+        lib.oracle_lensing_lrange.restype = None
+        lib.oracle_lensing_lrange.argtypes = [ip, C.c_int, C.c_int, C.c_int, C.c_double, ip]
+        lib.oracle_interpolate_cls.restype = None
+        lib.oracle_interpolate_cls.argtypes = [ip, C.c_int, dp, dp, C.c_double, dp]
+        lib.oracle_lens_cls_apodized.restype = C.c_int
+        lib.oracle_lens_cls_apodized.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp]
         lib.oracle_mode_setup.restype = C.c_int
         lib.oracle_mode_setup.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_int), dp]
         _lib = lib
@@ -68,3 +75,42 @@ def mode_setup(tables, q):
     ts = C.c_double()
     load().oracle_mode_setup(C.addressof(tables.view), q, l3, C.byref(ts))
     return (l3[0], l3[1], l3[2]), ts.value
+
+
+def load_template():
+    """The high-L template table [8001][4] (TT, EE, TE, PP by l) shipped with the package."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "camb_gb300", "data", "highl_template.f64")
+    return np.fromfile(path, dtype="<f8").reshape(8001, 4)
+
+
+def interpolate_cls(ls, icl, scale, tmpl=None):
+    """InterpolateCls: icl [nl][6] at the sampled ls -> [ls[-1]+1][6] at every l."""
+    tmpl = load_template() if tmpl is None else tmpl
+    ls = np.ascontiguousarray(ls, dtype=np.int32)
+    icl = np.ascontiguousarray(icl, dtype=np.float64)
+    out = np.zeros((int(ls[-1]) + 1, 6))
+    load().oracle_interpolate_cls(ls.ctypes.data_as(C.POINTER(C.c_int)), len(ls), _dp(icl), _dp(tmpl), scale,
+                                  _dp(out))
+    return out
+
+
+def lensing_lrange(ls, max_l, lens_output_margin=200, lens_accuracy_boost=1.0):
+    ls = np.ascontiguousarray(ls, dtype=np.int32)
+    out = (C.c_int * 2)()
+    load().oracle_lensing_lrange(ls.ctypes.data_as(C.POINTER(C.c_int)), len(ls), max_l, lens_output_margin,
+                                 lens_accuracy_boost, out)
+    return out[0], out[1]
+
+
+def lens_cls(all_cls, ls, max_l, lmin=2, lens_output_margin=200, lens_accuracy_boost=1.0, tmpl=None):
+    """CorrFuncFullSkyApodized: all_cls [max_l+1][>=4] holding TT EE TE and the C_Phi
+    column of InterpolateCls -> lensed [lmax_lensed+1][4] TT EE BB TE."""
+    tmpl = load_template() if tmpl is None else tmpl
+    lmax, lmax_lensed = lensing_lrange(ls, max_l, lens_output_margin, lens_accuracy_boost)
+    cl = np.ascontiguousarray(all_cls[: max_l + 1, :4], dtype=np.float64)
+    out = np.zeros((lmax_lensed + 1, 4))
+    rc = load().oracle_lens_cls_apodized(_dp(cl), max_l, lmin, lmax, lmax_lensed, lens_output_margin,
+                                         lens_accuracy_boost, _dp(tmpl), _dp(out))
+    if rc:
+        raise RuntimeError("lensing amplitude check failed")
+    return out
