@@ -1,4 +1,5 @@
-"""Benchmark: cosmologies/s of the GB300 scalar-perturbation path.
+"""Benchmark: cosmologies/s of the GB300 scalar-perturbation path at <=1e-4 relative C_l
+error.
 
 One step = one batch of B seeded cosmology draws (each of ombh2, omch2, H0, tau,
 As, ns uniform in fiducial +-5%, one massive neutrino eigenstate with mnu uniform in
@@ -6,7 +7,10 @@ As, ns uniform in fiducial +-5%, one massive neutrino eigenstate with mnu unifor
 line-of-sight projection, C_l.  `value` times the device pipeline on tables already
 resident in HBM (CUDA events on the library's stream); `e2e` times the C ABI call a
 user makes (cambgpu_get_results_batch: host parameters in, host C_l out, host table
-build and host<->device copies inside the timed region).
+build and host<->device copies inside the timed region).  The batch is timed twice on the
+device: the FP64 form (reported as fp64_form) and the timed form (--precision, default 1:
+FP32 line-of-sight projection), whose C_l error against the FP64 form over the whole
+batch and against the FP64 CPU restatement is reported beside the number.
 
 --impl reference times the reference's CPU path for the same workload on this
 machine's host cores: the C++ restatement of the reference (oracle/) with OpenMP
@@ -40,6 +44,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=4)
     ap.add_argument("--mnu-max", type=float, default=0.2)
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1],
+                    help="timed form: 0 FP64 throughout, 1 mixed-precision line-of-sight projection")
     return ap.parse_args()
 
 
@@ -180,7 +186,8 @@ def run_reference(args, rank, world):
     times = [cpu_reference(ps, nth) for _ in range(args.steps)]
     t = statistics.mean(times)
     v = len(ps) / t
-    line = {"impl": "reference", "metric": "cosmologies/s (unlensed scalar C_l to l=2500, FP64)", "value": v,
+    line = {"impl": "reference", "metric": "cosmologies/s to l=2500 at <=1e-4 rel C_l err (unlensed scalar TT/EE/TE)",
+            "value": v,
             "unit": "cosmologies/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic seeded draws",
@@ -213,31 +220,48 @@ def main():
         times = np.zeros(8)
         _lib.check(lib.cambgpu_autotune_ode(arr, B, best, _lib.dptr(times)))
         tuned = {"team": best[0], "queue_order": best[1], "candidate_ode_ms": [round(x, 2) for x in times[:5]]}
-    # ---- device-resident pipeline ----
+    # ---- device-resident pipeline, FP64 form then mixed precision ----
     _lib.check(lib.cambgpu_batch_prepare(arr, B))
-    ms = np.zeros(3)
-    for _ in range(args.warmup):
-        _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
-    stage = np.zeros(3)
-    evals = 0
-    lib.cambgpu_kernel_launches(1)
-    barrier(world)
-    torch.cuda.synchronize()
-    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
+
+    def resident(mode):
+        _lib.check(lib.cambgpu_set_precision(mode))
+        ms = np.zeros(3)
+        for _ in range(args.warmup):
             _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
-            stage += ms
-            evals += lib.cambgpu_last_ode_evals()
+        stage = np.zeros(3)
+        evals = 0
+        lib.cambgpu_kernel_launches(1)
+        barrier(world)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    launches = lib.cambgpu_kernel_launches(1)
-    barrier(world)
-    dev_ms = stage.sum() / args.steps
-    step_ms = barrier_max(dev_ms, world)
-    value = world * B / (step_ms * 1e-3)
+        with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
+                stage += ms
+                evals += lib.cambgpu_last_ode_evals()
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        launches = lib.cambgpu_kernel_launches(1)
+        barrier(world)
+        step_ms = barrier_max(stage.sum() / args.steps, world)
+        out = np.zeros((B, args.lmax + 1, 4))
+        _lib.check(lib.cambgpu_batch_fetch(args.lmax, _lib.dptr(out)))
+        return dict(step_ms=step_ms, stage=stage / args.steps, evals=evals / args.steps, launches=launches,
+                    wall=wall, clocks=clk.summary(), cls=out)
+
+    plain = resident(0)
+    mixed = resident(args.precision)
     lib.cambgpu_batch_release()
-    # ---- end to end through the C ABI (host params -> host C_l) ----
+    run = mixed
+    value = world * B / (run["step_ms"] * 1e-3)
+    # C_l error of the timed form against the FP64 form over the whole batch
+    sl = slice(2, args.lmax + 1)
+    a, r = run["cls"][:, sl], plain["cls"][:, sl]
+    batch_err = {"vs": f"FP64 GPU form, all {B} draws, 2<=l<={args.lmax}",
+                 "max_rel_TT": float(np.max(np.abs(a[..., 0] / r[..., 0] - 1))),
+                 "max_rel_EE": float(np.max(np.abs(a[..., 1] / r[..., 1] - 1))),
+                 "max_TE_over_sqrt_TTEE": float(np.max(np.abs(a[..., 3] - r[..., 3]) / np.sqrt(r[..., 0] * r[..., 1])))}
+    # ---- end to end through the C ABI (host params -> host C_l), timed form ----
     cls = np.zeros((B, args.lmax + 1, 4))
     st = np.zeros(B, dtype=np.int32)
     _lib.check(lib.cambgpu_get_results_batch(arr, B, args.lmax, _lib.dptr(cls), _lib.iptr(st)))
@@ -248,27 +272,35 @@ def main():
     e2e_s = barrier_max((time.perf_counter() - t0) / args.steps, world)
     xfer = (C.c_longlong * 2)()
     lib.cambgpu_last_transfer_bytes(xfer)
+    stage, evals, launches, wall, clk = run["stage"], run["evals"], run["launches"], run["wall"], run["clocks"]
+    step_ms = run["step_ms"]
     # ---- roofline of the dominant kernel (ODE, FP64 pipe) ----
     tf = C.c_double()
     _lib.check(lib.cambgpu_probe_fp64_tflops(C.byref(tf)))
-    ode_ms = stage[0] / args.steps
-    evals_step = evals / args.steps
+    ode_ms = stage[0]
+    evals_step = evals
     # FP64 flops per right-hand-side evaluation, stage combinations and error norm
     # included: 2*DFMA + DMUL + DADD thread instructions per evaluation counted by ncu on
     # this workload (mnu 0-0.2 eV, lmax 2500), profiles/ode_thread_kernel_batch32_lmax2500.md
     flops_per_eval = float(os.environ.get("CAMBGPU_FLOPS_PER_EVAL", "1315"))
     achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
-    line = {"metric": "cosmologies/s (unlensed scalar C_l to l=2500, FP64)", "value": value,
+    prec = {0: "FP64 throughout",
+            1: "FP64 ODE, source k-spline, C_l integral; FP32 line-of-sight projection with FP64 chunk sums"}
+    line = {"metric": "cosmologies/s to l=2500 at <=1e-4 rel C_l err (unlensed scalar TT/EE/TE)", "value": value,
             "unit": "cosmologies/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic seeded draws",
-            "config": {"workload": f"batch of {B} seeded draws (fiducial LCDM +-5%, mnu 0-{args.mnu_max:g} eV), "
+            "dtype": "f64" if args.precision == 0 else "f64+f32", "data": "synthetic seeded draws",
+            "config": {"precision": prec[args.precision],
+                       "workload": f"batch of {B} seeded draws (fiducial LCDM +-5%, mnu 0-{args.mnu_max:g} eV), "
                                    f"unlensed TT/EE/TE to lmax={args.lmax}, max_eta_k={2.5 * args.lmax:g}",
                        "global_batch": B * world, "per_gpu_batch": B, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (per-cosmology tables ~3 MB x batch)",
                        "ode_autotune": tuned,
-                       "stage_ms": {"ode": stage[0] / args.steps, "spline_los": stage[1] / args.steps,
-                                    "cls": stage[2] / args.steps}},
+                       "stage_ms": {"ode": stage[0], "spline_los": stage[1], "cls_interp_lens": stage[2]}},
+            "fp64_form": {"value": world * B / (plain["step_ms"] * 1e-3), "ms_per_step": plain["step_ms"],
+                          "stage_ms": {"ode": plain["stage"][0], "spline_los": plain["stage"][1],
+                                       "cls_interp_lens": plain["stage"][2]}},
+            "accuracy_vs_fp64_gpu": batch_err,
             "e2e": {"value": world * B / e2e_s, "unit": "cosmologies/s", "h2d_bytes_per_step": int(xfer[0]),
                     "d2h_bytes_per_step": int(xfer[1])},
             "gpu_launches": int(launches),
@@ -283,7 +315,7 @@ def main():
         cpu_reference(cps[:1], nth)
         ref = []
         t = cpu_reference(cps, nth, keep=ref)
-        line["accuracy"] = accuracy_vs_fp64(cps, ref, args.lmax)
+        line["accuracy"] = accuracy_vs_fp64(cps, ref, args.lmax)  # timed form vs the FP64 CPU restatement
         line["cpu_baseline"] = {"value": len(cps) / t, "unit": "cosmologies/s", "cores": nth, "kind": "port",
                                 "sample": f"{len(cps)} draws of the same workload, host tables + ODE + LOS + C_l"}
         print(json.dumps(line))

@@ -99,6 +99,8 @@ SIGNATURES = {
     "cambgpu_batch_fetch": (C.c_int, [C.c_int, _c_double_p]),
     "cambgpu_batch_release": (None, []),
     "cambgpu_set_ode_team": (C.c_int, [C.c_int]),
+    "cambgpu_set_precision": (C.c_int, [C.c_int]),
+    "cambgpu_get_precision": (C.c_int, []),
     "cambgpu_autotune_ode": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, _c_int_p, _c_double_p]),
     "cambgpu_last_timings": (C.c_int, [_c_double_p]),
     "cambgpu_last_ode_evals": (C.c_longlong, []),

@@ -25,6 +25,7 @@ cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s,
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
 __global__ void los_flat_kernel(const DevCosmo*);
+__global__ void los_flat_mixed_kernel(const DevCosmo*);
 __global__ void scal_cls_kernel(const DevCosmo*);
 }  // namespace cgdev
 
@@ -36,6 +37,7 @@ std::string g_err;
 std::atomic<long long> g_launches{0};
 double g_timings[6] = {0, 0, 0, 0, 0, 0};
 int g_team = 0;
+int g_precision = 0;  // 0: FP64 throughout; 1: mixed-precision line-of-sight projection
 // autotuned ODE configuration per batch-size class: [0] small (< 24 modes/SM), [1] large
 struct OdeCfg { int team; int order; };
 OdeCfg g_tuned[2] = {{32, 0}, {1, 0}};
@@ -85,7 +87,7 @@ struct Runtime {
   int nsm = 0;
   Arena arena;
   // Bessel tables resident on the device, keyed by host table address and shape
-  struct DevBessel { const double* host; size_t n; double* dev; double* devx; int num_xx; };
+  struct DevBessel { const double* host; size_t n; double* dev; double* devx; int num_xx; float4* devf; };
   std::vector<DevBessel> bessel;
   // pinned staging for uploads
   char* pinned = nullptr;
@@ -115,27 +117,42 @@ int rt_init() {
   CUDA_TRY(cudaStreamCreateWithFlags(&g_rt.stream, cudaStreamNonBlocking));
   for (auto& e : g_rt.ev) CUDA_TRY(cudaEventCreate(&e));
   CUDA_TRY(cudaFuncSetAttribute(los_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+  CUDA_TRY(cudaFuncSetAttribute(los_flat_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
   g_rt.init = true;
   return 0;
 }
 
-int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x) {
+int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4** dev_f) {
   size_t n = (size_t)t.nl * (t.num_xx - 1) * 4;
   for (auto& b : g_rt.bessel)
-    if (b.host == t.bessel_horner && b.n == n && b.num_xx == t.num_xx) { *dev_h = b.dev; *dev_x = b.devx; return 0; }
-  Runtime::DevBessel b{t.bessel_horner, n, nullptr, nullptr, t.num_xx};
+    if (b.host == t.bessel_horner && b.n == n && b.num_xx == t.num_xx) {
+      *dev_h = b.dev;
+      *dev_x = b.devx;
+      *dev_f = b.devf;
+      return 0;
+    }
+  Runtime::DevBessel b{t.bessel_horner, n, nullptr, nullptr, t.num_xx, nullptr};
   CUDA_TRY(cudaMalloc(&b.dev, n * sizeof(double)));
   CUDA_TRY(cudaMalloc(&b.devx, (size_t)t.num_xx * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&b.devf, n * sizeof(float)));
   CUDA_TRY(cudaMemcpy(b.dev, t.bessel_horner, n * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(b.devx, t.bess_x, (size_t)t.num_xx * sizeof(double), cudaMemcpyHostToDevice));
+  {
+    // the FP32 copy of the Horner coefficients for the mixed-precision projection
+    std::vector<float> f(n);
+    for (size_t i = 0; i < n; ++i) f[i] = (float)t.bessel_horner[i];
+    CUDA_TRY(cudaMemcpy(b.devf, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  }
   if (g_rt.bessel.size() >= 4) {
     cudaFree(g_rt.bessel.front().dev);
     cudaFree(g_rt.bessel.front().devx);
+    cudaFree(g_rt.bessel.front().devf);
     g_rt.bessel.erase(g_rt.bessel.begin());
   }
   g_rt.bessel.push_back(b);
   *dev_h = b.dev;
   *dev_x = b.devx;
+  *dev_f = b.devf;
   return 0;
 }
 
@@ -335,9 +352,11 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.lmax_lensed = 0;
   spline_factors(t, u.spl);
   double *bh, *bx;
-  int rc = device_bessel(t, &bh, &bx);
+  float4* bf;
+  int rc = device_bessel(t, &bh, &bx, &bf);
   if (rc) return rc;
   d.bessel_horner = bh;
+  d.bessel_f32 = bf;
   d.bess_x = bx;
   d.num_xx = t.num_xx;
   d.nsrc = t.nsrc; d.want_late_time = t.want_late_time; d.max_etak_scalar = t.max_etak_scalar; d.tol1 = t.tol1;
@@ -546,7 +565,8 @@ int run_los(Batch& B) {
   }
   size_t smem = (size_t)B.max_ntau * (3 + 1 + 1) * 8 + (size_t)B.max_ntau * 4 + 64;
   dim3 g2(B.max_nq, n);
-  los_flat_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
+  if (g_precision == 1) los_flat_mixed_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
+  else los_flat_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
   g_launches++;
   CUDA_TRY(cudaGetLastError());
   return 0;
@@ -886,6 +906,15 @@ void cambgpu_batch_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_res.reset();
 }
+
+int cambgpu_set_precision(int mode) {
+  if (mode != 0 && mode != 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "precision mode must be 0 or 1");
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_precision = mode;
+  return 0;
+}
+
+int cambgpu_get_precision(void) { return g_precision; }
 
 int cambgpu_set_ode_team(int lanes) {
   if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 3 && lanes != 8 && lanes != 16 && lanes != 32)

@@ -56,6 +56,7 @@ struct DevCosmo {
   // Bessel table
   const double* bess_x;
   const double* bessel_horner;  // [nl][num_xx-1][4]
+  const float4* bessel_f32;     // [nl][num_xx-1] the same coefficients in FP32 (mixed precision)
   int num_xx;
   // settings
   int nsrc, want_late_time;

@@ -8,6 +8,8 @@
 //                         table index and weight of every time step are staged in
 //                         shared memory once, then one warp per sampled l sums
 //                         S(q,tau_n) j_l(q(tau0-tau_n)) dtau_n over its window.
+//   los_flat_mixed_kernel the same projection with the Bessel table and sources in FP32
+//                         and FP64 accumulation of FP32 chunk sums (mixed precision).
 //   scal_cls_kernel       CalcScalCls (cmbmain.f90:3179-3343): one CTA per sampled l,
 //                         block reduction over q of P(k) Delta_X Delta_Y dlnk.
 #include <cuda_runtime.h>
@@ -74,16 +76,22 @@ __global__ void source_spline_kernel(const DevCosmo* __restrict__ cosmos, const 
 
 constexpr int LOS_THREADS = 256;
 
-__global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* __restrict__ cosmos) {
-  const DevCosmo& C = cosmos[blockIdx.y];
-  const int q_ix = blockIdx.x;
-  if (q_ix >= C.nq) return;
-  extern __shared__ double smem[];
+// One CTA per integration wavenumber q.  F32 selects the mixed-precision projection:
+// Bessel table (float4 Horner coefficients) and staged sources in FP32, products summed
+// in FP32 over chunks of kChunk time steps per lane and the chunk sums accumulated in
+// FP64.  Everything before the projection (source k-interpolation, Bessel interval
+// search) and the Limber branch stay FP64.
+constexpr int kChunk = 16;
+
+template <bool F32>
+__device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, double* smem) {
   const int ntau = C.ntau, nsrc = C.nsrc, nk = C.nk;
-  double* s_src = smem;                          // [ntau][3]
-  double* s_w = s_src + (size_t)ntau * 3;        // [ntau] Horner variable (left weight)
-  double* s_raw3 = s_w + ntau;                   // [ntau] lensing source without dtau (Limber)
-  int* s_bix = (int*)(s_raw3 + ntau);            // [ntau] 0-based Bessel interval
+  double* s_src = smem;                                      // [ntau][3] (FP64 variant)
+  float* s_srcf = reinterpret_cast<float*>(smem);            // [ntau][3] (FP32 variant)
+  double* s_w = s_src + (size_t)ntau * 3;                    // [ntau] Horner variable (left weight)
+  float* s_wf = reinterpret_cast<float*>(s_w);               // [ntau] (FP32 variant)
+  double* s_raw3 = s_w + ntau;                               // [ntau] lensing source without dtau (Limber)
+  int* s_bix = (int*)(s_raw3 + ntau);                        // [ntau] 0-based Bessel interval
   const double q = C.q_int[q_ix];
   const double tau0 = C.tau0;
   const double max_etak = C.want_late_time ? 0.0 : C.max_etak_scalar;
@@ -118,7 +126,8 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
     int bi = bsearch_lo(C.bess_x, nbx, xx);
     double x_hi = ldgd(C.bess_x + bi + 1), dx = x_hi - ldgd(C.bess_x + bi);
     s_bix[i] = bi;
-    s_w[i] = (x_hi - xx) / dx;
+    if (F32) s_wf[i] = (float)((x_hi - xx) / dx);
+    else s_w[i] = (x_hi - xx) / dx;
     const double dt = C.tau_dpoints[i];
     for (int s = 0; s < 3; ++s) {
       double v = 0;
@@ -128,7 +137,8 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
             (a03 * C.dd_src[b + klo] + b03 * C.dd_src[b + khi]) * ho2o6;
       }
       // the time weight dtau_n is folded into the staged source
-      s_src[i * 3 + s] = v * dt;
+      if (F32) s_srcf[i * 3 + s] = (float)(v * dt);
+      else s_src[i * 3 + s] = v * dt;
       if (s == 2) s_raw3[i] = v;
     }
   }
@@ -155,16 +165,41 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
     if (doint) {
       const int nstart = time_index_of(tp, ntau, tmin);
       const int nend = min(source_steps, time_index_of(tp, ntau, tmax));
-      const double* __restrict__ H = C.bessel_horner + (size_t)j * (nbx - 1) * 4;
-      for (int n = nstart + lane; n <= nend; n += 32) {
-        const int i = n - 1;  // 0-based row
-        const double a2 = s_w[i];
-        const double2* hp = reinterpret_cast<const double2*>(H + (size_t)s_bix[i] * 4);
-        const double2 c01 = __ldg(hp), c23 = __ldg(hp + 1);
-        const double J = c01.x + a2 * (c01.y + a2 * (c23.x + a2 * c23.y));
-        acc0 += s_src[i * 3 + 0] * J;
-        acc1 += s_src[i * 3 + 1] * J;
-        acc2 += s_src[i * 3 + 2] * J;
+      if (F32) {
+        const float4* __restrict__ H = C.bessel_f32 + (size_t)j * (nbx - 1);
+        float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+        int k = 0;
+        for (int n = nstart + lane; n <= nend; n += 32) {
+          const int i = n - 1;
+          const float a2 = s_wf[i];
+          const float4 c = __ldg(H + s_bix[i]);
+          const float J = fmaf(a2, fmaf(a2, fmaf(a2, c.w, c.z), c.y), c.x);
+          f0 = fmaf(s_srcf[i * 3 + 0], J, f0);
+          f1 = fmaf(s_srcf[i * 3 + 1], J, f1);
+          f2 = fmaf(s_srcf[i * 3 + 2], J, f2);
+          if (++k == kChunk) {
+            acc0 += f0;
+            acc1 += f1;
+            acc2 += f2;
+            f0 = f1 = f2 = 0.f;
+            k = 0;
+          }
+        }
+        acc0 += f0;
+        acc1 += f1;
+        acc2 += f2;
+      } else {
+        const double* __restrict__ H = C.bessel_horner + (size_t)j * (nbx - 1) * 4;
+        for (int n = nstart + lane; n <= nend; n += 32) {
+          const int i = n - 1;  // 0-based row
+          const double a2 = s_w[i];
+          const double2* hp = reinterpret_cast<const double2*>(H + (size_t)s_bix[i] * 4);
+          const double2 c01 = __ldg(hp), c23 = __ldg(hp + 1);
+          const double J = c01.x + a2 * (c01.y + a2 * (c23.x + a2 * c23.y));
+          acc0 += s_src[i * 3 + 0] * J;
+          acc1 += s_src[i * 3 + 1] * J;
+          acc2 += s_src[i * 3 + 2] * J;
+        }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -191,6 +226,20 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* _
       if (nsrc > 2) D[2] = acc2;
     }
   }
+}
+
+__global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* __restrict__ cosmos) {
+  const DevCosmo& C = cosmos[blockIdx.y];
+  if ((int)blockIdx.x >= C.nq) return;
+  extern __shared__ double smem[];
+  los_flat_body<false>(C, blockIdx.x, smem);
+}
+
+__global__ void __launch_bounds__(LOS_THREADS) los_flat_mixed_kernel(const DevCosmo* __restrict__ cosmos) {
+  const DevCosmo& C = cosmos[blockIdx.y];
+  if ((int)blockIdx.x >= C.nq) return;
+  extern __shared__ double smem[];
+  los_flat_body<true>(C, blockIdx.x, smem);
 }
 
 constexpr int CLS_THREADS = 256;

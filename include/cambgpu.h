@@ -211,6 +211,14 @@ int cambgpu_batch_fetch(int lmax_out, double* cl_out);
 void cambgpu_batch_release(void);
 
 /* ---- runtime ---- */
+/* Arithmetic of the line-of-sight projection (no counterpart in the reference, which is
+ * FP64 throughout).  0 (default): FP64 everywhere -- the plain form whose transfer
+ * functions and C_l match the reference's algorithm to rounding.  1: mixed precision --
+ * Bessel interpolation and source products in FP32, summed in FP32 over 16 time steps
+ * per lane and accumulated in FP64; the ODE, source k-spline, Bessel interval search,
+ * Limber branch, C_l k-integral, interpolation and lensing stay FP64. */
+int cambgpu_set_precision(int mode);
+int cambgpu_get_precision(void);
 /* ODE kernel variant: 32/16/8 = lanes per k-mode (warp teams); 1/2/3 = one thread per
  * k-mode with 3/4/5 resident blocks per SM; 0 = the autotuned choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
