@@ -375,6 +375,8 @@ struct Batch {
   WorkItem* d_items = nullptr;
   WorkItem* d_items_rev = nullptr;
   std::vector<WorkItem> h_items_rev;
+  WorkItem* d_items_grp = nullptr;  // q bands, cosmologies of similar neutrino mass together
+  std::vector<WorkItem> h_items_grp;
   int nitems = 0;
   int* d_counter = nullptr;
   int* d_status = nullptr;
@@ -435,7 +437,7 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   total += 2 * rr((size_t)n * (B.out_lmax + 1) * 4 * 8) + rr((size_t)n * (B.out_lmax + 1) * 3 * 8);
   size_t nitems = 0;
   for (auto* v : B.views) nitems += v->nk;
-  total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + 2 * (nitems * sizeof(WorkItem) + 255) +
+  total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + 3 * (nitems * sizeof(WorkItem) + 255) +
            1024 + ((size_t)n * 4 + 255);
   rc = g_rt.arena.reserve(total);
   if (rc) return set_err(rc, "device allocation failed");
@@ -499,6 +501,27 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   B.h_items_rev.assign(items.rbegin(), items.rend());
   B.d_items_rev = g_rt.arena.take<WorkItem>(items.size());
   copies.push_back({B.d_items_rev, {B.h_items_rev.data(), items.size() * sizeof(WorkItem)}});
+  // third order: bands of 1.6% in q (high q first), and inside a band the cosmologies by
+  // neutrino mass, so that a warp's 32 modes share hierarchy sizes and switch sequences
+  B.h_items_grp = items;
+  {
+    auto band = [&](const WorkItem& w) { return (long)std::floor(std::log(B.views[w.cosmo]->q_evolve[w.mode]) * 64); };
+    auto mass = [&](const WorkItem& w) {
+      const CambGpuTables* v = B.views[w.cosmo];
+      double m = 0;
+      for (int i = 0; i < v->nu_eig; ++i) m += v->nu_masses[i];
+      return m;
+    };
+    std::stable_sort(B.h_items_grp.begin(), B.h_items_grp.end(), [&](const WorkItem& a, const WorkItem& b) {
+      long ba = band(a), bb = band(b);
+      if (ba != bb) return ba > bb;
+      double ma = mass(a), mb = mass(b);
+      if (ma != mb) return ma < mb;
+      return B.views[a.cosmo]->q_evolve[a.mode] > B.views[b.cosmo]->q_evolve[b.mode];
+    });
+  }
+  B.d_items_grp = g_rt.arena.take<WorkItem>(items.size());
+  copies.push_back({B.d_items_grp, {B.h_items_grp.data(), items.size() * sizeof(WorkItem)}});
   // single pinned staging buffer for all uploads
   size_t stage = 0;
   for (auto& cp : copies) stage += (cp.second.second + 255) & ~size_t(255);
@@ -548,7 +571,8 @@ int run_ode(Batch& B) {
   int per_sm = std::max(1, ode_blocks_per_sm(team, 128));
   int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * lanes + 127) / 128);
   if (blocks < 1) blocks = 1;
-  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, order ? B.d_items_rev : B.d_items, B.nitems,
+  const WorkItem* queue = order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
+  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, queue, B.nitems,
                              B.d_counter));
   g_launches++;
   return 0;
@@ -933,7 +957,7 @@ long long cambgpu_last_ode_evals(void) { return g_last_evals; }
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times) {
   // candidates: (team code, queue order); team 32 = warp per mode, 1/2/3 = thread per mode
   // with 3/4/5 resident blocks per SM
-  static const int cand[][2] = {{32, 0}, {1, 0}, {2, 0}, {3, 0}, {2, 1}};
+  static const int cand[][2] = {{32, 0}, {1, 0}, {2, 0}, {3, 0}, {2, 1}, {1, 2}, {2, 2}, {3, 2}};
   const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
   int rc = cambgpu_batch_prepare(p, n);
   if (rc) return rc;

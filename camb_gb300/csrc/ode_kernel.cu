@@ -1259,8 +1259,10 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   }
 }
 
+// The eight stage vectors live in rows of b; the state, trial state and first/last stage
+// rows are named by slot indices so that accepting a step swaps indices, not vectors.
 struct Work {
-  double y[NV], k1[NV], k2[NV], k3[NV], k4[NV], k5[NV], k6[NV], yt[NV];
+  double b[8][NV];
   double dl[NL], dl2[NL], pf[20];
 };
 
@@ -1268,6 +1270,9 @@ struct Work {
 struct Run {
   double src[3];
   double tau, target, sw_time, h, err, call_hmax;
+  double ny;            // min(max|y|, 1) of the current state (valid when ny_valid)
+  int sy, syt, sk1, sk2;  // rows of Work::b holding y, the trial state, k1 and k2 (= k7)
+  bool ny_valid;
   long long evals;
   int j, fails, status, sw_kind, sw_eig;
   bool active, target_is_switch, need_f, first, fsal, reset, src_valid;
@@ -1317,13 +1322,19 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
     R.status = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
     return;
   }
+  R.sy = 0;
+  R.sk1 = 1;
+  R.sk2 = 2;
+  R.syt = 7;
+  R.ny_valid = false;
+  double* const Y = W.b[R.sy];
   for (int l = 1; l <= lm; ++l) {
     const double dn = 1.0 / (2 * l + 1);
     W.dl[l] = dn * M.k * l;
     W.dl2[l] = dn * M.k * (l + 1);
     if (l < 20) W.pf[l] = ((double)((l + 3) * (l - 1)) / (l + 1)) * M.k * dn;
   }
-  for (int i = 0; i < M.nvar; ++i) W.y[i] = 0;
+  for (int i = 0; i < M.nvar; ++i) Y[i] = 0;
   // initial (equations.f90:1891-2112), adiabatic
   const double tau = ms.taustart, k = M.k;
   const double x = k * tau, x2 = x * x, x3 = x2 * x;
@@ -1342,21 +1353,21 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   const double iv_pir = 4.0 / 3 * x2 / Rp15 * (1 + omtau / 4 * (4 * Rv - 5) / (2 * Rv + 15));
   const double iv_aj3r = 4 / 21.0 / Rp15 * x3;
   const double iv_eta = -2 * (1 - x2 / 12 * (-10.0 / Rp15 + 1));
-  W.y[0] = iv_eta * k / 2;
-  W.y[1] = -iv_clxb;
-  W.y[2] = -iv_clxb;
-  W.y[3] = -iv_vb;
-  W.y[M.g_ix] = -iv_clxg;
-  W.y[M.g_ix + 1] = -iv_qg;
-  W.y[M.r_ix] = -iv_clxg;
-  W.y[M.r_ix + 1] = -iv_qr;
-  W.y[M.r_ix + 2] = -iv_pir;
-  if (M.lmaxnr > 2) W.y[M.r_ix + 3] = -iv_aj3r;
+  Y[0] = iv_eta * k / 2;
+  Y[1] = -iv_clxb;
+  Y[2] = -iv_clxb;
+  Y[3] = -iv_vb;
+  Y[M.g_ix] = -iv_clxg;
+  Y[M.g_ix + 1] = -iv_qg;
+  Y[M.r_ix] = -iv_clxg;
+  Y[M.r_ix + 1] = -iv_qr;
+  Y[M.r_ix + 2] = -iv_pir;
+  if (M.lmaxnr > 2) Y[M.r_ix + 3] = -iv_aj3r;
   for (int i = 0; i < C.nu_eig; ++i) {
     int ind = M.nu_ix[i];
     for (int iq = 0; iq < M.nq[i]; ++iq) {
-      for (int jj = 0; jj < 3; ++jj) W.y[ind + jj] = W.y[M.r_ix + jj];
-      if (M.lmaxnu_tau[i] > 2) W.y[ind + 3] = -iv_aj3r;
+      for (int jj = 0; jj < 3; ++jj) Y[ind + jj] = Y[M.r_ix + jj];
+      if (M.lmaxnu_tau[i] > 2) Y[ind + 3] = -iv_aj3r;
       ind += M.lmaxnu_tau[i] + 1;
     }
   }
@@ -1447,28 +1458,41 @@ __device__ bool next_target(const DevCosmo& C, St& M, Run& R) {
 }
 
 // the switch branches of EvolveScal (equations.f90:333-451); layout changes repack y via yt
+// the trial-state row becomes the state row
+__device__ __forceinline__ void swap_rows(Run& R, double*& Y, double*& YT) {
+  const int t = R.sy;
+  R.sy = R.syt;
+  R.syt = t;
+  double* p = Y;
+  Y = YT;
+  YT = p;
+}
+
 __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
   const double noSwitch = C.tau0 + 1;
   St N = M;
+  double* Y = W.b[R.sy];
+  double* YT = W.b[R.syt];
+  R.ny_valid = false;
   const int kind = R.sw_kind, e = R.sw_eig;
   if (kind == SW_TC) {
     N.tc = false;
     N.tight_off = noSwitch;
     setup_indices(C, N, false);
-    copy_vars(C, M, N, W.y, W.yt);
+    copy_vars(C, M, N, Y, YT);
     M = N;
-    for (int i = 0; i < M.nvar; ++i) W.y[i] = W.yt[i];
+    swap_rows(R, Y, YT);
     R.reset = true;
     const double tau = R.tau, itau = 1.0 / tau;
     double a, cs2, opac, dopac;
     thermo_values(C, tau, itau, a, cs2, opac, dopac);
     const double kb = M.k, op2 = opac * opac;
-    W.y[M.g_ix + 2] = M.pig;
-    W.y[M.g_ix + 3] = (3.0 / 7.0) * M.pig * (kb / opac) * (1.0 + dopac / op2) + (3.0 / 7.0) * M.pigdot * (kb / op2) * (-1.0);
+    Y[M.g_ix + 2] = M.pig;
+    Y[M.g_ix + 3] = (3.0 / 7.0) * M.pig * (kb / opac) * (1.0 + dopac / op2) + (3.0 / 7.0) * M.pigdot * (kb / op2) * (-1.0);
     const double p2 = M.pig / 4 + M.pigdot * (1.0 / opac) * (-5.0 / 8.0 - (25.0 / 16.0) * dopac / op2) +
                       M.pig * (kb / opac) * (kb / opac) * (-5.0 / 56.0);
-    W.y[M.pol0 + 2] = p2;
-    W.y[M.pol0 + 3] = (3.0 / 7.0) * (kb / opac) * p2 * (1.0 + dopac / op2) +
+    Y[M.pol0 + 2] = p2;
+    Y[M.pol0 + 3] = (3.0 / 7.0) * (kb / opac) * p2 * (1.0 + dopac / op2) +
                       (3.0 / 7.0) * (kb / op2) * ((M.pigdot / 4.0) * (1.0 + (5.0 / 2.0) * dopac / op2)) * (-1.0);
   } else if (kind == SW_NU_MASSIVE) {
     // SwitchToMassiveNuApprox (equations.f90:1072-1111)
@@ -1478,14 +1502,14 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
     const double a2 = a * a;
     N.approx[e] = true;
     setup_indices(C, N, false);
-    copy_vars(C, M, N, W.y, W.yt);
+    copy_vars(C, M, N, Y, YT);
     double rhonu, pnu, clxnu, qnu, dpnu, pinu;
     nuf::rho_P(a * C.nu_masses[e], rhonu, pnu);
-    nu_integrate<true>(C, M, W.y, a, e, clxnu, qnu, dpnu, pinu);
-    W.yt[N.nu_ix[e]] = clxnu / rhonu;
-    W.yt[N.nu_ix[e] + 1] = dpnu / rhonu;
-    W.yt[N.nu_ix[e] + 2] = qnu / rhonu;
-    W.yt[N.nu_ix[e] + 3] = pinu / rhonu;
+    nu_integrate<true>(C, M, Y, a, e, clxnu, qnu, dpnu, pinu);
+    YT[N.nu_ix[e]] = clxnu / rhonu;
+    YT[N.nu_ix[e] + 1] = dpnu / rhonu;
+    YT[N.nu_ix[e] + 2] = qnu / rhonu;
+    YT[N.nu_ix[e] + 3] = pinu / rhonu;
     // Nu_Intvsq (equations.f90:1331-1356) on the old layout
     double G11 = 0, G30 = 0;
     const double am = a * C.nu_masses[e];
@@ -1493,14 +1517,14 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
     for (int iq = 0; iq < M.nq[e]; ++iq) {
       const double aq = am / C.nu_q[iq];
       const double v = 1.0 / sqrt(1.0 + aq * aq);
-      G11 += C.nu_int_kernel[iq] * W.y[ind + 1] * v * v;
-      if (M.lmaxnu_tau[e] > 2) G30 += C.nu_int_kernel[iq] * W.y[ind + 3] * v * v;
+      G11 += C.nu_int_kernel[iq] * Y[ind + 1] * v * v;
+      if (M.lmaxnu_tau[e] > 2) G30 += C.nu_int_kernel[iq] * Y[ind + 3] * v * v;
       ind += M.lmaxnu_tau[e] + 1;
     }
     N.G11[e] = G11 * a2 * a / rhonu;
     N.G30[e] = G30 * a2 * a / rhonu;
     M = N;
-    for (int i = 0; i < M.nvar; ++i) W.y[i] = W.yt[i];
+    swap_rows(R, Y, YT);
   } else {
     if (kind == SW_KTAU) {
       N.hk = true;
@@ -1518,9 +1542,9 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
       N.nophot = true;
     }
     setup_indices(C, N, false);
-    copy_vars(C, M, N, W.y, W.yt);
+    copy_vars(C, M, N, Y, YT);
     M = N;
-    for (int i = 0; i < M.nvar; ++i) W.y[i] = W.yt[i];
+    swap_rows(R, Y, YT);
   }
   R.fsal = false;
 }
@@ -1530,19 +1554,30 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   using namespace dp;
   const double tol = C.tol1;
   const int n = M.n;
+  double* __restrict__ y = W.b[R.sy];
+  double* __restrict__ yt = W.b[R.syt];
+  double* __restrict__ k1 = W.b[R.sk1];
+  double* __restrict__ k2 = W.b[R.sk2];
+  double* __restrict__ k3 = W.b[3];
+  double* __restrict__ k4 = W.b[4];
+  double* __restrict__ k5 = W.b[5];
+  double* __restrict__ k6 = W.b[6];
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
-      derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, W.k1, nullptr);
+      derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, y, k1, nullptr);
       R.evals++;
     }
     R.need_f = false;
   }
   if (R.evals > kMaxEvalsPerMode) return -1;
-  unsigned long long nb = 0;
-  for (int i = 0; i < n; ++i) nb = max(nb, (unsigned long long)__double_as_longlong(W.y[i]) & 0x7fffffffffffffffULL);
-  double ny = __longlong_as_double((long long)nb);
-  ny = ny < 1.0 ? ny : 1.0;
+  if (!R.ny_valid) {
+    unsigned long long nb = 0;
+    for (int i = 0; i < n; ++i) nb = max(nb, (unsigned long long)__double_as_longlong(y[i]) & 0x7fffffffffffffffULL);
+    R.ny = __longlong_as_double((long long)nb);
+    R.ny_valid = true;
+  }
+  const double ny = R.ny < 1.0 ? R.ny : 1.0;
   const double x = R.tau;
   const double hmin = 10.0 * fmax(tiny, eps * fmax(ny / tol, fabs(x)));
   const double hmax = R.call_hmax != 0.0 ? R.call_hmax : 20.0;
@@ -1575,30 +1610,37 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   const double c51 = hs * a51, c52 = hs * a52, c53 = hs * a53, c54 = hs * a54;
   const double c61 = hs * a61, c62 = hs * a62, c63 = hs * a63, c64 = hs * a64, c65 = hs * a65;
   const double cb1 = hs * b1, cb3 = hs * b3, cb4 = hs * b4, cb5 = hs * b5, cb6 = hs * b6;
-  for (int i = 0; i < n; ++i) W.yt[i] = fma(c21, W.k1[i], W.y[i]);
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, W.yt, W.k2, nullptr);
-  for (int i = 0; i < n; ++i) W.yt[i] = fma(c32, W.k2[i], fma(c31, W.k1[i], W.y[i]));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), W.yt, W.k3, nullptr);
-  for (int i = 0; i < n; ++i) W.yt[i] = fma(c43, W.k3[i], fma(c42, W.k2[i], fma(c41, W.k1[i], W.y[i])));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), W.yt, W.k4, nullptr);
+  for (int i = 0; i < n; ++i) yt[i] = fma(c21, k1[i], y[i]);
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, yt, k2, nullptr);
+  for (int i = 0; i < n; ++i) yt[i] = fma(c32, k2[i], fma(c31, k1[i], y[i]));
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), yt, k3, nullptr);
+  for (int i = 0; i < n; ++i) yt[i] = fma(c43, k3[i], fma(c42, k2[i], fma(c41, k1[i], y[i])));
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), yt, k4, nullptr);
+  for (int i = 0; i < n; ++i) yt[i] = fma(c54, k4[i], fma(c53, k3[i], fma(c52, k2[i], fma(c51, k1[i], y[i]))));
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), yt, k5, nullptr);
   for (int i = 0; i < n; ++i)
-    W.yt[i] = fma(c54, W.k4[i], fma(c53, W.k3[i], fma(c52, W.k2[i], fma(c51, W.k1[i], W.y[i]))));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), W.yt, W.k5, nullptr);
-  for (int i = 0; i < n; ++i)
-    W.yt[i] = fma(c65, W.k5[i], fma(c64, W.k4[i], fma(c63, W.k3[i], fma(c62, W.k2[i], fma(c61, W.k1[i], W.y[i])))));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k6, nullptr);
-  for (int i = 0; i < n; ++i)
-    W.yt[i] = fma(cb6, W.k6[i], fma(cb5, W.k5[i], fma(cb4, W.k4[i], fma(cb3, W.k3[i], fma(cb1, W.k1[i], W.y[i])))));
+    yt[i] = fma(c65, k5[i], fma(c64, k4[i], fma(c63, k3[i], fma(c62, k2[i], fma(c61, k1[i], y[i])))));
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k6, nullptr);
+  // the fifth-order solution, the error combination of k1, k3..k6 (k3 is dead afterwards
+  // and holds it) and max|yt| for the next step's hmin, in one pass
+  unsigned long long nbt = 0;
+  for (int i = 0; i < n; ++i) {
+    const double a1 = k1[i], a3 = k3[i], a4 = k4[i], a5 = k5[i], a6 = k6[i];
+    const double v = fma(cb6, a6, fma(cb5, a5, fma(cb4, a4, fma(cb3, a3, fma(cb1, a1, y[i])))));
+    yt[i] = v;
+    k3[i] = fma(e6, a6, fma(e5, a5, fma(e4, a4, fma(e3, a3, e1 * a1))));
+    nbt = max(nbt, (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL);
+  }
   // stage 7 (FSAL) into k2; at an output time it is the output() evaluation too
   const bool want_src = (xt == xend) && !R.target_is_switch;
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, W.yt, W.k2, want_src ? R.src : nullptr);
+  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k2, want_src ? R.src : nullptr);
   R.src_valid = want_src;
   R.evals += 6;
   // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry
   double num = 0, den = 1;
   for (int i = 0; i < n; ++i) {
-    const double ee = fma(e7, W.k2[i], fma(e6, W.k6[i], fma(e5, W.k5[i], fma(e4, W.k4[i], fma(e3, W.k3[i], e1 * W.k1[i])))));
-    const double ae = fabs(ee), ay = fabs(W.y[i]);
+    const double ee = fma(e7, k2[i], k3[i]);
+    const double ae = fabs(ee), ay = fabs(y[i]);
     const double sc = ay > 1.0 ? ay : 1.0;
     if (ae * den > num * sc) {
       num = ae;
@@ -1608,10 +1650,14 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   R.err = (num / den) * R.h;
   if (R.err <= tol) {
     R.tau = xt;
-    for (int i = 0; i < n; ++i) {
-      W.y[i] = W.yt[i];
-      W.k1[i] = W.k2[i];
-    }
+    // accept: the trial state and k7 become y and k1 by swapping rows
+    int t = R.sy;
+    R.sy = R.syt;
+    R.syt = t;
+    t = R.sk1;
+    R.sk1 = R.sk2;
+    R.sk2 = t;
+    R.ny = __longlong_as_double((long long)nbt);
     R.fails = 0;
     if (xt == xend) R.fsal = true;
   } else {
@@ -1663,7 +1709,7 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
         apply_switch(C, M, W, R);
       } else {
         if (!R.src_valid) {
-          derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.y, W.yt, R.src);
+          derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.b[R.sy], W.b[R.syt], R.src);
         }
         R.evals++;  // the output() evaluation of the reference
         const int nsrc = C.nsrc, nk = C.nk;

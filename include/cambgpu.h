@@ -223,8 +223,10 @@ int cambgpu_get_precision(void);
  * k-mode with 3/4/5 resident blocks per SM; 0 = the autotuned choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
 /* In-library autotuner: times every ODE variant and work-queue order on n cosmologies
- * and keeps the fastest for that batch-size class.  best = [team, order, class];
- * times (optional, >= 5 entries) receives ms per candidate. */
+ * and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
+ * 1 = increasing q, 2 = bands of q with the cosmologies of each band ordered by neutrino
+ * mass.  best = [team, order, class]; times (optional, >= 8 entries) receives ms per
+ * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Kernel timing of the last GPU call, in ms: [ode, spline, los, cls, h2d, d2h]. */
 int cambgpu_last_timings(double* out6);
