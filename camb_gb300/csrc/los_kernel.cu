@@ -82,6 +82,7 @@ constexpr int LOS_THREADS = 256;
 // FP64.  Everything before the projection (source k-interpolation, Bessel interval
 // search) and the Limber branch stay FP64.
 constexpr int kChunk = 16;
+constexpr int kLosMaxL = 512;  // sampled l per cosmology (the host rejects more)
 
 template <bool F32>
 __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, double* smem) {
@@ -147,24 +148,61 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
   int llmax = (int)llrint(q * tau0);
   if (llmax < 15) llmax = 17;
   else llmax = (int)llrint(q * (tau0 + 6 * 3.14159265358979323846 / q));
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const double BessIntBoost = C.AccuracyBoost * C.BessIntBoost;
   const double limber_l = 400 * sqrt(C.AccuracyBoost * C.LimberBoost);
   const double* __restrict__ tp = C.tau_points;
-  for (int j = warp; j < C.nl; j += nwarps) {
+  // Per sampled l: the integration window in time steps, whether to integrate, and the
+  // Limber value of the lensing source -- computed by one thread per l (the scalar FP64
+  // set-up would otherwise run once per warp on the FP64 pipe for each l).
+  __shared__ int s_ns[kLosMaxL], s_ne[kLosMaxL], s_flag[kLosMaxL];
+  __shared__ double s_limb[kLosMaxL];
+  enum { F_SKIP = 1, F_INT = 2, F_LIMBER = 4 };
+  for (int j = threadIdx.x; j < C.nl; j += blockDim.x) {
     const int l = C.ls[j];
-    if (l > llmax) continue;
-    const double xlim = fmax(0.0, l - 4.2 * cbrt((double)l));
-    const double xlmax1 = 80 * l * BessIntBoost;
-    const double tmin = fmax(tp[1], tau0 - xlmax1 / q);
-    const double tmax = tau0 - xlim / q;
-    if (tmax < tp[1]) continue;
-    bool doint = true;
-    if (nsrc > 2) doint = q < max(850, l) * 3 * BessIntBoost / tau0 * 1.2;
+    int flag = 0, ns = 0, ne = -1;
+    double limb = 0;
+    if (l > llmax) flag = F_SKIP;
+    else {
+      const double xlim = fmax(0.0, l - 4.2 * cbrt((double)l));
+      const double xlmax1 = 80 * l * BessIntBoost;
+      const double tmin = fmax(tp[1], tau0 - xlmax1 / q);
+      const double tmax = tau0 - xlim / q;
+      if (tmax < tp[1]) flag = F_SKIP;
+      else {
+        bool doint = true;
+        if (nsrc > 2) doint = q < max(850, l) * 3 * BessIntBoost / tau0 * 1.2;
+        if (doint) {
+          flag |= F_INT;
+          ns = time_index_of(tp, ntau, tmin);
+          ne = min(source_steps, time_index_of(tp, ntau, tmax));
+        }
+        if (nsrc > 2 && (!doint || l > limber_l)) {
+          // Limber approximation for the lensing potential (cmbmain.f90:1821-1832)
+          flag |= F_LIMBER;
+          double xf = tau0 - (l + 0.5) / q;
+          if (xf < tp[ntau - 1] && xf > tp[0]) {
+            int n = time_index_of(tp, ntau, xf);  // 1-based
+            double f = (xf - tp[n - 1]) / (tp[n] - tp[n - 1]);
+            double s_lo = (n - 1 < source_steps) ? s_raw3[n - 1] : 0.0;
+            double s_hi = (n < source_steps) ? s_raw3[n] : 0.0;
+            limb = (s_lo * (1 - f) + f * s_hi) * sqrt(3.14159265358979323846 / 2 / (l + 0.5)) / q;
+          }
+        }
+      }
+    }
+    s_flag[j] = flag;
+    s_ns[j] = ns;
+    s_ne[j] = ne;
+    s_limb[j] = limb;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int j = warp; j < C.nl; j += nwarps) {
+    const int flag = s_flag[j];
+    if (flag & F_SKIP) continue;
     double acc0 = 0, acc1 = 0, acc2 = 0;
-    if (doint) {
-      const int nstart = time_index_of(tp, ntau, tmin);
-      const int nend = min(source_steps, time_index_of(tp, ntau, tmax));
+    if (flag & F_INT) {
+      const int nstart = s_ns[j], nend = s_ne[j];
       if (F32) {
         const float4* __restrict__ H = C.bessel_f32 + (size_t)j * (nbx - 1);
         float f0 = 0.f, f1 = 0.f, f2 = 0.f;
@@ -208,17 +246,7 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
         acc2 += __shfl_xor_sync(0xffffffffu, acc2, o);
       }
     }
-    if (nsrc > 2 && (!doint || l > limber_l)) {
-      // Limber approximation for the lensing potential (cmbmain.f90:1821-1832)
-      double xf = tau0 - (l + 0.5) / q;
-      if (xf < tp[ntau - 1] && xf > tp[0]) {
-        int n = time_index_of(tp, ntau, xf);  // 1-based
-        double f = (xf - tp[n - 1]) / (tp[n] - tp[n - 1]);
-        double s_lo = (n - 1 < source_steps) ? s_raw3[n - 1] : 0.0;
-        double s_hi = (n < source_steps) ? s_raw3[n] : 0.0;
-        acc2 = (s_lo * (1 - f) + f * s_hi) * sqrt(3.14159265358979323846 / 2 / (l + 0.5)) / q;
-      } else acc2 = 0;
-    }
+    if (flag & F_LIMBER) acc2 = s_limb[j];
     if (lane == 0) {
       double* D = C.delta + ((size_t)q_ix * C.nl + j) * nsrc;
       D[0] = acc0;
@@ -230,14 +258,14 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
 
 __global__ void __launch_bounds__(LOS_THREADS) los_flat_kernel(const DevCosmo* __restrict__ cosmos) {
   const DevCosmo& C = cosmos[blockIdx.y];
-  if ((int)blockIdx.x >= C.nq) return;
+  if ((int)blockIdx.x >= C.nq || C.nl > kLosMaxL) return;
   extern __shared__ double smem[];
   los_flat_body<false>(C, blockIdx.x, smem);
 }
 
 __global__ void __launch_bounds__(LOS_THREADS) los_flat_mixed_kernel(const DevCosmo* __restrict__ cosmos) {
   const DevCosmo& C = cosmos[blockIdx.y];
-  if ((int)blockIdx.x >= C.nq) return;
+  if ((int)blockIdx.x >= C.nq || C.nl > kLosMaxL) return;
   extern __shared__ double smem[];
   los_flat_body<true>(C, blockIdx.x, smem);
 }

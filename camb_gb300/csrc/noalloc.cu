@@ -65,7 +65,8 @@ __global__ void noalloc_spline_factors(const double* __restrict__ x, int n, doub
 extern "C" int cambgpu_los_flat_noalloc(const CambGpuTables* t, const double* linear_src_dev, double* delta_dev,
                                         void* stream) {
   if (!t || !linear_src_dev || !delta_dev) return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
-  if (t->nk < 3 || t->ntau < 3 || t->nq < 1 || t->nl < 1 || t->nsrc < 2 || t->nsrc > 3 || t->num_xx < 2)
+  if (t->nk < 3 || t->ntau < 3 || t->nq < 1 || t->nl < 1 || t->nl > 512 || t->nsrc < 2 || t->nsrc > 3 ||
+      t->num_xx < 2)
     return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int dev = 0;
