@@ -87,7 +87,19 @@ struct Runtime {
   int nsm = 0;
   Arena arena;
   // Bessel tables resident on the device, keyed by host table address and shape
-  struct DevBessel { const double* host; size_t n; double* dev; double* devx; int num_xx; float4* devf; };
+  // tables stay while a staged batch may use them: only tables last used by an earlier
+  // staging (an older epoch) are evicted
+  struct DevBessel {
+    const double* host;
+    size_t n;
+    double* dev;
+    double* devx;
+    int num_xx;
+    float4* devf;
+    unsigned long epoch;
+    unsigned long long print;  // content fingerprint: host tables are freed and their addresses reused
+  };
+  unsigned long epoch = 0;
   std::vector<DevBessel> bessel;
   // pinned staging for uploads
   char* pinned = nullptr;
@@ -122,16 +134,40 @@ int rt_init() {
   return 0;
 }
 
+// FNV-1a over the shape and 64 sampled words of the table and its x grid
+unsigned long long bessel_print(const CambGpuTables& t, size_t n) {
+  unsigned long long h = 1469598103934665603ULL;
+  auto mix = [&](unsigned long long v) {
+    for (int b = 0; b < 8; ++b) {
+      h ^= (v >> (8 * b)) & 0xff;
+      h *= 1099511628211ULL;
+    }
+  };
+  mix(n);
+  mix((unsigned long long)t.num_xx);
+  for (int k = 0; k < 32; ++k) {
+    double a = t.bessel_horner[(n - 1) * k / 31], x = t.bess_x[(size_t)(t.num_xx - 1) * k / 31];
+    unsigned long long ua, ux;
+    std::memcpy(&ua, &a, 8);
+    std::memcpy(&ux, &x, 8);
+    mix(ua);
+    mix(ux);
+  }
+  return h;
+}
+
 int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4** dev_f) {
   size_t n = (size_t)t.nl * (t.num_xx - 1) * 4;
+  const unsigned long long print = bessel_print(t, n);
   for (auto& b : g_rt.bessel)
-    if (b.host == t.bessel_horner && b.n == n && b.num_xx == t.num_xx) {
+    if (b.host == t.bessel_horner && b.n == n && b.num_xx == t.num_xx && b.print == print) {
+      b.epoch = g_rt.epoch;
       *dev_h = b.dev;
       *dev_x = b.devx;
       *dev_f = b.devf;
       return 0;
     }
-  Runtime::DevBessel b{t.bessel_horner, n, nullptr, nullptr, t.num_xx, nullptr};
+  Runtime::DevBessel b{t.bessel_horner, n, nullptr, nullptr, t.num_xx, nullptr, g_rt.epoch, print};
   CUDA_TRY(cudaMalloc(&b.dev, n * sizeof(double)));
   CUDA_TRY(cudaMalloc(&b.devx, (size_t)t.num_xx * sizeof(double)));
   CUDA_TRY(cudaMalloc(&b.devf, n * sizeof(float)));
@@ -144,10 +180,15 @@ int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4
     CUDA_TRY(cudaMemcpy(b.devf, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   }
   if (g_rt.bessel.size() >= 4) {
-    cudaFree(g_rt.bessel.front().dev);
-    cudaFree(g_rt.bessel.front().devx);
-    cudaFree(g_rt.bessel.front().devf);
-    g_rt.bessel.erase(g_rt.bessel.begin());
+    for (size_t i = 0; i < g_rt.bessel.size(); ++i) {
+      auto& o = g_rt.bessel[i];
+      if (o.epoch == g_rt.epoch) continue;  // used by the batch being staged
+      cudaFree(o.dev);
+      cudaFree(o.devx);
+      cudaFree(o.devf);
+      g_rt.bessel.erase(g_rt.bessel.begin() + i);
+      break;
+    }
   }
   g_rt.bessel.push_back(b);
   *dev_h = b.dev;
@@ -400,6 +441,7 @@ struct Batch {
 int stage_batch(Batch& B, int lmax_out = 0) {
   int rc = rt_init();
   if (rc) return rc;
+  ++g_rt.epoch;
   int n = (int)B.views.size();
   size_t total = 0;
   for (auto* v : B.views) total += bytes_for(*v);

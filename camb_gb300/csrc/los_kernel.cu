@@ -207,7 +207,37 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
         const float4* __restrict__ H = C.bessel_f32 + (size_t)j * (nbx - 1);
         float f0 = 0.f, f1 = 0.f, f2 = 0.f;
         int k = 0;
-        for (int n = nstart + lane; n <= nend; n += 32) {
+        int n = nstart + lane;
+        // four independent table gathers in flight per lane
+        for (; n + 96 <= nend; n += 128) {
+          float J[4];
+          int ii[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) ii[u] = n - 1 + 32 * u;
+          float4 c[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) c[u] = __ldg(H + s_bix[ii[u]]);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float a2 = s_wf[ii[u]];
+            J[u] = fmaf(a2, fmaf(a2, fmaf(a2, c[u].w, c[u].z), c[u].y), c[u].x);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            f0 = fmaf(s_srcf[ii[u] * 3 + 0], J[u], f0);
+            f1 = fmaf(s_srcf[ii[u] * 3 + 1], J[u], f1);
+            f2 = fmaf(s_srcf[ii[u] * 3 + 2], J[u], f2);
+          }
+          k += 4;
+          if (k >= kChunk) {
+            acc0 += f0;
+            acc1 += f1;
+            acc2 += f2;
+            f0 = f1 = f2 = 0.f;
+            k = 0;
+          }
+        }
+        for (; n <= nend; n += 32) {
           const int i = n - 1;
           const float a2 = s_wf[i];
           const float4 c = __ldg(H + s_bix[i]);
@@ -215,13 +245,6 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
           f0 = fmaf(s_srcf[i * 3 + 0], J, f0);
           f1 = fmaf(s_srcf[i * 3 + 1], J, f1);
           f2 = fmaf(s_srcf[i * 3 + 2], J, f2);
-          if (++k == kChunk) {
-            acc0 += f0;
-            acc1 += f1;
-            acc2 += f2;
-            f0 = f1 = f2 = 0.f;
-            k = 0;
-          }
         }
         acc0 += f0;
         acc1 += f1;
