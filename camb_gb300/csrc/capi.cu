@@ -609,7 +609,7 @@ int run_ode(Batch& B) {
   CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
   int team = pick_team(B);
   int order = g_order >= 0 ? g_order : g_tuned[size_class(B)].order;
-  int lanes = team <= 3 ? 1 : team;
+  int lanes = team <= 5 ? 1 : team;
   int per_sm = std::max(1, ode_blocks_per_sm(team, 128));
   int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * lanes + 127) / 128);
   if (blocks < 1) blocks = 1;
@@ -983,8 +983,8 @@ int cambgpu_set_precision(int mode) {
 int cambgpu_get_precision(void) { return g_precision; }
 
 int cambgpu_set_ode_team(int lanes) {
-  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 3 && lanes != 8 && lanes != 16 && lanes != 32)
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team code must be 0, 1, 2, 3, 8, 16 or 32");
+  if (lanes < 0 || (lanes > 5 && lanes != 8 && lanes != 16 && lanes != 32))
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team code must be 0-5, 8, 16 or 32");
   g_team = lanes;
   return 0;
 }

@@ -1610,20 +1610,26 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   const double c51 = hs * a51, c52 = hs * a52, c53 = hs * a53, c54 = hs * a54;
   const double c61 = hs * a61, c62 = hs * a62, c63 = hs * a63, c64 = hs * a64, c65 = hs * a65;
   const double cb1 = hs * b1, cb3 = hs * b3, cb4 = hs * b4, cb5 = hs * b5, cb6 = hs * b6;
+#pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c21, k1[i], y[i]);
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, yt, k2, nullptr);
+#pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c32, k2[i], fma(c31, k1[i], y[i]));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), yt, k3, nullptr);
+#pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c43, k3[i], fma(c42, k2[i], fma(c41, k1[i], y[i])));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), yt, k4, nullptr);
+#pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c54, k4[i], fma(c53, k3[i], fma(c52, k2[i], fma(c51, k1[i], y[i]))));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), yt, k5, nullptr);
+#pragma unroll 4
   for (int i = 0; i < n; ++i)
     yt[i] = fma(c65, k5[i], fma(c64, k4[i], fma(c63, k3[i], fma(c62, k2[i], fma(c61, k1[i], y[i])))));
   derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k6, nullptr);
   // the fifth-order solution, the error combination of k1, k3..k6 (k3 is dead afterwards
   // and holds it) and max|yt| for the next step's hmin, in one pass
   unsigned long long nbt = 0;
+#pragma unroll 4
   for (int i = 0; i < n; ++i) {
     const double a1 = k1[i], a3 = k3[i], a4 = k4[i], a5 = k5[i], a6 = k6[i];
     const double v = fma(cb6, a6, fma(cb5, a5, fma(cb4, a4, fma(cb3, a3, fma(cb1, a1, y[i])))));
@@ -1762,6 +1768,8 @@ int ode_blocks_per_sm(int team, int threads) {
   if (team == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<3>, threads, 0);
   else if (team == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<4>, threads, 0);
   else if (team == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<5>, threads, 0);
+  else if (team == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<6>, threads, 0);
+  else if (team == 5) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<8>, threads, 0);
   else if (team == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<32>, threads, 0);
   else if (team == 16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<16>, threads, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<8>, threads, 0);
@@ -1773,6 +1781,8 @@ cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s,
   if (team == 1) tpm::ode_thread_kernel<3><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 2) tpm::ode_thread_kernel<4><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 3) tpm::ode_thread_kernel<5><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 4) tpm::ode_thread_kernel<6><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 5) tpm::ode_thread_kernel<8><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 32) ode_persistent_kernel<32><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 16) ode_persistent_kernel<16><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else ode_persistent_kernel<8><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);

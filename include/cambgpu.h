@@ -219,8 +219,9 @@ void cambgpu_batch_release(void);
  * Limber branch, C_l k-integral, interpolation and lensing stay FP64. */
 int cambgpu_set_precision(int mode);
 int cambgpu_get_precision(void);
-/* ODE kernel variant: 32/16/8 = lanes per k-mode (warp teams); 1/2/3 = one thread per
- * k-mode with 3/4/5 resident blocks per SM; 0 = the autotuned choice. */
+/* ODE kernel variant: 32/16/8 = lanes per k-mode (warp teams); 1/2/3/4/5 = one thread
+ * per k-mode compiled for 3/4/5/6/8 resident blocks of 128 per SM; 0 = the autotuned
+ * choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
 /* In-library autotuner: times every ODE variant and work-queue order on n cosmologies
  * and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
