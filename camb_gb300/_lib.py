@@ -98,6 +98,8 @@ SIGNATURES = {
     "cambgpu_batch_run": (C.c_int, [_c_double_p]),
     "cambgpu_batch_fetch": (C.c_int, [C.c_int, _c_double_p]),
     "cambgpu_batch_release": (None, []),
+    "cambgpu_batch_spectra_from_transfer": (C.c_int, [_c_double_p, _c_double_p, _c_double_p, _c_double_p, C.c_int,
+                                                        _c_double_p, _c_double_p, _c_double_p, _c_int_p]),
     "cambgpu_set_ode_team": (C.c_int, [C.c_int]),
     "cambgpu_set_precision": (C.c_int, [C.c_int]),
     "cambgpu_get_precision": (C.c_int, []),

@@ -968,6 +968,36 @@ int cambgpu_batch_fetch(int lmax_out, double* cl_out) {
   return fetch_spectra(g_res->B, lmax_out, cl_out, nullptr, nullptr);
 }
 
+int cambgpu_batch_spectra_from_transfer(const double* As, const double* ns, const double* nrun,
+                                        const double* pivot_scalar, int lmax_out, double* unlensed, double* lensed,
+                                        double* lens_potential, int* lmax_lensed) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
+  Batch& B = g_res->B;
+  const int n = (int)B.views.size();
+  if (As || ns || nrun || pivot_scalar) {
+    std::vector<DevCosmo> hc(n);
+    for (int c = 0; c < n; ++c) {
+      DevCosmo& d = B.ups[c].d;
+      if (As) d.As = As[c];
+      if (ns) d.ns = ns[c];
+      if (nrun) d.nrun = nrun[c];
+      if (pivot_scalar) d.pivot_scalar = pivot_scalar[c];
+      if (!(d.As > 0) || !(d.pivot_scalar > 0))
+        return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "As and pivot_scalar must be positive");
+      hc[c] = d;
+    }
+    CUDA_TRY(cudaMemcpyAsync(B.d_cosmos, hc.data(), (size_t)n * sizeof(DevCosmo), cudaMemcpyHostToDevice,
+                             g_rt.stream));
+  }
+  // CalcScalCls, InterpolateCls and lens_Cls from the resident transfer functions
+  int rc = run_all(B, false, false, true);
+  if (rc) return rc;
+  if (lmax_lensed)
+    for (int c = 0; c < n; ++c) lmax_lensed[c] = B.ups[c].d.lensed ? B.ups[c].d.lmax_lensed : 0;
+  return fetch_spectra(B, lmax_out, unlensed, lensed, lens_potential);
+}
+
 void cambgpu_batch_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_res.reset();

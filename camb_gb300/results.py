@@ -112,3 +112,75 @@ def get_results(params, lmax_out=None):
 def get_results_batch(params_list, lmax_out=None):
     """Many cosmologies in one persistent launch per stage."""
     return _run(params_list, max(p.max_l for p in params_list) if lmax_out is None else lmax_out)
+
+
+class _ResidentBatch:
+    """A batch whose tables and transfer functions stay on the device (one at a time:
+    staging another batch retires this one)."""
+
+    generation = 0
+
+    def __init__(self, params_list):
+        lib = _lib.load()
+        self.params = list(params_list)
+        n = len(self.params)
+        arr = (_lib.CambGpuParams * n)(*[p.to_struct() for p in self.params])
+        _lib.check(lib.cambgpu_batch_prepare(arr, n))
+        _lib.check(lib.cambgpu_batch_run(None))
+        _ResidentBatch.generation += 1
+        self.gen = _ResidentBatch.generation
+        self.lmax = max(p.max_l for p in self.params)
+
+    def spectra(self):
+        """Recomputes C_l from the resident transfer functions with every member's current
+        primordial power."""
+        if self.gen != _ResidentBatch.generation:
+            raise _lib.CAMBError("these transfer functions are no longer resident on the device")
+        lib = _lib.load()
+        n = len(self.params)
+        As = np.array([p.InitPower.As for p in self.params])
+        ns = np.array([p.InitPower.ns for p in self.params])
+        nrun = np.array([p.InitPower.nrun for p in self.params])
+        piv = np.array([p.InitPower.pivot_scalar for p in self.params])
+        cls = np.zeros((n, self.lmax + 1, 4))
+        lensed = np.zeros((n, self.lmax + 1, 4))
+        pot = np.zeros((n, self.lmax + 1, 3))
+        lml = np.zeros(n, dtype=np.int32)
+        _lib.check(lib.cambgpu_batch_spectra_from_transfer(_lib.dptr(As), _lib.dptr(ns), _lib.dptr(nrun),
+                                                           _lib.dptr(piv), self.lmax, _lib.dptr(cls),
+                                                           _lib.dptr(lensed), _lib.dptr(pot), _lib.iptr(lml)))
+        return cls, lensed, pot, lml
+
+
+class CAMBdataTransfers(CAMBdata):
+    """CAMBdata from get_transfer_functions: the transfer functions stay on the device and
+    power_spectra_from_transfer recomputes the spectra for new primordial power without
+    re-evolving (camb/results.py power_spectra_from_transfer, camb.f90:25-58)."""
+
+    def __init__(self, batch, index):
+        self._batch, self._index = batch, index
+        super().__init__(batch.params[index], None)
+        self._refresh(batch.spectra())
+
+    def _refresh(self, out):
+        cls, lensed, pot, lml = out
+        i = self._index
+        self._cls = cls[i][: self.Params.max_l + 1]
+        self._lensed = lensed[i] if self.Params.DoLensing else None
+        self._pot = pot[i][: self.Params.max_l + 1] if self.Params.DoLensing else None
+        self._lmax_lensed = int(lml[i])
+
+    def power_spectra_from_transfer(self, initial_power_params=None, silent=False):
+        if initial_power_params is not None:
+            self.Params.InitPower = initial_power_params
+        self._refresh(self._batch.spectra())
+
+
+def get_transfer_functions(params):
+    """camb.get_transfer_functions (camb.py:64-79) for the scalar CMB path."""
+    return CAMBdataTransfers(_ResidentBatch([params]), 0)
+
+
+def get_transfer_functions_batch(params_list):
+    batch = _ResidentBatch(params_list)
+    return [CAMBdataTransfers(batch, i) for i in range(len(params_list))]

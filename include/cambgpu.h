@@ -208,6 +208,14 @@ int cambgpu_batch_prepare(const CambGpuParams* p, int n);
 int cambgpu_batch_run(double* ms3);
 /* C_l of the last run, [n][lmax_out+1][4] as cambgpu_get_results. */
 int cambgpu_batch_fetch(int lmax_out, double* cl_out);
+/* CAMBdata.power_spectra_from_transfer (camb/results.py, camb.f90:25-58): new primordial
+ * power (per-cosmology As, ns, nrun, pivot_scalar; a NULL array keeps the current
+ * values) applied to the resident batch's transfer functions Delta_p_l_k without
+ * re-evolving: C_l k-integral, interpolation and lensing rerun on the device.  Outputs as
+ * cambgpu_get_spectra_batch (any may be NULL). */
+int cambgpu_batch_spectra_from_transfer(const double* As, const double* ns, const double* nrun,
+                                        const double* pivot_scalar, int lmax_out, double* unlensed, double* lensed,
+                                        double* lens_potential, int* lmax_lensed);
 void cambgpu_batch_release(void);
 
 /* ---- runtime ---- */
