@@ -35,6 +35,9 @@ class CambGpuParams(C.Structure):
         ("TimeSwitchBoost", C.c_double), ("LimberBoost", C.c_double), ("BackgroundTimeStepBoost", C.c_double),
         ("accurate_polarization", C.c_int), ("accurate_reionization", C.c_int),
         ("LensingBoost", C.c_double),
+        ("want_cls", C.c_int), ("want_transfer", C.c_int), ("transfer_high_precision", C.c_int),
+        ("transfer_kmax", C.c_double), ("num_transfer_redshifts", C.c_int), ("transfer_redshifts", C.c_double * 16),
+        ("reion_use_optical_depth", C.c_int), ("reion_redshift", C.c_double),
     ]
 
 
@@ -74,6 +77,8 @@ class CambGpuTables(C.Structure):
         ("Alens", C.c_double),
         ("max_l", C.c_int), ("do_lensing", C.c_int), ("cl_template_scale", C.c_double),
         ("lens_accuracy_boost", C.c_double),
+        ("transfer_only", C.c_int), ("num_transfer_times", C.c_int), ("transfer_times", _c_double_p),
+        ("hubble_h", C.c_double), ("want_cls", C.c_int), ("late_phot_switch_boost_min", C.c_double),
     ]
 
 
@@ -93,6 +98,8 @@ SIGNATURES = {
     "cambgpu_get_results_batch": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, _c_double_p, _c_int_p]),
     "cambgpu_get_spectra_batch": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, _c_double_p, _c_double_p,
                                               _c_double_p, _c_int_p, _c_int_p]),
+    "cambgpu_get_transfer_batch": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, C.POINTER(C.c_float),
+                                               _c_int_p, _c_double_p, _c_double_p, _c_int_p]),
     "cambgpu_lensing_range": (C.c_int, [C.POINTER(CambGpuTables), _c_int_p]),
     "cambgpu_batch_prepare": (C.c_int, [C.POINTER(CambGpuParams), C.c_int]),
     "cambgpu_batch_run": (C.c_int, [_c_double_p]),

@@ -827,6 +827,14 @@ void cambgpu_default_params(CambGpuParams* p) {
   p->accurate_polarization = 1;
   p->accurate_reionization = 1;
   p->LensingBoost = 1;
+  p->want_cls = 1;
+  p->want_transfer = 0;
+  p->transfer_high_precision = 1;
+  p->transfer_kmax = 1.2;  // set_matter_power default kmax
+  p->num_transfer_redshifts = 1;
+  p->transfer_redshifts[0] = 0;
+  p->reion_use_optical_depth = 1;
+  p->reion_redshift = 10;
 }
 
 int cambgpu_tables_create(const CambGpuParams* p, void** handle) {

@@ -710,14 +710,17 @@ static double get_tau_start(const Cosmology& c, double q) {
 }
 
 // MassiveNuTransferSwitchBoost / MassiveNuTransferLAccuracyBoost (equations.f90:484-510)
+// high-precision matter transfer functions requested (Transfer%high_precision with WantTransfer)
+static bool transfer_hp(const CambGpuParams& P) { return P.want_transfer && P.transfer_high_precision; }
 static double nu_switch_boost(const Cosmology& c, double nu_mass) {
   double b = c.P.AccuracyBoost * c.P.TimeSwitchBoost;
-  if (nu_mass > 600) b *= 2;  // AccuracyTarget > 0 and WantCls
+  // AccuracyTarget > 0 and (high-precision transfers or WantCls)
+  if (nu_mass > 600 && (transfer_hp(c.P) || c.P.want_cls)) b *= 2;
   return b;
 }
 static double nu_l_boost(const Cosmology& c, double nu_mass, double q, double tau_nonrel_phys) {
   double b = c.P.lAccuracyBoost;
-  if (nu_mass > 600 && q * tau_nonrel_phys < 500) b *= 2.0;
+  if (nu_mass > 600 && q * tau_nonrel_phys < 500) b *= transfer_hp(c.P) ? 2.15 : 2.0;
   return b;
 }
 
@@ -1012,7 +1015,7 @@ static double opacity_to_time(const Cosmology& c, double opacity) {
   return std::exp(j * c.dlntau) * c.tauminn;
 }
 
-static CambGpuModeSpec mode_setup(const Cosmology& c, double q) {
+static CambGpuModeSpec mode_setup(const Cosmology& c, double q, bool transfer_only = false) {
   const CambGpuParams& P = c.P;
   CambGpuModeSpec m{};
   m.q = q;
@@ -1031,11 +1034,16 @@ static CambGpuModeSpec mode_setup(const Cosmology& c, double q) {
       m.nq0[i] = (q_rel >= c.nqmax - 2) ? c.nqmax : q_rel;
       m.nu_l_boost[i] = nu_l_boost(c, c.nu_masses[i], q, c.nu_tau_nonrel_phys[i]);
     }
-    lmaxnu = std::max(3, nint(10 * lab));
-    if (max_nu_mass > 700) lmaxnu = std::max(3, nint(15 * lab));
-    for (int i = 0; i < c.nu_eig; ++i) {
-      lmaxnu = std::max(lmaxnu, nint(10 * m.nu_l_boost[i]));
-      if (c.nu_masses[i] > 700) lmaxnu = std::max(lmaxnu, nint(15 * m.nu_l_boost[i]));
+    if (transfer_hp(P)) {
+      lmaxnu = nint(25 * lab);
+      for (int i = 0; i < c.nu_eig; ++i) lmaxnu = std::max(lmaxnu, nint(25 * m.nu_l_boost[i]));
+    } else {
+      lmaxnu = std::max(3, nint(10 * lab));
+      if (max_nu_mass > 700) lmaxnu = std::max(3, nint(15 * lab));
+      for (int i = 0; i < c.nu_eig; ++i) {
+        lmaxnu = std::max(lmaxnu, nint(10 * m.nu_l_boost[i]));
+        if (c.nu_masses[i] > 700) lmaxnu = std::max(lmaxnu, nint(15 * m.nu_l_boost[i]));
+      }
     }
   }
   m.lmaxnu = lmaxnu;
@@ -1044,7 +1052,7 @@ static CambGpuModeSpec mode_setup(const Cosmology& c, double q) {
   if (max_nu_mass > 700) lmaxnr = std::max(nint(32 * lab), min_lmaxnr);
   int lmaxgpol = lmaxg;
   if (!P.accurate_polarization) lmaxgpol = std::max(nint(4 * lab), 3);
-  else if (q > 0.15) {  // AccuracyTarget > 0 and Want_CMB
+  else if (P.want_cls && q > 0.15) {  // AccuracyTarget > 0 and Want_CMB
     lmaxg = std::max(lmaxg, nint(13 * lab));
     lmaxgpol = std::max(lmaxgpol, nint(14 * lab));
   }
@@ -1057,6 +1065,25 @@ static CambGpuModeSpec mode_setup(const Cosmology& c, double q) {
       lmaxg = lmaxg * 8;  // AccuracyTarget > 0
       lmaxgpol = lmaxgpol * 2;
     }
+  }
+  if (transfer_only) {
+    lmaxgpol = std::min(lmaxgpol, nint(5 * lab));
+    lmaxg = std::min(lmaxg, nint(6 * lab));
+  }
+  if (transfer_hp(P) && q > 0.03 && q < 0.2) {  // AccuracyTarget > 0
+    lmaxg = std::max(lmaxg, nint(12 * lab));
+    lmaxgpol = std::max(lmaxgpol, nint(5 * lab));
+  }
+  if (transfer_hp(P)) {
+    // the massless-neutrino hierarchy across transfer scales (equations.f90:979-993)
+    if (q >= 0.005) lmaxnr = std::max(lmaxnr, nint(4 * lab));
+    if (q >= 0.010 && q < 0.05)
+      lmaxnr = std::max(std::max(lmaxnr, nint((8.0 + 6.0 * (q - 0.010) / 0.040) * lab)), min_lmaxnr);
+    else if (q >= 0.05 && q < 0.12)
+      lmaxnr = std::max(std::max(lmaxnr, nint((14.0 + 31.0 * (q - 0.05) / 0.07) * lab)), min_lmaxnr);
+    else if (q >= 0.12)
+      lmaxnr = std::max(nint(45 * lab), min_lmaxnr);
+    if (q > 0.04 && q < 0.5) lmaxg = std::max(lmaxg, nint(10 * lab));
   }
   if (lmaxnr < lmaxnu) lmaxnr = lmaxnu;
   m.lmaxg = lmaxg;
@@ -1234,8 +1261,11 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
   Reion& R = c.reion;
   R.fHe = c.fHe;
   R.delta_redshift = P.reion_delta_redshift;
-  R.on = P.optical_depth >= 0.001;
-  if (R.on) {
+  R.on = P.reion_use_optical_depth ? P.optical_depth >= 0.001 : P.reion_redshift > 0;
+  if (R.on && !P.reion_use_optical_depth) {
+    R.fraction = 1 + c.fHe;
+    R.set_zre(P.reion_redshift);
+  } else if (R.on) {
     R.fraction = 1 + c.fHe;
     auto reion_tau = [&](double zre) {
       R.set_zre(zre);
@@ -1257,12 +1287,32 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
   c.dtaurec = 4 / c.qmax / initAccuracyBoost;
   c.max_etak_scalar = initAccuracyBoost * std::max(1700.0, c.maximum_qeta) / 20;
   if (c.maximum_qeta < 3500 && P.AccuracyBoost < 2) c.max_etak_scalar *= 1.5;
-  double taumin = get_tau_start(c, c.qmax);
+  const bool transfer_only = P.want_transfer && !P.want_cls;
+  if (P.want_transfer && P.want_cls) {
+    err = "transfer functions are computed without the CMB (set want_cls = 0)";
+    return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  }
+  if (P.want_transfer) {
+    if (!(P.transfer_kmax > 0) || P.num_transfer_redshifts < 1 || P.num_transfer_redshifts > 16) {
+      err = "transfer kmax and 1-16 redshifts required";
+      return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+    }
+    for (int i = 1; i < P.num_transfer_redshifts; ++i)
+      if (!(P.transfer_redshifts[i] < P.transfer_redshifts[i - 1])) {
+        err = "transfer redshifts must be strictly decreasing";
+        return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+      }
+  }
+  // maxq: qmax with the CMB, Transfer%kmax without; the transfer grid runs 5% past kmax
+  double maxq = transfer_only ? P.transfer_kmax : c.qmax;
+  if (P.want_transfer) maxq = std::max(maxq, P.transfer_kmax * 1.05);
+  double taumin = get_tau_start(c, maxq);
   int rc = recfast_init(c, err);
   if (rc) return rc;
   rc = thermo_init(c, taumin, err);
   if (rc) return rc;
   // The logarithmic part of the source k grid ends at min(dkn1/dlnk0, q_switch),
+  // (CMB only)
   // which exceeds qmax when max_eta_k is small (lmax below ~220): its modes would start
   // before the thermal tables (the reference stops with 'thermo out of bounds' there).
   // Extend the tables back to the start time of the largest grid wavenumber.
@@ -1272,7 +1322,7 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
     if (P.accurate_reionization) dlnk0 /= 2;
     if (c.reion.on && P.accurate_polarization && P.accurate_reionization) dlnk0 = std::min(dlnk0, 0.075);
     double qlog_end = std::min(0.6 / c.taurst / SAB / dlnk0, 2 * 6.3 / c.taurst);
-    if (qlog_end > c.qmax * 1.0001) {
+    if (!transfer_only && qlog_end > c.qmax * 1.0001) {
       double dtaurec0 = 4 / c.qmax / initAccuracyBoost;
       c.dtaurec = dtaurec0;
       rc = thermo_init(c, get_tau_start(c, 1.2 * qlog_end), err);
@@ -1346,7 +1396,54 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
   }
   c.tol1 = 1e-4 / std::exp(P.AccuracyBoost * P.IntTolBoost - 1);
   c.modes.clear();
-  for (double q : c.evolve_q.points) c.modes.push_back(mode_setup(c, q));
+  if (transfer_only) {
+    if (transfer_hp(P)) c.tol1 /= 100;  // CalcScalarSources / GetTransfer
+    // transfer times: cumulative DeltaTime over the decreasing redshifts (TimeOfzArr,
+    // results.f90:683-711)
+    c.transfer_times.assign(P.num_transfer_redshifts, 0.0);
+    for (int i = 0; i < P.num_transfer_redshifts; ++i) {
+      double t = i == 0 ? c.delta_time(0, 1 / (1 + P.transfer_redshifts[0]))
+                        : c.delta_time(1 / (1 + P.transfer_redshifts[i - 1]), 1 / (1 + P.transfer_redshifts[i]));
+      c.transfer_times[i] = i == 0 ? t : c.transfer_times[i - 1] + t;
+    }
+    // InitTransfer optimized spacing, no CMB (cmbmain.f90:573-645); k_per_logint = 0,
+    // TransferkBoost = 1
+    double boost = P.AccuracyBoost * (transfer_hp(P) ? 1.5 : 1.0);
+    double kmax = P.transfer_kmax;
+    double q_switch_lowk1 = 0.7 / c.taurst, dlog_lowk1 = 2 * boost;
+    double q_switch_lowk = 8 / c.taurst, dlog_lowk = 8 * boost * 2.5;
+    double q_switch_osc = std::min(kmax, 30 / c.taurst), d_osc = 200 * boost * 1.8;
+    double dlog_osc = 17 * boost;
+    double q_switch_highk = std::min(kmax, 90 / c.taurst);
+    double dlog_highk = 3 * boost;
+    const double amin = 5e-5;
+    std::vector<double>& qt = c.q_trans;
+    qt.clear();
+    int nq = (int)(std::log(q_switch_lowk1 / amin) * dlog_lowk1) + 1;
+    for (int i = 1; i <= nq; ++i) qt.push_back(amin * std::exp((i - 1) / dlog_lowk1));
+    double last = qt.back();
+    nq = (int)(std::log(q_switch_lowk / last) * dlog_lowk) + 1;
+    for (int i = 1; i <= nq; ++i) qt.push_back(last * std::exp(i / dlog_lowk));
+    last = qt.back();
+    if (q_switch_osc > q_switch_lowk) {
+      nq = (int)((q_switch_osc - last) * d_osc) + 1;
+      for (int i = 1; i <= nq; ++i) qt.push_back(last + i / d_osc);
+      last = qt.back();
+    }
+    if (kmax > last) {
+      nq = (int)(std::log(q_switch_highk / last) * dlog_osc) + 1;
+      for (int i = 1; i <= nq; ++i) qt.push_back(last * std::exp(i / dlog_osc));
+      last = qt.back();
+    }
+    if (kmax > last) {
+      nq = (int)(std::log(kmax / last) * dlog_highk) + 1;
+      dlog_highk = nq / std::log(kmax * 1.05 / last);
+      for (int i = 1; i <= nq; ++i) qt.push_back(last * std::exp(i / dlog_highk));
+    }
+    for (double q : qt) c.modes.push_back(mode_setup(c, q, true));
+  } else {
+    for (double q : c.evolve_q.points) c.modes.push_back(mode_setup(c, q));
+  }
   return 0;
 }
 
@@ -1501,7 +1598,19 @@ void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   v.emmu = c.emmu.data(); v.demmu = c.demmu.data();
   v.ntau = c.timesteps.npoints(); v.tau_points = c.timesteps.points.data();
   v.tau_dpoints = c.timesteps.dpoints.data();
-  v.nk = c.evolve_q.npoints(); v.q_evolve = c.evolve_q.points.data(); v.modes = c.modes.data();
+  const bool transfer_only = c.P.want_transfer && !c.P.want_cls;
+  if (transfer_only) {
+    v.nk = (int)c.q_trans.size(); v.q_evolve = c.q_trans.data(); v.modes = c.modes.data();
+  } else {
+    v.nk = c.evolve_q.npoints(); v.q_evolve = c.evolve_q.points.data(); v.modes = c.modes.data();
+  }
+  v.transfer_only = transfer_only ? 1 : 0;
+  v.num_transfer_times = transfer_only ? (int)c.transfer_times.size() : 0;
+  v.transfer_times = transfer_only ? c.transfer_times.data() : nullptr;
+  v.hubble_h = c.P.H0 / 100;
+  v.want_cls = c.P.want_cls;
+  // latePhotSwitchBoost >= 2 for high-precision transfers (AccuracyTarget > 0)
+  v.late_phot_switch_boost_min = transfer_hp(c.P) ? 2.0 : 0.0;
   v.nq = c.q_int.npoints(); v.q_int = c.q_int.points.data(); v.dq_int = c.q_int.dpoints.data();
   v.nl = (int)c.ls.size(); v.ls = c.ls.data();
   v.num_xx = (int)b.x.size(); v.bess_x = b.x.data(); v.bessel_horner = b.horner.data();

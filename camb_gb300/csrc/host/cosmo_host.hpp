@@ -104,7 +104,8 @@ struct Cosmology {
   // grids
   Ranges timesteps, evolve_q, q_int;
   std::vector<int> ls;
-  std::vector<CambGpuModeSpec> modes;
+  std::vector<CambGpuModeSpec> modes;       // per k mode: the source grid, or q_trans without the CMB
+  std::vector<double> q_trans, transfer_times;  // transfer k grid and times (transfer functions only)
   int nsrc;
   double tol1;
 

@@ -58,6 +58,15 @@ typedef struct CambGpuParams {
     double TimeSwitchBoost, LimberBoost, BackgroundTimeStepBoost;
     int accurate_polarization, accurate_reionization;
     double LensingBoost;         /* AccuracyParams%LensingBoost (lensing theta sampling and range) */
+    /* matter transfer functions (CAMBparams%Transfer, model.py set_matter_power) */
+    int want_cls;                /* 1: CMB sources and C_l; 0: matter transfer functions only */
+    int want_transfer;           /* 1: transfer functions at transfer_redshifts (with want_cls = 0) */
+    int transfer_high_precision; /* Transfer%high_precision (set_matter_power sets it) */
+    double transfer_kmax;        /* Transfer%kmax in 1/Mpc */
+    int num_transfer_redshifts;  /* 1..16, in decreasing order as set_matter_power sorts them */
+    double transfer_redshifts[16];
+    int reion_use_optical_depth; /* 1: optical_depth fixes the reionization redshift; 0: reion_redshift does */
+    double reion_redshift;
 } CambGpuParams;
 
 /* Per-k-mode setup: the hierarchy sizes of GetNumEqns (equations.f90:860-1070)
@@ -136,6 +145,15 @@ typedef struct CambGpuTables {
     int do_lensing;             /* lens the C_l (CP%DoLensing) */
     double cl_template_scale;   /* lSamples%template_l_scale (results.f90:1517-1520) */
     double lens_accuracy_boost; /* AccuracyBoost * LensingBoost */
+    /* transfer functions only: q_evolve/modes are then the transfer k grid (InitTransfer,
+     * cmbmain.f90:564-704) and every mode is evolved to each transfer time (GetTransfer,
+     * cmbmain.f90:1167-1188) */
+    int transfer_only;
+    int num_transfer_times;
+    const double* transfer_times; /* tau of the transfer redshifts, increasing */
+    double hubble_h;              /* H0/100 */
+    int want_cls;
+    double late_phot_switch_boost_min; /* 2 for high-precision transfers (equations.f90:318-320), else 0 */
 } CambGpuTables;
 
 /* Fills p with the reference's defaults (model.f90:36-209, Python set_params). */
@@ -196,6 +214,21 @@ int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, doubl
  * lmax_lensed[n] (0 for cosmologies without lensing) when that pointer is not NULL. */
 int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
                               double* lens_potential, int* lmax_lensed, int* status);
+/* Matter transfer functions of n cosmologies with want_cls = 0 and want_transfer = 1
+ * (camb.get_results after set_matter_power; outtransf, equations.f90:2256-2271, and
+ * Transfer_Get_sigmas, results.f90:4115-4182).  Per cosmology, with nq_max entries
+ * reserved per redshift:
+ *   transfer: [n][nz][nq_max][13] float, MatterTransferData%TransferData(13, nq, nz) in
+ *             Fortran order (k/h, then CDM, baryon, photon, massless nu, massive nu, total,
+ *             total without nu, total with dark energy, Weyl k^2 Phi, Newtonian CDM and
+ *             baryon velocities, baryon-CDM velocity, each over k^2), single precision as
+ *             the reference stores it;
+ *   nq:       [n] number of transfer wavenumbers used;
+ *   sigma8, sigma2_vdelta_8: [n][nz] at R = 8 Mpc/h (the redshift order of the input).
+ * Any output pointer may be NULL. */
+int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float* transfer, int* nq, double* sigma8,
+                               double* sigma2_vdelta_8, int* status);
+
 /* Lensing l range of a cosmology's tables: out3 = {lmax of the lensing sums
  * (LensingExtrapLmax, lensing.f90:161-177), lmax_lensed (InitLensedClArrays,
  * lensing.f90:230-247), number of theta points}. */
