@@ -78,7 +78,8 @@ class CambGpuTables(C.Structure):
         ("max_l", C.c_int), ("do_lensing", C.c_int), ("cl_template_scale", C.c_double),
         ("lens_accuracy_boost", C.c_double),
         ("transfer_only", C.c_int), ("num_transfer_times", C.c_int), ("transfer_times", _c_double_p),
-        ("hubble_h", C.c_double), ("want_cls", C.c_int), ("late_phot_switch_boost_min", C.c_double),
+        ("hubble_h", C.c_double), ("want_cls", C.c_int), ("transfer_high_precision", C.c_int),
+        ("late_phot_switch_boost_min", C.c_double),
     ]
 
 

@@ -933,6 +933,12 @@ int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, doubl
   return cambgpu_get_spectra_batch(p, n, lmax_out, cl_out, nullptr, nullptr, nullptr, status);
 }
 
+int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float* transfer, int* nq, double* sigma8,
+                               double* sigma2_vdelta_8, int* status) {
+  (void)p; (void)n; (void)nq_max; (void)transfer; (void)nq; (void)sigma8; (void)sigma2_vdelta_8; (void)status;
+  return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "not built");
+}
+
 int cambgpu_lensing_range(const CambGpuTables* t, int* out3) {
   HostLensGeom h;
   int rc = lens_geometry(*t, h);

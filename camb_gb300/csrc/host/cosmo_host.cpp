@@ -1609,6 +1609,7 @@ void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   v.transfer_times = transfer_only ? c.transfer_times.data() : nullptr;
   v.hubble_h = c.P.H0 / 100;
   v.want_cls = c.P.want_cls;
+  v.transfer_high_precision = transfer_hp(c.P) ? 1 : 0;
   // latePhotSwitchBoost >= 2 for high-precision transfers (AccuracyTarget > 0)
   v.late_phot_switch_boost_min = transfer_hp(c.P) ? 2.0 : 0.0;
   v.nq = c.q_int.npoints(); v.q_int = c.q_int.points.data(); v.dq_int = c.q_int.dpoints.data();

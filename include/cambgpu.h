@@ -153,6 +153,7 @@ typedef struct CambGpuTables {
     const double* transfer_times; /* tau of the transfer redshifts, increasing */
     double hubble_h;              /* H0/100 */
     int want_cls;
+    int transfer_high_precision;       /* Transfer%high_precision with transfers requested */
     double late_phot_switch_boost_min; /* 2 for high-precision transfers (equations.f90:318-320), else 0 */
 } CambGpuTables;
 

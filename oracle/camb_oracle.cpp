@@ -53,6 +53,7 @@ struct EvolutionVars {
   double MassiveNuApproxTime[max_nu], G11[max_nu], G30[max_nu], nu_l_boost[max_nu];
   double denlk[max_l_evolve + 1], denlk2[max_l_evolve + 1], polfack[max_l_evolve + 1];
   double* OutputSources;  // non-null inside output()
+  double* OutputTransfer;  // non-null inside outtransf(): 13 transfer variables
 };
 
 struct RKSettings {
@@ -193,11 +194,16 @@ void get_num_eqns(const Ctx& C, EvolutionVars& EV, const CambGpuModeSpec& ms) {
       EV.nu_nonrelativistic[i] = false;
       EV.nu_l_boost[i] = ms.nu_l_boost[i];  // MassiveNuTransferLAccuracyBoost, a host input
     }
-    EV.lmaxnu = std::max(3, nint(10 * lab));
-    if (max_nu_mass > 700) EV.lmaxnu = std::max(3, nint(15 * lab));
-    for (int i = 0; i < T->nu_eig; ++i) {
-      EV.lmaxnu = std::max(EV.lmaxnu, nint(10 * EV.nu_l_boost[i]));
-      if (T->nu_masses[i] > 700) EV.lmaxnu = std::max(EV.lmaxnu, nint(15 * EV.nu_l_boost[i]));
+    if (T->transfer_high_precision) {
+      EV.lmaxnu = nint(25 * lab);
+      for (int i = 0; i < T->nu_eig; ++i) EV.lmaxnu = std::max(EV.lmaxnu, nint(25 * EV.nu_l_boost[i]));
+    } else {
+      EV.lmaxnu = std::max(3, nint(10 * lab));
+      if (max_nu_mass > 700) EV.lmaxnu = std::max(3, nint(15 * lab));
+      for (int i = 0; i < T->nu_eig; ++i) {
+        EV.lmaxnu = std::max(EV.lmaxnu, nint(10 * EV.nu_l_boost[i]));
+        if (T->nu_masses[i] > 700) EV.lmaxnu = std::max(EV.lmaxnu, nint(15 * EV.nu_l_boost[i]));
+      }
     }
   }
   EV.high_ktau_neutrino_approx = false;
@@ -211,7 +217,7 @@ void get_num_eqns(const Ctx& C, EvolutionVars& EV, const CambGpuModeSpec& ms) {
   if (max_nu_mass > 700) EV.lmaxnr = std::max(nint(32 * lab), min_lmaxnr);
   EV.lmaxgpol = EV.lmaxg;
   if (!T->accurate_polarization) EV.lmaxgpol = std::max(nint(4 * lab), 3);
-  else if (EV.q > 0.15) {
+  else if (T->want_cls && EV.q > 0.15) {  // AccuracyTarget > 0 and Want_CMB
     EV.lmaxg = std::max(EV.lmaxg, nint(13 * lab));
     EV.lmaxgpol = std::max(EV.lmaxgpol, nint(14 * lab));
   }
@@ -224,6 +230,27 @@ void get_num_eqns(const Ctx& C, EvolutionVars& EV, const CambGpuModeSpec& ms) {
       EV.lmaxg = EV.lmaxg * 8;
       EV.lmaxgpol = EV.lmaxgpol * 2;
     }
+  }
+  if (T->transfer_only) {  // EV%TransferOnly (equations.f90:968-971)
+    EV.lmaxgpol = std::min(EV.lmaxgpol, nint(5 * lab));
+    EV.lmaxg = std::min(EV.lmaxg, nint(6 * lab));
+  }
+  if (T->transfer_high_precision && EV.q > 0.03 && EV.q < 0.2) {  // equations.f90:974-978
+    EV.lmaxg = std::max(EV.lmaxg, nint(12 * lab));
+    EV.lmaxgpol = std::max(EV.lmaxgpol, nint(5 * lab));
+  }
+  if (T->transfer_high_precision) {  // equations.f90:979-996
+    if (EV.q >= 0.005) EV.lmaxnr = std::max(EV.lmaxnr, nint(4 * lab));
+    if (EV.q >= 0.010 && EV.q < 0.05) {
+      double t = (8.0 + 6.0 * (EV.q - 0.010) / 0.040) * lab;
+      EV.lmaxnr = std::max(std::max(EV.lmaxnr, nint(t)), min_lmaxnr);
+    } else if (EV.q >= 0.05 && EV.q < 0.12) {
+      double t = (14.0 + 31.0 * (EV.q - 0.05) / 0.07) * lab;
+      EV.lmaxnr = std::max(std::max(EV.lmaxnr, nint(t)), min_lmaxnr);
+    } else if (EV.q >= 0.12) {
+      EV.lmaxnr = std::max(nint(45 * lab), min_lmaxnr);
+    }
+    if (EV.q > 0.04 && EV.q < 0.5) EV.lmaxg = std::max(EV.lmaxg, nint(10 * lab));
   }
   if (EV.lmaxnr < EV.lmaxnu) EV.lmaxnr = EV.lmaxnu;
   EV.poltruncfac = (double)EV.lmaxgpol / std::max(1, EV.lmaxgpol - 2);
@@ -603,8 +630,8 @@ void derivs(const Ctx& C, EvolutionVars& EV, int n, double tau, const double* ay
     ind2++;
     ayprime[ind] = k * (ay[ind - 1] - a2 * ay[ind2 - 1]) - (EV.lmaxnu_pert + 1) * cothxor * ay[ind];
   }
-  if (!EV.OutputSources) return;
-  // ---- source output (equations.f90:2775-2912) ----
+  if (!EV.OutputSources && !EV.OutputTransfer) return;
+  // ---- source and transfer output (equations.f90:2775-2912) ----
   double E[4] = {0, 0, 0, 0}, Edot[4] = {0, 0, 0, 0}, octg, octgdot;
   if (!(EV.TightCoupling || EV.no_phot_multpoles)) {
     E[2] = ay[EV.polind + 2];
@@ -637,6 +664,7 @@ void derivs(const Ctx& C, EvolutionVars& EV, int n, double tau, const double* ay
   double dgpi = grhor_t * pir + grhog_t * pig;
   double dgpi_diff = 0;
   double pidot_sum = grhog_t * pigdot + grhor_t * pirdot;
+  double grhonu_out = 0, dgrhonu_out = 0;
   for (int i = 0; i < T->nu_eig; ++i) {  // MassiveNuVarsOut (equations.f90:1113-1176)
     double grhormass_t = T->grhormass[i] / (a * a), rhonu, pnu, clxnu, qnu, pinu, pinudot;
     nufit::rho_P(a * T->nu_masses[i], rhonu, pnu);
@@ -655,9 +683,10 @@ void derivs(const Ctx& C, EvolutionVars& EV, int n, double tau, const double* ay
       pinudot = nu_pinudot(EV, ay, ayprime, a, adotoa, i);
       pinudot = pinudot / rhonu - rhonudot / rhonu * pinu;
     }
-    (void)clxnu;
     (void)qnu;
     double g_t = grhormass_t * rhonu, gp_t = grhormass_t * pnu;
+    grhonu_out += g_t;
+    dgrhonu_out += g_t * clxnu;
     dgpi += g_t * pinu;
     dgpi_diff += pinu * (3 * gp_t - g_t);
     pidot_sum += g_t * pinudot;
@@ -665,6 +694,23 @@ void derivs(const Ctx& C, EvolutionVars& EV, int n, double tau, const double* ay
   gpres = gpres_noDE + w_dark_energy_t * grhov_t;
   double diff_rhopi = pidot_sum - (4 * dgpi + dgpi_diff) * adotoa;
   double phi = -((dgrho + 3 * dgq * adotoa / k) + dgpi) / (2 * k2);
+  if (EV.OutputTransfer) {  // equations.f90:2832-2845
+    double* O = EV.OutputTransfer;
+    O[0] = k / T->hubble_h;
+    O[1] = clxc;
+    O[2] = clxb;
+    O[3] = clxg;
+    O[4] = clxr;
+    O[5] = T->nu_eig > 0 ? dgrhonu_out / grhonu_out : 0.0;  // clxnu_all
+    O[6] = dgrho_matter / grho_matter;
+    O[7] = (grhob_t * clxb + grhoc_t * clxc) / (grhob_t + grhoc_t);
+    O[8] = dgrho / grho_matter;
+    O[9] = k2 * phi;
+    O[10] = -k * sigma / adotoa;
+    O[11] = -k * (vb + sigma) / adotoa;
+    O[12] = vb;
+  }
+  if (!EV.OutputSources) return;
   double ddopacity, visibility, dvisibility, ddvisibility, exptau;
   ionization_functions(C, tau, a, opacity, dopacity, ddopacity, visibility, dvisibility, ddvisibility, exptau);
   double tau0 = T->tau0;
@@ -845,7 +891,7 @@ void switch_to_massive_nu_approx(EvolutionVars& EV, double a, std::vector<double
 
 bool scal_ev(const Ctx& C, EvolutionVars& EV, double* y, double& tau, double tauend, double tol1, int& ind,
              RKSettings& s, std::vector<double>* w, ModeStats& st) {
-  if (EV.q < 2e-3 && tau <= C.T->taurend) s.max_step_size = 2.0;  // WantCls
+  if (EV.q < 2e-3 && tau <= C.T->taurend && C.T->want_cls) s.max_step_size = 2.0;
   else s.max_step_size = 20.0 / C.T->IntTolBoost;
   s.reuse_first_derivative = true;
   long before = s.function_evaluations;
@@ -879,7 +925,9 @@ bool evolve_scal(const Ctx& C, EvolutionVars& EV, double& tau, std::vector<doubl
       tau_switch_no_nu_multpoles = std::max(15 / EV.k_buf * switchBoost, std::min(T->taurend, T->matter_verydom_tau));
     if (!EV.no_phot_multpoles) {
       double latePhotSwitchBoost = switchBoost;
-      if (EV.k_buf > 0.03 * latePhotSwitchBoost)  // WantCls
+      // high-precision transfers keep the photon hierarchy longer (equations.f90:317-320)
+      if (T->transfer_high_precision) latePhotSwitchBoost = std::max(latePhotSwitchBoost, 2.0);
+      if (!T->want_cls || EV.k_buf > 0.03 * latePhotSwitchBoost)
         tau_switch_no_phot_multpoles = std::max(15 / EV.k_buf, T->taurend) * latePhotSwitchBoost;
     }
     double next_switch = std::min(std::min(std::min(tau_switch_ktau, tau_switch_nu_massless), EV.TightSwitchoffTime),
@@ -1073,6 +1121,45 @@ void calc_scalar_sources(const Ctx& C, int q_ix, double* LinearSrc, ModeStats& s
   }
 }
 
+// GetTransfer (cmbmain.f90:1167-1188) + outtransf (equations.f90:2256-2271): the mode is
+// evolved to every transfer time and the 13 transfer variables are stored in single
+// precision as MatterTransferData%TransferData(:, q_ix, itf), the entries after k/h
+// divided by k^2 after the float store.
+void calc_transfer(const Ctx& C, int q_ix, float* out, ModeStats& st) {
+  const CambGpuTables* T = C.T;
+  C_ = &C;
+  EvolutionVars EV{};
+  EV.q = T->q_evolve[q_ix];
+  EV.q2 = EV.q * EV.q;
+  EV.OutputSources = nullptr;
+  EV.OutputTransfer = nullptr;
+  const CambGpuModeSpec& ms = T->modes[q_ix];
+  get_num_eqns(C, EV, ms);
+  setup_indices(EV, true);
+  for (int i = 0; i < T->nu_eig; ++i) EV.MassiveNuApproxTime[i] = ms.nu_approx_time[i];
+  std::vector<double> w[10];
+  for (int j = 1; j <= 9; ++j) w[j].assign(EV.nvar + 2, 0.0);
+  std::vector<double> y(EV.nvar + 2, 0.0);
+  double tau = tau_start(T, EV.q);
+  initial(C, EV, y, tau);
+  int ind = 1;
+  RKSettings s;
+  for (int itf = 0; itf < T->num_transfer_times; ++itf) {
+    if (!evolve_scal(C, EV, tau, y, T->transfer_times[itf], T->tol1, ind, s, w, st)) return;
+    double O[13];
+    std::vector<double> yprime(EV.nvar + 2, 0.0);
+    EV.OutputTransfer = O;
+    derivs(C, EV, EV.ScalEqsToPropagate, tau, y.data(), yprime.data());
+    EV.OutputTransfer = nullptr;
+    float* o = out + ((size_t)itf * T->nk + q_ix) * 13;
+    o[0] = (float)O[0];
+    for (int v = 1; v < 13; ++v) {
+      float f = (float)O[v];
+      o[v] = (float)(f / EV.k2_buf);
+    }
+  }
+}
+
 void init_ctx(Ctx& C, const CambGpuTables* T) {
   C.T = T;
   for (int j = 2; j <= max_l_evolve; ++j) C.polfac[j] = (double)((j + 3) * (j - 1)) / (j + 1);
@@ -1133,6 +1220,65 @@ int oracle_mode_setup(const CambGpuTables* T, double q, int* lmax3, double* tigh
   lmax3[2] = EV.lmaxnr;
   *tight_switch = EV.TightSwitchoffTime;
   return 0;
+}
+
+// TransferOut (cmbmain.f90:1136-1165) -- OpenMP over the transfer k, descending.
+// out: [num_transfer_times][nk][13] floats.
+int oracle_evolve_transfer(const CambGpuTables* T, float* out, int nthreads, long* evals) {
+  Ctx C;
+  init_ctx(C, T);
+  int nk = T->nk, status = 0;
+  if (!T->transfer_only) return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic)
+  for (int i = nk - 1; i >= 0; --i) {
+    ModeStats st;
+    calc_transfer(C, i, out, st);
+    if (evals) evals[i] = st.evals;
+    if (st.status) {
+#pragma omp critical
+      status = st.status;
+    }
+  }
+  return status;
+}
+
+// Transfer_Get_sigmas (results.f90:4115-4182) at R = 8 Mpc/h with delta = total matter
+// (Transfer_tot) and v = Newtonian CDM velocity, for every transfer time.
+void oracle_sigma8(const CambGpuTables* T, const float* tr, double* sigma8, double* sigma2_vdelta_8) {
+  const double pi = 3.1415926535897932384626433832795;
+  (void)pi;
+  int nz = T->num_transfer_times, nk = T->nk;
+  double h = T->hubble_h;
+  for (int z = 0; z < nz; ++z) {
+    double lnko = 0, dsig8o = 0, sig8 = 0, dsigvo = 0, sigv = 0;
+    for (int ik = 0; ik < nk; ++ik) {
+      double kh = tr[((size_t)0 * nk + ik) * 13 + 0];
+      if (kh == 0) continue;
+      double k = kh * h;
+      double delta = tr[((size_t)z * nk + ik) * 13 + 6];
+      double dsig8 = delta * delta;
+      double dsigv = delta * tr[((size_t)z * nk + ik) * 13 + 10];
+      double x = kh * 8.0, win;
+      if (x < 1e-2) win = 1.0 - x * x / 10;
+      else win = 3 * (std::sin(x) - x * std::cos(x)) / (x * x * x);
+      double lnk = std::log(k), dlnk;
+      if (ik == 0) dlnk = 0.5;
+      else dlnk = lnk - lnko;
+      double lnrat = std::log(k / T->pivot_scalar);
+      double pk = T->As * std::exp(lnrat * (T->ns - 1 + lnrat * (T->nrun / 2)));
+      double powers = (win * k * k) * (win * k * k) * pk;
+      dsig8 = powers * dsig8;
+      sig8 += (dsig8 + dsig8o) * dlnk / 2;
+      dsig8o = dsig8;
+      dsigv = powers * dsigv;
+      sigv += (dsigv + dsigvo) * dlnk / 2;
+      dsigvo = dsigv;
+      lnko = lnk;
+    }
+    sigma8[z] = std::sqrt(sig8);
+    sigma2_vdelta_8[z] = sigv;
+  }
 }
 
 // cmbmain.f90:205-209 -- OpenMP over k, dynamic schedule, k descending.

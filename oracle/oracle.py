@@ -114,3 +114,32 @@ def lens_cls(all_cls, ls, max_l, lmin=2, lens_output_margin=200, lens_accuracy_b
     if rc:
         raise RuntimeError("lensing amplitude check failed")
     return out
+
+
+def evolve_transfer(tables, nthreads=0, with_evals=False):
+    """GetTransfer for every transfer k: [ntimes][nk][13] float32 (TransferData order)."""
+    v = tables.view
+    lib = load()
+    lib.oracle_evolve_transfer.restype = C.c_int
+    lib.oracle_evolve_transfer.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_long)]
+    out = np.zeros((v.num_transfer_times, v.nk, 13), dtype=np.float32)
+    evals = np.zeros(v.nk, dtype=np.int64)
+    rc = lib.oracle_evolve_transfer(C.addressof(v), out.ctypes.data_as(C.POINTER(C.c_float)), nthreads,
+                                    evals.ctypes.data_as(C.POINTER(C.c_long)))
+    if rc:
+        raise RuntimeError(f"oracle transfer evolution failed: {rc}")
+    return (out, evals) if with_evals else out
+
+
+def sigma8(tables, tr):
+    """Transfer_Get_sigmas at R = 8 Mpc/h: (sigma8, sigma2_vdelta_8) per transfer time."""
+    v = tables.view
+    lib = load()
+    lib.oracle_sigma8.restype = None
+    lib.oracle_sigma8.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]
+    tr = np.ascontiguousarray(tr, dtype=np.float32)
+    s8 = np.zeros(v.num_transfer_times)
+    sv = np.zeros(v.num_transfer_times)
+    lib.oracle_sigma8(C.addressof(v), tr.ctypes.data_as(C.POINTER(C.c_float)), _dp(s8), _dp(sv))
+    return s8, sv
