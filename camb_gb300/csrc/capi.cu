@@ -21,7 +21,8 @@
 namespace cgdev {
 int ode_blocks_per_sm(int team, int threads);
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
-                              const WorkItem* items, int nitems, int* counter);
+                              const WorkItem* items, int nitems, int* counter, bool transfer);
+cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s);
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
 __global__ void los_flat_kernel(const DevCosmo*);
@@ -316,6 +317,9 @@ size_t bytes_for(const CambGpuTables& t) {
   s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256);
   s += 2 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
   s += r((size_t)(t.max_l + 1) * 6 * 8) + r((size_t)(t.max_l + 1) * 4 * 8);  // all-l C_l, lensed C_l
+  if (t.transfer_only)
+    s += r((size_t)t.num_transfer_times * 8) + r((size_t)t.num_transfer_times * t.nk * 13 * 4) +
+         r((size_t)t.num_transfer_times * 16);
   return s;
 }
 
@@ -392,12 +396,24 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.lensed = nullptr;
   d.lmax_lensed = 0;
   spline_factors(t, u.spl);
-  double *bh, *bx;
-  float4* bf;
-  int rc = device_bessel(t, &bh, &bx, &bf);
-  if (rc) return rc;
+  double *bh = nullptr, *bx = nullptr;
+  float4* bf = nullptr;
+  if (t.bessel_horner) {  // transfer-function cosmologies have no Bessel table
+    int rc = device_bessel(t, &bh, &bx, &bf);
+    if (rc) return rc;
+  }
   d.bessel_horner = bh;
   d.bessel_f32 = bf;
+  d.transfer_only = t.transfer_only;
+  d.want_cls = t.want_cls;
+  d.hubble_h = t.hubble_h;
+  d.late_phot_boost_min = t.late_phot_switch_boost_min;
+  d.n_tt = t.transfer_only ? t.num_transfer_times : 0;
+  if (t.transfer_only) {
+    d.transfer_times = (const double*)put(t.transfer_times, (size_t)t.num_transfer_times * 8);
+    d.transfer_out = g_rt.arena.take<float>((size_t)t.num_transfer_times * t.nk * 13);
+    d.sigma8 = g_rt.arena.take<double>((size_t)t.num_transfer_times * 2);
+  }
   d.bess_x = bx;
   d.num_xx = t.num_xx;
   d.nsrc = t.nsrc; d.want_late_time = t.want_late_time; d.max_etak_scalar = t.max_etak_scalar; d.tol1 = t.tol1;
@@ -424,6 +440,7 @@ struct Batch {
   unsigned long long* d_evals = nullptr;
   int max_ntau = 0, max_nq = 0, max_nl = 0, max_rows = 0;
   bool massive_nu = false;  // some cosmology has massive neutrinos (thread-per-mode kernel only)
+  bool transfer = false;    // transfer functions only (every cosmology of the batch)
   // cosmologies to lens, grouped by lensing geometry
   struct LensGroup {
     HostLensGeom h;
@@ -498,6 +515,9 @@ int stage_batch(Batch& B, int lmax_out = 0) {
     B.max_nl = std::max(B.max_nl, B.views[c]->nl);
     B.max_rows = std::max(B.max_rows, B.views[c]->ntau * B.views[c]->nsrc);
     B.massive_nu |= B.views[c]->nu_eig > 0;
+    if (c == 0) B.transfer = B.views[c]->transfer_only != 0;
+    else if (B.transfer != (B.views[c]->transfer_only != 0))
+      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "a batch is either all CMB or all transfer functions");
   }
   std::vector<DevCosmo> hc(n);
   std::vector<const double*> hspl(n);
@@ -599,8 +619,9 @@ int size_class(const Batch& B) { return B.nitems >= 24 * g_rt.nsm ? 1 : 0; }
 
 int pick_team(const Batch& B) {
   int t = g_team ? g_team : g_tuned[size_class(B)].team;
-  // the warp-per-mode kernel evolves the massless-neutrino equation layout only
-  if (B.massive_nu && t >= 8) t = 2;
+  // the warp-per-mode kernel evolves the massless-neutrino CMB layout only
+  if ((B.massive_nu || B.transfer) && t >= 8) t = 2;
+  if (B.transfer && t > 3) t = 2;
   return t;
 }
 
@@ -614,8 +635,8 @@ int run_ode(Batch& B) {
   int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * lanes + 127) / 128);
   if (blocks < 1) blocks = 1;
   const WorkItem* queue = order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
-  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, queue, B.nitems,
-                             B.d_counter));
+  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, queue, B.nitems, B.d_counter,
+                             B.transfer));
   g_launches++;
   return 0;
 }
@@ -739,14 +760,19 @@ int make_handle(const CambGpuParams* p, Handle*& h) {
     h = nullptr;
     return set_err(rc, err);
   }
-  try {
-    h->bt = cg::get_bessel_table(h->c.ls, h->c.maximum_qeta, p->BesselBoost, p->AccuracyBoost);
-  } catch (const std::exception& e) {
-    delete h;
-    h = nullptr;
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, e.what());
+  if (p->want_cls || !p->want_transfer) {
+    try {
+      h->bt = cg::get_bessel_table(h->c.ls, h->c.maximum_qeta, p->BesselBoost, p->AccuracyBoost);
+    } catch (const std::exception& e) {
+      delete h;
+      h = nullptr;
+      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, e.what());
+    }
+    cg::fill_view(h->c, *h->bt, h->view);
+  } else {
+    static const cg::BesselTable empty;  // transfer functions need no Bessel table
+    cg::fill_view(h->c, empty, h->view);
   }
-  cg::fill_view(h->c, *h->bt, h->view);
   return 0;
 }
 
@@ -920,6 +946,7 @@ int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, doubl
   for (auto* h : hs) B.views.push_back(&h->view);
   rc = stage_batch(B, lmax_out);
   if (rc) return rc;
+  if (B.transfer) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "want_cls = 0: use cambgpu_get_transfer_batch");
   rc = run_all(B, true, true, true);
   if (rc) return rc;
   rc = check_status(B, status);
@@ -935,8 +962,50 @@ int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, doubl
 
 int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float* transfer, int* nq, double* sigma8,
                                double* sigma2_vdelta_8, int* status) {
-  (void)p; (void)n; (void)nq_max; (void)transfer; (void)nq; (void)sigma8; (void)sigma2_vdelta_8; (void)status;
-  return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "not built");
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
+  for (int c = 0; c < n; ++c)
+    if (!p[c].want_transfer || p[c].want_cls)
+      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "transfer batches need want_transfer = 1 and want_cls = 0");
+  std::vector<Handle*> hs;
+  int rc = build_handles(p, n, hs, status);
+  struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
+  if (rc) return rc;
+  for (auto* h : hs)
+    if (transfer && h->view.nk > nq_max) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "nq_max too small");
+  Batch B;
+  for (auto* h : hs) B.views.push_back(&h->view);
+  rc = stage_batch(B);
+  if (rc) return rc;
+  rc = run_all(B, true, false, false);
+  if (rc) return rc;
+  CUDA_TRY(launch_sigma8(B.d_cosmos, n, g_rt.stream));
+  g_launches++;
+  rc = check_status(B, status);
+  if (rc) return rc;
+  const int nz = p[0].num_transfer_redshifts;
+  std::vector<double> s8(2 * (size_t)nz);
+  for (int c = 0; c < n; ++c) {
+    const CambGpuTables& v = hs[c]->view;
+    if (nq) nq[c] = v.nk;
+    if (transfer) {
+      for (int z = 0; z < v.num_transfer_times; ++z) {
+        float* dst = transfer + (((size_t)c * nz + z) * nq_max) * 13;
+        CUDA_TRY(cudaMemcpyAsync(dst, B.ups[c].d.transfer_out + (size_t)z * v.nk * 13, (size_t)v.nk * 13 * 4,
+                                 cudaMemcpyDeviceToHost, g_rt.stream));
+      }
+    }
+    if (sigma8 || sigma2_vdelta_8) {
+      CUDA_TRY(cudaMemcpyAsync(s8.data(), B.ups[c].d.sigma8, s8.size() * 8, cudaMemcpyDeviceToHost, g_rt.stream));
+      CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+      for (int z = 0; z < nz; ++z) {
+        if (sigma8) sigma8[(size_t)c * nz + z] = s8[2 * z];
+        if (sigma2_vdelta_8) sigma2_vdelta_8[(size_t)c * nz + z] = s8[2 * z + 1];
+      }
+    }
+  }
+  CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+  return 0;
 }
 
 int cambgpu_lensing_range(const CambGpuTables* t, int* out3) {

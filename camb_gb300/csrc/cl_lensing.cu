@@ -418,7 +418,52 @@ __global__ void pack_spectra_kernel(const DevCosmo* __restrict__ cosmos, int lma
   }
 }
 
+// Transfer_Get_sigmas (results.f90:4115-4182) at R = 8 Mpc/h: trapezoid in ln k over the
+// transfer k grid of the single-precision transfer functions, delta = total matter
+// (Transfer_tot) and v = Newtonian CDM velocity; one thread per (cosmology, redshift),
+// summing in the reference's k order.
+__global__ void sigma8_kernel(const DevCosmo* __restrict__ cosmos, int n) {
+  const int c = blockIdx.x;
+  const int z = threadIdx.x;
+  if (c >= n) return;
+  const DevCosmo& C = cosmos[c];
+  if (!C.transfer_only || z >= C.n_tt) return;
+  const int nk = C.nk;
+  const double h = C.hubble_h;
+  double lnko = 0, dsig8o = 0, sig8 = 0, dsigvo = 0, sigv = 0;
+  for (int ik = 0; ik < nk; ++ik) {
+    const double kh = C.transfer_out[(size_t)ik * 13];
+    if (kh == 0) continue;
+    const double k = kh * h;
+    const float* T = C.transfer_out + ((size_t)z * nk + ik) * 13;
+    const double delta = T[6];
+    double dsig8 = delta * delta;
+    double dsigv = delta * (double)T[10];
+    const double x = kh * 8.0;
+    const double win = x < 1e-2 ? 1.0 - x * x / 10 : 3 * (sin(x) - x * cos(x)) / (x * x * x);
+    const double lnk = log(k);
+    const double dlnk = ik == 0 ? 0.5 : lnk - lnko;
+    const double lnrat = log(k / C.pivot_scalar);
+    const double pk = C.As * exp(lnrat * (C.ns - 1 + lnrat * (C.nrun / 2)));
+    const double powers = (win * k * k) * (win * k * k) * pk;
+    dsig8 = powers * dsig8;
+    sig8 += (dsig8 + dsig8o) * dlnk / 2;
+    dsig8o = dsig8;
+    dsigv = powers * dsigv;
+    sigv += (dsigv + dsigvo) * dlnk / 2;
+    dsigvo = dsigv;
+    lnko = lnk;
+  }
+  C.sigma8[2 * z] = sqrt(sig8);
+  C.sigma8[2 * z + 1] = sigv;
+}
+
 // ---- launch helpers (called from the C API) ----
+cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s) {
+  sigma8_kernel<<<n, 32, 0, s>>>(cosmos, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_interp_cls(const DevCosmo* cosmos, int n, const double* tmpl, cudaStream_t s) {
   interp_cls_kernel<<<dim3(6, n), 256, 0, s>>>(cosmos, tmpl);
   return cudaGetLastError();

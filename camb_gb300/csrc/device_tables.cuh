@@ -45,6 +45,12 @@ struct DevCosmo {
   double* lensed;      // [lmax_lensed+1][4] TT EE BB TE (lensed cosmologies only)
   int max_l, lmax_lensed;
   double cl_template_scale;
+  // matter transfer functions only: every mode evolved to each transfer time
+  int transfer_only, n_tt, want_cls;
+  const double* transfer_times;  // [n_tt], increasing
+  float* transfer_out;           // [n_tt][nk][13] (TransferData order, single precision)
+  double* sigma8;                // [n_tt][2]: sigma8, sigma2_vdelta_8
+  double hubble_h, late_phot_boost_min;
   int* status;         // per-cosmology status word
   unsigned long long* evals;  // derivative evaluations (shared counter)
   // integration grid and l sampling

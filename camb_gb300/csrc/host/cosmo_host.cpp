@@ -1614,7 +1614,9 @@ void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   v.late_phot_switch_boost_min = transfer_hp(c.P) ? 2.0 : 0.0;
   v.nq = c.q_int.npoints(); v.q_int = c.q_int.points.data(); v.dq_int = c.q_int.dpoints.data();
   v.nl = (int)c.ls.size(); v.ls = c.ls.data();
-  v.num_xx = (int)b.x.size(); v.bess_x = b.x.data(); v.bessel_horner = b.horner.data();
+  v.num_xx = (int)b.x.size();
+  v.bess_x = b.x.empty() ? nullptr : b.x.data();
+  v.bessel_horner = b.horner.empty() ? nullptr : b.horner.data();
   v.nsrc = c.nsrc; v.want_late_time = c.P.do_lensing ? 1 : 0;
   v.max_etak_scalar = c.max_etak_scalar; v.tol1 = c.tol1; v.max_bessels_etak = c.maximum_qeta;
   v.AccuracyBoost = c.P.AccuracyBoost; v.IntTolBoost = c.P.IntTolBoost;

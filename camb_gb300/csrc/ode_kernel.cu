@@ -764,7 +764,7 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
     w = tm.bcast_i(w, 0);
     if (w >= nitems) break;
     WorkItem it = items[w];
-    if (cosmos[it.cosmo].nu_eig > 0) {  // this kernel carries the massless-neutrino layout only
+    if (cosmos[it.cosmo].nu_eig > 0 || cosmos[it.cosmo].transfer_only) {  // massless CMB layout only
       if (tm.t == 0) atomicExch(cosmos[it.cosmo].status, (int)CAMBGPU_ERROR_UNSUPPORTED_PARAMS);
       continue;
     }
@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
 // ---------------------------------------------------------------------------
 namespace tpm {
 
-constexpr int NV = 320;  // largest packed scalar system handled (mode_init rejects larger ones)
+constexpr int NV = 448;  // largest packed scalar system handled (mode_init rejects larger ones)
 constexpr int NL = 66;
 constexpr int NUE = 3;
 
@@ -1014,6 +1014,7 @@ __device__ double nu_pinudot(const DevCosmo& C, const St& M, const double* __res
 }
 
 // derivs (equations.f90:2273-2773) + sources (2775-2912), one thread per mode
+template <bool TR>
 __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* __restrict__ dl,
                                         const double* __restrict__ dl2, const double* __restrict__ pf, double tau,
                                         const double* __restrict__ y, double* __restrict__ dy, double* src) {
@@ -1049,6 +1050,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
     dgq += g_t * qnu;
     wnu[i] = pnu / rhonu;
   }
+  const double dgrho_matter = dgrho, grho_matter = grhonu_t + grhob_t + grhoc_t;
   const double grho = (grhonu_t + grhob_t + grhoc_t) + grhor_t + grhog_t + grhov_t;
   const double gpres_noDE = gpres_nu + (grhor_t + grhog_t) * (1.0 / 3);
   const double g3 = grho * (1.0 / 3);
@@ -1210,22 +1212,27 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
     double dgpi = grhor_t * pir + grhog_t * pig;
     double dgpi_diff = 0;
     double pidot_sum = grhog_t * pigdot + grhor_t * pirdot;
+    double grhonu_out = 0, dgrhonu_out = 0;
     for (int i = 0; i < C.nu_eig; ++i) {  // MassiveNuVarsOut (equations.f90:1113-1176)
       const double gm_t = C.grhormass[i] * ia2;
-      double rhonu, pnu, pinu, pinudot;
+      double rhonu, pnu, pinu, pinudot, clxnu;
       nuf::rho_P(a * C.nu_masses[i], rhonu, pnu);
       if (M.approx[i]) {
+        clxnu = y[M.nu_ix[i]];
         pinu = y[M.nu_ix[i] + 3];
         pinudot = dy[M.nu_ix[i] + 3];
       } else {
-        double clxnu, qnu, dpnu;
+        double qnu, dpnu;
         nu_integrate<true>(C, M, y, a, i, clxnu, qnu, dpnu, pinu);
+        clxnu = clxnu / rhonu;
         pinu = pinu / rhonu;
         const double rhonudot = nuf::drho(a * C.nu_masses[i], adotoa);
         pinudot = nu_pinudot(C, M, y, dy, a, adotoa, i);
         pinudot = pinudot / rhonu - rhonudot / rhonu * pinu;
       }
       const double g_t = gm_t * rhonu, gp_t = gm_t * pnu;
+      grhonu_out += g_t;
+      dgrhonu_out += g_t * clxnu;
       dgpi += g_t * pinu;
       dgpi_diff += pinu * (3 * gp_t - g_t);
       pidot_sum += g_t * pinudot;
@@ -1233,6 +1240,22 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
     const double gpres = gpres_noDE - grhov_t;
     const double diff_rhopi = pidot_sum - (4 * dgpi + dgpi_diff) * adotoa;
     const double phi = -((dgrho + 3 * dgq * adotoa * ik) + dgpi) / (2 * M.k2);
+    if constexpr (TR) {  // outtransf's variables (equations.f90:2832-2845), src holds 13
+      src[0] = k / C.hubble_h;
+      src[1] = clxc;
+      src[2] = clxb;
+      src[3] = clxg;
+      src[4] = clxr;
+      src[5] = C.nu_eig > 0 ? dgrhonu_out / grhonu_out : 0.0;
+      src[6] = dgrho_matter / grho_matter;
+      src[7] = (grhob_t * clxb + grhoc_t * clxc) / (grhob_t + grhoc_t);
+      src[8] = dgrho / grho_matter;
+      src[9] = M.k2 * phi;
+      src[10] = -k * sigma / adotoa;
+      src[11] = -k * (vb + sigma) / adotoa;
+      src[12] = vb;
+      return;
+    }
     double op2, dop2, vis, dvis, ddvis, exptau;
     ionization(C, tau, itau, op2, dop2, vis, dvis, ddvis, exptau);
     const double k2 = M.k2;
@@ -1268,7 +1291,7 @@ struct Work {
 
 // state of one mode's integration, advanced one trial step per loop iteration
 struct Run {
-  double src[3];
+  double src[13];  // source functions, or the 13 transfer variables without the CMB
   double tau, target, sw_time, h, err, call_hmax;
   double ny;            // min(max|y|, 1) of the current state (valid when ny_valid)
   int sy, syt, sk1, sk2;  // rows of Work::b holding y, the trial state, k1 and k2 (= k7)
@@ -1372,7 +1395,7 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
     }
   }
   R.tau = tau;
-  R.j = 1;
+  R.j = C.transfer_only ? 0 : 1;
   R.h = R.err = 0;
   R.fails = 0;
   R.fsal = false;
@@ -1391,10 +1414,17 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
 // Picks the next integration target with the switch logic of EvolveScal
 // (equations.f90:261-331) and records which switch the target is.  Returns false
 // when the mode is finished.
+template <bool TR>
 __device__ bool next_target(const DevCosmo& C, St& M, Run& R) {
-  if (R.j >= C.ntau) return false;
-  const double tauend = C.tau_points[R.j];
-  if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time) return false;
+  double tauend;
+  if constexpr (TR) {  // GetTransfer: the transfer times in turn
+    if (R.j >= C.n_tt) return false;
+    tauend = C.transfer_times[R.j];
+  } else {
+    if (R.j >= C.ntau) return false;
+    tauend = C.tau_points[R.j];
+    if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time) return false;
+  }
   const double noSwitch = C.tau0 + 1;
   const double smallTime = fmin(R.tau, M.ik) / 100;
   const double switchBoost = C.AccuracyBoost * C.TimeSwitchBoost;
@@ -1413,7 +1443,8 @@ __device__ bool next_target(const DevCosmo& C, St& M, Run& R) {
     }
   }
   if (!M.nonu) t_nonu = fmax(15 / M.k * switchBoost, fmin(C.taurend, C.matter_verydom_tau));
-  if (!M.nophot && M.k > 0.03 * switchBoost) t_nophot = fmax(15 / M.k, C.taurend) * switchBoost;
+  const double lp = fmax(switchBoost, C.late_phot_boost_min);  // latePhotSwitchBoost
+  if (!M.nophot && (!C.want_cls || M.k > 0.03 * lp)) t_nophot = fmax(15 / M.k, C.taurend) * lp;
   const double next = fmin(fmin(fmin(t_ktau, t_massless), M.tight_off),
                            fmin(fmin(t_massive, t_nonu), fmin(fmin(t_nophot, t_nonrel), noSwitch)));
   // the order of the reference's if-chain decides ties
@@ -1443,7 +1474,7 @@ __device__ bool next_target(const DevCosmo& C, St& M, Run& R) {
     is_switch = false;
   }
   // start of a GaugeInterface_ScalEv / RungeKuttaDP45 call
-  const double ms_user = (M.q < 2e-3 && R.tau <= C.taurend) ? 2.0 : 20.0 / C.IntTolBoost;
+  const double ms_user = (M.q < 2e-3 && R.tau <= C.taurend && C.want_cls) ? 2.0 : 20.0 / C.IntTolBoost;
   R.call_hmax = R.reset ? 0.0 : ms_user;
   R.first = R.reset;
   if (R.reset) {
@@ -1550,6 +1581,7 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
 }
 
 // one trial step of RungeKuttaDP45 toward R.target; returns <0 on failure
+template <bool TR>
 __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   using namespace dp;
   const double tol = C.tol1;
@@ -1565,7 +1597,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
-      derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, y, k1, nullptr);
+      derivs1<TR>(C, M, W.dl, W.dl2, W.pf, R.tau, y, k1, nullptr);
       R.evals++;
     }
     R.need_f = false;
@@ -1612,20 +1644,20 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   const double cb1 = hs * b1, cb3 = hs * b3, cb4 = hs * b4, cb5 = hs * b5, cb6 = hs * b6;
 #pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c21, k1[i], y[i]);
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, yt, k2, nullptr);
+  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, yt, k2, nullptr);
 #pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c32, k2[i], fma(c31, k1[i], y[i]));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), yt, k3, nullptr);
+  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), yt, k3, nullptr);
 #pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c43, k3[i], fma(c42, k2[i], fma(c41, k1[i], y[i])));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), yt, k4, nullptr);
+  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), yt, k4, nullptr);
 #pragma unroll 4
   for (int i = 0; i < n; ++i) yt[i] = fma(c54, k4[i], fma(c53, k3[i], fma(c52, k2[i], fma(c51, k1[i], y[i]))));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), yt, k5, nullptr);
+  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), yt, k5, nullptr);
 #pragma unroll 4
   for (int i = 0; i < n; ++i)
     yt[i] = fma(c65, k5[i], fma(c64, k4[i], fma(c63, k3[i], fma(c62, k2[i], fma(c61, k1[i], y[i])))));
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k6, nullptr);
+  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k6, nullptr);
   // the fifth-order solution, the error combination of k1, k3..k6 (k3 is dead afterwards
   // and holds it) and max|yt| for the next step's hmin, in one pass
   unsigned long long nbt = 0;
@@ -1639,7 +1671,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   }
   // stage 7 (FSAL) into k2; at an output time it is the output() evaluation too
   const bool want_src = (xt == xend) && !R.target_is_switch;
-  derivs1(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k2, want_src ? R.src : nullptr);
+  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k2, want_src ? R.src : nullptr);
   R.src_valid = want_src;
   R.evals += 6;
   // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry
@@ -1673,7 +1705,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   return 0;
 }
 
-template <int MINB>
+template <int MINB, bool TR>
 __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* __restrict__ cosmos,
                                                                const WorkItem* __restrict__ items, int nitems,
                                                                int* __restrict__ counter) {
@@ -1694,7 +1726,7 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
         atomicExch(cosmos[cosmo].status, R.status);
         continue;
       }
-      if (!next_target(cosmos[cosmo], M, R)) {
+      if (!next_target<TR>(cosmos[cosmo], M, R)) {
         R.active = false;
         atomicAdd(cosmos[cosmo].evals, (unsigned long long)R.evals);
         continue;
@@ -1702,7 +1734,7 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
     }
     const DevCosmo& C = cosmos[cosmo];
     int rc = 0;
-    if (R.target != R.tau) rc = trial_step(C, M, W, R);
+    if (R.target != R.tau) rc = trial_step<TR>(C, M, W, R);
     if (rc) {
       atomicExch(C.status, (int)CAMBGPU_ERROR_EVOLUTION);
       atomicAdd(C.evals, (unsigned long long)R.evals);
@@ -1715,16 +1747,24 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
         apply_switch(C, M, W, R);
       } else {
         if (!R.src_valid) {
-          derivs1(C, M, W.dl, W.dl2, W.pf, R.tau, W.b[R.sy], W.b[R.syt], R.src);
+          derivs1<TR>(C, M, W.dl, W.dl2, W.pf, R.tau, W.b[R.sy], W.b[R.syt], R.src);
         }
         R.evals++;  // the output() evaluation of the reference
-        const int nsrc = C.nsrc, nk = C.nk;
-        for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = R.src[s];
+        const int nk = C.nk;
+        if constexpr (TR) {
+          // TransferData is single precision: store, then divide the stored value by k^2
+          float* o = C.transfer_out + ((size_t)R.j * nk + q_ix) * 13;
+          o[0] = (float)R.src[0];
+          for (int v = 1; v < 13; ++v) o[v] = (float)((double)(float)R.src[v] / M.k2);
+        } else {
+          const int nsrc = C.nsrc;
+          for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = R.src[s];
+        }
         R.j++;
       }
       int guard = 0;
       for (;;) {
-        more = next_target(C, M, R);
+        more = next_target<TR>(C, M, R);
         if (!more || !(R.target_is_switch && R.target == R.tau) || ++guard > 16) break;
         apply_switch(C, M, W, R);  // switches due at the current time
       }
@@ -1765,11 +1805,11 @@ cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, c
 // team 1 = thread per mode with 3 resident blocks per SM, 2 = 4 blocks, 3 = 5 blocks
 int ode_blocks_per_sm(int team, int threads) {
   int per_sm = 0;
-  if (team == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<3>, threads, 0);
-  else if (team == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<4>, threads, 0);
-  else if (team == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<5>, threads, 0);
-  else if (team == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<6>, threads, 0);
-  else if (team == 5) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<8>, threads, 0);
+  if (team == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<3, false>, threads, 0);
+  else if (team == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<4, false>, threads, 0);
+  else if (team == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<5, false>, threads, 0);
+  else if (team == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<6, false>, threads, 0);
+  else if (team == 5) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<8, false>, threads, 0);
   else if (team == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<32>, threads, 0);
   else if (team == 16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<16>, threads, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<8>, threads, 0);
@@ -1777,12 +1817,18 @@ int ode_blocks_per_sm(int team, int threads) {
 }
 
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
-                              const WorkItem* items, int nitems, int* counter) {
-  if (team == 1) tpm::ode_thread_kernel<3><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
-  else if (team == 2) tpm::ode_thread_kernel<4><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
-  else if (team == 3) tpm::ode_thread_kernel<5><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
-  else if (team == 4) tpm::ode_thread_kernel<6><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
-  else if (team == 5) tpm::ode_thread_kernel<8><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+                              const WorkItem* items, int nitems, int* counter, bool transfer) {
+  if (transfer) {  // matter transfer functions: thread per mode only
+    if (team == 1) tpm::ode_thread_kernel<3, true><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+    else if (team == 3) tpm::ode_thread_kernel<5, true><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+    else tpm::ode_thread_kernel<4, true><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+    return cudaGetLastError();
+  }
+  if (team == 1) tpm::ode_thread_kernel<3, false><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 2) tpm::ode_thread_kernel<4, false><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 3) tpm::ode_thread_kernel<5, false><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 4) tpm::ode_thread_kernel<6, false><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else if (team == 5) tpm::ode_thread_kernel<8, false><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 32) ode_persistent_kernel<32><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else if (team == 16) ode_persistent_kernel<16><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
   else ode_persistent_kernel<8><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);

@@ -40,11 +40,39 @@ class InitialPowerLaw:
 
 
 class TanhReionization:
-    """tanh reionization set from the optical depth (reionization.f90:97-360)."""
+    """tanh reionization set from the optical depth or the redshift (reionization.f90:97-360)."""
 
     def __init__(self):
+        self.use_optical_depth = True
         self.optical_depth = 0.06
+        self.redshift = 10.0
         self.delta_redshift = 0.5
+
+    def set_tau(self, tau, delta_redshift=None):
+        self.use_optical_depth, self.optical_depth = True, tau
+        if delta_redshift is not None:
+            self.delta_redshift = delta_redshift
+        return self
+
+    def set_zrei(self, zrei, delta_redshift=None):
+        self.use_optical_depth, self.redshift = False, zrei
+        if delta_redshift is not None:
+            self.delta_redshift = delta_redshift
+        return self
+
+
+class TransferParams:
+    """CAMBparams%Transfer (model.f90:160-175): matter transfer function settings."""
+
+    def __init__(self):
+        self.high_precision = False
+        self.kmax = 0.9
+        self.k_per_logint = 0
+        self.PK_redshifts = [0.0]
+
+    @property
+    def PK_num_redshifts(self):
+        return len(self.PK_redshifts)
 
 
 class CAMBparams:
@@ -55,6 +83,8 @@ class CAMBparams:
         self.Alens = 1.0
         self.max_l, self.max_eta_k = 2500, 6250.0
         self.DoLensing = True  # model.f90:122
+        self.WantTransfer = False
+        self.Transfer = TransferParams()
         self.WantCls, self.WantScalars = True, True
         self.InitPower = InitialPowerLaw()
         self.Reion = TanhReionization()
@@ -95,6 +125,24 @@ class CAMBparams:
             self.max_eta_k = max(self.max_eta_k, lens_k_eta_reference * lens_potential_accuracy)
         return self
 
+    def set_matter_power(self, redshifts=(0.0,), kmax=1.2, k_per_logint=None, nonlinear=None,
+                         accurate_massive_neutrino_transfers=False, silent=False):
+        """model.py:951-1016: transfer functions at the given redshifts to kmax (1/Mpc),
+        high precision, optimized k spacing.  Non-linear corrections are out of scope."""
+        if not len(redshifts):
+            raise CAMBError("set_matter_power redshifts list is empty")
+        if nonlinear:
+            raise CAMBError("non-linear matter power is not part of the GPU path")
+        if k_per_logint:
+            raise CAMBError("only the optimized transfer k spacing (k_per_logint = 0) is built")
+        if len(redshifts) > 16:
+            raise CAMBError("at most 16 transfer redshifts")
+        self.WantTransfer = True
+        self.Transfer.high_precision = True
+        self.Transfer.kmax = kmax
+        self.Transfer.PK_redshifts = sorted(redshifts, reverse=True)
+        return self
+
     def scalar_power(self, k):
         p = self.InitPower
         lnrat = math.log(k / p.pivot_scalar)
@@ -115,6 +163,16 @@ class CAMBparams:
             setattr(s, n, getattr(self.Accuracy, n))
         s.accurate_polarization = int(bool(self.Accuracy.AccuratePolarization))
         s.accurate_reionization = int(bool(self.Accuracy.AccurateReionization))
+        s.want_cls = 1 if self.WantCls else 0
+        s.want_transfer = 1 if self.WantTransfer else 0
+        s.transfer_high_precision = 1 if self.Transfer.high_precision else 0
+        s.transfer_kmax = self.Transfer.kmax
+        zs = list(self.Transfer.PK_redshifts)
+        s.num_transfer_redshifts = len(zs)
+        for i, z in enumerate(zs):
+            s.transfer_redshifts[i] = z
+        s.reion_use_optical_depth = 1 if self.Reion.use_optical_depth else 0
+        s.reion_redshift = self.Reion.redshift
         return s
 
 

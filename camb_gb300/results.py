@@ -105,12 +105,17 @@ def _run(params_list, lmax_out):
 
 
 def get_results(params, lmax_out=None):
-    """camb.get_results (camb.py:47-61): one cosmology through the GPU pipeline."""
+    """camb.get_results (camb.py:47-61): one cosmology through the GPU pipeline (the CMB
+    spectra, or with WantTransfer and WantCls off the matter transfer functions)."""
+    if params.WantTransfer:
+        return _run_transfer([params])[0]
     return _run([params], params.max_l if lmax_out is None else lmax_out)[0]
 
 
 def get_results_batch(params_list, lmax_out=None):
     """Many cosmologies in one persistent launch per stage."""
+    if all(p.WantTransfer for p in params_list):
+        return _run_transfer(params_list)
     return _run(params_list, max(p.max_l for p in params_list) if lmax_out is None else lmax_out)
 
 
@@ -184,3 +189,83 @@ def get_transfer_functions(params):
 def get_transfer_functions_batch(params_list):
     batch = _ResidentBatch(params_list)
     return [CAMBdataTransfers(batch, i) for i in range(len(params_list))]
+
+
+class MatterTransferData:
+    """MatterTransferData (results.f90, camb/results.py get_matter_transfer_data):
+    transfer_data[13, nq, nz] single precision, q (1/Mpc), sigma_8, sigma2_vdelta_8."""
+
+    def __init__(self, transfer_data, q, sigma_8, sigma2_vdelta_8):
+        self.transfer_data = transfer_data
+        self.q = q
+        self.sigma_8 = sigma_8
+        self.sigma2_vdelta_8 = sigma2_vdelta_8
+        self.nq = len(q)
+
+
+class CAMBdataMatter(CAMBdata):
+    """Results of a transfer-function run (WantTransfer, WantCls off): sigma8, f sigma8,
+    the transfer functions and the linear matter power spectrum (camb/results.py:806-998)."""
+
+    def __init__(self, params, mtd):
+        super().__init__(params, np.zeros((params.max_l + 1, 4)))
+        self._mtd = mtd
+
+    def get_matter_transfer_data(self):
+        return self._mtd
+
+    def get_sigma8(self):
+        return np.array(self._mtd.sigma_8)
+
+    def get_sigma8_0(self):
+        if self.Params.Transfer.PK_redshifts[-1] > 1e-5:
+            raise _lib.CAMBError("sigma8 requested at z=0, but P(z=0) not calculated")
+        return self.get_sigma8()[-1]
+
+    def get_fsigma8(self):
+        return self._mtd.sigma2_vdelta_8 / self._mtd.sigma_8
+
+    def get_linear_matter_power_spectrum(self, var1=None, var2=None, hubble_units=True, k_hunit=True, **kwargs):
+        """Transfer_GetUnsplinedPower (results.f90:3472-3513) on the transfer k grid:
+        returns k/h (or k), z increasing, PK[z, k]."""
+        td = self._mtd.transfer_data
+        s1 = 6 if var1 is None else int(var1) - 1
+        s2 = 6 if var2 is None else int(var2) - 1
+        ip = self.Params.InitPower
+        h = self.Params.H0 / 100
+        kh = td[0, :, 0].astype(np.float64)
+        k = kh * h
+        lnrat = np.log(k / ip.pivot_scalar)
+        power = ip.As * np.exp(lnrat * (ip.ns - 1 + lnrat * (ip.nrun / 2)))
+        nz = td.shape[2]
+        pk = np.empty((nz, len(k)))
+        for zix in range(nz):
+            it = nz - 1 - zix
+            pk[zix] = td[s1, :, it].astype(np.float64) * td[s2, :, it] * k * np.pi * 2 * np.pi * power
+        if hubble_units:
+            pk *= h ** 3
+        z = np.array(self.Params.Transfer.PK_redshifts[::-1], dtype=np.float64)
+        return (kh if k_hunit else k), z, pk
+
+
+def _run_transfer(params_list):
+    lib = _lib.load()
+    n = len(params_list)
+    nz = params_list[0].Transfer.PK_num_redshifts
+    if any(p.Transfer.PK_num_redshifts != nz for p in params_list):
+        raise _lib.CAMBError("a transfer batch needs the same number of redshifts")
+    arr = (_lib.CambGpuParams * n)(*[p.to_struct() for p in params_list])
+    nq_max = 4096
+    tr = np.zeros((n, nz, nq_max, 13), dtype=np.float32)
+    nq = np.zeros(n, dtype=np.int32)
+    s8 = np.zeros((n, nz))
+    sv = np.zeros((n, nz))
+    st = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.cambgpu_get_transfer_batch(arr, n, nq_max, tr.ctypes.data_as(C.POINTER(C.c_float)),
+                                              _lib.iptr(nq), _lib.dptr(s8), _lib.dptr(sv), _lib.iptr(st)))
+    out = []
+    for i, p in enumerate(params_list):
+        td = np.ascontiguousarray(tr[i, :, : nq[i], :].transpose(2, 1, 0))  # [13, nq, nz]
+        q = td[0, :, 0].astype(np.float64) * p.H0 / 100
+        out.append(CAMBdataMatter(p, MatterTransferData(td, q, s8[i], sv[i])))
+    return out

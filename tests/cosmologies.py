@@ -65,3 +65,20 @@ def draws(n, seed=1234, lmax=1000, frac=0.05, mnu_max=0.0):
 def template():
     g = json.load(open(os.path.join(HERE, "golden", "template_cls.json")))
     return {int(k): np.array(v) for k, v in g["cls"].items()}
+
+
+def sigma8_known_answer():
+    """camb_test.py testPowers cosmology for the sigma8 known answers, as a transfer-function
+    run (want_cls = 0): H0 67.5, ombh2 0.022, omch2 0.122, one 0.07 eV neutrino, As 2e-9,
+    ns 0.965, reionization at z = 10, transfers at z = 3.1, 0.17, 0 to kmax 1.2 /Mpc."""
+    g = json.load(open(os.path.join(HERE, "golden", "known_answers.json")))["sigma8"]
+    c = g["cosmology"]
+    p = _lib.default_params()
+    p.H0, p.ombh2, p.omch2, p.mnu, p.num_massive_neutrinos, p.nnu = c["H0"], c["ombh2"], c["omch2"], c["mnu"], 1, 3.044
+    p.As, p.ns = c["As"], c["ns"]
+    p.reion_use_optical_depth, p.reion_redshift = 0, c["zre"]
+    p.want_cls, p.want_transfer, p.transfer_high_precision, p.transfer_kmax = 0, 1, 1, c["kmax"]
+    p.num_transfer_redshifts = len(g["redshifts"])
+    for i, z in enumerate(g["redshifts"]):
+        p.transfer_redshifts[i] = z
+    return p, g

@@ -41,5 +41,16 @@ src = open(os.path.join(ref, "camb", "tests", "camb_test.py")).read()
 m = re.search(r"assertAlmostEqual\(pars\.scalar_power\(1\)[^,]*,\s*([0-9.e\-]+)", src)
 known = {"scalar_power_k1": float(m.group(1)) if m else 1.801e-9, "scalar_power_As": 2e-9,
          "scalar_power_ns": 0.965, "source": "camb/tests/camb_test.py testPowers"}
+# testPowers sigma8 / f sigma8 (places=3) for H0 67.5, ombh2 0.022, omch2 0.122, mnu 0.07,
+# As 2e-9, ns 0.965, reionization at z = 10 (the CAMBparams default), linear transfer
+# functions at z = [3.1, 0.17, 0] to kmax 1.2 with high precision
+def almost(expr):
+    m = re.search(r"assertAlmostEqual\(" + re.escape(expr) + r",\s*([0-9.e\-]+),\s*([0-9]+)\)", src)
+    return [float(m.group(1)), int(m.group(2))]
+known["sigma8"] = {"redshifts": [3.1, 0.17, 0.0], "s8_z3.1": almost("s8[0]"), "s8_z0": almost("s8[2]"),
+                   "fs8_z3.1": almost("fs8[0]"), "fs8_z0": almost("fs8[2]"),
+                   "cosmology": {"H0": 67.5, "ombh2": 0.022, "omch2": 0.122, "mnu": 0.07, "As": 2e-9,
+                                 "ns": 0.965, "zre": 10.0, "kmax": 1.2},
+                   "source": "camb/tests/camb_test.py testPowers"}
 json.dump(known, open(os.path.join(here, "known_answers.json"), "w"), indent=1)
 print("wrote", len(rows), "template rows")

@@ -1,0 +1,79 @@
+"""GPU matter transfer functions (cambgpu_get_transfer_batch) against the oracle on the
+same inputs, and the reference's sigma8 / f sigma8 known answers through the GPU path.
+Tolerance: each transfer variable within 1e-5 of its peak over k (single-precision
+storage, as the reference), sigma8 within 1e-6 relative of the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from camb_gb300 import _lib
+from oracle import oracle as orc
+from tests.cosmologies import sigma8_known_answer
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_transfer(ps, nq_max=2048):
+    lib = _lib.load()
+    n = len(ps)
+    nz = ps[0].num_transfer_redshifts
+    arr = (_lib.CambGpuParams * n)(*ps)
+    tr = np.zeros((n, nz, nq_max, 13), dtype=np.float32)
+    nq = np.zeros(n, dtype=np.int32)
+    s8 = np.zeros((n, nz))
+    sv = np.zeros((n, nz))
+    st = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.cambgpu_get_transfer_batch(arr, n, nq_max, tr.ctypes.data_as(C.POINTER(C.c_float)),
+                                              _lib.iptr(nq), _lib.dptr(s8), _lib.dptr(sv), _lib.iptr(st)))
+    assert not st.any()
+    return tr, nq, s8, sv
+
+
+def test_transfer_functions_match_oracle_and_known_answers():
+    p, g = sigma8_known_answer()
+    T = _lib.Tables(p)
+    ref = orc.evolve_transfer(T)
+    rs8, rsv = orc.sigma8(T, ref)
+    tr, nq, s8, sv = gpu_transfer([p])
+    assert nq[0] == T.view.nk
+    got = tr[0, :, : nq[0]]
+    peak = np.max(np.abs(ref), axis=1, keepdims=True)
+    assert np.max(np.abs(got - ref) / np.where(peak > 0, peak, 1)) < 1e-5
+    assert np.max(np.abs(s8[0] / rs8 - 1)) < 1e-6
+    assert np.max(np.abs(sv[0] / rsv - 1)) < 1e-6
+    fs8 = sv[0] / s8[0]
+    for got_v, key in [(s8[0][0], "s8_z3.1"), (s8[0][2], "s8_z0"), (fs8[0], "fs8_z3.1"), (fs8[2], "fs8_z0")]:
+        want, places = g[key]
+        assert round(abs(got_v - want), places) == 0, (key, got_v, want)
+
+
+def test_transfer_batch_of_masses():
+    ps = []
+    for m in (0.0, 0.06, 0.2):
+        p, _ = sigma8_known_answer()
+        p.mnu = m
+        ps.append(p)
+    tr, nq, s8, sv = gpu_transfer(ps)
+    for i, p in enumerate(ps):
+        T = _lib.Tables(p)
+        ref = orc.evolve_transfer(T)
+        rs8, _ = orc.sigma8(T, ref)
+        assert np.max(np.abs(s8[i] / rs8 - 1)) < 1e-6
+    # heavier neutrinos suppress the growth of structure
+    assert s8[0][2] > s8[1][2] > s8[2][2]
+
+
+def test_python_surface_sigma8():
+    from camb_gb300 import model, results
+    cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.07, As=2e-9, ns=0.965)
+    cp.Reion.set_zrei(10)
+    cp.WantCls = False
+    cp.set_matter_power(redshifts=[0.0, 0.17, 3.1], kmax=1.2)
+    r = results.get_results(cp)
+    s8 = r.get_sigma8()
+    assert abs(s8[0] - 0.24686) < 5e-4 and abs(s8[2] - 0.80044) < 5e-4
+    assert abs(r.get_fsigma8()[2] - 0.424712) < 5e-4
+    kh, z, pk = r.get_linear_matter_power_spectrum()
+    assert list(z) == [0.0, 0.17, 3.1] and pk.shape == (3, len(kh))
+    assert np.all(pk > 0) and pk[0].max() > pk[2].max()
