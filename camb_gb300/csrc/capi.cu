@@ -964,9 +964,12 @@ int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float*
                                double* sigma2_vdelta_8, int* status) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
-  for (int c = 0; c < n; ++c)
+  for (int c = 0; c < n; ++c) {
     if (!p[c].want_transfer || p[c].want_cls)
       return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "transfer batches need want_transfer = 1 and want_cls = 0");
+    if (p[c].num_transfer_redshifts != p[0].num_transfer_redshifts)
+      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "every cosmology of a transfer batch needs the same redshift count");
+  }
   std::vector<Handle*> hs;
   int rc = build_handles(p, n, hs, status);
   struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
