@@ -271,6 +271,8 @@ def main():
     for _ in range(args.steps):
         _lib.check(lib.cambgpu_get_results_batch(arr, B, args.lmax, _lib.dptr(cls), _lib.iptr(st)))
     e2e_s = barrier_max((time.perf_counter() - t0) / args.steps, world)
+    host_ms = np.zeros(4)
+    lib.cambgpu_last_host_timings(_lib.dptr(host_ms))
     xfer = (C.c_longlong * 2)()
     lib.cambgpu_last_transfer_bytes(xfer)
     stage, evals, launches, wall, clk = run["stage"], run["evals"], run["launches"], run["wall"], run["clocks"]
@@ -303,7 +305,9 @@ def main():
                                        "cls_interp_lens": plain["stage"][2]}},
             "accuracy_vs_fp64_gpu": batch_err,
             "e2e": {"value": world * B / e2e_s, "unit": "cosmologies/s", "h2d_bytes_per_step": int(xfer[0]),
-                    "d2h_bytes_per_step": int(xfer[1])},
+                    "d2h_bytes_per_step": int(xfer[1]),
+                    "last_call_ms": {"host_tables": host_ms[0], "staging": host_ms[1], "device": host_ms[2],
+                                     "fetch": host_ms[3]}},
             "gpu_launches": int(launches),
             "roofline": {"bound": "fp64", "kernel": "ode_thread_kernel", "achieved": achieved, "peak": tf.value,
                          "unit": "TFLOP/s", "frac": achieved / tf.value, "traffic": None,

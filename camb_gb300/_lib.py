@@ -113,6 +113,7 @@ SIGNATURES = {
     "cambgpu_get_precision": (C.c_int, []),
     "cambgpu_autotune_ode": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, _c_int_p, _c_double_p]),
     "cambgpu_last_timings": (C.c_int, [_c_double_p]),
+    "cambgpu_last_host_timings": (C.c_int, [_c_double_p]),
     "cambgpu_last_ode_evals": (C.c_longlong, []),
     "cambgpu_last_transfer_bytes": (C.c_int, [C.POINTER(C.c_longlong)]),
     "cambgpu_probe_fp64_tflops": (C.c_int, [_c_double_p]),

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -37,6 +38,10 @@ namespace {
 std::string g_err;
 std::atomic<long long> g_launches{0};
 double g_timings[6] = {0, 0, 0, 0, 0, 0};
+double g_host_ms[4] = {0, 0, 0, 0};  // host tables, staging, device pipeline, fetch (wall ms)
+double wall_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 int g_team = 0;
 int g_precision = 0;  // 0: FP64 throughout; 1: mixed-precision line-of-sight projection
 // autotuned ODE configuration per batch-size class: [0] small (< 24 modes/SM), [1] large
@@ -380,10 +385,6 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.modes = (const CambGpuModeSpec*)put(t.modes, (size_t)t.nk * sizeof(CambGpuModeSpec));
   d.q_evolve = (const double*)put(t.q_evolve, (size_t)t.nk * 8);
   d.nk = t.nk;
-  d.linear_src = g_rt.arena.take<double>((size_t)t.ntau * t.nsrc * t.nk);
-  d.dd_src = g_rt.arena.take<double>((size_t)t.ntau * t.nsrc * t.nk);
-  d.delta = g_rt.arena.take<double>((size_t)t.nq * t.nl * t.nsrc);
-  d.icl = g_rt.arena.take<double>((size_t)t.nl * 6);
   d.status = status_dev;
   d.q_int = (const double*)put(t.q_int, (size_t)t.nq * 8);
   d.dq_int = (const double*)put(t.dq_int, (size_t)t.nq * 8);
@@ -392,7 +393,6 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.nl = t.nl;
   d.max_l = t.max_l;
   d.cl_template_scale = t.cl_template_scale;
-  d.all_cl = g_rt.arena.take<double>((size_t)(t.max_l + 1) * 6);
   d.lensed = nullptr;
   d.lmax_lensed = 0;
   spline_factors(t, u.spl);
@@ -411,6 +411,14 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.n_tt = t.transfer_only ? t.num_transfer_times : 0;
   if (t.transfer_only) {
     d.transfer_times = (const double*)put(t.transfer_times, (size_t)t.num_transfer_times * 8);
+  }
+  // outputs and scratch after every uploaded array, so that the uploads are contiguous
+  d.linear_src = g_rt.arena.take<double>((size_t)t.ntau * t.nsrc * t.nk);
+  d.dd_src = g_rt.arena.take<double>((size_t)t.ntau * t.nsrc * t.nk);
+  d.delta = g_rt.arena.take<double>((size_t)t.nq * t.nl * t.nsrc);
+  d.icl = g_rt.arena.take<double>((size_t)t.nl * 6);
+  d.all_cl = g_rt.arena.take<double>((size_t)(t.max_l + 1) * 6);
+  if (t.transfer_only) {
     d.transfer_out = g_rt.arena.take<float>((size_t)t.num_transfer_times * t.nk * 13);
     d.sigma8 = g_rt.arena.take<double>((size_t)t.num_transfer_times * 2);
   }
@@ -595,14 +603,38 @@ int stage_batch(Batch& B, int lmax_out = 0) {
     g_rt.pinned_cap = stage + (1 << 20);
   }
   CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
-  size_t off = 0;
   g_h2d = 0;
   g_d2h = 0;
-  for (auto& cp : copies) {
-    g_h2d += (long long)cp.second.second;
-    std::memcpy(g_rt.pinned + off, cp.second.first, cp.second.second);
-    CUDA_TRY(cudaMemcpyAsync(cp.first, g_rt.pinned + off, cp.second.second, cudaMemcpyHostToDevice, g_rt.stream));
-    off += (cp.second.second + 255) & ~size_t(255);
+  // staging offsets, then the host copies into the pinned buffer on all cores
+  std::vector<size_t> offs(copies.size());
+  {
+    size_t off = 0;
+    for (size_t i = 0; i < copies.size(); ++i) {
+      offs[i] = off;
+      g_h2d += (long long)copies[i].second.second;
+      off += (copies[i].second.second + 255) & ~size_t(255);
+    }
+    unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nth; ++t)
+      th.emplace_back([&]() {
+        for (size_t i = next++; i < copies.size(); i = next++)
+          std::memcpy(g_rt.pinned + offs[i], copies[i].second.first, copies[i].second.second);
+      });
+    for (auto& t : th) t.join();
+  }
+  // one device copy per run of copies that are contiguous on both sides (the arena and the
+  // staging buffer use the same 256-byte rounding)
+  for (size_t i = 0; i < copies.size();) {
+    size_t j = i, bytes = copies[i].second.second;
+    while (j + 1 < copies.size() && (char*)copies[j + 1].first == (char*)copies[j].first + (offs[j + 1] - offs[j]) &&
+           copies[j + 1].first > copies[j].first) {
+      ++j;
+      bytes = offs[j] - offs[i] + copies[j].second.second;
+    }
+    CUDA_TRY(cudaMemcpyAsync(copies[i].first, g_rt.pinned + offs[i], bytes, cudaMemcpyHostToDevice, g_rt.stream));
+    i = j + 1;
   }
   CUDA_TRY(cudaMemsetAsync(B.d_status, 0, (size_t)n * 4, g_rt.stream));
   for (int c = 0; c < n; ++c) {
@@ -821,6 +853,11 @@ int build_handles(const CambGpuParams* p, int n, std::vector<Handle*>& hs, int* 
   }
   for (int i = 0; i < n; ++i) {
     if (!hs[i]) continue;
+    if (p[i].want_transfer && !p[i].want_cls) {  // transfer functions need no Bessel table
+      static const cg::BesselTable empty;
+      cg::fill_view(hs[i]->c, empty, hs[i]->view);
+      continue;
+    }
     try {
       hs[i]->bt = cg::get_bessel_table(hs[i]->c.ls, hs[i]->c.maximum_qeta, p[i].BesselBoost, p[i].AccuracyBoost);
     } catch (const std::exception& e) {
@@ -938,22 +975,37 @@ int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, doubl
   std::lock_guard<std::mutex> lk(g_mu);
   if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
   if (lmax_out < 0 || lmax_out > 8000) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lmax_out out of range");
+  const double t0 = wall_ms();
   std::vector<Handle*> hs;
   int rc = build_handles(p, n, hs, status);
   struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
   if (rc) return rc;
+  const double t1 = wall_ms();
   Batch B;
   for (auto* h : hs) B.views.push_back(&h->view);
   rc = stage_batch(B, lmax_out);
   if (rc) return rc;
   if (B.transfer) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "want_cls = 0: use cambgpu_get_transfer_batch");
+  const double t2 = wall_ms();
   rc = run_all(B, true, true, true);
   if (rc) return rc;
   rc = check_status(B, status);
   if (rc) return rc;
+  const double t3 = wall_ms();
   if (lmax_lensed)
     for (int c = 0; c < n; ++c) lmax_lensed[c] = B.ups[c].d.lensed ? B.ups[c].d.lmax_lensed : 0;
-  return fetch_spectra(B, lmax_out, unlensed, lensed, lens_potential);
+  rc = fetch_spectra(B, lmax_out, unlensed, lensed, lens_potential);
+  const double t4 = wall_ms();
+  g_host_ms[0] = t1 - t0;
+  g_host_ms[1] = t2 - t1;
+  g_host_ms[2] = t3 - t2;
+  g_host_ms[3] = t4 - t3;
+  return rc;
+}
+
+int cambgpu_last_host_timings(double* out4) {
+  for (int i = 0; i < 4; ++i) out4[i] = g_host_ms[i];
+  return 0;
 }
 
 int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, double* cl_out, int* status) {

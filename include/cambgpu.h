@@ -271,6 +271,9 @@ int cambgpu_set_ode_team(int lanes_per_mode);
  * mass.  best = [team, order, class]; times (optional, >= 8 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
+/* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch call, in ms:
+ * [host tables, staging (pinned copy + uploads enqueued), device pipeline, packing + D2H]. */
+int cambgpu_last_host_timings(double* out4);
 /* Kernel timing of the last GPU call, in ms: [ode, spline, los, cls, h2d, d2h]. */
 int cambgpu_last_timings(double* out6);
 /* Derivative evaluations of the last ODE launch (all modes of all cosmologies). */
