@@ -146,6 +146,87 @@ def accuracy_vs_fp64(params, ref, lmax):
             "max_TE_over_sqrt_TTEE": te}
 
 
+def single_configs(nthreads):
+    """One cosmology per configuration of the benchmark suite, GPU (C ABI, host buffers)
+    against the CPU restatement on the host cores, both with their host tables: the
+    plain massless lmax 1000 case; one 0.06 eV neutrino with lensed TT/EE/BB/TE and the
+    lensing potential to lmax 2500; and that cosmology's matter transfer functions to
+    kmax = 10 h/Mpc at z = 0 (computed without the CMB)."""
+    from camb_gb300 import _lib
+    from oracle import oracle as orc
+    lib = _lib.load()
+
+    def base(lmax, lensing, mnu):
+        p = _lib.default_params()
+        p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
+        p.nnu = 3.046
+        p.mnu, p.num_massive_neutrinos = mnu, 1
+        p.do_lensing = 1 if lensing else 0
+        p.max_l = lmax + (200 if lensing else 0)
+        p.max_eta_k = 2.5 * p.max_l
+        return p
+
+    def gpu_cmb(p):
+        n = p.max_l + 1
+        unl = np.zeros((n, 4))
+        lens = np.zeros((n, 4)) if p.do_lensing else None
+        pot = np.zeros((n, 3)) if p.do_lensing else None
+        st = (C.c_int * 1)()
+        lml = (C.c_int * 1)()
+        _lib.check(lib.cambgpu_get_spectra_batch(C.byref(p), 1, p.max_l, _lib.dptr(unl),
+                                                 _lib.dptr(lens) if lens is not None else None,
+                                                 _lib.dptr(pot) if pot is not None else None, lml, st))
+
+    def cpu_cmb(p):
+        T = _lib.Tables(p)
+        icl = orc.cls(T, orc.los(T, orc.evolve_sources(T, nthreads), nthreads))
+        allc = orc.interpolate_cls(T.ls, icl, T.view.cl_template_scale)
+        if p.do_lensing:
+            orc.lens_cls(allc[:, :4], T.ls, p.max_l)
+
+    def transfer_params():
+        p = base(2500, False, 0.06)
+        p.want_cls, p.want_transfer, p.transfer_high_precision = 0, 1, 1
+        p.transfer_kmax = 10 * p.H0 / 100
+        p.num_transfer_redshifts = 1
+        p.transfer_redshifts[0] = 0.0
+        return p
+
+    def gpu_tr(p):
+        tr = np.zeros((1, 1, 4096, 13), dtype=np.float32)
+        nq = (C.c_int * 1)()
+        s8 = np.zeros(1)
+        sv = np.zeros(1)
+        st = (C.c_int * 1)()
+        _lib.check(lib.cambgpu_get_transfer_batch(C.byref(p), 1, 4096, tr.ctypes.data_as(C.POINTER(C.c_float)), nq,
+                                                  _lib.dptr(s8), _lib.dptr(sv), st))
+        return s8[0]
+
+    def cpu_tr(p):
+        T = _lib.Tables(p)
+        return orc.sigma8(T, orc.evolve_transfer(T, nthreads))[0][0]
+
+    def timed(f, p, reps=2):
+        f(p)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = f(p)
+        return (time.perf_counter() - t0) / reps * 1e3, r
+
+    out = {}
+    for name, p in [("lmax1000_unlensed_massless", base(1000, False, 0.0)),
+                    ("lmax2500_lensed_mnu0.06", base(2500, True, 0.06))]:
+        g, _ = timed(gpu_cmb, p)
+        c, _ = timed(cpu_cmb, p, reps=1)
+        out[name] = {"gpu_ms": g, "cpu_ms": c, "cpu_threads": nthreads}
+    p = transfer_params()
+    g, s8g = timed(gpu_tr, p)
+    c, s8c = timed(cpu_tr, p, reps=1)
+    out["transfer_kmax10h_mnu0.06_z0"] = {"gpu_ms": g, "cpu_ms": c, "cpu_threads": nthreads, "sigma8_gpu": s8g,
+                                           "sigma8_cpu": s8c}
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -321,6 +402,7 @@ def main():
         ref = []
         t = cpu_reference(cps, nth, keep=ref)
         line["accuracy"] = accuracy_vs_fp64(cps, ref, args.lmax)  # timed form vs the FP64 CPU restatement
+        line["single_cosmology_configs"] = single_configs(nth)
         line["cpu_baseline"] = {"value": len(cps) / t, "unit": "cosmologies/s", "cores": nth, "kind": "port",
                                 "sample": f"{len(cps)} draws of the same workload, host tables + ODE + LOS + C_l"}
         print(json.dumps(line))

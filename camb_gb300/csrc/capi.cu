@@ -678,10 +678,7 @@ int run_los(Batch& B) {
   dim3 g1((B.max_rows + 127) / 128, n);
   source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
   g_launches++;
-  for (int c = 0; c < n; ++c) {
-    const auto& v = *B.views[c];
-    CUDA_TRY(cudaMemsetAsync(B.ups[c].d.delta, 0, (size_t)v.nq * v.nl * v.nsrc * 8, g_rt.stream));
-  }
+  // every Delta_p_l_k entry is written by the LOS kernel (zeros where it skips)
   size_t smem = (size_t)B.max_ntau * (3 + 1 + 1) * 8 + (size_t)B.max_ntau * 4 + 64;
   dim3 g2(B.max_nq, n);
   if (g_precision == 1) los_flat_mixed_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);

@@ -199,7 +199,13 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int j = warp; j < C.nl; j += nwarps) {
     const int flag = s_flag[j];
-    if (flag & F_SKIP) continue;
+    if (flag & F_SKIP) {  // nothing to integrate: the transfer function is zero
+      if (lane == 0) {
+        double* D = C.delta + ((size_t)q_ix * C.nl + j) * nsrc;
+        for (int s = 0; s < nsrc; ++s) D[s] = 0;
+      }
+      continue;
+    }
     double acc0 = 0, acc1 = 0, acc2 = 0;
     if (flag & F_INT) {
       const int nstart = s_ns[j], nend = s_ne[j];

@@ -1714,9 +1714,15 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
   Run R;
   int cosmo = -1, q_ix = 0;
   R.active = false;
+  // The first item of every thread is its global index, so each block starts on 128
+  // consecutive queue entries independent of atomic ordering; later items come from the
+  // shared counter (past the statically assigned ones).
+  const int nthreads = gridDim.x * blockDim.x;
+  int first = blockIdx.x * blockDim.x + threadIdx.x;
   for (;;) {
     if (!R.active) {
-      const int w = atomicAdd(counter, 1);
+      const int w = first >= 0 ? first : nthreads + atomicAdd(counter, 1);
+      first = -1;
       if (w >= nitems) break;
       const WorkItem it = items[w];
       cosmo = it.cosmo;
