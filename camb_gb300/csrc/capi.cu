@@ -663,11 +663,15 @@ int run_ode(Batch& B) {
   int team = pick_team(B);
   int order = g_order >= 0 ? g_order : g_tuned[size_class(B)].order;
   int lanes = team <= 5 ? 1 : team;
-  int per_sm = std::max(1, ode_blocks_per_sm(team, 128));
-  int blocks = std::min(g_rt.nsm * per_sm, (B.nitems * lanes + 127) / 128);
+  // Few modes (a single cosmology): one warp per block, so that the warps spread over the
+  // SMs and none shares an SM's FP64 pipe; otherwise blocks of 128.
+  const long threads_needed = (long)B.nitems * lanes;
+  const int tpb = threads_needed < 2L * 128 * g_rt.nsm ? 32 : 128;
+  int per_sm = std::max(1, ode_blocks_per_sm(team, tpb));
+  int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
   const WorkItem* queue = order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
-  CUDA_TRY(launch_ode_kernel(team, blocks, 128, g_rt.stream, B.d_cosmos, queue, B.nitems, B.d_counter,
+  CUDA_TRY(launch_ode_kernel(team, blocks, tpb, g_rt.stream, B.d_cosmos, queue, B.nitems, B.d_counter,
                              B.transfer));
   g_launches++;
   return 0;
