@@ -309,6 +309,7 @@ int device_lens_geom(const HostLensGeom& h, LensGeomDev& G) {
 struct Upload {
   const CambGpuTables* t;
   std::vector<double> spl;  // [5][nk]
+  std::vector<double> inv_q;  // 1/nu_q
   DevCosmo d;
 };
 
@@ -320,7 +321,7 @@ size_t bytes_for(const CambGpuTables& t) {
   s += 2 * r((size_t)t.ntau * t.nsrc * t.nk * 8);
   s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
   s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256);
-  s += 2 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
+  s += 3 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
   s += r((size_t)(t.max_l + 1) * 6 * 8) + r((size_t)(t.max_l + 1) * 4 * 8);  // all-l C_l, lensed C_l
   if (t.transfer_only)
     s += r((size_t)t.num_transfer_times * 8) + r((size_t)t.num_transfer_times * t.nk * 13 * 4) +
@@ -364,7 +365,11 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
     d.grhormass[i] = t.grhormass[i];
     d.nu_tau_nonrel[i] = t.nu_tau_nonrel[i];
   }
+  d.photbar_fac = 0.75 / d.photbar_a;
   if (t.nu_eig > 0) {
+    u.inv_q.resize(t.nqmax);
+    for (int i = 0; i < t.nqmax; ++i) u.inv_q[i] = 1.0 / t.nu_q[i];
+    d.nu_inv_q = (const double*)put(u.inv_q.data(), (size_t)t.nqmax * 8);
     d.nu_q = (const double*)put(t.nu_q, (size_t)t.nqmax * 8);
     d.nu_int_kernel = (const double*)put(t.nu_int_kernel, (size_t)t.nqmax * 8);
     d.nu_tau_notmassless = (const double*)put(t.nu_tau_notmassless, (size_t)t.nu_eig * t.nqmax * 8);

@@ -19,6 +19,8 @@ struct DevCosmo {
   const double* nu_q;
   const double* nu_int_kernel;
   const double* nu_tau_notmassless;  // [nu_eig][nqmax]
+  const double* nu_inv_q;            // 1/nu_q
+  double photbar_fac;                // 3/(4 photbar_a)
   // thermal history
   const double* thermo_horner;  // [nthermo][16]
   const double* dddotmu;

@@ -951,37 +951,53 @@ __device__ void copy_vars(const DevCosmo& C, const St& O, const St& N, const dou
   }
 }
 
+// Per momentum bin of one eigenstate at scale factor a: a m/q, 1/sqrt(1+(a m/q)^2) and
+// sqrt(1+(a m/q)^2), formed once per right-hand side and shared by the momentum
+// integrals, the equations of motion and the source terms (q^-1 is tabulated).
+constexpr int NQ = 16;
+struct NuBins {
+  double aq[NQ], v[NQ], s[NQ];
+};
+
+__device__ __forceinline__ void nu_bins(const DevCosmo& C, double a, int i, NuBins& b) {
+  const double am = a * C.nu_masses[i];
+  for (int iq = 0; iq < C.nqmax; ++iq) {
+    const double aq = am * C.nu_inv_q[iq];
+    const double s2 = fma(aq, aq, 1.0);
+    const double v = rsqrt(s2);
+    b.aq[iq] = aq;
+    b.v[iq] = v;
+    b.s[iq] = s2 * v;
+  }
+}
+
 // Nu_Integrate_L01/L012 (equations.f90:1178-1270): momentum integrals of one eigenstate
 template <bool L2>
-__device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, const double* __restrict__ y, double a,
-                                             int i, double& drhonu, double& fnu, double& dpnu, double& pinu) {
+__device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, const double* __restrict__ y,
+                                             const NuBins& b, int i, double& drhonu, double& fnu, double& dpnu,
+                                             double& pinu) {
   drhonu = fnu = dpnu = pinu = 0;
-  const double am = a * C.nu_masses[i];
   int ind = M.nu_ix[i];
   for (int iq = 0; iq < M.nq[i]; ++iq) {
-    const double aq = am / C.nu_q[iq], w = C.nu_int_kernel[iq];
-    const double s1 = sqrt(1.0 + aq * aq);
-    drhonu += w * y[ind] * s1;
+    const double w = C.nu_int_kernel[iq];
+    drhonu += w * y[ind] * b.s[iq];
     fnu += w * y[ind + 1];
     if (L2) {
-      const double v = 1.0 / s1;
-      dpnu += w * y[ind] * v;
-      pinu += w * y[ind + 2] * v;
+      dpnu += w * y[ind] * b.v[iq];
+      pinu += w * y[ind + 2] * b.v[iq];
     }
     ind += M.lmaxnu_tau[i] + 1;
   }
   ind = M.nu_pert_ix;
   for (int iq = M.nq[i]; iq < C.nqmax; ++iq) {
-    const double qq = C.nu_q[iq], aq = am / qq, w = C.nu_int_kernel[iq];
-    const double ps = (C.nu_masses[i] / qq) * (C.nu_masses[i] / qq) / 2;
+    const double w = C.nu_int_kernel[iq];
+    const double mq = C.nu_masses[i] * C.nu_inv_q[iq], ps = mq * mq * 0.5;
     const double tmp = w * (y[M.r_ix] + ps * y[ind]);
-    const double s1 = sqrt(1.0 + aq * aq);
-    drhonu += tmp * s1;
+    drhonu += tmp * b.s[iq];
     fnu += w * (y[M.r_ix + 1] + ps * y[ind + 1]);
     if (L2) {
-      const double v = 1.0 / s1;
-      dpnu += tmp * v;
-      pinu += w * (y[M.r_ix + 2] + ps * y[ind + 2]) * v;
+      dpnu += tmp * b.v[iq];
+      pinu += w * (y[M.r_ix + 2] + ps * y[ind + 2]) * b.v[iq];
     }
   }
   if (L2) dpnu = dpnu / 3;
@@ -989,23 +1005,20 @@ __device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, con
 
 // Nu_pinudot (equations.f90:1272-1313)
 __device__ double nu_pinudot(const DevCosmo& C, const St& M, const double* __restrict__ y,
-                             const double* __restrict__ ydot, double a, double adotoa, int i) {
+                             const double* __restrict__ ydot, const NuBins& b, double adotoa, int i) {
   double pinudot = 0;
   int ind = M.nu_ix[i] + 2;
-  const double am = a * C.nu_masses[i];
   for (int iq = 0; iq < M.nq[i]; ++iq) {
-    const double aq = am / C.nu_q[iq], aqdot = aq * adotoa;
-    const double v = 1.0 / sqrt(1.0 + aq * aq);
-    const double vdot = -aq * aqdot * (v * v * v);
+    const double aq = b.aq[iq], v = b.v[iq];
+    const double vdot = -aq * (aq * adotoa) * (v * v * v);
     pinudot += C.nu_int_kernel[iq] * (ydot[ind] * v + y[ind] * vdot);
     ind += M.lmaxnu_tau[i] + 1;
   }
   ind = M.nu_pert_ix + 2;
   for (int iq = M.nq[i]; iq < C.nqmax; ++iq) {
-    const double qq = C.nu_q[iq], aq = am / qq, aqdot = aq * adotoa;
-    const double ps = (C.nu_masses[i] / qq) * (C.nu_masses[i] / qq) / 2;
-    const double v = 1.0 / sqrt(1.0 + aq * aq);
-    const double vdot = -aq * aqdot * (v * v * v);
+    const double aq = b.aq[iq], v = b.v[iq];
+    const double mq = C.nu_masses[i] * C.nu_inv_q[iq], ps = mq * mq * 0.5;
+    const double vdot = -aq * (aq * adotoa) * (v * v * v);
     const double psi2dot = ydot[M.r_ix + 2] + ps * ydot[ind];
     const double psi2 = y[M.r_ix + 2] + ps * y[ind];
     pinudot += C.nu_int_kernel[iq] * (psi2dot * v + psi2 * vdot);
@@ -1029,17 +1042,19 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   double dgrho = grhob_t * clxb + grhoc_t * clxc;
   double dgq = grhob_t * vb;
   double grhonu_t = 0, gpres_nu = 0, wnu[NUE] = {0, 0, 0};
+  NuBins bins[NUE];
   for (int i = 0; i < C.nu_eig; ++i) {  // MassiveNuVars (equations.f90:1358-1401)
     const double gm_t = C.grhormass[i] * ia2;
     double rhonu, pnu, clxnu, qnu;
     nuf::rho_P(a * C.nu_masses[i], rhonu, pnu);
+    const double ir = 1.0 / rhonu;
     if (M.approx[i]) {
       clxnu = y[M.nu_ix[i]];
       qnu = y[M.nu_ix[i] + 2];
     } else {
+      nu_bins(C, a, i, bins[i]);
       double dp, pn;
-      nu_integrate<false>(C, M, y, a, i, clxnu, qnu, dp, pn);
-      const double ir = 1.0 / rhonu;
+      nu_integrate<false>(C, M, y, bins[i], i, clxnu, qnu, dp, pn);
       qnu = qnu * ir;
       clxnu = clxnu * ir;
     }
@@ -1048,7 +1063,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
     gpres_nu += gm_t * pnu;
     dgrho += g_t * clxnu;
     dgq += g_t * qnu;
-    wnu[i] = pnu / rhonu;
+    wnu[i] = pnu * ir;
   }
   const double dgrho_matter = dgrho, grho_matter = grhonu_t + grhob_t + grhoc_t;
   const double grho = (grhonu_t + grhob_t + grhoc_t) + grhor_t + grhog_t + grhov_t;
@@ -1124,7 +1139,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   double qgdot = 0, polter = 0, E2 = 0;
   if (!M.nophot) {
     dy[g] = clxgdot;
-    const double inv_pb43 = 0.75 * a / C.photbar_a;
+    const double inv_pb43 = a * C.photbar_fac;  // 3/(4 photbar)
     qgdot = 4.0 / 3 * (-vbdot - adotoa * vb + delta_p_b * k) * inv_pb43 + dl[1] * clxg - dl2[1] * pig;
     dy[g + 1] = qgdot;
     if (!M.tc) {
@@ -1171,8 +1186,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       int ind = M.nu_ix[i];
       const int lt = M.lmaxnu_tau[i];
       for (int iq = 0; iq < M.nq[i]; ++iq) {
-        const double aq = a * C.nu_masses[i] / C.nu_q[iq];
-        const double v = rsqrt(1.0 + aq * aq);
+        const double v = bins[i].v[iq];
         dy[ind] = -k * (4.0 / 3.0 * z + v * y[ind + 1]);
         dy[ind + 1] = v * (dl[1] * y[ind] - dl2[1] * y[ind + 2]);
         if (lt == 2) {
@@ -1223,11 +1237,11 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
         pinudot = dy[M.nu_ix[i] + 3];
       } else {
         double qnu, dpnu;
-        nu_integrate<true>(C, M, y, a, i, clxnu, qnu, dpnu, pinu);
+        nu_integrate<true>(C, M, y, bins[i], i, clxnu, qnu, dpnu, pinu);
         clxnu = clxnu / rhonu;
         pinu = pinu / rhonu;
         const double rhonudot = nuf::drho(a * C.nu_masses[i], adotoa);
-        pinudot = nu_pinudot(C, M, y, dy, a, adotoa, i);
+        pinudot = nu_pinudot(C, M, y, dy, bins[i], adotoa, i);
         pinudot = pinudot / rhonu - rhonudot / rhonu * pinu;
       }
       const double g_t = gm_t * rhonu, gp_t = gm_t * pnu;
@@ -1340,7 +1354,7 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   R.active = true;
   R.status = 0;
   const int lm = max(max(M.lmaxg, M.lmaxgpol), max(M.lmaxnr, M.lmaxnu));
-  if (M.nvar > NV || lm >= NL || M.lmaxgpol >= 20 || C.nu_eig > NUE) {
+  if (M.nvar > NV || lm >= NL || M.lmaxgpol >= 20 || C.nu_eig > NUE || C.nqmax > NQ) {
     R.active = false;
     R.status = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
     return;
@@ -1536,7 +1550,9 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
     copy_vars(C, M, N, Y, YT);
     double rhonu, pnu, clxnu, qnu, dpnu, pinu;
     nuf::rho_P(a * C.nu_masses[e], rhonu, pnu);
-    nu_integrate<true>(C, M, Y, a, e, clxnu, qnu, dpnu, pinu);
+    NuBins b;
+    nu_bins(C, a, e, b);
+    nu_integrate<true>(C, M, Y, b, e, clxnu, qnu, dpnu, pinu);
     YT[N.nu_ix[e]] = clxnu / rhonu;
     YT[N.nu_ix[e] + 1] = dpnu / rhonu;
     YT[N.nu_ix[e] + 2] = qnu / rhonu;
@@ -1546,8 +1562,7 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
     const double am = a * C.nu_masses[e];
     int ind = M.nu_ix[e];
     for (int iq = 0; iq < M.nq[e]; ++iq) {
-      const double aq = am / C.nu_q[iq];
-      const double v = 1.0 / sqrt(1.0 + aq * aq);
+      const double v = b.v[iq];
       G11 += C.nu_int_kernel[iq] * Y[ind + 1] * v * v;
       if (M.lmaxnu_tau[e] > 2) G30 += C.nu_int_kernel[iq] * Y[ind + 3] * v * v;
       ind += M.lmaxnu_tau[e] + 1;
