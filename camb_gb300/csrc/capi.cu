@@ -310,13 +310,14 @@ struct Upload {
   const CambGpuTables* t;
   std::vector<double> spl;  // [5][nk]
   std::vector<double> inv_q;  // 1/nu_q
+  std::vector<double> inv_tgrid;  // 1/tau_j of the thermal log grid
   DevCosmo d;
 };
 
 size_t bytes_for(const CambGpuTables& t) {
   auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
   size_t s = 0;
-  s += r((size_t)t.nthermo * 16 * 8) + 4 * r((size_t)t.nthermo * 8);
+  s += r((size_t)t.nthermo * 16 * 8) + 4 * r((size_t)t.nthermo * 8) + r(((size_t)t.nthermo + 1) * 8);
   s += 2 * r((size_t)t.ntau * 8) + r((size_t)t.nk * sizeof(CambGpuModeSpec)) + r((size_t)t.nk * 8);
   s += 2 * r((size_t)t.ntau * t.nsrc * t.nk * 8);
   s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
@@ -381,6 +382,10 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.demmu = (const double*)put(t.demmu, (size_t)t.nthermo * 8);
   d.nthermo = t.nthermo;
   d.tauminn = t.tauminn; d.inv_tauminn = 1.0 / t.tauminn; d.dlntau = t.dlntau; d.dlntau_inv = t.dlntau_inv;
+  d.dlntau_inv_log2 = (float)(0.69314718055994530942 * t.dlntau_inv);
+  u.inv_tgrid.resize((size_t)t.nthermo + 1);
+  for (int j = 0; j <= t.nthermo; ++j) u.inv_tgrid[j] = 1.0 / (t.tauminn * std::exp(j * t.dlntau));
+  d.inv_tgrid = (const double*)put(u.inv_tgrid.data(), u.inv_tgrid.size() * 8);
   int e = t.nthermo - 1;
   d.cs2_end = t.cs2[e]; d.dotmu_end = t.dotmu[e]; d.ddotmu_end = t.ddotmu[e]; d.dddotmu_end = t.dddotmu[e];
   d.emmu_end = t.emmu[e];

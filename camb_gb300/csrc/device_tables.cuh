@@ -29,6 +29,8 @@ struct DevCosmo {
   const double* demmu;
   int nthermo;
   double tauminn, inv_tauminn, dlntau, dlntau_inv;
+  const double* inv_tgrid;  // [nthermo+1] 1/(tauminn exp(j dlntau)), the ideal log grid
+  float dlntau_inv_log2;    // ln 2 / dlntau
   double cs2_end, dotmu_end, ddotmu_end, dddotmu_end, emmu_end;
   // time grid
   const double* tau_points;

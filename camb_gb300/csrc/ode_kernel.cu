@@ -85,9 +85,21 @@ struct SrcOut {
 __device__ __forceinline__ double ldg(const double* p) { return __ldg(p); }
 
 // Thermo_values (results.f90:1848-1880)
+// Position of tau on the thermal-history grid, 1 + ln(tau/tau_min)/dln(tau): an FP32
+// estimate picks a grid point j, then ln(tau/tau_j) = ln(1 + u) with |u| <= dln(tau) (a few
+// 1e-3) is a six-term series in FP64 -- no FP64 log on the FP64 pipe.
+__device__ __forceinline__ double thermo_index(const DevCosmo& C, double tau) {
+  const float df = __log2f((float)(tau * C.inv_tauminn)) * C.dlntau_inv_log2;
+  int j = (int)df;
+  j = j < 0 ? 0 : (j > C.nthermo ? C.nthermo : j);
+  const double u = fma(tau, C.inv_tgrid[j], -1.0);
+  const double l1p = u * (1.0 + u * (-0.5 + u * (1.0 / 3.0 + u * (-0.25 + u * (0.2 - u * (1.0 / 6.0))))));
+  return (double)j + l1p * C.dlntau_inv + 1.0;
+}
+
 __device__ __forceinline__ void thermo_values(const DevCosmo& C, double tau, double itau, double& a, double& cs2,
                                               double& opac, double& dopac, bool want_dop = true) {
-  double d = log(tau * C.inv_tauminn) * C.dlntau_inv + 1.0;
+  double d = thermo_index(C, tau);
   int i = (int)d;
   d = d - i;
   if (i < 1) {  // before the table start (never reached: every mode starts after tauminn)
@@ -113,7 +125,7 @@ __device__ __forceinline__ void ionization(const DevCosmo& C, double tau, double
                                            double& vis, double& dvis, double& ddvis, double& expmmu) {
   double a, cs2;
   thermo_values(C, tau, itau, a, cs2, opac, dopac);
-  double d = log(tau * C.inv_tauminn) * C.dlntau_inv + 1.0;
+  double d = thermo_index(C, tau);
   int i = (int)d;
   d = d - i;
   if (i < 1) {
