@@ -26,6 +26,7 @@ cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s,
 cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s);
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
+__global__ void source_spline_f32_kernel(const DevCosmo*, const double* const*);
 __global__ void los_flat_kernel(const DevCosmo*);
 __global__ void los_flat_mixed_kernel(const DevCosmo*);
 __global__ void scal_cls_kernel(const DevCosmo*);
@@ -104,6 +105,10 @@ struct Runtime {
     float4* devf;
     unsigned long epoch;
     unsigned long long print;  // content fingerprint: host tables are freed and their addresses reused
+    float* inv_dxf;            // 1/(x_{i+1}-x_i) in FP32
+    int nseg;                  // runs of uniform spacing in x (0: more than kBessSegMax)
+    double seg_x0[cgdev::kBessSegMax], seg_inv_h[cgdev::kBessSegMax];
+    int seg_i0[cgdev::kBessSegMax], seg_n[cgdev::kBessSegMax];
   };
   unsigned long epoch = 0;
   std::vector<DevBessel> bessel;
@@ -162,7 +167,8 @@ unsigned long long bessel_print(const CambGpuTables& t, size_t n) {
   return h;
 }
 
-int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4** dev_f) {
+int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4** dev_f,
+                  const Runtime::DevBessel** entry) {
   size_t n = (size_t)t.nl * (t.num_xx - 1) * 4;
   const unsigned long long print = bessel_print(t, n);
   for (auto& b : g_rt.bessel)
@@ -171,9 +177,38 @@ int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4
       *dev_h = b.dev;
       *dev_x = b.devx;
       *dev_f = b.devf;
+      *entry = &b;
       return 0;
     }
-  Runtime::DevBessel b{t.bessel_horner, n, nullptr, nullptr, t.num_xx, nullptr, g_rt.epoch, print};
+  Runtime::DevBessel b{t.bessel_horner, n, nullptr, nullptr, t.num_xx, nullptr, g_rt.epoch, print, nullptr, 0,
+                       {}, {}, {}, {}};
+  {
+    // The x grid is a few runs of uniform spacing (bessels.f90:170-178): record them so
+    // that the projection kernels find a point's interval arithmetically, not by bisection
+    const int nx = t.num_xx;
+    const double* x = t.bess_x;
+    int k = 0;
+    b.nseg = 0;
+    while (k < nx - 1) {
+      const double h = x[k + 1] - x[k];
+      int e = k + 1;  // the run covers intervals [k, e)
+      while (e < nx - 1 && std::fabs((x[e + 1] - x[e]) - h) <= 1e-6 * h) ++e;
+      if (b.nseg == cgdev::kBessSegMax) {
+        b.nseg = 0;
+        break;
+      }
+      b.seg_x0[b.nseg] = x[k];
+      b.seg_inv_h[b.nseg] = (e - k) / (x[e] - x[k]);
+      b.seg_i0[b.nseg] = k;
+      b.seg_n[b.nseg] = e - k;
+      ++b.nseg;
+      k = e;
+    }
+    std::vector<float> inv_dx(nx - 1);
+    for (int i = 0; i < nx - 1; ++i) inv_dx[i] = (float)(1.0 / (x[i + 1] - x[i]));
+    CUDA_TRY(cudaMalloc(&b.inv_dxf, (size_t)(nx - 1) * sizeof(float)));
+    CUDA_TRY(cudaMemcpy(b.inv_dxf, inv_dx.data(), (size_t)(nx - 1) * sizeof(float), cudaMemcpyHostToDevice));
+  }
   CUDA_TRY(cudaMalloc(&b.dev, n * sizeof(double)));
   CUDA_TRY(cudaMalloc(&b.devx, (size_t)t.num_xx * sizeof(double)));
   CUDA_TRY(cudaMalloc(&b.devf, n * sizeof(float)));
@@ -192,6 +227,7 @@ int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4
       cudaFree(o.dev);
       cudaFree(o.devx);
       cudaFree(o.devf);
+      cudaFree(o.inv_dxf);
       g_rt.bessel.erase(g_rt.bessel.begin() + i);
       break;
     }
@@ -200,6 +236,7 @@ int device_bessel(const CambGpuTables& t, double** dev_h, double** dev_x, float4
   *dev_h = b.dev;
   *dev_x = b.devx;
   *dev_f = b.devf;
+  *entry = &g_rt.bessel.back();
   return 0;
 }
 
@@ -409,8 +446,17 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   double *bh = nullptr, *bx = nullptr;
   float4* bf = nullptr;
   if (t.bessel_horner) {  // transfer-function cosmologies have no Bessel table
-    int rc = device_bessel(t, &bh, &bx, &bf);
+    const Runtime::DevBessel* be = nullptr;
+    int rc = device_bessel(t, &bh, &bx, &bf, &be);
     if (rc) return rc;
+    d.bess_inv_dxf = be->inv_dxf;
+    d.nseg = be->nseg;
+    for (int r = 0; r < be->nseg; ++r) {
+      d.seg_x0[r] = be->seg_x0[r];
+      d.seg_inv_h[r] = be->seg_inv_h[r];
+      d.seg_i0[r] = be->seg_i0[r];
+      d.seg_n[r] = be->seg_n[r];
+    }
   }
   d.bessel_horner = bh;
   d.bessel_f32 = bf;
@@ -690,13 +736,19 @@ int run_ode(Batch& B) {
 int run_los(Batch& B) {
   int n = (int)B.views.size();
   dim3 g1((B.max_rows + 127) / 128, n);
-  source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
+  // mixed precision: the spline leaves FP32 {source, d2} pairs in dd_src for the FP32 staging
+  if (g_precision == 1) source_spline_f32_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
+  else source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
   g_launches++;
   // every Delta_p_l_k entry is written by the LOS kernel (zeros where it skips)
-  size_t smem = (size_t)B.max_ntau * (3 + 1 + 1) * 8 + (size_t)B.max_ntau * 4 + 64;
   dim3 g2(B.max_nq, n);
-  if (g_precision == 1) los_flat_mixed_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
-  else los_flat_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
+  if (g_precision == 1) {
+    const size_t smem = (size_t)B.max_ntau * (3 + 1 + 1 + 1) * 4 + 64;
+    los_flat_mixed_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
+  } else {
+    const size_t smem = (size_t)B.max_ntau * (3 + 1 + 1) * 8 + (size_t)B.max_ntau * 4 + 64;
+    los_flat_kernel<<<g2, 256, smem, g_rt.stream>>>(B.d_cosmos);
+  }
   g_launches++;
   CUDA_TRY(cudaGetLastError());
   return 0;

@@ -9,6 +9,8 @@
 
 namespace cgdev {
 
+constexpr int kBessSegMax = 8;
+
 struct DevCosmo {
   // background
   double grhog, grhornomass, grhoc, grhob, grhov, tau0, taurend, tau_maxvis, matter_verydom_tau;
@@ -67,6 +69,13 @@ struct DevCosmo {
   const double* bess_x;
   const double* bessel_horner;  // [nl][num_xx-1][4]
   const float4* bessel_f32;     // [nl][num_xx-1] the same coefficients in FP32 (mixed precision)
+  const float* bess_inv_dxf;    // [num_xx-1] 1 / (x_{i+1} - x_i) in FP32
+  // the x grid as runs of uniform spacing (nseg = 0: none recorded, bisect instead)
+  int nseg;
+  double seg_x0[kBessSegMax];   // first point of each run
+  double seg_inv_h[kBessSegMax];
+  int seg_i0[kBessSegMax];      // grid index of the first point
+  int seg_n[kBessSegMax];       // intervals in the run
   int num_xx;
   // settings
   int nsrc, want_late_time;
