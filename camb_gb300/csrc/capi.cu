@@ -20,9 +20,9 @@
 #include "host/cosmo_host.hpp"
 
 namespace cgdev {
-int ode_blocks_per_sm(int team, int threads);
+int ode_blocks_per_sm(int team, int threads, int warp_stride);
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
-                              const WorkItem* items, int nitems, int* counter, bool transfer);
+                              const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride);
 cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s);
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
@@ -47,7 +47,10 @@ int g_team = 0;
 int g_precision = 0;  // 0: FP64 throughout; 1: mixed-precision line-of-sight projection
 // autotuned ODE configuration per batch-size class: [0] small (< 24 modes/SM), [1] large
 struct OdeCfg { int team; int order; };
-OdeCfg g_tuned[2] = {{32, 0}, {1, 0}};
+// untuned defaults: warp per mode (shared-memory rows) for few modes, where latency
+// decides; thread per mode for large batches, where FP64 throughput does
+OdeCfg g_tuned[2] = {{6, 0}, {1, 0}};
+constexpr int kWarpStrideMax = 448;  // the shared-memory warp kernel's largest state row
 int g_order = -1;  // forced queue order (-1: use the tuned one)
 long long g_last_evals = 0;
 long long g_h2d = 0, g_d2h = 0;
@@ -505,6 +508,7 @@ struct Batch {
   int max_ntau = 0, max_nq = 0, max_nl = 0, max_rows = 0;
   bool massive_nu = false;  // some cosmology has massive neutrinos (thread-per-mode kernel only)
   bool transfer = false;    // transfer functions only (every cosmology of the batch)
+  int warp_stride = 0;      // state-row length of the warp-per-mode kernel (largest system)
   // cosmologies to lens, grouped by lensing geometry
   struct LensGroup {
     HostLensGeom h;
@@ -579,6 +583,17 @@ int stage_batch(Batch& B, int lmax_out = 0) {
     B.max_nl = std::max(B.max_nl, B.views[c]->nl);
     B.max_rows = std::max(B.max_rows, B.views[c]->ntau * B.views[c]->nsrc);
     B.massive_nu |= B.views[c]->nu_eig > 0;
+    {
+      // largest packed system of GetNumEqns: photons, massless neutrinos, the massive
+      // eigenstates' full momentum grids and the relativistic perturbation hierarchy
+      const CambGpuTables& t = *B.views[c];
+      for (int m = 0; m < t.nk; ++m) {
+        const CambGpuModeSpec& ms = t.modes[m];
+        int nv = 4 + (ms.lmaxg + 1) + (ms.lmaxnr + 1) + ms.lmaxgpol - 1;
+        if (t.nu_eig > 0) nv += (ms.lmaxnu + 1) * (1 + t.nu_eig * t.nqmax);
+        B.warp_stride = std::max(B.warp_stride, (nv + 1) & ~1);
+      }
+    }
     if (c == 0) B.transfer = B.views[c]->transfer_only != 0;
     else if (B.transfer != (B.views[c]->transfer_only != 0))
       return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "a batch is either all CMB or all transfer functions");
@@ -707,9 +722,11 @@ int size_class(const Batch& B) { return B.nitems >= 24 * g_rt.nsm ? 1 : 0; }
 
 int pick_team(const Batch& B) {
   int t = g_team ? g_team : g_tuned[size_class(B)].team;
-  // the warp-per-mode kernel evolves the massless-neutrino CMB layout only
-  if ((B.massive_nu || B.transfer) && t >= 8) t = 2;
-  if (B.transfer && t > 3) t = 2;
+  // the register-resident warp kernels (8/16/32 lanes) evolve the massless-neutrino CMB
+  // layout only; the shared-memory warp kernel (6) any layout up to kWarpStrideMax entries
+  if ((B.massive_nu || B.transfer) && t >= 8) t = 6;
+  if (B.transfer && t > 3 && t != 6) t = 2;
+  if (t == 6 && B.warp_stride > kWarpStrideMax) t = 2;
   return t;
 }
 
@@ -718,17 +735,18 @@ int run_ode(Batch& B) {
   CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
   int team = pick_team(B);
   int order = g_order >= 0 ? g_order : g_tuned[size_class(B)].order;
-  int lanes = team <= 5 ? 1 : team;
+  const int lanes = team <= 5 ? 1 : team == 6 ? 32 : team;
   // Few modes (a single cosmology): one warp per block, so that the warps spread over the
-  // SMs and none shares an SM's FP64 pipe; otherwise blocks of 128.
+  // SMs and none shares an SM's FP64 pipe; otherwise blocks of 128.  The shared-memory
+  // warp kernel always runs one warp per block.
   const long threads_needed = (long)B.nitems * lanes;
-  const int tpb = threads_needed < 2L * 128 * g_rt.nsm ? 32 : 128;
-  int per_sm = std::max(1, ode_blocks_per_sm(team, tpb));
+  const int tpb = (team == 6 || threads_needed < 2L * 128 * g_rt.nsm) ? 32 : 128;
+  int per_sm = std::max(1, ode_blocks_per_sm(team, tpb, B.warp_stride));
   int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
   const WorkItem* queue = order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
   CUDA_TRY(launch_ode_kernel(team, blocks, tpb, g_rt.stream, B.d_cosmos, queue, B.nitems, B.d_counter,
-                             B.transfer));
+                             B.transfer, B.warp_stride));
   g_launches++;
   return 0;
 }
@@ -1214,8 +1232,8 @@ int cambgpu_set_precision(int mode) {
 int cambgpu_get_precision(void) { return g_precision; }
 
 int cambgpu_set_ode_team(int lanes) {
-  if (lanes < 0 || (lanes > 5 && lanes != 8 && lanes != 16 && lanes != 32))
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team code must be 0-5, 8, 16 or 32");
+  if (lanes < 0 || (lanes > 6 && lanes != 8 && lanes != 16 && lanes != 32))
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team code must be 0-6, 8, 16 or 32");
   g_team = lanes;
   return 0;
 }
@@ -1228,9 +1246,10 @@ int cambgpu_last_timings(double* out6) {
 long long cambgpu_last_ode_evals(void) { return g_last_evals; }
 
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times) {
-  // candidates: (team code, queue order); team 32 = warp per mode, 1/2/3 = thread per mode
+  // candidates: (team code, queue order); team 32 = warp per mode with registers
+  // (massless layout), 6 = warp per mode with shared-memory rows, 1/2/3 = thread per mode
   // with 3/4/5 resident blocks per SM
-  static const int cand[][2] = {{32, 0}, {1, 0}, {2, 0}, {3, 0}, {2, 1}, {1, 2}, {2, 2}, {3, 2}};
+  static const int cand[][2] = {{32, 0}, {1, 0}, {2, 0}, {3, 0}, {2, 1}, {1, 2}, {2, 2}, {3, 2}, {6, 0}};
   const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
   int rc = cambgpu_batch_prepare(p, n);
   if (rc) return rc;
@@ -1241,7 +1260,10 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   int bi = 0;
   for (int c = 0; c < nc; ++c) {
     if (times) times[c] = 0;
-    if (B.massive_nu && cand[c][0] >= 8) continue;  // massless-only warp kernel
+    if ((B.massive_nu || B.transfer) && cand[c][0] >= 8) continue;  // massless-only warp kernel
+    // the shared-memory warp kernel is the latency choice for few modes; on large batches
+    // its redundant per-lane scalar work loses to thread per mode several times over
+    if (cand[c][0] == 6 && (B.warp_stride > kWarpStrideMax || size_class(B) == 1)) continue;
     g_team = cand[c][0];
     g_order = cand[c][1];
     rc = run_all(B, true, false, false);  // warm-up

@@ -859,6 +859,48 @@ __device__ __forceinline__ double drho(double am, double adotoa) {
 }
 }  // namespace nuf
 
+// W = 1: one thread integrates one mode.  W = 32: the 32 lanes of a warp integrate one
+// mode together -- every lane evaluates the scalar part of the equations (identical
+// values, identical control flow), the multipole hierarchies, momentum bins and stage
+// combinations are split across lanes, and the state rows live in shared memory.
+template <int W>
+__device__ __forceinline__ int wlane() {
+  if constexpr (W == 1) return 0;
+  else return threadIdx.x & 31;
+}
+template <int W>
+__device__ __forceinline__ void wsync() {
+  if constexpr (W > 1) __syncwarp();
+}
+// butterfly sum: every lane ends with the same bits (each level adds the same pair)
+template <int W>
+__device__ __forceinline__ double wsum(double v) {
+  if constexpr (W > 1) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+template <int W>
+__device__ __forceinline__ double wmax(double v) {
+  if constexpr (W > 1) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+template <int W>
+__device__ __forceinline__ unsigned long long wmax_u64(unsigned long long v) {
+  if constexpr (W > 1) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+      v = t > v ? t : v;
+    }
+  }
+  return v;
+}
+
 // per-mode control state (EvolutionVars, equations.f90:66-151), indices 0-based
 struct St {
   double q, k, ik, k2, ik2;
@@ -919,9 +961,11 @@ __device__ void setup_indices(const DevCosmo& C, St& M, bool want_max) {
 }
 
 // CopyScalarVariableArray (equations.f90:703-791) from layout O to layout N
+template <int W>
 __device__ void copy_vars(const DevCosmo& C, const St& O, const St& N, const double* __restrict__ y,
                           double* __restrict__ yo) {
-  for (int i = 0; i < N.nvar; ++i) yo[i] = 0;
+  for (int i = wlane<W>(); i < N.nvar; i += W) yo[i] = 0;
+  wsync<W>();  // the copies below are made by every lane
   for (int i = 0; i < 4; ++i) yo[i] = y[i];
   if (!O.nophot && !N.nophot) {
     int lmax = (O.tc || N.tc) ? 1 : min(O.lmaxg, N.lmaxg);
@@ -971,9 +1015,10 @@ struct NuBins {
   double aq[NQ], v[NQ], s[NQ];
 };
 
+template <int W>
 __device__ __forceinline__ void nu_bins(const DevCosmo& C, double a, int i, NuBins& b) {
   const double am = a * C.nu_masses[i];
-  for (int iq = 0; iq < C.nqmax; ++iq) {
+  for (int iq = wlane<W>(); iq < C.nqmax; iq += W) {
     const double aq = am * C.nu_inv_q[iq];
     const double s2 = fma(aq, aq, 1.0);
     const double v = rsqrt(s2);
@@ -981,16 +1026,18 @@ __device__ __forceinline__ void nu_bins(const DevCosmo& C, double a, int i, NuBi
     b.v[iq] = v;
     b.s[iq] = s2 * v;
   }
+  wsync<W>();
 }
 
 // Nu_Integrate_L01/L012 (equations.f90:1178-1270): momentum integrals of one eigenstate
-template <bool L2>
+template <bool L2, int W>
 __device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, const double* __restrict__ y,
                                              const NuBins& b, int i, double& drhonu, double& fnu, double& dpnu,
                                              double& pinu) {
   drhonu = fnu = dpnu = pinu = 0;
-  int ind = M.nu_ix[i];
-  for (int iq = 0; iq < M.nq[i]; ++iq) {
+  const int lane = wlane<W>();
+  int ind = M.nu_ix[i] + lane * (M.lmaxnu_tau[i] + 1);
+  for (int iq = lane; iq < M.nq[i]; iq += W) {
     const double w = C.nu_int_kernel[iq];
     drhonu += w * y[ind] * b.s[iq];
     fnu += w * y[ind + 1];
@@ -998,10 +1045,10 @@ __device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, con
       dpnu += w * y[ind] * b.v[iq];
       pinu += w * y[ind + 2] * b.v[iq];
     }
-    ind += M.lmaxnu_tau[i] + 1;
+    ind += W * (M.lmaxnu_tau[i] + 1);
   }
   ind = M.nu_pert_ix;
-  for (int iq = M.nq[i]; iq < C.nqmax; ++iq) {
+  for (int iq = M.nq[i] + lane; iq < C.nqmax; iq += W) {
     const double w = C.nu_int_kernel[iq];
     const double mq = C.nu_masses[i] * C.nu_inv_q[iq], ps = mq * mq * 0.5;
     const double tmp = w * (y[M.r_ix] + ps * y[ind]);
@@ -1012,22 +1059,32 @@ __device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, con
       pinu += w * (y[M.r_ix + 2] + ps * y[ind + 2]) * b.v[iq];
     }
   }
+  if constexpr (W > 1) {
+    drhonu = wsum<W>(drhonu);
+    fnu = wsum<W>(fnu);
+    if (L2) {
+      dpnu = wsum<W>(dpnu);
+      pinu = wsum<W>(pinu);
+    }
+  }
   if (L2) dpnu = dpnu / 3;
 }
 
 // Nu_pinudot (equations.f90:1272-1313)
+template <int W>
 __device__ double nu_pinudot(const DevCosmo& C, const St& M, const double* __restrict__ y,
                              const double* __restrict__ ydot, const NuBins& b, double adotoa, int i) {
   double pinudot = 0;
-  int ind = M.nu_ix[i] + 2;
-  for (int iq = 0; iq < M.nq[i]; ++iq) {
+  const int lane = wlane<W>();
+  int ind = M.nu_ix[i] + 2 + lane * (M.lmaxnu_tau[i] + 1);
+  for (int iq = lane; iq < M.nq[i]; iq += W) {
     const double aq = b.aq[iq], v = b.v[iq];
     const double vdot = -aq * (aq * adotoa) * (v * v * v);
     pinudot += C.nu_int_kernel[iq] * (ydot[ind] * v + y[ind] * vdot);
-    ind += M.lmaxnu_tau[i] + 1;
+    ind += W * (M.lmaxnu_tau[i] + 1);
   }
   ind = M.nu_pert_ix + 2;
-  for (int iq = M.nq[i]; iq < C.nqmax; ++iq) {
+  for (int iq = M.nq[i] + lane; iq < C.nqmax; iq += W) {
     const double aq = b.aq[iq], v = b.v[iq];
     const double mq = C.nu_masses[i] * C.nu_inv_q[iq], ps = mq * mq * 0.5;
     const double vdot = -aq * (aq * adotoa) * (v * v * v);
@@ -1035,14 +1092,17 @@ __device__ double nu_pinudot(const DevCosmo& C, const St& M, const double* __res
     const double psi2 = y[M.r_ix + 2] + ps * y[ind];
     pinudot += C.nu_int_kernel[iq] * (psi2dot * v + psi2 * vdot);
   }
-  return pinudot;
+  return wsum<W>(pinudot);
 }
 
-// derivs (equations.f90:2273-2773) + sources (2775-2912), one thread per mode
-template <bool TR>
+// derivs (equations.f90:2273-2773) + sources (2775-2912), one mode per thread (W = 1)
+// or per warp (W = 32, sbins: the warp's momentum-bin factors in shared memory)
+template <bool TR, int W>
 __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* __restrict__ dl,
                                         const double* __restrict__ dl2, const double* __restrict__ pf, double tau,
-                                        const double* __restrict__ y, double* __restrict__ dy, double* src) {
+                                        const double* __restrict__ y, double* __restrict__ dy, double* src,
+                                        NuBins* sbins = nullptr) {
+  const int lane = wlane<W>();
   const double k = M.k, ik = M.ik;
   const double itau = 1.0 / tau;
   double a, cs2, opac, dopac = 0;
@@ -1054,7 +1114,8 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   double dgrho = grhob_t * clxb + grhoc_t * clxc;
   double dgq = grhob_t * vb;
   double grhonu_t = 0, gpres_nu = 0, wnu[NUE] = {0, 0, 0};
-  NuBins bins[NUE];
+  NuBins lbins[W == 1 ? NUE : 1];
+  NuBins* const bins = W == 1 ? lbins : sbins;
   for (int i = 0; i < C.nu_eig; ++i) {  // MassiveNuVars (equations.f90:1358-1401)
     const double gm_t = C.grhormass[i] * ia2;
     double rhonu, pnu, clxnu, qnu;
@@ -1064,9 +1125,9 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       clxnu = y[M.nu_ix[i]];
       qnu = y[M.nu_ix[i] + 2];
     } else {
-      nu_bins(C, a, i, bins[i]);
+      nu_bins<W>(C, a, i, bins[i]);
       double dp, pn;
-      nu_integrate<false>(C, M, y, bins[i], i, clxnu, qnu, dp, pn);
+      nu_integrate<false, W>(C, M, y, bins[i], i, clxnu, qnu, dp, pn);
       qnu = qnu * ir;
       clxnu = clxnu * ir;
     }
@@ -1160,11 +1221,12 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       pigdot = dl[2] * qg - dl2[2] * y[g + 3] - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
       dy[g + 2] = pigdot;
       const int lg = M.lmaxg;
-      for (int l = 3; l < lg; ++l) dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
+      for (int l = 3 + lane; l < lg; l += W) dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
       dy[g + lg] = k * y[g + lg - 1] - (lg + 1) * itau * y[g + lg] - opac * y[g + lg];
       dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * y[pol + 3];
       const int lp = M.lmaxgpol;
-      for (int l = 3; l < lp; ++l) dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
+      for (int l = 3 + lane; l < lp; l += W)
+        dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
       dy[pol + lp] = -opac * y[pol + lp] + M.kptf * y[pol + lp - 1] - (lp + 3) * itau * y[pol + lp];
     }
   }
@@ -1180,7 +1242,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       pirdot = dl[2] * qr - dl2[2] * y[r + 3] + 8.0 / 15.0 * k * sigma;
       dy[r + 2] = pirdot;
       const int ln = M.lmaxnr;
-      for (int l = 3; l < ln; ++l) dy[r + l] = dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1];
+      for (int l = 3 + lane; l < ln; l += W) dy[r + l] = dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1];
       dy[r + ln] = k * y[r + ln - 1] - (ln + 1) * itau * y[r + ln];
     }
   }
@@ -1194,7 +1256,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       dy[off + 1] = (3 * w - 2) * adotoa * y[off + 1] - 5.0 / 3 * k * z * w - k / 3 * G11_t;
       dy[off + 2] = (3 * w - 1) * adotoa * y[off + 2] - k * (2.0 / 3 * y[off + 3] - y[off + 1]);
       dy[off + 3] = (3 * w - 2) * adotoa * y[off + 3] + 2 * w * k * sigma - k / 5 * (3 * G30_t - 2 * G11_t);
-    } else {
+    } else if constexpr (W == 1) {
       int ind = M.nu_ix[i];
       const int lt = M.lmaxnu_tau[i];
       for (int iq = 0; iq < M.nq[i]; ++iq) {
@@ -1210,16 +1272,38 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
         }
         ind += lt + 1;
       }
+    } else {
+      // the (momentum bin, l) entries of the eigenstate, flattened over the lanes
+      const int lt = M.lmaxnu_tau[i], lt1 = lt + 1, tot = M.nq[i] * lt1;
+      int iq = lane / lt1, l = lane - iq * lt1;
+      for (int e = lane; e < tot; e += W) {
+        const int ind = M.nu_ix[i] + iq * lt1;
+        const double v = bins[i].v[iq];
+        double d;
+        if (l == 0) d = -k * (4.0 / 3.0 * z + v * y[ind + 1]);
+        else if (l == 1) d = v * (dl[1] * y[ind] - dl2[1] * y[ind + 2]);
+        else if (l == 2 && lt == 2) d = k * (4.0 / 3.0 * z + v * y[ind + 1]) - 3 * itau * y[ind + 2];
+        else if (l == 2) d = v * (dl[2] * y[ind + 1] - dl2[2] * y[ind + 3]) + k * 8.0 / 15.0 * sigma;
+        else if (l < lt) d = v * (dl[l] * y[ind + l - 1] - dl2[l] * y[ind + l + 1]);
+        else d = k * v * y[ind + lt - 1] - (lt + 1) * itau * y[ind + lt];
+        dy[ind + l] = d;
+        l += W;
+        while (l >= lt1) {
+          l -= lt1;
+          ++iq;
+        }
+      }
     }
   }
   if (M.has_nu_rel) {
     const int p0 = M.nu_pert_ix, lp = M.lmaxnu_pert;
     dy[p0] = k * a2 * qr - k * y[p0 + 1];
-    for (int l = 1; l < lp; ++l)
+    for (int l = 1 + lane; l < lp; l += W)
       dy[p0 + l] = -a2 * (dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1]) + (dl[l] * y[p0 + l - 1] - dl2[l] * y[p0 + l + 1]);
     dy[p0 + lp] = k * (y[p0 + lp - 1] - a2 * y[r + lp - 1]) - (lp + 1) * itau * y[p0 + lp];
   }
   if (src) {
+    wsync<W>();  // the source terms read derivatives written by other lanes
     double Ed2 = 0, Ed3 = 0, octgdot = 0, E2s = 0;
     if (M.nophot) {
       pigdot = 0;
@@ -1249,11 +1333,11 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
         pinudot = dy[M.nu_ix[i] + 3];
       } else {
         double qnu, dpnu;
-        nu_integrate<true>(C, M, y, bins[i], i, clxnu, qnu, dpnu, pinu);
+        nu_integrate<true, W>(C, M, y, bins[i], i, clxnu, qnu, dpnu, pinu);
         clxnu = clxnu / rhonu;
         pinu = pinu / rhonu;
         const double rhonudot = nuf::drho(a * C.nu_masses[i], adotoa);
-        pinudot = nu_pinudot(C, M, y, dy, bins[i], adotoa, i);
+        pinudot = nu_pinudot<W>(C, M, y, dy, bins[i], adotoa, i);
         pinudot = pinudot / rhonu - rhonudot / rhonu * pinu;
       }
       const double g_t = gm_t * rhonu, gp_t = gm_t * pnu;
@@ -1315,6 +1399,20 @@ struct Work {
   double dl[NL], dl2[NL], pf[20];
 };
 
+// The same rows for a warp's mode, in the warp's slice of shared memory
+struct WorkS {
+  double* b;  // [8][stride]
+  int stride;
+  double *dl, *dl2, *pf;
+  NuBins* bins;  // [NUE] momentum-bin factors of the current right-hand side
+};
+__device__ __forceinline__ double* row(Work& w, int s) { return w.b[s]; }
+__device__ __forceinline__ double* row(const WorkS& w, int s) { return w.b + (size_t)s * w.stride; }
+__device__ __forceinline__ NuBins* sbins(Work&) { return nullptr; }
+__device__ __forceinline__ NuBins* sbins(const WorkS& w) { return w.bins; }
+__device__ __forceinline__ int row_cap(const Work&) { return NV; }
+__device__ __forceinline__ int row_cap(const WorkS& w) { return w.stride; }
+
 // state of one mode's integration, advanced one trial step per loop iteration
 struct Run {
   double src[13];  // source functions, or the 13 transfer variables without the CMB
@@ -1335,7 +1433,9 @@ __device__ __forceinline__ int next_nu_nq(const DevCosmo& C, int nq) {
   return qq >= 10 ? C.nqmax : nq + 1;
 }
 
-__device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
+template <int W, class WK>
+__device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
+  const int lane = wlane<W>();
   const CambGpuModeSpec ms = C.modes[q_ix];
   M.q = ms.q;
   M.k = ms.q;
@@ -1366,7 +1466,7 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   R.active = true;
   R.status = 0;
   const int lm = max(max(M.lmaxg, M.lmaxgpol), max(M.lmaxnr, M.lmaxnu));
-  if (M.nvar > NV || lm >= NL || M.lmaxgpol >= 20 || C.nu_eig > NUE || C.nqmax > NQ) {
+  if (M.nvar > row_cap(Wk) || lm >= NL || M.lmaxgpol >= 20 || C.nu_eig > NUE || C.nqmax > NQ) {
     R.active = false;
     R.status = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
     return;
@@ -1376,14 +1476,15 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
   R.sk2 = 2;
   R.syt = 7;
   R.ny_valid = false;
-  double* const Y = W.b[R.sy];
-  for (int l = 1; l <= lm; ++l) {
+  double* const Y = row(Wk, R.sy);
+  for (int l = 1 + lane; l <= lm; l += W) {
     const double dn = 1.0 / (2 * l + 1);
-    W.dl[l] = dn * M.k * l;
-    W.dl2[l] = dn * M.k * (l + 1);
-    if (l < 20) W.pf[l] = ((double)((l + 3) * (l - 1)) / (l + 1)) * M.k * dn;
+    Wk.dl[l] = dn * M.k * l;
+    Wk.dl2[l] = dn * M.k * (l + 1);
+    if (l < 20) Wk.pf[l] = ((double)((l + 3) * (l - 1)) / (l + 1)) * M.k * dn;
   }
-  for (int i = 0; i < M.nvar; ++i) Y[i] = 0;
+  for (int i = lane; i < M.nvar; i += W) Y[i] = 0;
+  wsync<W>();  // the initial values below are written by every lane
   // initial (equations.f90:1891-2112), adiabatic
   const double tau = ms.taustart, k = M.k;
   const double x = k * tau, x2 = x * x, x3 = x2 * x;
@@ -1420,6 +1521,7 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, Work& W, Run& R) {
       ind += M.lmaxnu_tau[i] + 1;
     }
   }
+  wsync<W>();
   R.tau = tau;
   R.j = C.transfer_only ? 0 : 1;
   R.h = R.err = 0;
@@ -1525,18 +1627,19 @@ __device__ __forceinline__ void swap_rows(Run& R, double*& Y, double*& YT) {
   YT = p;
 }
 
-__device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
+template <int W, class WK>
+__device__ void apply_switch(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   const double noSwitch = C.tau0 + 1;
   St N = M;
-  double* Y = W.b[R.sy];
-  double* YT = W.b[R.syt];
+  double* Y = row(Wk, R.sy);
+  double* YT = row(Wk, R.syt);
   R.ny_valid = false;
   const int kind = R.sw_kind, e = R.sw_eig;
   if (kind == SW_TC) {
     N.tc = false;
     N.tight_off = noSwitch;
     setup_indices(C, N, false);
-    copy_vars(C, M, N, Y, YT);
+    copy_vars<W>(C, M, N, Y, YT);
     M = N;
     swap_rows(R, Y, YT);
     R.reset = true;
@@ -1559,19 +1662,22 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
     const double a2 = a * a;
     N.approx[e] = true;
     setup_indices(C, N, false);
-    copy_vars(C, M, N, Y, YT);
+    copy_vars<W>(C, M, N, Y, YT);
     double rhonu, pnu, clxnu, qnu, dpnu, pinu;
     nuf::rho_P(a * C.nu_masses[e], rhonu, pnu);
-    NuBins b;
-    nu_bins(C, a, e, b);
-    nu_integrate<true>(C, M, Y, b, e, clxnu, qnu, dpnu, pinu);
+    NuBins lb;
+    NuBins* bp;
+    if constexpr (W == 1) bp = &lb;
+    else bp = sbins(Wk) + e;
+    NuBins& b = *bp;
+    nu_bins<W>(C, a, e, b);
+    nu_integrate<true, W>(C, M, Y, b, e, clxnu, qnu, dpnu, pinu);
     YT[N.nu_ix[e]] = clxnu / rhonu;
     YT[N.nu_ix[e] + 1] = dpnu / rhonu;
     YT[N.nu_ix[e] + 2] = qnu / rhonu;
     YT[N.nu_ix[e] + 3] = pinu / rhonu;
     // Nu_Intvsq (equations.f90:1331-1356) on the old layout
     double G11 = 0, G30 = 0;
-    const double am = a * C.nu_masses[e];
     int ind = M.nu_ix[e];
     for (int iq = 0; iq < M.nq[e]; ++iq) {
       const double v = b.v[iq];
@@ -1600,31 +1706,35 @@ __device__ void apply_switch(const DevCosmo& C, St& M, Work& W, Run& R) {
       N.nophot = true;
     }
     setup_indices(C, N, false);
-    copy_vars(C, M, N, Y, YT);
+    copy_vars<W>(C, M, N, Y, YT);
     M = N;
     swap_rows(R, Y, YT);
   }
   R.fsal = false;
+  wsync<W>();
 }
 
 // one trial step of RungeKuttaDP45 toward R.target; returns <0 on failure
-template <bool TR>
-__device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
+template <bool TR, int W, class WK>
+__device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   using namespace dp;
   const double tol = C.tol1;
   const int n = M.n;
-  double* __restrict__ y = W.b[R.sy];
-  double* __restrict__ yt = W.b[R.syt];
-  double* __restrict__ k1 = W.b[R.sk1];
-  double* __restrict__ k2 = W.b[R.sk2];
-  double* __restrict__ k3 = W.b[3];
-  double* __restrict__ k4 = W.b[4];
-  double* __restrict__ k5 = W.b[5];
-  double* __restrict__ k6 = W.b[6];
+  const int lane = wlane<W>();
+  NuBins* const sb = sbins(Wk);
+  double* __restrict__ y = row(Wk, R.sy);
+  double* __restrict__ yt = row(Wk, R.syt);
+  double* __restrict__ k1 = row(Wk, R.sk1);
+  double* __restrict__ k2 = row(Wk, R.sk2);
+  double* __restrict__ k3 = row(Wk, 3);
+  double* __restrict__ k4 = row(Wk, 4);
+  double* __restrict__ k5 = row(Wk, 5);
+  double* __restrict__ k6 = row(Wk, 6);
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
-      derivs1<TR>(C, M, W.dl, W.dl2, W.pf, R.tau, y, k1, nullptr);
+      derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, R.tau, y, k1, nullptr, sb);
+      wsync<W>();
       R.evals++;
     }
     R.need_f = false;
@@ -1632,8 +1742,8 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   if (R.evals > kMaxEvalsPerMode) return -1;
   if (!R.ny_valid) {
     unsigned long long nb = 0;
-    for (int i = 0; i < n; ++i) nb = max(nb, (unsigned long long)__double_as_longlong(y[i]) & 0x7fffffffffffffffULL);
-    R.ny = __longlong_as_double((long long)nb);
+    for (int i = lane; i < n; i += W) nb = max(nb, (unsigned long long)__double_as_longlong(y[i]) & 0x7fffffffffffffffULL);
+    R.ny = __longlong_as_double((long long)wmax_u64<W>(nb));
     R.ny_valid = true;
   }
   const double ny = R.ny < 1.0 ? R.ny : 1.0;
@@ -1670,40 +1780,52 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   const double c61 = hs * a61, c62 = hs * a62, c63 = hs * a63, c64 = hs * a64, c65 = hs * a65;
   const double cb1 = hs * b1, cb3 = hs * b3, cb4 = hs * b4, cb5 = hs * b5, cb6 = hs * b6;
 #pragma unroll 4
-  for (int i = 0; i < n; ++i) yt[i] = fma(c21, k1[i], y[i]);
-  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs / 5.0, yt, k2, nullptr);
+  for (int i = lane; i < n; i += W) yt[i] = fma(c21, k1[i], y[i]);
+  wsync<W>();
+  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs / 5.0, yt, k2, nullptr, sb);
+  wsync<W>();
 #pragma unroll 4
-  for (int i = 0; i < n; ++i) yt[i] = fma(c32, k2[i], fma(c31, k1[i], y[i]));
-  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs * (3.0 / 10.0), yt, k3, nullptr);
+  for (int i = lane; i < n; i += W) yt[i] = fma(c32, k2[i], fma(c31, k1[i], y[i]));
+  wsync<W>();
+  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs * (3.0 / 10.0), yt, k3, nullptr, sb);
+  wsync<W>();
 #pragma unroll 4
-  for (int i = 0; i < n; ++i) yt[i] = fma(c43, k3[i], fma(c42, k2[i], fma(c41, k1[i], y[i])));
-  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs * (4.0 / 5.0), yt, k4, nullptr);
+  for (int i = lane; i < n; i += W) yt[i] = fma(c43, k3[i], fma(c42, k2[i], fma(c41, k1[i], y[i])));
+  wsync<W>();
+  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs * (4.0 / 5.0), yt, k4, nullptr, sb);
+  wsync<W>();
 #pragma unroll 4
-  for (int i = 0; i < n; ++i) yt[i] = fma(c54, k4[i], fma(c53, k3[i], fma(c52, k2[i], fma(c51, k1[i], y[i]))));
-  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs * (8.0 / 9.0), yt, k5, nullptr);
+  for (int i = lane; i < n; i += W) yt[i] = fma(c54, k4[i], fma(c53, k3[i], fma(c52, k2[i], fma(c51, k1[i], y[i]))));
+  wsync<W>();
+  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs * (8.0 / 9.0), yt, k5, nullptr, sb);
+  wsync<W>();
 #pragma unroll 4
-  for (int i = 0; i < n; ++i)
+  for (int i = lane; i < n; i += W)
     yt[i] = fma(c65, k5[i], fma(c64, k4[i], fma(c63, k3[i], fma(c62, k2[i], fma(c61, k1[i], y[i])))));
-  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k6, nullptr);
+  wsync<W>();
+  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs, yt, k6, nullptr, sb);
+  wsync<W>();
   // the fifth-order solution, the error combination of k1, k3..k6 (k3 is dead afterwards
   // and holds it) and max|yt| for the next step's hmin, in one pass
   unsigned long long nbt = 0;
 #pragma unroll 4
-  for (int i = 0; i < n; ++i) {
+  for (int i = lane; i < n; i += W) {
     const double a1 = k1[i], a3 = k3[i], a4 = k4[i], a5 = k5[i], a6 = k6[i];
     const double v = fma(cb6, a6, fma(cb5, a5, fma(cb4, a4, fma(cb3, a3, fma(cb1, a1, y[i])))));
     yt[i] = v;
     k3[i] = fma(e6, a6, fma(e5, a5, fma(e4, a4, fma(e3, a3, e1 * a1))));
     nbt = max(nbt, (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL);
   }
+  wsync<W>();
   // stage 7 (FSAL) into k2; at an output time it is the output() evaluation too
   const bool want_src = (xt == xend) && !R.target_is_switch;
-  derivs1<TR>(C, M, W.dl, W.dl2, W.pf, x + hs, yt, k2, want_src ? R.src : nullptr);
+  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs, yt, k2, want_src ? R.src : nullptr, sb);
+  wsync<W>();
   R.src_valid = want_src;
   R.evals += 6;
   // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry
   double num = 0, den = 1;
-  for (int i = 0; i < n; ++i) {
+  for (int i = lane; i < n; i += W) {
     const double ee = fma(e7, k2[i], k3[i]);
     const double ae = fabs(ee), ay = fabs(y[i]);
     const double sc = ay > 1.0 ? ay : 1.0;
@@ -1712,7 +1834,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
       den = sc;
     }
   }
-  R.err = (num / den) * R.h;
+  R.err = wmax<W>(num / den) * R.h;
   if (R.err <= tol) {
     R.tau = xt;
     // accept: the trial state and k7 become y and k1 by swapping rows
@@ -1722,7 +1844,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
     t = R.sk1;
     R.sk1 = R.sk2;
     R.sk2 = t;
-    R.ny = __longlong_as_double((long long)nbt);
+    R.ny = __longlong_as_double((long long)wmax_u64<W>(nbt));
     R.fails = 0;
     if (xt == xend) R.fsal = true;
   } else {
@@ -1732,66 +1854,75 @@ __device__ int trial_step(const DevCosmo& C, St& M, Work& W, Run& R) {
   return 0;
 }
 
-template <int MINB, bool TR>
-__global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* __restrict__ cosmos,
-                                                               const WorkItem* __restrict__ items, int nitems,
-                                                               int* __restrict__ counter) {
+// The work loop: each thread (W = 1) or warp (W = 32) takes a mode from the queue and
+// advances it one trial step per iteration.  The first item is the thread's (warp's)
+// global index, so each block starts on consecutive queue entries independent of atomic
+// ordering; later items come from the shared counter (past the statically assigned ones).
+template <bool TR, int W, class WK>
+__device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, const WorkItem* __restrict__ items,
+                                          int nitems, int* __restrict__ counter, WK& Wk, int first, int nstatic) {
   St M;
-  Work W;
   Run R;
   int cosmo = -1, q_ix = 0;
+  const bool leader = wlane<W>() == 0;
   R.active = false;
-  // The first item of every thread is its global index, so each block starts on 128
-  // consecutive queue entries independent of atomic ordering; later items come from the
-  // shared counter (past the statically assigned ones).
-  const int nthreads = gridDim.x * blockDim.x;
-  int first = blockIdx.x * blockDim.x + threadIdx.x;
   for (;;) {
     if (!R.active) {
-      const int w = first >= 0 ? first : nthreads + atomicAdd(counter, 1);
+      int w = first;
+      if (first < 0) {
+        int t = 0;
+        if (leader) t = atomicAdd(counter, 1);
+        if constexpr (W > 1) t = __shfl_sync(0xffffffffu, t, 0);
+        w = nstatic + t;
+      }
       first = -1;
       if (w >= nitems) break;
       const WorkItem it = items[w];
       cosmo = it.cosmo;
       q_ix = it.mode;
-      mode_init(cosmos[cosmo], q_ix, M, W, R);
+      mode_init<W>(cosmos[cosmo], q_ix, M, Wk, R);
       if (!R.active) {
-        atomicExch(cosmos[cosmo].status, R.status);
+        if (leader) atomicExch(cosmos[cosmo].status, R.status);
         continue;
       }
       if (!next_target<TR>(cosmos[cosmo], M, R)) {
         R.active = false;
-        atomicAdd(cosmos[cosmo].evals, (unsigned long long)R.evals);
+        if (leader) atomicAdd(cosmos[cosmo].evals, (unsigned long long)R.evals);
         continue;
       }
     }
     const DevCosmo& C = cosmos[cosmo];
     int rc = 0;
-    if (R.target != R.tau) rc = trial_step<TR>(C, M, W, R);
+    if (R.target != R.tau) rc = trial_step<TR, W>(C, M, Wk, R);
     if (rc) {
-      atomicExch(C.status, (int)CAMBGPU_ERROR_EVOLUTION);
-      atomicAdd(C.evals, (unsigned long long)R.evals);
+      if (leader) {
+        atomicExch(C.status, (int)CAMBGPU_ERROR_EVOLUTION);
+        atomicAdd(C.evals, (unsigned long long)R.evals);
+      }
       R.active = false;
       continue;
     }
     if (R.tau == R.target) {
       bool more = true;
       if (R.target_is_switch) {
-        apply_switch(C, M, W, R);
+        apply_switch<W>(C, M, Wk, R);
       } else {
         if (!R.src_valid) {
-          derivs1<TR>(C, M, W.dl, W.dl2, W.pf, R.tau, W.b[R.sy], W.b[R.syt], R.src);
+          derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, R.tau, row(Wk, R.sy), row(Wk, R.syt), R.src, sbins(Wk));
+          wsync<W>();
         }
         R.evals++;  // the output() evaluation of the reference
         const int nk = C.nk;
-        if constexpr (TR) {
-          // TransferData is single precision: store, then divide the stored value by k^2
-          float* o = C.transfer_out + ((size_t)R.j * nk + q_ix) * 13;
-          o[0] = (float)R.src[0];
-          for (int v = 1; v < 13; ++v) o[v] = (float)((double)(float)R.src[v] / M.k2);
-        } else {
-          const int nsrc = C.nsrc;
-          for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = R.src[s];
+        if (leader) {
+          if constexpr (TR) {
+            // TransferData is single precision: store, then divide the stored value by k^2
+            float* o = C.transfer_out + ((size_t)R.j * nk + q_ix) * 13;
+            o[0] = (float)R.src[0];
+            for (int v = 1; v < 13; ++v) o[v] = (float)((double)(float)R.src[v] / M.k2);
+          } else {
+            const int nsrc = C.nsrc;
+            for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = R.src[s];
+          }
         }
         R.j++;
       }
@@ -1799,16 +1930,46 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
       for (;;) {
         more = next_target<TR>(C, M, R);
         if (!more || !(R.target_is_switch && R.target == R.tau) || ++guard > 16) break;
-        apply_switch(C, M, W, R);  // switches due at the current time
+        apply_switch<W>(C, M, Wk, R);  // switches due at the current time
       }
       if (guard > 16) R.status = CAMBGPU_ERROR_EVOLUTION, more = false;
       if (!more) {
-        if (R.status) atomicExch(C.status, R.status);
-        atomicAdd(C.evals, (unsigned long long)R.evals);
+        if (leader) {
+          if (R.status) atomicExch(C.status, R.status);
+          atomicAdd(C.evals, (unsigned long long)R.evals);
+        }
         R.active = false;
       }
     }
   }
+}
+
+template <int MINB, bool TR>
+__global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* __restrict__ cosmos,
+                                                               const WorkItem* __restrict__ items, int nitems,
+                                                               int* __restrict__ counter) {
+  Work Wk;
+  run_modes<TR, 1>(cosmos, items, nitems, counter, Wk, blockIdx.x * blockDim.x + threadIdx.x,
+                   gridDim.x * blockDim.x);
+}
+
+// Warp per mode, one warp per block: the block's dynamic shared memory holds the eight
+// state rows of `stride` entries, the recurrence factors and the momentum-bin factors.
+size_t warp_smem_bytes(int stride) { return ((size_t)8 * stride + 2 * NL + 20) * sizeof(double) + NUE * sizeof(NuBins); }
+
+template <bool TR>
+__global__ void __launch_bounds__(32) ode_warp_kernel(const DevCosmo* __restrict__ cosmos,
+                                                      const WorkItem* __restrict__ items, int nitems,
+                                                      int* __restrict__ counter, int stride) {
+  extern __shared__ double wsm[];
+  WorkS Wk;
+  Wk.b = wsm;
+  Wk.stride = stride;
+  Wk.dl = wsm + (size_t)8 * stride;
+  Wk.dl2 = Wk.dl + NL;
+  Wk.pf = Wk.dl2 + NL;
+  Wk.bins = reinterpret_cast<NuBins*>(Wk.pf + 20);
+  run_modes<TR, 32>(cosmos, items, nitems, counter, Wk, blockIdx.x, gridDim.x);
 }
 
 }  // namespace tpm
@@ -1836,13 +1997,15 @@ cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, c
 
 // host-side launch helpers (template kernels stay in this translation unit)
 // team 1 = thread per mode with 3 resident blocks per SM, 2 = 4 blocks, 3 = 5 blocks
-int ode_blocks_per_sm(int team, int threads) {
+int ode_blocks_per_sm(int team, int threads, int warp_stride) {
   int per_sm = 0;
   if (team == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<3, false>, threads, 0);
   else if (team == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<4, false>, threads, 0);
   else if (team == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<5, false>, threads, 0);
   else if (team == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<6, false>, threads, 0);
   else if (team == 5) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<8, false>, threads, 0);
+  else if (team == 6) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_warp_kernel<false>, 32,
+                                                                     tpm::warp_smem_bytes(warp_stride));
   else if (team == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<32>, threads, 0);
   else if (team == 16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<16>, threads, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ode_persistent_kernel<8>, threads, 0);
@@ -1850,8 +2013,14 @@ int ode_blocks_per_sm(int team, int threads) {
 }
 
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
-                              const WorkItem* items, int nitems, int* counter, bool transfer) {
-  if (transfer) {  // matter transfer functions: thread per mode only
+                              const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride) {
+  if (team == 6) {  // warp per mode (any layout), one warp per block
+    const size_t smem = tpm::warp_smem_bytes(warp_stride);
+    if (transfer) tpm::ode_warp_kernel<true><<<blocks, 32, smem, s>>>(cosmos, items, nitems, counter, warp_stride);
+    else tpm::ode_warp_kernel<false><<<blocks, 32, smem, s>>>(cosmos, items, nitems, counter, warp_stride);
+    return cudaGetLastError();
+  }
+  if (transfer) {  // matter transfer functions: thread per mode
     if (team == 1) tpm::ode_thread_kernel<3, true><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
     else if (team == 3) tpm::ode_thread_kernel<5, true><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
     else tpm::ode_thread_kernel<4, true><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);

@@ -261,14 +261,15 @@ void cambgpu_batch_release(void);
  * Limber branch, C_l k-integral, interpolation and lensing stay FP64. */
 int cambgpu_set_precision(int mode);
 int cambgpu_get_precision(void);
-/* ODE kernel variant: 32/16/8 = lanes per k-mode (warp teams); 1/2/3/4/5 = one thread
- * per k-mode compiled for 3/4/5/6/8 resident blocks of 128 per SM; 0 = the autotuned
- * choice. */
+/* ODE kernel variant: 32/16/8 = lanes per k-mode with the state in registers (massless
+ * neutrinos, CMB sources); 6 = one warp per k-mode with the state rows in shared memory
+ * (any layout: massive neutrinos, transfer functions); 1/2/3/4/5 = one thread per k-mode
+ * compiled for 3/4/5/6/8 resident blocks of 128 per SM; 0 = the autotuned choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
 /* In-library autotuner: times every ODE variant and work-queue order on n cosmologies
  * and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
  * 1 = increasing q, 2 = bands of q with the cosmologies of each band ordered by neutrino
- * mass.  best = [team, order, class]; times (optional, >= 8 entries) receives ms per
+ * mass.  best = [team, order, class]; times (optional, >= 9 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch call, in ms:

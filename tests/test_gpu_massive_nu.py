@@ -36,9 +36,20 @@ def planck():
     return T, src
 
 
-def test_sources_parity_006ev(planck):
+def with_team(team, f):
+    lib = _lib.load()
+    _lib.check(lib.cambgpu_set_ode_team(team))
+    try:
+        return f()
+    finally:
+        lib.cambgpu_set_ode_team(0)
+
+
+@pytest.mark.parametrize("team", [0, 6, 2])
+def test_sources_parity_006ev(planck, team):
+    """Autotuned choice, warp per mode (shared-memory rows), thread per mode."""
     T, src = planck
-    g = T.evolve_sources_gpu()
+    g = with_team(team, T.evolve_sources_gpu)
     assert rel_peak(g, src, axis=0) < 1e-6
 
 
@@ -51,19 +62,20 @@ def test_end_to_end_cls_006ev(planck):
     check_cls(cls[T.ls], icl)
 
 
+@pytest.mark.parametrize("team", [0, 6])
 @pytest.mark.parametrize("mnu", [0.2, 0.6])
-def test_sources_parity_heavier(mnu):
+def test_sources_parity_heavier(mnu, team):
     """Heavier eigenstates: more momentum bins, longer hierarchies, earlier switches."""
     T = _lib.Tables(fiducial(600, mnu=mnu, num_massive_neutrinos=1))
     src = orc.evolve_sources(T)
-    g = T.evolve_sources_gpu()
+    g = with_team(team, T.evolve_sources_gpu)
     assert rel_peak(g, src, axis=0) < 1e-6
 
 
 def test_batch_mixed_massive_and_massless():
     """A batch of draws with mnu uniform in [0, 0.2] eV plus one massless cosmology: the
-    warp-per-mode kernel is massless-only, so the batch runs on the thread-per-mode
-    kernel whichever team was tuned."""
+    register-resident warp kernel (32 lanes) is massless-only, so a request for it runs
+    the batch on the shared-memory warp-per-mode kernel."""
     ps = draws(3, seed=11, lmax=600, mnu_max=0.2) + [fiducial(600)]
     arr = (_lib.CambGpuParams * len(ps))(*ps)
     cls = np.zeros((len(ps), 601, 4))

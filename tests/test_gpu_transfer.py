@@ -30,12 +30,19 @@ def gpu_transfer(ps, nq_max=2048):
     return tr, nq, s8, sv
 
 
-def test_transfer_functions_match_oracle_and_known_answers():
+@pytest.mark.parametrize("team", [0, 6, 2])
+def test_transfer_functions_match_oracle_and_known_answers(team):
+    """Autotuned kernel choice, warp per mode (shared-memory rows), thread per mode."""
     p, g = sigma8_known_answer()
     T = _lib.Tables(p)
     ref = orc.evolve_transfer(T)
     rs8, rsv = orc.sigma8(T, ref)
-    tr, nq, s8, sv = gpu_transfer([p])
+    lib = _lib.load()
+    _lib.check(lib.cambgpu_set_ode_team(team))
+    try:
+        tr, nq, s8, sv = gpu_transfer([p])
+    finally:
+        lib.cambgpu_set_ode_team(0)
     assert nq[0] == T.view.nk
     got = tr[0, :, : nq[0]]
     peak = np.max(np.abs(ref), axis=1, keepdims=True)
