@@ -109,6 +109,7 @@ SIGNATURES = {
     "cambgpu_batch_spectra_from_transfer": (C.c_int, [_c_double_p, _c_double_p, _c_double_p, _c_double_p, C.c_int,
                                                         _c_double_p, _c_double_p, _c_double_p, _c_int_p]),
     "cambgpu_set_ode_team": (C.c_int, [C.c_int]),
+    "cambgpu_set_ode_launch": (C.c_int, [C.c_int, C.c_int]),
     "cambgpu_set_precision": (C.c_int, [C.c_int]),
     "cambgpu_get_precision": (C.c_int, []),
     "cambgpu_autotune_ode": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, _c_int_p, _c_double_p]),

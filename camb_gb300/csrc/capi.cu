@@ -46,12 +46,13 @@ double wall_ms() {
 int g_team = 0;
 int g_precision = 0;  // 0: FP64 throughout; 1: mixed-precision line-of-sight projection
 // autotuned ODE configuration per batch-size class: [0] small (< 24 modes/SM), [1] large
-struct OdeCfg { int team; int order; };
+struct OdeCfg { int team; int order; int cap; };
 // untuned defaults: warp per mode (shared-memory rows) for few modes, where latency
 // decides; thread per mode for large batches, where FP64 throughput does
-OdeCfg g_tuned[2] = {{6, 0}, {1, 0}};
+OdeCfg g_tuned[2] = {{6, 0, 0}, {1, 2, 2}};
 constexpr int kWarpStrideMax = 448;  // the shared-memory warp kernel's largest state row
 int g_order = -1;  // forced queue order (-1: use the tuned one)
+int g_blocks_cap = 0;  // resident ODE blocks per SM (0: as many as fit)
 long long g_last_evals = 0;
 long long g_h2d = 0, g_d2h = 0;
 
@@ -742,6 +743,9 @@ int run_ode(Batch& B) {
   const long threads_needed = (long)B.nitems * lanes;
   const int tpb = (team == 6 || threads_needed < 2L * 128 * g_rt.nsm) ? 32 : 128;
   int per_sm = std::max(1, ode_blocks_per_sm(team, tpb, B.warp_stride));
+  // a cap below the occupancy limit leaves modes in the queue for threads that finish early
+  const int cap = g_blocks_cap > 0 ? g_blocks_cap : g_team ? 0 : g_tuned[size_class(B)].cap;
+  if (cap > 0) per_sm = std::min(per_sm, cap);
   int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
   const WorkItem* queue = order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
@@ -1238,6 +1242,14 @@ int cambgpu_set_ode_team(int lanes) {
   return 0;
 }
 
+int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm) {
+  if (queue_order < -1 || queue_order > 2 || blocks_per_sm < 0)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "queue order must be -1..2 and blocks per SM >= 0");
+  g_order = queue_order;
+  g_blocks_cap = blocks_per_sm;
+  return 0;
+}
+
 int cambgpu_last_timings(double* out6) {
   for (int i = 0; i < 6; ++i) out6[i] = g_timings[i];
   return 0;
@@ -1246,16 +1258,18 @@ int cambgpu_last_timings(double* out6) {
 long long cambgpu_last_ode_evals(void) { return g_last_evals; }
 
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times) {
-  // candidates: (team code, queue order); team 32 = warp per mode with registers
-  // (massless layout), 6 = warp per mode with shared-memory rows, 1/2/3 = thread per mode
-  // with 3/4/5 resident blocks per SM
-  static const int cand[][2] = {{32, 0}, {1, 0}, {2, 0}, {3, 0}, {2, 1}, {1, 2}, {2, 2}, {3, 2}, {6, 0}};
+  // candidates: (team code, queue order, resident-block cap); team 32 = warp per mode with
+  // registers (massless layout), 6 = warp per mode with shared-memory rows, 1/2/3 = thread
+  // per mode compiled for 3/4/5 resident blocks per SM (cap 0: that many; 2: two, so that
+  // threads finishing early take the queue's remaining modes)
+  static const int cand[][3] = {{32, 0, 0}, {1, 0, 0}, {1, 2, 0}, {2, 2, 0}, {3, 2, 0},
+                                {1, 2, 2}, {2, 2, 2}, {1, 1, 2}, {6, 0, 0}};
   const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
   int rc = cambgpu_batch_prepare(p, n);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(g_mu);
   Batch& B = g_res->B;
-  int saved_team = g_team, saved_order = g_order;
+  int saved_team = g_team, saved_order = g_order, saved_cap = g_blocks_cap;
   double best_ms = 1e30;
   int bi = 0;
   for (int c = 0; c < nc; ++c) {
@@ -1266,6 +1280,7 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
     if (cand[c][0] == 6 && (B.warp_stride > kWarpStrideMax || size_class(B) == 1)) continue;
     g_team = cand[c][0];
     g_order = cand[c][1];
+    g_blocks_cap = cand[c][2];
     rc = run_all(B, true, false, false);  // warm-up
     if (rc) break;
     rc = run_all(B, true, false, false);
@@ -1275,9 +1290,15 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   }
   g_team = saved_team;
   g_order = saved_order;
+  g_blocks_cap = saved_cap;
   if (rc) return rc;
-  g_tuned[size_class(B)] = {cand[bi][0], cand[bi][1]};
-  if (best) { best[0] = cand[bi][0]; best[1] = cand[bi][1]; best[2] = size_class(B); }
+  g_tuned[size_class(B)] = {cand[bi][0], cand[bi][1], cand[bi][2]};
+  if (best) {
+    best[0] = cand[bi][0];
+    best[1] = cand[bi][1];
+    best[2] = size_class(B);
+    best[3] = cand[bi][2];
+  }
   return 0;
 }
 

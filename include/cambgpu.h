@@ -266,10 +266,14 @@ int cambgpu_get_precision(void);
  * (any layout: massive neutrinos, transfer functions); 1/2/3/4/5 = one thread per k-mode
  * compiled for 3/4/5/6/8 resident blocks of 128 per SM; 0 = the autotuned choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
-/* In-library autotuner: times every ODE variant and work-queue order on n cosmologies
- * and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
+/* ODE launch shape: queue order (-1 = the autotuned one, else as for the autotuner) and a
+ * cap on resident blocks per SM (0 = as many as fit; a lower cap leaves modes in the work
+ * queue for threads that finish early). */
+int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm);
+/* In-library autotuner: times ODE variants, work-queue orders and resident-block caps on
+ * n cosmologies and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
  * 1 = increasing q, 2 = bands of q with the cosmologies of each band ordered by neutrino
- * mass.  best = [team, order, class]; times (optional, >= 9 entries) receives ms per
+ * mass.  best = [team, order, class, cap]; times (optional, >= 9 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch call, in ms:
