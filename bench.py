@@ -46,7 +46,127 @@ def parse():
     ap.add_argument("--mnu-max", type=float, default=0.2)
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1],
                     help="timed form: 0 FP64 throughout, 1 mixed-precision line-of-sight projection")
+    ap.add_argument("--lensed-batch", type=int, default=0,
+                    help="instead of the headline run: N lensed draws (lmax 2500 + 200 margin) through the FP64 "
+                         "and the mixed-precision projection, device time per form and the mixed form's C_l "
+                         "error against FP64 per l band")
+    ap.add_argument("--kernel-case", choices=["warp1", "thread8", "thread256"],
+                    help="profiling driver: prepare one fixed case, run the device pipeline 4 times, print the "
+                         "last ODE time and exit (warp1: one massless lmax-1000 cosmology, warp per mode; "
+                         "thread8 / thread256: 8 / 256 draws of the workload, thread per mode)")
     return ap.parse_args()
+
+
+# DRAM bytes (read + write) of one ODE launch of the headline workload, from the ncu
+# capture summarised in profiles/ode_thread_kernel_dram_batch256_lmax2500.md
+ODE_TRAFFIC_BYTES = 1.10e12 + 0.493e12
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+def gradient_rate(n=64, lmax=2500, seed=3000, mnu_max=0.2):
+    """Gradients dC_l/d(ombh2, omch2, H0, tau, As, ns) of n seeded draws through
+    camb_gb300.gradients (central differences: 9 cosmologies per gradient in one batch),
+    one warm-up call and one timed call, wall clock including the host tables."""
+    from camb_gb300 import gradients, model
+    rng = np.random.default_rng(seed)
+    ps = []
+    for _ in range(n):
+        f = lambda v: v * (1 + 0.05 * (2 * rng.random() - 1))  # noqa: E731
+        ps.append(model.set_params(lmax=lmax, DoLensing=False, H0=f(67.5), ombh2=f(0.022), omch2=f(0.122),
+                                   tau=f(0.06), As=f(2.1e-9), ns=f(0.965), mnu=mnu_max * rng.random(),
+                                   nnu=3.046))
+    gradients.cl_gradients(ps[:4])
+    t0 = time.perf_counter()
+    cls, g = gradients.cl_gradients(ps)
+    t = time.perf_counter() - t0
+    return {"value": n / t, "unit": "gradients/s (dC_l/d 6 parameters, l <= %d, unlensed)" % lmax, "batch": n,
+            "seconds": t, "method": "central differences through the batched pipeline: ombh2, omch2, H0, tau "
+                                    "re-evolved (+-1e-4 relative, 9 cosmologies per gradient in one launch); "
+                                    "As, ns by reweighting the resident transfer functions"}
+
+
+def lensed_batch(n, lmax=2500, seed=5000, mnu_max=0.2):
+    """n lensed draws resident on the device: the pipeline once in the FP64 form and once
+    with the mixed-precision projection, lensed TT/EE/BB/TE of both, the mixed form's
+    error against FP64 per l band."""
+    from camb_gb300 import _lib
+    lib = _lib.load()
+    ps = workload(n, lmax, seed=seed, mnu_max=mnu_max)
+    for p in ps:
+        p.do_lensing = 1
+        p.max_l = lmax + 200
+        p.max_eta_k = 2.5 * p.max_l
+    arr = (_lib.CambGpuParams * n)(*ps)
+    t0 = time.perf_counter()
+    _lib.check(lib.cambgpu_batch_prepare(arr, n))
+    prep = time.perf_counter() - t0
+    out, ms_form = {}, {}
+    for mode in (0, 1):
+        _lib.check(lib.cambgpu_set_precision(mode))
+        ms = np.zeros(3)
+        _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
+        ms_form[mode] = ms.copy()
+        unl = np.zeros((n, lmax + 201, 4))
+        len_ = np.zeros((n, lmax + 201, 4))
+        lml = np.zeros(n, dtype=np.int32)
+        _lib.check(lib.cambgpu_batch_spectra_from_transfer(None, None, None, None, lmax + 200, _lib.dptr(unl),
+                                                           _lib.dptr(len_), None, _lib.iptr(lml)))
+        out[mode] = len_
+    lib.cambgpu_batch_release()
+    _lib.check(lib.cambgpu_set_precision(1))
+    ref, got = out[0], out[1]
+    bands = [(2, 100), (100, 500), (500, 1000), (1000, 1500), (1500, 2000), (2000, lmax)]
+    err = {}
+    for lo, hi in bands:
+        sl = slice(lo, hi + 1)
+        tt = np.max(np.abs(got[:, sl, 0] / ref[:, sl, 0] - 1))
+        ee = np.max(np.abs(got[:, sl, 1] / ref[:, sl, 1] - 1))
+        bb = np.max(np.abs(got[:, sl, 2] / ref[:, sl, 2] - 1))
+        te = np.max(np.abs(got[:, sl, 3] - ref[:, sl, 3]) / np.sqrt(ref[:, sl, 0] * ref[:, sl, 1]))
+        err[f"{lo}-{hi}"] = {"TT": tt, "EE": ee, "BB": bb, "TE_over_sqrt_TTEE": te}
+    stage = {k: {"ode": v[0], "spline_los": v[1], "cls_interp_lens": v[2]} for k, v in
+             (("fp64", ms_form[0]), ("mixed", ms_form[1]))}
+    return {"config": {"workload": f"{n} seeded draws (fiducial LCDM +-5%, mnu 0-{mnu_max:g} eV), lensed "
+                                   f"TT/EE/BB/TE to lmax={lmax} (+200 margin)", "batch": n},
+            "prepare_s": prep, "stage_ms": stage,
+            "cosmologies_per_s_mixed": n / (sum(ms_form[1]) * 1e-3),
+            "cosmologies_per_s_fp64": n / (sum(ms_form[0]) * 1e-3),
+            "mixed_vs_fp64_lensed_error_per_l_band": err}
+
+
+def kernel_case(name):
+    """A fixed case for ncu captures: the batch is staged once and the whole device
+    pipeline (ODE, spline, mixed LOS, C_l) runs four times, so `-s 3 -c 1` with a kernel
+    filter captures the fourth launch of that kernel."""
+    from camb_gb300 import _lib
+    lib = _lib.load()
+    if name == "warp1":
+        p = _lib.default_params()
+        p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
+        p.nnu, p.mnu, p.num_massive_neutrinos = 3.046, 0.0, 1
+        p.max_l, p.max_eta_k = 1000, 2500
+        ps, team, order, cap = [p], 6, -1, 0
+    elif name == "thread8":
+        ps, team, order, cap = workload(8, 2500, seed=7), 2, -1, 0
+    else:
+        ps, team, order, cap = workload(256, 2500, seed=1000), 1, 2, 2
+    arr = (_lib.CambGpuParams * len(ps))(*ps)
+    _lib.check(lib.cambgpu_set_ode_team(team))
+    _lib.check(lib.cambgpu_set_ode_launch(order, cap))
+    _lib.check(lib.cambgpu_set_precision(1))
+    _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
+    ms = np.zeros(3)
+    for _ in range(4):
+        _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
+    print(json.dumps({"kernel_case": name, "ode_ms": ms[0], "spline_los_ms": ms[1], "cls_ms": ms[2]}))
+    lib.cambgpu_batch_release()
 
 
 def workload(n, lmax, seed, mnu_max=0.2):
@@ -282,6 +402,12 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
+    if args.kernel_case:
+        kernel_case(args.kernel_case)
+        return
+    if args.lensed_batch:
+        print(json.dumps(lensed_batch(args.lensed_batch, args.lmax, mnu_max=args.mnu_max)))
+        return
     rank, world = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
@@ -392,9 +518,16 @@ def main():
                                      "fetch": host_ms[3]}},
             "gpu_launches": int(launches),
             "roofline": {"bound": "fp64", "kernel": "ode_thread_kernel", "achieved": achieved, "peak": tf.value,
-                         "unit": "TFLOP/s", "frac": achieved / tf.value, "traffic": None,
+                         "unit": "TFLOP/s", "frac": achieved / tf.value, "traffic": ODE_TRAFFIC_BYTES,
                          "peak_source": "DFMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64)",
-                         "flops_per_eval": flops_per_eval, "evals_per_step": evals_step},
+                         "flops_per_eval": flops_per_eval, "evals_per_step": evals_step,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw "
+                                           "ODE launch (team 1, queue order 2, 2 blocks/SM), "
+                                           "profiles/ode_thread_kernel_dram_batch256_lmax2500.md",
+                         "dram_gbs": ODE_TRAFFIC_BYTES / (ode_ms * 1e-3) / 1e9,
+                         "dram_frac_of_measured_copy": ODE_TRAFFIC_BYTES / (ode_ms * 1e-3) / 1e9 / hbm_peak(),
+                         "reading": "stage rows of the resident modes (~250 MB) exceed L2 and stream through DRAM; "
+                                    "the kernel is bound by the latency of those local-memory streams"},
             "clocks": clk, "wall_s_timed": wall}
     if rank == 0:
         nth = os.cpu_count() or 1
@@ -404,6 +537,7 @@ def main():
         t = cpu_reference(cps, nth, keep=ref)
         line["accuracy"] = accuracy_vs_fp64(cps, ref, args.lmax)  # timed form vs the FP64 CPU restatement
         line["single_cosmology_configs"] = single_configs(nth)
+        line["gradients"] = gradient_rate()
         line["cpu_baseline"] = {"value": len(cps) / t, "unit": "cosmologies/s", "cores": nth, "kind": "port",
                                 "sample": f"{len(cps)} draws of the same workload, host tables + ODE + LOS + C_l"}
         print(json.dumps(line))
