@@ -1030,8 +1030,8 @@ __device__ __forceinline__ void nu_bins(const DevCosmo& C, double a, int i, NuBi
 }
 
 // Nu_Integrate_L01/L012 (equations.f90:1178-1270): momentum integrals of one eigenstate
-template <bool L2, int W>
-__device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, const double* __restrict__ y,
+template <bool L2, int W, class YV>
+__device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, const YV y,
                                              const NuBins& b, int i, double& drhonu, double& fnu, double& dpnu,
                                              double& pinu) {
   drhonu = fnu = dpnu = pinu = 0;
@@ -1071,8 +1071,8 @@ __device__ __forceinline__ void nu_integrate(const DevCosmo& C, const St& M, con
 }
 
 // Nu_pinudot (equations.f90:1272-1313)
-template <int W>
-__device__ double nu_pinudot(const DevCosmo& C, const St& M, const double* __restrict__ y,
+template <int W, class YV>
+__device__ double nu_pinudot(const DevCosmo& C, const St& M, const YV y,
                              const double* __restrict__ ydot, const NuBins& b, double adotoa, int i) {
   double pinudot = 0;
   const int lane = wlane<W>();
@@ -1097,10 +1097,10 @@ __device__ double nu_pinudot(const DevCosmo& C, const St& M, const double* __res
 
 // derivs (equations.f90:2273-2773) + sources (2775-2912), one mode per thread (W = 1)
 // or per warp (W = 32, sbins: the warp's momentum-bin factors in shared memory)
-template <bool TR, int W>
+template <bool TR, int W, class YV>
 __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* __restrict__ dl,
                                         const double* __restrict__ dl2, const double* __restrict__ pf, double tau,
-                                        const double* __restrict__ y, double* __restrict__ dy, double* src,
+                                        const YV y, double* __restrict__ dy, double* src,
                                         NuBins* sbins = nullptr) {
   const int lane = wlane<W>();
   const double k = M.k, ik = M.ik;
@@ -1218,16 +1218,41 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
     if (!M.tc) {
       E2 = y[pol + 2];
       polter = pig * 0.1 + 9.0 / 15 * E2;
-      pigdot = dl[2] * qg - dl2[2] * y[g + 3] - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
+      const double g3v = y[g + 3];
+      pigdot = dl[2] * qg - dl2[2] * g3v - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
       dy[g + 2] = pigdot;
       const int lg = M.lmaxg;
-      for (int l = 3 + lane; l < lg; l += W) dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
-      dy[g + lg] = k * y[g + lg - 1] - (lg + 1) * itau * y[g + lg] - opac * y[g + lg];
-      dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * y[pol + 3];
       const int lp = M.lmaxgpol;
-      for (int l = 3 + lane; l < lp; l += W)
-        dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
-      dy[pol + lp] = -opac * y[pol + lp] + M.kptf * y[pol + lp - 1] - (lp + 3) * itau * y[pol + lp];
+      if constexpr (W == 1) {
+        // one read of each entry: the neighbours travel in registers
+        double ym = pig, y0 = g3v;
+        for (int l = 3; l < lg; ++l) {
+          const double yp = y[g + l + 1];
+          dy[g + l] = (dl[l] * ym - dl2[l] * yp) - opac * y0;
+          ym = y0;
+          y0 = yp;
+        }
+        dy[g + lg] = k * ym - (lg + 1) * itau * y0 - opac * y0;
+        const double p3v = y[pol + 3];
+        dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * p3v;
+        ym = E2;
+        y0 = p3v;
+        for (int l = 3; l < lp; ++l) {
+          const double yp = y[pol + l + 1];
+          dy[pol + l] = -opac * y0 + (dl[l] * ym - pf[l] * yp);
+          ym = y0;
+          y0 = yp;
+        }
+        dy[pol + lp] = -opac * y0 + M.kptf * ym - (lp + 3) * itau * y0;
+      } else {
+        for (int l = 3 + lane; l < lg; l += W)
+          dy[g + l] = (dl[l] * y[g + l - 1] - dl2[l] * y[g + l + 1]) - opac * y[g + l];
+        dy[g + lg] = k * y[g + lg - 1] - (lg + 1) * itau * y[g + lg] - opac * y[g + lg];
+        dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * y[pol + 3];
+        for (int l = 3 + lane; l < lp; l += W)
+          dy[pol + l] = -opac * y[pol + l] + (dl[l] * y[pol + l - 1] - pf[l] * y[pol + l + 1]);
+        dy[pol + lp] = -opac * y[pol + lp] + M.kptf * y[pol + lp - 1] - (lp + 3) * itau * y[pol + lp];
+      }
     }
   }
   double clxrdot = 0, pirdot = 0;
@@ -1239,11 +1264,23 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       pirdot = -3 * pir * itau - clxrdot;
       dy[r + 2] = pirdot;
     } else {
-      pirdot = dl[2] * qr - dl2[2] * y[r + 3] + 8.0 / 15.0 * k * sigma;
+      const double n3v = y[r + 3];
+      pirdot = dl[2] * qr - dl2[2] * n3v + 8.0 / 15.0 * k * sigma;
       dy[r + 2] = pirdot;
       const int ln = M.lmaxnr;
-      for (int l = 3 + lane; l < ln; l += W) dy[r + l] = dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1];
-      dy[r + ln] = k * y[r + ln - 1] - (ln + 1) * itau * y[r + ln];
+      if constexpr (W == 1) {
+        double ym = pir, y0 = n3v;
+        for (int l = 3; l < ln; ++l) {
+          const double yp = y[r + l + 1];
+          dy[r + l] = dl[l] * ym - dl2[l] * yp;
+          ym = y0;
+          y0 = yp;
+        }
+        dy[r + ln] = k * ym - (ln + 1) * itau * y0;
+      } else {
+        for (int l = 3 + lane; l < ln; l += W) dy[r + l] = dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1];
+        dy[r + ln] = k * y[r + ln - 1] - (ln + 1) * itau * y[r + ln];
+      }
     }
   }
   // massive neutrinos (equations.f90:2710-2773)
@@ -1261,14 +1298,23 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       const int lt = M.lmaxnu_tau[i];
       for (int iq = 0; iq < M.nq[i]; ++iq) {
         const double v = bins[i].v[iq];
-        dy[ind] = -k * (4.0 / 3.0 * z + v * y[ind + 1]);
-        dy[ind + 1] = v * (dl[1] * y[ind] - dl2[1] * y[ind + 2]);
+        const double y0v = y[ind], y1v = y[ind + 1], y2v = y[ind + 2];
+        const double d0 = -k * (4.0 / 3.0 * z + v * y1v);
+        dy[ind] = d0;
+        dy[ind + 1] = v * (dl[1] * y0v - dl2[1] * y2v);
         if (lt == 2) {
-          dy[ind + 2] = -dy[ind] - 3 * itau * y[ind + 2];
+          dy[ind + 2] = -d0 - 3 * itau * y2v;
         } else {
-          dy[ind + 2] = v * (dl[2] * y[ind + 1] - dl2[2] * y[ind + 3]) + k * 8.0 / 15.0 * sigma;
-          for (int l = 3; l < lt; ++l) dy[ind + l] = v * (dl[l] * y[ind + l - 1] - dl2[l] * y[ind + l + 1]);
-          dy[ind + lt] = k * v * y[ind + lt - 1] - (lt + 1) * itau * y[ind + lt];
+          const double y3v = y[ind + 3];
+          dy[ind + 2] = v * (dl[2] * y1v - dl2[2] * y3v) + k * 8.0 / 15.0 * sigma;
+          double ym = y2v, yc = y3v;
+          for (int l = 3; l < lt; ++l) {
+            const double yp = y[ind + l + 1];
+            dy[ind + l] = v * (dl[l] * ym - dl2[l] * yp);
+            ym = yc;
+            yc = yp;
+          }
+          dy[ind + lt] = k * v * ym - (lt + 1) * itau * yc;
         }
         ind += lt + 1;
       }
@@ -1297,10 +1343,24 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   }
   if (M.has_nu_rel) {
     const int p0 = M.nu_pert_ix, lp = M.lmaxnu_pert;
-    dy[p0] = k * a2 * qr - k * y[p0 + 1];
-    for (int l = 1 + lane; l < lp; l += W)
-      dy[p0 + l] = -a2 * (dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1]) + (dl[l] * y[p0 + l - 1] - dl2[l] * y[p0 + l + 1]);
-    dy[p0 + lp] = k * (y[p0 + lp - 1] - a2 * y[r + lp - 1]) - (lp + 1) * itau * y[p0 + lp];
+    if constexpr (W == 1) {
+      double pm = y[p0], pc = y[p0 + 1], rm = y[r], rc = y[r + 1];
+      dy[p0] = k * a2 * qr - k * pc;
+      for (int l = 1; l < lp; ++l) {
+        const double rp = y[r + l + 1], pp = y[p0 + l + 1];
+        dy[p0 + l] = -a2 * (dl[l] * rm - dl2[l] * rp) + (dl[l] * pm - dl2[l] * pp);
+        rm = rc;
+        rc = rp;
+        pm = pc;
+        pc = pp;
+      }
+      dy[p0 + lp] = k * (pm - a2 * rm) - (lp + 1) * itau * pc;
+    } else {
+      dy[p0] = k * a2 * qr - k * y[p0 + 1];
+      for (int l = 1 + lane; l < lp; l += W)
+        dy[p0 + l] = -a2 * (dl[l] * y[r + l - 1] - dl2[l] * y[r + l + 1]) + (dl[l] * y[p0 + l - 1] - dl2[l] * y[p0 + l + 1]);
+      dy[p0 + lp] = k * (y[p0 + lp - 1] - a2 * y[r + lp - 1]) - (lp + 1) * itau * y[p0 + lp];
+    }
   }
   if (src) {
     wsync<W>();  // the source terms read derivatives written by other lanes
