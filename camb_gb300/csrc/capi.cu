@@ -522,6 +522,12 @@ struct Batch {
   // packed outputs [n][out_lmax+1][4 | 4 | 3]
   int out_lmax = 0;
   double *d_unl = nullptr, *d_len = nullptr, *d_pot = nullptr;
+  // repeated runs of a resident batch replay the stage sequence as a CUDA graph,
+  // captured on the second run (the first one allocates the lazily built device tables)
+  int runs = 0;
+  long long graph_key = -1;
+  cudaGraphExec_t graph = nullptr;
+  long long graph_launches = 0;
 };
 
 int stage_batch(Batch& B, int lmax_out = 0) {
@@ -731,11 +737,14 @@ int pick_team(const Batch& B) {
   return t;
 }
 
+int ode_order(const Batch& B) { return g_order >= 0 ? g_order : g_tuned[size_class(B)].order; }
+int ode_cap(const Batch& B) { return g_blocks_cap > 0 ? g_blocks_cap : g_team ? 0 : g_tuned[size_class(B)].cap; }
+
 int run_ode(Batch& B) {
   CUDA_TRY(cudaMemsetAsync(B.d_counter, 0, sizeof(int), g_rt.stream));
   CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
   int team = pick_team(B);
-  int order = g_order >= 0 ? g_order : g_tuned[size_class(B)].order;
+  int order = ode_order(B);
   const int lanes = team <= 5 ? 1 : team == 6 ? 32 : team;
   // Few modes (a single cosmology): one warp per block, so that the warps spread over the
   // SMs and none shares an SM's FP64 pipe; otherwise blocks of 128.  The shared-memory
@@ -744,7 +753,7 @@ int run_ode(Batch& B) {
   const int tpb = (team == 6 || threads_needed < 2L * 128 * g_rt.nsm) ? 32 : 128;
   int per_sm = std::max(1, ode_blocks_per_sm(team, tpb, B.warp_stride));
   // a cap below the occupancy limit leaves modes in the queue for threads that finish early
-  const int cap = g_blocks_cap > 0 ? g_blocks_cap : g_team ? 0 : g_tuned[size_class(B)].cap;
+  const int cap = ode_cap(B);
   if (cap > 0) per_sm = std::min(per_sm, cap);
   int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
@@ -822,15 +831,73 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 // runs every stage on a staged batch, with events between stages
+// under stream capture the stage boundaries are external event records, so that in the
+// graph they stay event-record nodes the host can time and wait on
+int enqueue_all(Batch& B, bool do_ode, bool do_los, bool do_cls, bool capturing) {
+  cudaStream_t s = g_rt.stream;
+  const unsigned fl = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  CUDA_TRY(cudaEventRecordWithFlags(g_rt.ev[0], s, fl));
+  if (do_ode) { int rc = run_ode(B); if (rc) return rc; }
+  CUDA_TRY(cudaEventRecordWithFlags(g_rt.ev[1], s, fl));
+  if (do_los) { int rc = run_los(B); if (rc) return rc; }
+  CUDA_TRY(cudaEventRecordWithFlags(g_rt.ev[2], s, fl));
+  if (do_cls) { int rc = run_cls(B); if (rc) return rc; }
+  CUDA_TRY(cudaEventRecordWithFlags(g_rt.ev[3], s, fl));
+  return 0;
+}
+
+// everything the enqueued sequence depends on besides the batch itself
+long long run_key(const Batch& B, bool do_ode, bool do_los, bool do_cls) {
+  long long k = pick_team(B);
+  k = k * 8 + (ode_order(B) + 1);
+  k = k * 64 + ode_cap(B);
+  k = k * 4 + g_precision;
+  return k * 8 + (do_ode ? 4 : 0) + (do_los ? 2 : 0) + (do_cls ? 1 : 0);
+}
+
+int capture_graph(Batch& B, bool do_ode, bool do_los, bool do_cls, long long key) {
+  cudaStream_t s = g_rt.stream;
+  if (B.graph) {
+    cudaGraphExecDestroy(B.graph);
+    B.graph = nullptr;
+    B.graph_key = -1;
+  }
+  const long long l0 = g_launches.load();
+  CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_all(B, do_ode, do_los, do_cls, true);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);  // always leave capture mode
+  B.graph_launches = g_launches.load() - l0;
+  g_launches = l0;
+  if (rc || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc ? rc : set_err(CAMBGPU_ERROR_CUDA, cudaGetErrorString(e));
+  }
+  e = cudaGraphInstantiate(&B.graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    B.graph = nullptr;
+    return set_err(CAMBGPU_ERROR_CUDA, cudaGetErrorString(e));
+  }
+  B.graph_key = key;
+  return 0;
+}
+
 int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
   cudaStream_t s = g_rt.stream;
-  CUDA_TRY(cudaEventRecord(g_rt.ev[0], s));
-  if (do_ode) { int rc = run_ode(B); if (rc) return rc; }
-  CUDA_TRY(cudaEventRecord(g_rt.ev[1], s));
-  if (do_los) { int rc = run_los(B); if (rc) return rc; }
-  CUDA_TRY(cudaEventRecord(g_rt.ev[2], s));
-  if (do_cls) { int rc = run_cls(B); if (rc) return rc; }
-  CUDA_TRY(cudaEventRecord(g_rt.ev[3], s));
+  if (B.runs == 0) {
+    int rc = enqueue_all(B, do_ode, do_los, do_cls, false);
+    if (rc) return rc;
+  } else {
+    const long long key = run_key(B, do_ode, do_los, do_cls);
+    if (key != B.graph_key) {
+      int rc = capture_graph(B, do_ode, do_los, do_cls, key);
+      if (rc) return rc;
+    }
+    CUDA_TRY(cudaGraphLaunch(B.graph, s));
+    g_launches += B.graph_launches;
+  }
+  B.runs++;
   CUDA_TRY(cudaEventSynchronize(g_rt.ev[3]));
   g_timings[0] = elapsed(g_rt.ev[0], g_rt.ev[1]);
   g_timings[1] = 0;
@@ -898,6 +965,7 @@ struct Resident {
   std::vector<Handle*> handles;
   Batch B;
   ~Resident() {
+    if (B.graph) cudaGraphExecDestroy(B.graph);
     for (auto* h : handles) delete h;
   }
 };

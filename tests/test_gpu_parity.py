@@ -129,3 +129,26 @@ def test_invalid_batch_reports_error_without_fault():
     test = fiducial(300)
     _lib.check(lib.cambgpu_get_results(C.byref(test), 300, _lib.dptr(cls)))
     assert np.all(np.isfinite(cls)) and cls[100, 0] > 0
+
+
+def test_resident_batch_graph_replay_is_identical():
+    """Repeated runs of a resident batch replay the stage sequence as a CUDA graph (captured
+    on the second run); the C_l of the eager first run, the capturing run and a replay
+    are identical, and a replay counts the graph's kernel launches."""
+    ps = draws(3, seed=21, lmax=600, mnu_max=0.1)
+    arr = (_lib.CambGpuParams * len(ps))(*ps)
+    lib = _lib.load()
+    _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
+    try:
+        outs = []
+        for _ in range(3):
+            lib.cambgpu_kernel_launches(1)
+            _lib.check(lib.cambgpu_batch_run(None))
+            launches = lib.cambgpu_kernel_launches(1)
+            cls = np.zeros((len(ps), 601, 4))
+            _lib.check(lib.cambgpu_batch_fetch(600, _lib.dptr(cls)))
+            outs.append((cls, launches))
+    finally:
+        lib.cambgpu_batch_release()
+    assert outs[0][1] > 0 and outs[1][1] == outs[0][1] and outs[2][1] == outs[0][1]
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][0], outs[2][0])
