@@ -36,7 +36,7 @@ using namespace cgdev;
 
 namespace {
 
-std::string g_err;
+thread_local std::string g_err;  // per calling thread, as errno
 std::atomic<long long> g_launches{0};
 double g_timings[6] = {0, 0, 0, 0, 0, 0};
 double g_host_ms[4] = {0, 0, 0, 0};  // host tables, staging, device pipeline, fetch (wall ms)
@@ -1123,19 +1123,47 @@ int cambgpu_calc_scal_cls(const CambGpuTables* t, const double* delta, double* i
   return 0;
 }
 
-int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
-                              double* lens_potential, int* lmax_lensed, int* status) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
-  if (lmax_out < 0 || lmax_out > 8000) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lmax_out out of range");
-  const double t0 = wall_ms();
+}  // extern "C"
+
+// host tables of a batch built ahead of its device run
+struct CambGpuPrepared {
   std::vector<Handle*> hs;
-  int rc = build_handles(p, n, hs, status);
-  struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
-  if (rc) return rc;
+  double host_ms = 0;
+  ~CambGpuPrepared() {
+    for (auto* h : hs) delete h;
+  }
+};
+
+extern "C" {
+
+int cambgpu_prepare_tables(const CambGpuParams* p, int n, CambGpuPrepared** out, int* status) {
+  if (!out) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no output handle");
+  *out = nullptr;
+  if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
+  const double t0 = wall_ms();
+  auto* t = new CambGpuPrepared();
+  int rc = build_handles(p, n, t->hs, status);
+  if (rc) {
+    delete t;
+    return rc;
+  }
+  t->host_ms = wall_ms() - t0;
+  *out = t;
+  return 0;
+}
+
+void cambgpu_free_prepared(CambGpuPrepared* t) { delete t; }
+
+int cambgpu_get_spectra_prepared(const CambGpuPrepared* t, int lmax_out, double* unlensed, double* lensed,
+                                 double* lens_potential, int* lmax_lensed, int* status) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!t || t->hs.empty()) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no prepared tables");
+  if (lmax_out < 0 || lmax_out > 8000) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lmax_out out of range");
+  const int n = (int)t->hs.size();
+  int rc = 0;
   const double t1 = wall_ms();
   Batch B;
-  for (auto* h : hs) B.views.push_back(&h->view);
+  for (auto* h : t->hs) B.views.push_back(&h->view);
   rc = stage_batch(B, lmax_out);
   if (rc) return rc;
   if (B.transfer) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "want_cls = 0: use cambgpu_get_transfer_batch");
@@ -1149,10 +1177,21 @@ int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, doubl
     for (int c = 0; c < n; ++c) lmax_lensed[c] = B.ups[c].d.lensed ? B.ups[c].d.lmax_lensed : 0;
   rc = fetch_spectra(B, lmax_out, unlensed, lensed, lens_potential);
   const double t4 = wall_ms();
-  g_host_ms[0] = t1 - t0;
+  g_host_ms[0] = t->host_ms;
   g_host_ms[1] = t2 - t1;
   g_host_ms[2] = t3 - t2;
   g_host_ms[3] = t4 - t3;
+  return rc;
+}
+
+int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
+                              double* lens_potential, int* lmax_lensed, int* status) {
+  if (lmax_out < 0 || lmax_out > 8000) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lmax_out out of range");
+  CambGpuPrepared* t = nullptr;
+  int rc = cambgpu_prepare_tables(p, n, &t, status);
+  if (rc) return rc;
+  rc = cambgpu_get_spectra_prepared(t, lmax_out, unlensed, lensed, lens_potential, lmax_lensed, status);
+  cambgpu_free_prepared(t);
   return rc;
 }
 

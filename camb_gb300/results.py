@@ -104,6 +104,66 @@ def _run(params_list, lmax_out):
                      pot[i] if lens and p.DoLensing else None, int(lml[i])) for i, p in enumerate(params_list)]
 
 
+def _run_prepared(handle, params_list, lmax_out):
+    lib = _lib.load()
+    n = len(params_list)
+    cls = np.zeros((n, lmax_out + 1, 4))
+    lens = any(p.DoLensing for p in params_list)
+    lensed = np.zeros((n, lmax_out + 1, 4)) if lens else None
+    pot = np.zeros((n, lmax_out + 1, 3)) if lens else None
+    lml = np.zeros(n, dtype=np.int32)
+    status = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.cambgpu_get_spectra_prepared(handle, lmax_out, _lib.dptr(cls),
+                                                _lib.dptr(lensed) if lens else None,
+                                                _lib.dptr(pot) if lens else None, _lib.iptr(lml), _lib.iptr(status)))
+    return [CAMBdata(p, cls[i], lensed[i] if lens and p.DoLensing else None,
+                     pot[i] if lens and p.DoLensing else None, int(lml[i])) for i, p in enumerate(params_list)]
+
+
+def _prepare(params_list):
+    lib = _lib.load()
+    n = len(params_list)
+    arr = (_lib.CambGpuParams * n)(*[p.to_struct() for p in params_list])
+    handle = C.c_void_p()
+    status = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.cambgpu_prepare_tables(arr, n, C.byref(handle), _lib.iptr(status)))
+    return handle
+
+
+def get_results_stream(batches, lmax_out=None):
+    """get_results_batch over a sequence of batches, pipelined: while the device runs one
+    batch, a host thread builds the next batch's tables (cambgpu_prepare_tables).  Yields
+    each batch's list of CAMBdata in order."""
+    from concurrent.futures import ThreadPoolExecutor
+    lib = _lib.load()
+    it = iter(batches)
+    cur = next(it, None)
+    if cur is None:
+        return
+    with ThreadPoolExecutor(1) as ex:
+        fut = ex.submit(_prepare, cur)
+        try:
+            while cur is not None:
+                handle = fut.result()
+                fut = None
+                nxt = next(it, None)
+                if nxt is not None:
+                    fut = ex.submit(_prepare, nxt)
+                try:
+                    lmax = max(p.max_l for p in cur) if lmax_out is None else lmax_out
+                    out = _run_prepared(handle, cur, lmax)
+                finally:
+                    lib.cambgpu_free_prepared(handle)
+                yield out
+                cur = nxt
+        finally:
+            if fut is not None:  # the consumer stopped early: release the prepared batch
+                try:
+                    lib.cambgpu_free_prepared(fut.result())
+                except _lib.CAMBError:
+                    pass
+
+
 def get_results(params, lmax_out=None):
     """camb.get_results (camb.py:47-61): one cosmology through the GPU pipeline (the CMB
     spectra, or with WantTransfer and WantCls off the matter transfer functions)."""

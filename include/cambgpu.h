@@ -215,6 +215,20 @@ int cambgpu_get_results_batch(const CambGpuParams* p, int n, int lmax_out, doubl
  * lmax_lensed[n] (0 for cosmologies without lensing) when that pointer is not NULL. */
 int cambgpu_get_spectra_batch(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
                               double* lens_potential, int* lmax_lensed, int* status);
+
+/* The same call in two halves, so that a caller can build the host tables of the next
+ * batch while the device works on the current one (the reference builds them inside
+ * CAMB_GetResults, results.f90:1924-2779, cmbmain.f90:785-936).
+ * cambgpu_prepare_tables: background, thermal history, grids and Bessel table of n
+ * cosmologies on the host threads; touches no device state and may run concurrently
+ * with any other entry point.  cambgpu_get_spectra_prepared: upload, device pipeline
+ * and outputs as cambgpu_get_spectra_batch (the tables stay valid and may be run
+ * again); cambgpu_free_prepared releases them. */
+typedef struct CambGpuPrepared CambGpuPrepared;
+int cambgpu_prepare_tables(const CambGpuParams* p, int n, CambGpuPrepared** out, int* status);
+int cambgpu_get_spectra_prepared(const CambGpuPrepared* t, int lmax_out, double* unlensed, double* lensed,
+                                 double* lens_potential, int* lmax_lensed, int* status);
+void cambgpu_free_prepared(CambGpuPrepared* t);
 /* Matter transfer functions of n cosmologies with want_cls = 0 and want_transfer = 1
  * (camb.get_results after set_matter_power; outtransf, equations.f90:2256-2271, and
  * Transfer_Get_sigmas, results.f90:4115-4182).  Per cosmology, with nq_max entries

@@ -152,3 +152,21 @@ def test_resident_batch_graph_replay_is_identical():
         lib.cambgpu_batch_release()
     assert outs[0][1] > 0 and outs[1][1] == outs[0][1] and outs[2][1] == outs[0][1]
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][0], outs[2][0])
+
+
+def test_results_stream_matches_blocking_calls():
+    """get_results_stream (next batch's host tables built while the device runs this one)
+    gives the same spectra as one blocking call per batch, and releases a prepared batch
+    when the consumer stops early."""
+    from camb_gb300 import model, results
+    batches = [[model.set_params(lmax=500, DoLensing=False, mnu=0.0, H0=h, ombh2=0.022 + 0.0002 * i)
+                for i in range(2)] for h in (66.0, 67.5, 69.0)]
+    streamed = list(results.get_results_stream(batches))
+    assert len(streamed) == 3
+    for got, ps in zip(streamed, batches):
+        want = results.get_results_batch(ps)
+        for g, w in zip(got, want):
+            assert np.array_equal(g.get_unlensed_scalar_cls(500), w.get_unlensed_scalar_cls(500))
+    it = results.get_results_stream(batches)
+    next(it)
+    it.close()  # the second batch was being prepared: it is freed, nothing leaks or faults
