@@ -801,6 +801,24 @@ constexpr int NV = 448;  // largest packed scalar system handled (mode_init reje
 constexpr int NL = 66;
 constexpr int NUE = 3;
 
+// l-only factors of the multipole recurrences (initial(), equations.f90:1911-1916):
+// denlk = k a_l, denlk2 = k b_l, polfack = k p_l with a_l = l/(2l+1), b_l = (l+1)/(2l+1),
+// p_l = (l+3)(l-1)/((l+1)(2l+1)).  One table for every mode (k is applied in the
+// recurrence), read with uniform addresses across a warp instead of per-thread copies.
+struct RecTab {
+  double a[NL], b[NL], p[NL];
+};
+constexpr RecTab make_rec_tab() {
+  RecTab t{};
+  for (int l = 0; l < NL; ++l) {
+    t.a[l] = l / (2.0 * l + 1);
+    t.b[l] = (l + 1) / (2.0 * l + 1);
+    t.p[l] = l >= 1 ? ((double)((l + 3) * (l - 1)) / (l + 1)) / (2.0 * l + 1) : 0.0;
+  }
+  return t;
+}
+__device__ const RecTab kRec = make_rec_tab();
+
 // x**(1/5) for the step-size update: FP32 seed, two Newton steps on y^5 = x in FP64
 __device__ __forceinline__ double fifth_root(double x) {
   if (!(x > 1e-300) || !(x < 1e300)) return pow(x, 0.2);
@@ -1097,12 +1115,21 @@ __device__ double nu_pinudot(const DevCosmo& C, const St& M, const YV y,
 
 // derivs (equations.f90:2273-2773) + sources (2775-2912), one mode per thread (W = 1)
 // or per warp (W = 32, sbins: the warp's momentum-bin factors in shared memory)
+//
+// Multipole recurrences: one thread per mode reads the l-only factors from the global
+// table (uniform addresses across the warp) and applies k; a warp per mode (lanes at
+// different l) reads the mode's k-scaled factors from its shared memory (wrec: denlk,
+// denlk2, polfack, NL entries each).
 template <bool TR, int W, class YV>
-__device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* __restrict__ dl,
-                                        const double* __restrict__ dl2, const double* __restrict__ pf, double tau,
-                                        const YV y, double* __restrict__ dy, double* src,
-                                        NuBins* sbins = nullptr) {
+__device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, const YV y, double* __restrict__ dy,
+                                        double* src, NuBins* sbins = nullptr, const double* wrec = nullptr) {
   const int lane = wlane<W>();
+  const double* __restrict__ ra = kRec.a;
+  const double* __restrict__ rb = kRec.b;
+  const double* __restrict__ rp = kRec.p;
+  const double* __restrict__ dl = wrec;
+  const double* __restrict__ dl2 = wrec + NL;
+  const double* __restrict__ pf = wrec + 2 * NL;
   const double k = M.k, ik = M.ik;
   const double itau = 1.0 / tau;
   double a, cs2, opac, dopac = 0;
@@ -1213,13 +1240,13 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   if (!M.nophot) {
     dy[g] = clxgdot;
     const double inv_pb43 = a * C.photbar_fac;  // 3/(4 photbar)
-    qgdot = 4.0 / 3 * (-vbdot - adotoa * vb + delta_p_b * k) * inv_pb43 + dl[1] * clxg - dl2[1] * pig;
+    qgdot = 4.0 / 3 * (-vbdot - adotoa * vb + delta_p_b * k) * inv_pb43 + k * ((1.0 / 3) * clxg - (2.0 / 3) * pig);
     dy[g + 1] = qgdot;
     if (!M.tc) {
       E2 = y[pol + 2];
       polter = pig * 0.1 + 9.0 / 15 * E2;
       const double g3v = y[g + 3];
-      pigdot = dl[2] * qg - dl2[2] * g3v - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
+      pigdot = k * (0.4 * qg - 0.6 * g3v) - opac * (pig - polter) + 8.0 / 15.0 * k * sigma;
       dy[g + 2] = pigdot;
       const int lg = M.lmaxg;
       const int lp = M.lmaxgpol;
@@ -1228,7 +1255,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
         double ym = pig, y0 = g3v;
         for (int l = 3; l < lg; ++l) {
           const double yp = y[g + l + 1];
-          dy[g + l] = (dl[l] * ym - dl2[l] * yp) - opac * y0;
+          dy[g + l] = k * (__ldg(ra + l) * ym - __ldg(rb + l) * yp) - opac * y0;
           ym = y0;
           y0 = yp;
         }
@@ -1239,7 +1266,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
         y0 = p3v;
         for (int l = 3; l < lp; ++l) {
           const double yp = y[pol + l + 1];
-          dy[pol + l] = -opac * y0 + (dl[l] * ym - pf[l] * yp);
+          dy[pol + l] = -opac * y0 + k * (__ldg(ra + l) * ym - __ldg(rp + l) * yp);
           ym = y0;
           y0 = yp;
         }
@@ -1259,20 +1286,20 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
   if (!M.nonu) {
     clxrdot = -k * (4.0 / 3.0 * z + qr);
     dy[r] = clxrdot;
-    dy[r + 1] = dl[1] * clxr - dl2[1] * pir;
+    dy[r + 1] = k * ((1.0 / 3) * clxr - (2.0 / 3) * pir);
     if (M.hk) {
       pirdot = -3 * pir * itau - clxrdot;
       dy[r + 2] = pirdot;
     } else {
       const double n3v = y[r + 3];
-      pirdot = dl[2] * qr - dl2[2] * n3v + 8.0 / 15.0 * k * sigma;
+      pirdot = k * (0.4 * qr - 0.6 * n3v) + 8.0 / 15.0 * k * sigma;
       dy[r + 2] = pirdot;
       const int ln = M.lmaxnr;
       if constexpr (W == 1) {
         double ym = pir, y0 = n3v;
         for (int l = 3; l < ln; ++l) {
           const double yp = y[r + l + 1];
-          dy[r + l] = dl[l] * ym - dl2[l] * yp;
+          dy[r + l] = k * (__ldg(ra + l) * ym - __ldg(rb + l) * yp);
           ym = y0;
           y0 = yp;
         }
@@ -1297,20 +1324,20 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       int ind = M.nu_ix[i];
       const int lt = M.lmaxnu_tau[i];
       for (int iq = 0; iq < M.nq[i]; ++iq) {
-        const double v = bins[i].v[iq];
+        const double v = bins[i].v[iq], vk = v * k;
         const double y0v = y[ind], y1v = y[ind + 1], y2v = y[ind + 2];
         const double d0 = -k * (4.0 / 3.0 * z + v * y1v);
         dy[ind] = d0;
-        dy[ind + 1] = v * (dl[1] * y0v - dl2[1] * y2v);
+        dy[ind + 1] = vk * ((1.0 / 3) * y0v - (2.0 / 3) * y2v);
         if (lt == 2) {
           dy[ind + 2] = -d0 - 3 * itau * y2v;
         } else {
           const double y3v = y[ind + 3];
-          dy[ind + 2] = v * (dl[2] * y1v - dl2[2] * y3v) + k * 8.0 / 15.0 * sigma;
+          dy[ind + 2] = vk * (0.4 * y1v - 0.6 * y3v) + k * 8.0 / 15.0 * sigma;
           double ym = y2v, yc = y3v;
           for (int l = 3; l < lt; ++l) {
             const double yp = y[ind + l + 1];
-            dy[ind + l] = v * (dl[l] * ym - dl2[l] * yp);
+            dy[ind + l] = vk * (__ldg(ra + l) * ym - __ldg(rb + l) * yp);
             ym = yc;
             yc = yp;
           }
@@ -1324,12 +1351,12 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       int iq = lane / lt1, l = lane - iq * lt1;
       for (int e = lane; e < tot; e += W) {
         const int ind = M.nu_ix[i] + iq * lt1;
-        const double v = bins[i].v[iq];
+        const double v = bins[i].v[iq], vk = v * k;
         double d;
         if (l == 0) d = -k * (4.0 / 3.0 * z + v * y[ind + 1]);
-        else if (l == 1) d = v * (dl[1] * y[ind] - dl2[1] * y[ind + 2]);
+        else if (l == 1) d = vk * ((1.0 / 3) * y[ind] - (2.0 / 3) * y[ind + 2]);
         else if (l == 2 && lt == 2) d = k * (4.0 / 3.0 * z + v * y[ind + 1]) - 3 * itau * y[ind + 2];
-        else if (l == 2) d = v * (dl[2] * y[ind + 1] - dl2[2] * y[ind + 3]) + k * 8.0 / 15.0 * sigma;
+        else if (l == 2) d = vk * (0.4 * y[ind + 1] - 0.6 * y[ind + 3]) + k * 8.0 / 15.0 * sigma;
         else if (l < lt) d = v * (dl[l] * y[ind + l - 1] - dl2[l] * y[ind + l + 1]);
         else d = k * v * y[ind + lt - 1] - (lt + 1) * itau * y[ind + lt];
         dy[ind + l] = d;
@@ -1347,10 +1374,11 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
       double pm = y[p0], pc = y[p0 + 1], rm = y[r], rc = y[r + 1];
       dy[p0] = k * a2 * qr - k * pc;
       for (int l = 1; l < lp; ++l) {
-        const double rp = y[r + l + 1], pp = y[p0 + l + 1];
-        dy[p0 + l] = -a2 * (dl[l] * rm - dl2[l] * rp) + (dl[l] * pm - dl2[l] * pp);
+        const double rpv = y[r + l + 1], pp = y[p0 + l + 1];
+        const double al = __ldg(ra + l), bl = __ldg(rb + l);
+        dy[p0 + l] = k * (-a2 * (al * rm - bl * rpv) + (al * pm - bl * pp));
         rm = rc;
-        rc = rp;
+        rc = rpv;
         pm = pc;
         pc = pp;
       }
@@ -1456,15 +1484,14 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, const double* 
 // rows are named by slot indices so that accepting a step swaps indices, not vectors.
 struct Work {
   double b[8][NV];
-  double dl[NL], dl2[NL], pf[20];
 };
 
 // The same rows for a warp's mode, in the warp's slice of shared memory
 struct WorkS {
   double* b;  // [8][stride]
   int stride;
-  double *dl, *dl2, *pf;
   NuBins* bins;  // [NUE] momentum-bin factors of the current right-hand side
+  double* rec;   // [3][NL] the mode's denlk, denlk2, polfack
 };
 __device__ __forceinline__ double* row(Work& w, int s) { return w.b[s]; }
 __device__ __forceinline__ double* row(const WorkS& w, int s) { return w.b + (size_t)s * w.stride; }
@@ -1472,6 +1499,8 @@ __device__ __forceinline__ NuBins* sbins(Work&) { return nullptr; }
 __device__ __forceinline__ NuBins* sbins(const WorkS& w) { return w.bins; }
 __device__ __forceinline__ int row_cap(const Work&) { return NV; }
 __device__ __forceinline__ int row_cap(const WorkS& w) { return w.stride; }
+__device__ __forceinline__ const double* wrec(const Work&) { return nullptr; }
+__device__ __forceinline__ const double* wrec(const WorkS& w) { return w.rec; }
 
 // state of one mode's integration, advanced one trial step per loop iteration
 struct Run {
@@ -1537,11 +1566,13 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
   R.syt = 7;
   R.ny_valid = false;
   double* const Y = row(Wk, R.sy);
-  for (int l = 1 + lane; l <= lm; l += W) {
-    const double dn = 1.0 / (2 * l + 1);
-    Wk.dl[l] = dn * M.k * l;
-    Wk.dl2[l] = dn * M.k * (l + 1);
-    if (l < 20) Wk.pf[l] = ((double)((l + 3) * (l - 1)) / (l + 1)) * M.k * dn;
+  if constexpr (W > 1) {  // the warp's k-scaled recurrence factors (initial(), equations.f90:1911-1916)
+    for (int l = 1 + lane; l <= lm; l += W) {
+      const double dn = 1.0 / (2 * l + 1);
+      Wk.rec[l] = dn * M.k * l;
+      Wk.rec[NL + l] = dn * M.k * (l + 1);
+      Wk.rec[2 * NL + l] = ((double)((l + 3) * (l - 1)) / (l + 1)) * M.k * dn;
+    }
   }
   for (int i = lane; i < M.nvar; i += W) Y[i] = 0;
   wsync<W>();  // the initial values below are written by every lane
@@ -1793,7 +1824,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
-      derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, R.tau, y, k1, nullptr, sb);
+      derivs1<TR, W>(C, M, R.tau, y, k1, nullptr, sb, wrec(Wk));
       wsync<W>();
       R.evals++;
     }
@@ -1842,28 +1873,28 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
 #pragma unroll 4
   for (int i = lane; i < n; i += W) yt[i] = fma(c21, k1[i], y[i]);
   wsync<W>();
-  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs / 5.0, yt, k2, nullptr, sb);
+  derivs1<TR, W>(C, M, x + hs / 5.0, yt, k2, nullptr, sb, wrec(Wk));
   wsync<W>();
 #pragma unroll 4
   for (int i = lane; i < n; i += W) yt[i] = fma(c32, k2[i], fma(c31, k1[i], y[i]));
   wsync<W>();
-  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs * (3.0 / 10.0), yt, k3, nullptr, sb);
+  derivs1<TR, W>(C, M, x + hs * (3.0 / 10.0), yt, k3, nullptr, sb, wrec(Wk));
   wsync<W>();
 #pragma unroll 4
   for (int i = lane; i < n; i += W) yt[i] = fma(c43, k3[i], fma(c42, k2[i], fma(c41, k1[i], y[i])));
   wsync<W>();
-  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs * (4.0 / 5.0), yt, k4, nullptr, sb);
+  derivs1<TR, W>(C, M, x + hs * (4.0 / 5.0), yt, k4, nullptr, sb, wrec(Wk));
   wsync<W>();
 #pragma unroll 4
   for (int i = lane; i < n; i += W) yt[i] = fma(c54, k4[i], fma(c53, k3[i], fma(c52, k2[i], fma(c51, k1[i], y[i]))));
   wsync<W>();
-  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs * (8.0 / 9.0), yt, k5, nullptr, sb);
+  derivs1<TR, W>(C, M, x + hs * (8.0 / 9.0), yt, k5, nullptr, sb, wrec(Wk));
   wsync<W>();
 #pragma unroll 4
   for (int i = lane; i < n; i += W)
     yt[i] = fma(c65, k5[i], fma(c64, k4[i], fma(c63, k3[i], fma(c62, k2[i], fma(c61, k1[i], y[i])))));
   wsync<W>();
-  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs, yt, k6, nullptr, sb);
+  derivs1<TR, W>(C, M, x + hs, yt, k6, nullptr, sb, wrec(Wk));
   wsync<W>();
   // the fifth-order solution, the error combination of k1, k3..k6 (k3 is dead afterwards
   // and holds it) and max|yt| for the next step's hmin, in one pass
@@ -1879,7 +1910,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   wsync<W>();
   // stage 7 (FSAL) into k2; at an output time it is the output() evaluation too
   const bool want_src = (xt == xend) && !R.target_is_switch;
-  derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, x + hs, yt, k2, want_src ? R.src : nullptr, sb);
+  derivs1<TR, W>(C, M, x + hs, yt, k2, want_src ? R.src : nullptr, sb, wrec(Wk));
   wsync<W>();
   R.src_valid = want_src;
   R.evals += 6;
@@ -1968,7 +1999,7 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
         apply_switch<W>(C, M, Wk, R);
       } else {
         if (!R.src_valid) {
-          derivs1<TR, W>(C, M, Wk.dl, Wk.dl2, Wk.pf, R.tau, row(Wk, R.sy), row(Wk, R.syt), R.src, sbins(Wk));
+          derivs1<TR, W>(C, M, R.tau, row(Wk, R.sy), row(Wk, R.syt), R.src, sbins(Wk), wrec(Wk));
           wsync<W>();
         }
         R.evals++;  // the output() evaluation of the reference
@@ -2015,7 +2046,7 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
 
 // Warp per mode, one warp per block: the block's dynamic shared memory holds the eight
 // state rows of `stride` entries, the recurrence factors and the momentum-bin factors.
-size_t warp_smem_bytes(int stride) { return ((size_t)8 * stride + 2 * NL + 20) * sizeof(double) + NUE * sizeof(NuBins); }
+size_t warp_smem_bytes(int stride) { return ((size_t)8 * stride + 3 * NL) * sizeof(double) + NUE * sizeof(NuBins); }
 
 template <bool TR>
 __global__ void __launch_bounds__(32) ode_warp_kernel(const DevCosmo* __restrict__ cosmos,
@@ -2025,10 +2056,8 @@ __global__ void __launch_bounds__(32) ode_warp_kernel(const DevCosmo* __restrict
   WorkS Wk;
   Wk.b = wsm;
   Wk.stride = stride;
-  Wk.dl = wsm + (size_t)8 * stride;
-  Wk.dl2 = Wk.dl + NL;
-  Wk.pf = Wk.dl2 + NL;
-  Wk.bins = reinterpret_cast<NuBins*>(Wk.pf + 20);
+  Wk.rec = wsm + (size_t)8 * stride;
+  Wk.bins = reinterpret_cast<NuBins*>(Wk.rec + 3 * NL);
   run_modes<TR, 32>(cosmos, items, nitems, counter, Wk, blockIdx.x, gridDim.x);
 }
 
