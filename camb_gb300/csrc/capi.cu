@@ -753,8 +753,10 @@ int run_ode(Batch& B) {
   const int tpb = (team == 6 || threads_needed < 2L * 128 * g_rt.nsm) ? 32 : 128;
   int per_sm = std::max(1, ode_blocks_per_sm(team, tpb, B.warp_stride));
   // a cap below the occupancy limit leaves modes in the queue for threads that finish early
+  // the cap counts resident threads in units of 128 (a 32-thread-block launch may keep
+  // four times as many blocks)
   const int cap = ode_cap(B);
-  if (cap > 0) per_sm = std::min(per_sm, cap);
+  if (cap > 0) per_sm = std::min(per_sm, cap * (128 / tpb));
   int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
   const WorkItem* queue = order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;

@@ -281,8 +281,8 @@ int cambgpu_get_precision(void);
  * compiled for 3/4/5/6/8 resident blocks of 128 per SM; 0 = the autotuned choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
 /* ODE launch shape: queue order (-1 = the autotuned one, else as for the autotuner) and a
- * cap on resident blocks per SM (0 = as many as fit; a lower cap leaves modes in the work
- * queue for threads that finish early). */
+ * cap on resident threads per SM in units of 128 (0 = as many as fit; a lower cap leaves
+ * modes in the work queue for threads that finish early). */
 int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm);
 /* In-library autotuner: times ODE variants, work-queue orders and resident-block caps on
  * n cosmologies and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
