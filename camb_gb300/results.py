@@ -1,6 +1,7 @@
 """Results object, mirroring the reference's camb/results.py CAMBdata C_l getters
 (results.py:417-508, 1227-1290): unlensed and lensed scalar spectra and the lensing
 potential, all computed on the GPU through cambgpu_get_spectra_batch."""
+import copy
 import ctypes as C
 
 import numpy as np
@@ -164,19 +165,47 @@ def get_results_stream(batches, lmax_out=None):
                     pass
 
 
+def _split(p):
+    """(CMB-only copy, transfer-only copy) of a CAMBparams asking for both."""
+    cmb, tr = copy.deepcopy(p), copy.deepcopy(p)
+    cmb.WantTransfer = False
+    tr.WantCls = False
+    return cmb, tr
+
+
+def _run_both(params_list, lmax_out):
+    """WantCls and WantTransfer together: the CMB spectra and the matter transfer
+    functions as two batches (each as with the other request off), merged into one
+    CAMBdataMatter per cosmology."""
+    cmbs, trs = zip(*[_split(p) for p in params_list])
+    cmb_out = _run(list(cmbs), lmax_out)
+    tr_out = _run_transfer(list(trs))
+    out = []
+    for p, c, t in zip(params_list, cmb_out, tr_out):
+        r = CAMBdataMatter(p, t.get_matter_transfer_data())
+        r._cls, r._lensed, r._pot, r._lmax_lensed = c._cls, c._lensed, c._pot, c._lmax_lensed
+        out.append(r)
+    return out
+
+
 def get_results(params, lmax_out=None):
-    """camb.get_results (camb.py:47-61): one cosmology through the GPU pipeline (the CMB
-    spectra, or with WantTransfer and WantCls off the matter transfer functions)."""
-    if params.WantTransfer:
-        return _run_transfer([params])[0]
-    return _run([params], params.max_l if lmax_out is None else lmax_out)[0]
+    """camb.get_results (camb.py:47-61): one cosmology through the GPU pipeline -- the CMB
+    spectra, the matter transfer functions (WantTransfer), or both."""
+    return get_results_batch([params], lmax_out)[0]
 
 
 def get_results_batch(params_list, lmax_out=None):
     """Many cosmologies in one persistent launch per stage."""
-    if all(p.WantTransfer for p in params_list):
+    want_cls = [p.WantCls for p in params_list]
+    want_tr = [p.WantTransfer for p in params_list]
+    lmax = max(p.max_l for p in params_list) if lmax_out is None else lmax_out
+    if all(want_tr) and not any(want_cls):
         return _run_transfer(params_list)
-    return _run(params_list, max(p.max_l for p in params_list) if lmax_out is None else lmax_out)
+    if all(want_tr) and all(want_cls):
+        return _run_both(params_list, lmax)
+    if any(want_tr):
+        raise _lib.CAMBError("a batch either wants transfer functions in every member or in none")
+    return _run(params_list, lmax)
 
 
 class _ResidentBatch:

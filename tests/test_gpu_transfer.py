@@ -84,3 +84,18 @@ def test_python_surface_sigma8():
     kh, z, pk = r.get_linear_matter_power_spectrum()
     assert list(z) == [0.0, 0.17, 3.1] and pk.shape == (3, len(kh))
     assert np.all(pk > 0) and pk[0].max() > pk[2].max()
+
+
+def test_python_surface_cmb_and_matter_power_together():
+    """set_matter_power with the CMB on (the reference's usual call): one result object
+    carries both; each part equals the run that asks for it alone."""
+    from camb_gb300 import model, results
+    cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.06, As=2.1e-9, ns=0.965, lmax=800,
+                          DoLensing=False)
+    cp.set_matter_power(redshifts=[0.0], kmax=1.0)
+    both = results.get_results(cp)
+    cmb_only, tr_only = results._split(cp)
+    want_cls = results.get_results(cmb_only).get_unlensed_scalar_cls(800)
+    assert np.array_equal(both.get_unlensed_scalar_cls(800), want_cls)
+    assert both.get_sigma8()[0] == results.get_results(tr_only).get_sigma8()[0]
+    assert 0.7 < both.get_sigma8()[0] < 0.9
