@@ -352,6 +352,7 @@ struct Upload {
   std::vector<double> spl;  // [5][nk]
   std::vector<double> inv_q;  // 1/nu_q
   std::vector<double> inv_tgrid;  // 1/tau_j of the thermal log grid
+  std::vector<double> lfac;       // [2][nl] per sampled l: x_lim, sqrt(pi/2/(l+1/2))
   DevCosmo d;
 };
 
@@ -362,7 +363,7 @@ size_t bytes_for(const CambGpuTables& t) {
   s += 2 * r((size_t)t.ntau * 8) + r((size_t)t.nk * sizeof(CambGpuModeSpec)) + r((size_t)t.nk * 8);
   s += 2 * r((size_t)t.ntau * t.nsrc * t.nk * 8);
   s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
-  s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256);
+  s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256) + r((size_t)t.nl * 16);
   s += 3 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
   s += r((size_t)(t.max_l + 1) * 6 * 8) + r((size_t)(t.max_l + 1) * 4 * 8);  // all-l C_l, lensed C_l
   if (t.transfer_only)
@@ -442,6 +443,16 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.nq = t.nq;
   d.ls = (const int*)put(t.ls, (size_t)t.nl * 4);
   d.nl = t.nl;
+  // l-only factors of the projection windows and the Limber value (DoFlatIntegration,
+  // cmbmain.f90:1702-1716, 1821-1832), for the mixed-precision projection
+  u.lfac.resize(2 * (size_t)t.nl);
+  for (int j = 0; j < t.nl; ++j) {
+    const double l = t.ls[j];
+    u.lfac[j] = std::fmax(0.0, l - 4.2 * std::cbrt(l));
+    u.lfac[t.nl + j] = std::sqrt(3.14159265358979323846 / 2 / (l + 0.5));
+  }
+  d.l_xlim = (const double*)put(u.lfac.data(), u.lfac.size() * 8);
+  d.l_limb = d.l_xlim + t.nl;
   d.max_l = t.max_l;
   d.cl_template_scale = t.cl_template_scale;
   d.lensed = nullptr;

@@ -65,6 +65,8 @@ struct DevCosmo {
   int nq;
   const int* ls;
   int nl;
+  const double* l_xlim;  // [nl] max(0, l - 4.2 l^(1/3))
+  const double* l_limb;  // [nl] sqrt(pi / (2 l + 1))
   // Bessel table
   const double* bess_x;
   const double* bessel_horner;  // [nl][num_xx-1][4]

@@ -162,7 +162,9 @@ enum { F_SKIP = 1, F_INT = 2, F_LIMBER = 4 };
 // Per sampled l (DoSourceIntegration, flat): the integration window in time steps,
 // whether to integrate, and the Limber value of the lensing source -- one thread per l
 // (the scalar FP64 set-up would otherwise run once per warp on the FP64 pipe for each l).
-template <typename RawT>
+// FAST (mixed precision): the l-only factors come from the per-cosmology tables and 1/q is
+// formed once, instead of a cube root, two divisions and a square root per (q, l).
+template <bool FAST, typename RawT>
 __device__ __forceinline__ void window_setup(const DevCosmo& C, double q, int source_steps, const RawT* s_raw3,
                                              int* s_ns, int* s_ne, int* s_flag, double* s_limb) {
   const int ntau = C.ntau, nsrc = C.nsrc;
@@ -173,16 +175,17 @@ __device__ __forceinline__ void window_setup(const DevCosmo& C, double q, int so
   const double BessIntBoost = C.AccuracyBoost * C.BessIntBoost;
   const double limber_l = 400 * sqrt(C.AccuracyBoost * C.LimberBoost);
   const double* __restrict__ tp = C.tau_points;
+  const double inv_q = FAST ? 1.0 / q : 0.0;
   for (int j = threadIdx.x; j < C.nl; j += blockDim.x) {
     const int l = C.ls[j];
     int flag = 0, ns = 0, ne = -1;
     double limb = 0;
     if (l > llmax) flag = F_SKIP;
     else {
-      const double xlim = fmax(0.0, l - 4.2 * cbrt((double)l));
+      const double xlim = FAST ? C.l_xlim[j] : fmax(0.0, l - 4.2 * cbrt((double)l));
       const double xlmax1 = 80 * l * BessIntBoost;
-      const double tmin = fmax(tp[1], tau0 - xlmax1 / q);
-      const double tmax = tau0 - xlim / q;
+      const double tmin = fmax(tp[1], FAST ? tau0 - xlmax1 * inv_q : tau0 - xlmax1 / q);
+      const double tmax = FAST ? tau0 - xlim * inv_q : tau0 - xlim / q;
       if (tmax < tp[1]) flag = F_SKIP;
       else {
         bool doint = true;
@@ -195,13 +198,14 @@ __device__ __forceinline__ void window_setup(const DevCosmo& C, double q, int so
         if (nsrc > 2 && (!doint || l > limber_l)) {
           // Limber approximation for the lensing potential (cmbmain.f90:1821-1832)
           flag |= F_LIMBER;
-          double xf = tau0 - (l + 0.5) / q;
+          double xf = FAST ? tau0 - (l + 0.5) * inv_q : tau0 - (l + 0.5) / q;
           if (xf < tp[ntau - 1] && xf > tp[0]) {
             int n = time_index_of(tp, ntau, xf);  // 1-based
             double f = (xf - tp[n - 1]) / (tp[n] - tp[n - 1]);
             double s_lo = (n - 1 < source_steps) ? (double)s_raw3[n - 1] : 0.0;
             double s_hi = (n < source_steps) ? (double)s_raw3[n] : 0.0;
-            limb = (s_lo * (1 - f) + f * s_hi) * sqrt(3.14159265358979323846 / 2 / (l + 0.5)) / q;
+            limb = FAST ? (s_lo * (1 - f) + f * s_hi) * C.l_limb[j] * inv_q
+                        : (s_lo * (1 - f) + f * s_hi) * sqrt(3.14159265358979323846 / 2 / (l + 0.5)) / q;
           }
         }
       }
@@ -285,7 +289,7 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
   __syncthreads();
   __shared__ int s_ns[kLosMaxL], s_ne[kLosMaxL], s_flag[kLosMaxL];
   __shared__ double s_limb[kLosMaxL];
-  window_setup(C, q, source_steps, s_raw3, s_ns, s_ne, s_flag, s_limb);
+  window_setup<false>(C, q, source_steps, s_raw3, s_ns, s_ne, s_flag, s_limb);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int j = warp; j < C.nl; j += nwarps) {
@@ -391,7 +395,7 @@ __device__ __forceinline__ void los_mixed_body(const DevCosmo& C, int q_ix, floa
   __shared__ int s_ns[kLosMaxL], s_ne[kLosMaxL], s_flag[kLosMaxL];
   __shared__ double s_limb[kLosMaxL];
   __shared__ float2 s_res[kLosMaxL * 3];
-  window_setup(C, q, source_steps, s_raw3, s_ns, s_ne, s_flag, s_limb);
+  window_setup<true>(C, q, source_steps, s_raw3, s_ns, s_ne, s_flag, s_limb);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int j = warp; j < C.nl; j += nwarps) {
