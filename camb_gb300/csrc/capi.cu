@@ -513,6 +513,12 @@ struct Batch {
   std::vector<WorkItem> h_items_rev;
   WorkItem* d_items_grp = nullptr;  // q bands, cosmologies of similar neutrino mass together
   std::vector<WorkItem> h_items_grp;
+  // queue order 3: decreasing measured cost (evaluations x system size) of the last run
+  WorkItem* d_items_cost = nullptr;
+  std::vector<WorkItem> h_items_cost;
+  unsigned* d_mode_evals = nullptr;  // [nitems], cosmology-major
+  std::vector<size_t> mode_base;     // first mode_evals entry of each cosmology
+  bool costs_valid = false, cost_order = false;
   int nitems = 0;
   int* d_counter = nullptr;
   int* d_status = nullptr;
@@ -582,13 +588,16 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   total += 2 * rr((size_t)n * (B.out_lmax + 1) * 4 * 8) + rr((size_t)n * (B.out_lmax + 1) * 3 * 8);
   size_t nitems = 0;
   for (auto* v : B.views) nitems += v->nk;
-  total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + 3 * (nitems * sizeof(WorkItem) + 255) +
-           1024 + ((size_t)n * 4 + 255);
+  total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + 4 * (nitems * sizeof(WorkItem) + 255) +
+           1024 + ((size_t)n * 4 + 255) + (nitems * 4 + 255);
   rc = g_rt.arena.reserve(total);
   if (rc) return set_err(rc, "device allocation failed");
   B.d_status = g_rt.arena.take<int>(n);
   B.d_counter = g_rt.arena.take<int>(1);
   B.d_evals = g_rt.arena.take<unsigned long long>(1);
+  B.d_mode_evals = g_rt.arena.take<unsigned>(nitems);
+  B.mode_base.assign(n, 0);
+  for (int c = 1; c < n; ++c) B.mode_base[c] = B.mode_base[c - 1] + B.views[c - 1]->nk;
   std::vector<std::pair<void*, std::pair<const void*, size_t>>> copies;
   B.ups.resize(n);
   for (int c = 0; c < n; ++c) {
@@ -596,6 +605,7 @@ int stage_batch(Batch& B, int lmax_out = 0) {
     rc = upload(B.ups[c], B.d_status + c, copies);
     if (rc) return rc;
     B.ups[c].d.evals = B.d_evals;
+    B.ups[c].d.mode_evals = B.d_mode_evals + B.mode_base[c];
     B.max_ntau = std::max(B.max_ntau, B.views[c]->ntau);
     B.max_nq = std::max(B.max_nq, B.views[c]->nq);
     B.max_nl = std::max(B.max_nl, B.views[c]->nl);
@@ -681,6 +691,11 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   }
   B.d_items_grp = g_rt.arena.take<WorkItem>(items.size());
   copies.push_back({B.d_items_grp, {B.h_items_grp.data(), items.size() * sizeof(WorkItem)}});
+  // order 3 starts as order 2 and becomes the measured-cost order once a run has recorded
+  // every mode's evaluations (build_cost_order)
+  B.h_items_cost = B.h_items_grp;
+  B.d_items_cost = g_rt.arena.take<WorkItem>(items.size());
+  copies.push_back({B.d_items_cost, {B.h_items_cost.data(), items.size() * sizeof(WorkItem)}});
   // single pinned staging buffer for all uploads
   size_t stage = 0;
   for (auto& cp : copies) stage += (cp.second.second + 255) & ~size_t(255);
@@ -726,6 +741,7 @@ int stage_batch(Batch& B, int lmax_out = 0) {
     i = j + 1;
   }
   CUDA_TRY(cudaMemsetAsync(B.d_status, 0, (size_t)n * 4, g_rt.stream));
+  CUDA_TRY(cudaMemsetAsync(B.d_mode_evals, 0, (size_t)B.nitems * 4, g_rt.stream));
   for (int c = 0; c < n; ++c) {
     const auto& v = *B.views[c];
     CUDA_TRY(cudaMemsetAsync(B.ups[c].d.linear_src, 0, (size_t)v.ntau * v.nsrc * v.nk * 8, g_rt.stream));
@@ -770,7 +786,7 @@ int run_ode(Batch& B) {
   if (cap > 0) per_sm = std::min(per_sm, cap * (128 / tpb));
   int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
-  const WorkItem* queue = order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
+  const WorkItem* queue = order == 3 ? B.d_items_cost : order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
   CUDA_TRY(launch_ode_kernel(team, blocks, tpb, g_rt.stream, B.d_cosmos, queue, B.nitems, B.d_counter,
                              B.transfer, B.warp_stride));
   g_launches++;
@@ -844,6 +860,29 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 // runs every stage on a staged batch, with events between stages
+// Queue order 3 (longest processing time first): the modes in decreasing order of the
+// last run's evaluations times their largest packed system, so that the expensive modes
+// start first and cheap ones fill the tail; built once per batch from the first ODE run.
+int build_cost_order(Batch& B) {
+  std::vector<unsigned> ev(B.nitems);
+  CUDA_TRY(cudaMemcpy(ev.data(), B.d_mode_evals, ev.size() * 4, cudaMemcpyDeviceToHost));
+  std::vector<std::pair<double, WorkItem>> key;
+  key.reserve(B.nitems);
+  for (const WorkItem& w : B.h_items_grp) {
+    const CambGpuTables& t = *B.views[w.cosmo];
+    const CambGpuModeSpec& ms = t.modes[w.mode];
+    double nv = 4 + (ms.lmaxg + 1) + (ms.lmaxnr + 1) + ms.lmaxgpol - 1;
+    if (t.nu_eig > 0) nv += (ms.lmaxnu + 1) * (1 + t.nu_eig * t.nqmax);
+    key.push_back({(double)ev[B.mode_base[w.cosmo] + w.mode] * nv, w});
+  }
+  std::stable_sort(key.begin(), key.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+  for (int i = 0; i < B.nitems; ++i) B.h_items_cost[i] = key[i].second;
+  CUDA_TRY(cudaMemcpy(B.d_items_cost, B.h_items_cost.data(), (size_t)B.nitems * sizeof(WorkItem),
+                      cudaMemcpyHostToDevice));
+  B.cost_order = true;
+  return 0;
+}
+
 // under stream capture the stage boundaries are external event records, so that in the
 // graph they stay event-record nodes the host can time and wait on
 int enqueue_all(Batch& B, bool do_ode, bool do_los, bool do_cls, bool capturing) {
@@ -898,6 +937,10 @@ int capture_graph(Batch& B, bool do_ode, bool do_los, bool do_cls, long long key
 
 int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
   cudaStream_t s = g_rt.stream;
+  if (do_ode && B.costs_valid && !B.cost_order && ode_order(B) == 3) {
+    int rc = build_cost_order(B);  // outside any capture: a synchronous copy each way
+    if (rc) return rc;
+  }
   if (B.runs == 0) {
     int rc = enqueue_all(B, do_ode, do_los, do_cls, false);
     if (rc) return rc;
@@ -912,6 +955,7 @@ int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
   }
   B.runs++;
   CUDA_TRY(cudaEventSynchronize(g_rt.ev[3]));
+  if (do_ode) B.costs_valid = true;
   g_timings[0] = elapsed(g_rt.ev[0], g_rt.ev[1]);
   g_timings[1] = 0;
   g_timings[2] = elapsed(g_rt.ev[1], g_rt.ev[2]);
@@ -1363,8 +1407,8 @@ int cambgpu_set_ode_team(int lanes) {
 }
 
 int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm) {
-  if (queue_order < -1 || queue_order > 2 || blocks_per_sm < 0)
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "queue order must be -1..2 and blocks per SM >= 0");
+  if (queue_order < -1 || queue_order > 3 || blocks_per_sm < 0)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "queue order must be -1..3 and blocks per SM >= 0");
   g_order = queue_order;
   g_blocks_cap = blocks_per_sm;
   return 0;
@@ -1382,7 +1426,7 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   // registers (massless layout), 6 = warp per mode with shared-memory rows, 1/2/3 = thread
   // per mode compiled for 3/4/5 resident blocks per SM (cap 0: that many; 2: two, so that
   // threads finishing early take the queue's remaining modes)
-  static const int cand[][3] = {{32, 0, 0}, {1, 0, 0}, {1, 2, 0}, {2, 2, 0}, {3, 2, 0},
+  static const int cand[][3] = {{32, 0, 0}, {1, 0, 0}, {1, 2, 0}, {2, 2, 0}, {1, 3, 2},
                                 {1, 2, 2}, {2, 2, 2}, {1, 1, 2}, {6, 0, 0}};
   const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
   int rc = cambgpu_batch_prepare(p, n);

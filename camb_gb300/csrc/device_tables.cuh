@@ -59,6 +59,7 @@ struct DevCosmo {
   double hubble_h, late_phot_boost_min;
   int* status;         // per-cosmology status word
   unsigned long long* evals;  // derivative evaluations (shared counter)
+  unsigned* mode_evals;       // [nk] evaluations of each mode in the last run (queue ordering)
   // integration grid and l sampling
   const double* q_int;
   const double* dq_int;

@@ -762,7 +762,10 @@ __device__ void evolve_mode(const DevCosmo& C, int q_ix, const Team<T>& tm) {
       for (int s = 0; s < nsrc; ++s) out[((size_t)j * nsrc + s) * nk + q_ix] = so.s[s];
     }
   }
-  if (tm.t == 0) atomicAdd(C.evals, (unsigned long long)rk.evals);
+  if (tm.t == 0) {
+    atomicAdd(C.evals, (unsigned long long)rk.evals);
+    if (C.mode_evals) C.mode_evals[q_ix] = (unsigned)rk.evals;
+  }
 }
 
 template <int T>
@@ -2028,6 +2031,7 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
         if (leader) {
           if (R.status) atomicExch(C.status, R.status);
           atomicAdd(C.evals, (unsigned long long)R.evals);
+          if (C.mode_evals) C.mode_evals[q_ix] = (unsigned)R.evals;
         }
         R.active = false;
       }

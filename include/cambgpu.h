@@ -287,7 +287,9 @@ int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm);
 /* In-library autotuner: times ODE variants, work-queue orders and resident-block caps on
  * n cosmologies and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
  * 1 = increasing q, 2 = bands of q with the cosmologies of each band ordered by neutrino
- * mass.  best = [team, order, class, cap]; times (optional, >= 9 entries) receives ms per
+ * mass, 3 = decreasing cost measured by the batch's previous run (evaluations x system
+ * size; order 2 until a run has recorded it).  best = [team, order, class, cap]; times
+ * (optional, >= 9 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch call, in ms:

@@ -170,3 +170,28 @@ def test_results_stream_matches_blocking_calls():
     it = results.get_results_stream(batches)
     next(it)
     it.close()  # the second batch was being prepared: it is freed, nothing leaks or faults
+
+
+def test_queue_orders_and_caps_give_identical_results():
+    """Every k-mode is integrated independently, so the work-queue order (including the
+    measured-cost order built from the previous run) and the resident-block cap change
+    only the schedule, never a bit of the spectra."""
+    ps = draws(3, seed=5, lmax=500, mnu_max=0.1)
+    arr = (_lib.CambGpuParams * len(ps))(*ps)
+    lib = _lib.load()
+    _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
+    outs = []
+    try:
+        for team, order, cap in [(1, 0, 0), (1, 2, 2), (1, 3, 2), (1, 3, 1), (2, 1, 0)]:
+            _lib.check(lib.cambgpu_set_ode_team(team))
+            _lib.check(lib.cambgpu_set_ode_launch(order, cap))
+            _lib.check(lib.cambgpu_batch_run(None))
+            cls = np.zeros((len(ps), 501, 4))
+            _lib.check(lib.cambgpu_batch_fetch(500, _lib.dptr(cls)))
+            outs.append(cls)
+    finally:
+        lib.cambgpu_set_ode_team(0)
+        lib.cambgpu_set_ode_launch(-1, 0)
+        lib.cambgpu_batch_release()
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
