@@ -52,10 +52,11 @@ def parse():
                     help="instead of the headline run: N lensed draws (lmax 2500 + 200 margin) through the FP64 "
                          "and the mixed-precision projection, device time per form and the mixed form's C_l "
                          "error against FP64 per l band")
-    ap.add_argument("--kernel-case", choices=["warp1", "thread8", "thread96", "thread256"],
+    ap.add_argument("--kernel-case", choices=["warp1", "thread8", "thread96", "thread128", "thread256"],
                     help="profiling driver: prepare one fixed case, run the device pipeline 4 times, print the "
                          "last ODE time and exit (warp1: one massless lmax-1000 cosmology, warp per mode; "
-                         "thread8 / thread96 / thread256: 8 / 96 / 256 draws of the workload, thread per mode)")
+                         "thread8 / thread96 / thread128 / thread256: 8 / 96 / 128 / 256 draws of the workload, "
+                         "thread per mode)")
     return ap.parse_args()
 
 
@@ -181,8 +182,8 @@ def kernel_case(name):
         ps, team, order, cap = [p], 6, -1, 0
     elif name == "thread8":
         ps, team, order, cap = workload(8, 2500, seed=7), 2, -1, 0
-    elif name == "thread96":
-        ps, team, order, cap = workload(96, 2500, seed=1000), 1, 2, 2
+    elif name in ("thread96", "thread128"):
+        ps, team, order, cap = workload(int(name[6:]), 2500, seed=1000), 1, 2, 2
     else:
         ps, team, order, cap = workload(256, 2500, seed=1000), 1, 2, 2
     arr = (_lib.CambGpuParams * len(ps))(*ps)
