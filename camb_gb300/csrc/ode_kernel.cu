@@ -2105,8 +2105,29 @@ int ode_blocks_per_sm(int team, int threads, int warp_stride) {
   return per_sm;
 }
 
+// The thread-per-mode kernels use no shared memory: the whole of the SM's L1/shared
+// array goes to L1, which caches the stage rows held in local memory.
+template <int MINB, bool TR>
+void prefer_l1() {
+  cudaFuncSetAttribute(tpm::ode_thread_kernel<MINB, TR>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       (int)cudaSharedmemCarveoutMaxL1);
+}
+
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
                               const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride) {
+  static const bool carve = [] {
+    prefer_l1<3, false>();
+    prefer_l1<4, false>();
+    prefer_l1<5, false>();
+    prefer_l1<6, false>();
+    prefer_l1<8, false>();
+    prefer_l1<3, true>();
+    prefer_l1<4, true>();
+    prefer_l1<5, true>();
+    cudaGetLastError();  // a hint: a refusal leaves the default split
+    return true;
+  }();
+  (void)carve;
   if (team == 6) {  // warp per mode (any layout), one warp per block
     const size_t smem = tpm::warp_smem_bytes(warp_stride);
     if (transfer) tpm::ode_warp_kernel<true><<<blocks, 32, smem, s>>>(cosmos, items, nitems, counter, warp_stride);
