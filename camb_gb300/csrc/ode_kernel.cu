@@ -1256,6 +1256,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
       if constexpr (W == 1) {
         // one read of each entry: the neighbours travel in registers
         double ym = pig, y0 = g3v;
+#pragma unroll 4
         for (int l = 3; l < lg; ++l) {
           const double yp = y[g + l + 1];
           dy[g + l] = k * (__ldg(ra + l) * ym - __ldg(rb + l) * yp) - opac * y0;
@@ -1267,6 +1268,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
         dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * p3v;
         ym = E2;
         y0 = p3v;
+#pragma unroll 4
         for (int l = 3; l < lp; ++l) {
           const double yp = y[pol + l + 1];
           dy[pol + l] = -opac * y0 + k * (__ldg(ra + l) * ym - __ldg(rp + l) * yp);
@@ -1300,6 +1302,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
       const int ln = M.lmaxnr;
       if constexpr (W == 1) {
         double ym = pir, y0 = n3v;
+#pragma unroll 4
         for (int l = 3; l < ln; ++l) {
           const double yp = y[r + l + 1];
           dy[r + l] = k * (__ldg(ra + l) * ym - __ldg(rb + l) * yp);
@@ -1338,6 +1341,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
           const double y3v = y[ind + 3];
           dy[ind + 2] = vk * (0.4 * y1v - 0.6 * y3v) + k * 8.0 / 15.0 * sigma;
           double ym = y2v, yc = y3v;
+#pragma unroll 4
           for (int l = 3; l < lt; ++l) {
             const double yp = y[ind + l + 1];
             dy[ind + l] = vk * (__ldg(ra + l) * ym - __ldg(rb + l) * yp);
@@ -1376,6 +1380,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
     if constexpr (W == 1) {
       double pm = y[p0], pc = y[p0 + 1], rm = y[r], rc = y[r + 1];
       dy[p0] = k * a2 * qr - k * pc;
+#pragma unroll 4
       for (int l = 1; l < lp; ++l) {
         const double rpv = y[r + l + 1], pp = y[p0 + l + 1];
         const double al = __ldg(ra + l), bl = __ldg(rb + l);
