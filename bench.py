@@ -60,6 +60,31 @@ def parse():
     return ap.parse_args()
 
 
+# the benchmark's metric: `value` is the batched cosmologies/s (unlensed scalar TT/EE/TE);
+# the line also carries the plain GPU form ("batched_vs_plain_gpu") and grads/s ("gradients")
+METRIC = "cosmologies/s to l=2500 at <=1e-4 rel C_l err, batched vs plain GPU; grads/s"
+
+
+def plain_form_rate(n=3, lmax=2500, seed=1000, mnu_max=0.2):
+    """The plain GPU form: one cosmology per blocking call, FP64 throughout (no mixed
+    precision), draws of the same workload, host tables and copies included."""
+    from camb_gb300 import _lib
+    lib = _lib.load()
+    ps = workload(n + 1, lmax, seed=seed, mnu_max=mnu_max)
+    old = lib.cambgpu_get_precision()
+    _lib.check(lib.cambgpu_set_precision(0))
+    cls = np.zeros((lmax + 1, 4))
+    try:
+        _lib.check(lib.cambgpu_get_results(C.byref(ps[0]), lmax, _lib.dptr(cls)))
+        t0 = time.perf_counter()
+        for p in ps[1:]:
+            _lib.check(lib.cambgpu_get_results(C.byref(p), lmax, _lib.dptr(cls)))
+        t = time.perf_counter() - t0
+    finally:
+        lib.cambgpu_set_precision(old)
+    return n / t
+
+
 # DRAM bytes (read + write) of one ODE launch of the headline workload, from the ncu
 # capture summarised in profiles/ode_thread_kernel_dram_batch256_lmax2500.md
 ODE_TRAFFIC_BYTES = 1.10e12 + 0.493e12
@@ -416,7 +441,7 @@ def run_reference(args, rank, world):
     times = [cpu_reference(ps, nth) for _ in range(args.steps)]
     t = statistics.mean(times)
     v = len(ps) / t
-    line = {"impl": "reference", "metric": "cosmologies/s to l=2500 at <=1e-4 rel C_l err (unlensed scalar TT/EE/TE)",
+    line = {"impl": "reference", "metric": METRIC,
             "value": v,
             "unit": "cosmologies/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -534,7 +559,7 @@ def main():
     achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
     prec = {0: "FP64 throughout",
             1: "FP64 ODE, source k-spline, C_l integral; FP32 line-of-sight projection with FP64 chunk sums"}
-    line = {"metric": "cosmologies/s to l=2500 at <=1e-4 rel C_l err (unlensed scalar TT/EE/TE)", "value": value,
+    line = {"metric": METRIC, "value": value,
             "unit": "cosmologies/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == 0 else "f64+f32", "data": "synthetic seeded draws",
@@ -577,6 +602,11 @@ def main():
         line["accuracy"] = accuracy_vs_fp64(cps, ref, args.lmax)  # timed form vs the FP64 CPU restatement
         line["single_cosmology_configs"] = single_configs(nth)
         line["gradients"] = gradient_rate()
+        plain = plain_form_rate(mnu_max=args.mnu_max)
+        line["batched_vs_plain_gpu"] = {
+            "plain_fp64_gpu_cosmologies_per_s": plain,
+            "plain_form": "one cosmology per blocking C-ABI call, FP64 throughout, same workload, host tables included",
+            "ratio_value": line["value"] / plain, "ratio_e2e": line["e2e"]["value"] / plain}
         line["cpu_baseline"] = {"value": len(cps) / t, "unit": "cosmologies/s", "cores": nth, "kind": "port",
                                 "sample": f"{len(cps)} draws of the same workload, host tables + ODE + LOS + C_l"}
         print(json.dumps(line))
