@@ -1,0 +1,32 @@
+// Instantiates thread-per-mode ODE kernel variants (see ode_device.cuh); one translation
+// unit per few variants so that the library compiles in parallel.
+#include "ode_device.cuh"
+
+namespace cgdev {
+
+int occ_thread5(bool transfer, int threads) {
+  int per_sm = 0;
+  if (transfer) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<5, true>, threads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tpm::ode_thread_kernel<5, false>, threads, 0);
+  return per_sm;
+}
+
+cudaError_t launch_thread5(bool transfer, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
+                       const WorkItem* items, int nitems, int* counter) {
+  // no shared memory: the whole of the SM's L1/shared array goes to L1, which caches the
+  // stage rows held in local memory (a hint; a refusal leaves the default split)
+  static const bool carve = [] {
+    cudaFuncSetAttribute(tpm::ode_thread_kernel<5, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxL1);
+    cudaFuncSetAttribute(tpm::ode_thread_kernel<5, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxL1);
+    cudaGetLastError();
+    return true;
+  }();
+  (void)carve;
+  if (transfer) tpm::ode_thread_kernel<5, true><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  else tpm::ode_thread_kernel<5, false><<<blocks, threads, 0, s>>>(cosmos, items, nitems, counter);
+  return cudaGetLastError();
+}
+
+}  // namespace cgdev
