@@ -1,0 +1,46 @@
+"""Host-only entry points of the C ABI on CPU (no device call is made): building a batch's
+host tables ahead of its device run, error codes and per-cosmology status for invalid
+parameters, and the argument checks of the ODE controls."""
+import ctypes as C
+
+import numpy as np
+
+from camb_gb300 import _lib
+from tests.cosmologies import draws, fiducial
+
+
+def test_prepare_tables_builds_and_frees(lib):
+    ps = draws(3, seed=3, lmax=500, mnu_max=0.1)
+    arr = (_lib.CambGpuParams * len(ps))(*ps)
+    h = C.c_void_p()
+    st = np.full(len(ps), -1, dtype=np.int32)
+    _lib.check(lib.cambgpu_prepare_tables(arr, len(ps), C.byref(h), _lib.iptr(st)))
+    assert h.value and not st.any()
+    lib.cambgpu_free_prepared(h)
+
+
+def test_prepare_tables_reports_bad_members(lib):
+    bad = fiducial(500)
+    bad.omk = 0.05  # curved: not part of the flat path
+    ps = [fiducial(500), bad]
+    arr = (_lib.CambGpuParams * 2)(*ps)
+    h = C.c_void_p()
+    st = np.zeros(2, dtype=np.int32)
+    rc = lib.cambgpu_prepare_tables(arr, 2, C.byref(h), _lib.iptr(st))
+    assert rc == 2 and not h.value
+    assert st[0] == 0 and st[1] == 2
+    assert lib.cambgpu_last_error()
+    assert lib.cambgpu_prepare_tables(arr, 0, C.byref(h), None) == 2
+    # the device half refuses a missing batch before touching the device
+    assert lib.cambgpu_get_spectra_prepared(None, 500, None, None, None, None, None) == 2
+
+
+def test_ode_controls_validate_arguments(lib):
+    assert lib.cambgpu_set_ode_team(7) == 2
+    assert lib.cambgpu_set_ode_team(-1) == 2
+    assert lib.cambgpu_set_ode_launch(4, 0) == 2
+    assert lib.cambgpu_set_ode_launch(2, -1) == 2
+    for team in (0, 1, 5, 6, 8, 16, 32):
+        assert lib.cambgpu_set_ode_team(team) == 0
+    assert lib.cambgpu_set_ode_launch(3, 2) == 0
+    assert lib.cambgpu_set_ode_team(0) == 0 and lib.cambgpu_set_ode_launch(-1, 0) == 0
