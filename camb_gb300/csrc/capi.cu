@@ -542,6 +542,7 @@ struct Batch {
   // repeated runs of a resident batch replay the stage sequence as a CUDA graph,
   // captured on the second run (the first one allocates the lazily built device tables)
   int runs = 0;
+  unsigned long staged_epoch = 0;  // the arena holds this batch while no later staging happened
   long long graph_key = -1;
   cudaGraphExec_t graph = nullptr;
   long long graph_launches = 0;
@@ -551,6 +552,7 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   int rc = rt_init();
   if (rc) return rc;
   ++g_rt.epoch;
+  B.staged_epoch = g_rt.epoch;
   int n = (int)B.views.size();
   size_t total = 0;
   for (auto* v : B.views) total += bytes_for(*v);
@@ -1328,6 +1330,15 @@ int cambgpu_get_results(const CambGpuParams* p, int lmax_out, double* cl_out) {
 }
 
 // ---- resident batch (bench path: inputs staged in HBM before timing) ----
+// Any later staging (a one-shot call, a transfer batch) reuses the device arena, so the
+// resident batch is only usable while it is the last one staged.
+int resident_check() {
+  if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
+  if (g_res->B.staged_epoch != g_rt.epoch)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "the resident batch was replaced by a later staging");
+  return 0;
+}
+
 int cambgpu_batch_prepare(const CambGpuParams* p, int n) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_res.reset(new Resident());
@@ -1342,7 +1353,7 @@ int cambgpu_batch_prepare(const CambGpuParams* p, int n) {
 
 int cambgpu_batch_run(double* ms3) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
+  if (int rc = resident_check()) return rc;
   int rc = run_all(g_res->B, true, true, true);
   if (rc) return rc;
   if (ms3) { ms3[0] = g_timings[0]; ms3[1] = g_timings[2]; ms3[2] = g_timings[3]; }
@@ -1351,7 +1362,7 @@ int cambgpu_batch_run(double* ms3) {
 
 int cambgpu_batch_fetch(int lmax_out, double* cl_out) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
+  if (int rc = resident_check()) return rc;
   return fetch_spectra(g_res->B, lmax_out, cl_out, nullptr, nullptr);
 }
 
@@ -1359,7 +1370,7 @@ int cambgpu_batch_spectra_from_transfer(const double* As, const double* ns, cons
                                         const double* pivot_scalar, int lmax_out, double* unlensed, double* lensed,
                                         double* lens_potential, int* lmax_lensed) {
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_res) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "no resident batch");
+  if (int rc = resident_check()) return rc;
   Batch& B = g_res->B;
   const int n = (int)B.views.size();
   if (As || ns || nrun || pivot_scalar) {

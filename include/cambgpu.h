@@ -250,7 +250,8 @@ int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float*
 int cambgpu_lensing_range(const CambGpuTables* t, int* out3);
 
 /* ---- resident batch: tables staged in device memory once, then timed runs ---- */
-/* Builds and uploads n cosmologies; the batch stays resident until released. */
+/* Builds and uploads n cosmologies; the batch stays resident until released or until
+ * another call stages a batch (the arena is shared): the calls below then return 2. */
 int cambgpu_batch_prepare(const CambGpuParams* p, int n);
 /* Runs ODE, source spline + LOS, C_l on the resident batch; ms3 = device ms per stage. */
 int cambgpu_batch_run(double* ms3);

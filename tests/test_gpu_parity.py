@@ -2,6 +2,8 @@
 inputs.  Tolerances: transfer functions Delta_l(k) within 1e-6 relative and C_l
 within 1e-5 relative (the plain FP64 GPU form); sources per k-mode within 1e-6 of
 their peak."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -195,3 +197,25 @@ def test_queue_orders_and_caps_give_identical_results():
         lib.cambgpu_batch_release()
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+def test_resident_batch_refuses_after_a_later_staging():
+    """A one-shot call reuses the device arena: the resident batch then reports an error
+    instead of computing on overwritten tables, and the library stays usable."""
+    ps = draws(2, seed=9, lmax=400)
+    arr = (_lib.CambGpuParams * len(ps))(*ps)
+    lib = _lib.load()
+    _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
+    try:
+        _lib.check(lib.cambgpu_batch_run(None))
+        cls = np.zeros((401, 4))
+        one = fiducial(400)
+        _lib.check(lib.cambgpu_get_results(C.byref(one), 400, _lib.dptr(cls)))
+        assert lib.cambgpu_batch_run(None) == 2
+        out = np.zeros((len(ps), 401, 4))
+        assert lib.cambgpu_batch_fetch(400, _lib.dptr(out)) == 2
+    finally:
+        lib.cambgpu_batch_release()
+    _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
+    _lib.check(lib.cambgpu_batch_run(None))
+    lib.cambgpu_batch_release()
