@@ -271,9 +271,11 @@ void cambgpu_batch_release(void);
 /* Arithmetic of the line-of-sight projection (no counterpart in the reference, which is
  * FP64 throughout).  0 (default): FP64 everywhere -- the plain form whose transfer
  * functions and C_l match the reference's algorithm to rounding.  1: mixed precision --
- * Bessel interpolation and source products in FP32, summed in FP32 over 16 time steps
- * per lane and accumulated in FP64; the ODE, source k-spline, Bessel interval search,
- * Limber branch, C_l k-integral, interpolation and lensing stay FP64. */
+ * the staged sources (an FP32 copy of the source k-spline), the Bessel weights, the
+ * Bessel table and the products in FP32, summed in FP32 over 16 time steps per lane and
+ * accumulated as compensated FP32 pairs, converted to FP64 once per (q, l); the ODE, the
+ * spline itself, the window set-up, the Limber branch, the C_l k-integral, interpolation
+ * and lensing stay FP64.  C_l agree with the FP64 form to ~1e-6. */
 int cambgpu_set_precision(int mode);
 int cambgpu_get_precision(void);
 /* ODE kernel variant: 32/16/8 = lanes per k-mode with the state in registers (massless
@@ -293,8 +295,10 @@ int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm);
  * (optional, >= 9 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
-/* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch call, in ms:
- * [host tables, staging (pinned copy + uploads enqueued), device pipeline, packing + D2H]. */
+/* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch /
+ * get_spectra_prepared call, in ms: [host tables (for a prepared batch: its
+ * cambgpu_prepare_tables), staging (pinned copy + uploads enqueued), device pipeline,
+ * packing + D2H]. */
 int cambgpu_last_host_timings(double* out4);
 /* Kernel timing of the last GPU call, in ms: [ode, spline, los, cls, h2d, d2h]. */
 int cambgpu_last_timings(double* out6);
@@ -306,6 +310,7 @@ int cambgpu_last_transfer_bytes(long long* out2);
 int cambgpu_probe_fp64_tflops(double* tflops);
 /* Number of kernels the library launched since the counter was reset. */
 long long cambgpu_kernel_launches(int reset);
+/* Message of the calling thread's last error (empty if none). */
 const char* cambgpu_last_error(void);
 
 #ifdef __cplusplus
