@@ -676,20 +676,27 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   // neutrino mass, so that a warp's 32 modes share hierarchy sizes and switch sequences
   B.h_items_grp = items;
   {
-    auto band = [&](const WorkItem& w) { return (long)std::floor(std::log(B.views[w.cosmo]->q_evolve[w.mode]) * 64); };
-    auto mass = [&](const WorkItem& w) {
-      const CambGpuTables* v = B.views[w.cosmo];
-      double m = 0;
-      for (int i = 0; i < v->nu_eig; ++i) m += v->nu_masses[i];
-      return m;
+    // sort keys formed once per item (band of q, total neutrino mass, q), not per comparison
+    struct Key {
+      long band;
+      double mass, q;
+      WorkItem w;
     };
-    std::stable_sort(B.h_items_grp.begin(), B.h_items_grp.end(), [&](const WorkItem& a, const WorkItem& b) {
-      long ba = band(a), bb = band(b);
-      if (ba != bb) return ba > bb;
-      double ma = mass(a), mb = mass(b);
-      if (ma != mb) return ma < mb;
-      return B.views[a.cosmo]->q_evolve[a.mode] > B.views[b.cosmo]->q_evolve[b.mode];
+    std::vector<double> mass(n, 0.0);
+    for (int c = 0; c < n; ++c)
+      for (int i = 0; i < B.views[c]->nu_eig; ++i) mass[c] += B.views[c]->nu_masses[i];
+    std::vector<Key> keys;
+    keys.reserve(items.size());
+    for (const WorkItem& w : items) {
+      const double q = B.views[w.cosmo]->q_evolve[w.mode];
+      keys.push_back({(long)std::floor(std::log(q) * 64), mass[w.cosmo], q, w});
+    }
+    std::stable_sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
+      if (a.band != b.band) return a.band > b.band;
+      if (a.mass != b.mass) return a.mass < b.mass;
+      return a.q > b.q;
     });
+    for (size_t i = 0; i < keys.size(); ++i) B.h_items_grp[i] = keys[i].w;
   }
   B.d_items_grp = g_rt.arena.take<WorkItem>(items.size());
   copies.push_back({B.d_items_grp, {B.h_items_grp.data(), items.size() * sizeof(WorkItem)}});
