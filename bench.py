@@ -478,11 +478,12 @@ def main():
     tuned = None
     if not args.team and not args.no_autotune:
         best = (C.c_int * 4)()
-        times = np.zeros(9)
+        times = np.zeros(11)
         _lib.check(lib.cambgpu_autotune_ode(arr, B, best, _lib.dptr(times)))
         tuned = {"team": best[0], "queue_order": best[1], "blocks_per_sm_cap": best[3],
-                 "candidates": "team,order,blocks-per-SM cap: 32,0,0 1,0,0 1,2,0 2,2,0 1,3,2 1,2,2 2,2,2 1,1,2 6,0,0",
-                 "candidate_ode_ms": [round(x, 2) for x in times[:9]]}
+                 "candidates": "team,order,blocks-per-SM cap: 32,0,0 1,0,0 1,2,0 2,2,0 1,3,2 1,2,2 2,2,2 1,1,2 6,0,0 "
+                               "7,2,0 7,3,0",
+                 "candidate_ode_ms": [round(x, 2) for x in times[:11]]}
     # ---- device-resident pipeline, FP64 form then mixed precision ----
     _lib.check(lib.cambgpu_batch_prepare(arr, B))
 

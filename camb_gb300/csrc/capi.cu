@@ -781,7 +781,7 @@ int run_ode(Batch& B) {
   CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
   int team = pick_team(B);
   int order = ode_order(B);
-  const int lanes = team <= 5 ? 1 : team == 6 ? 32 : team;
+  const int lanes = (team <= 5 || team == 7) ? 1 : team == 6 ? 32 : team;
   // Few modes (a single cosmology): one warp per block, so that the warps spread over the
   // SMs and none shares an SM's FP64 pipe; otherwise blocks of 128.  The shared-memory
   // warp kernel always runs one warp per block.
@@ -1418,8 +1418,8 @@ int cambgpu_set_precision(int mode) {
 int cambgpu_get_precision(void) { return g_precision; }
 
 int cambgpu_set_ode_team(int lanes) {
-  if (lanes < 0 || (lanes > 6 && lanes != 8 && lanes != 16 && lanes != 32))
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team code must be 0-6, 8, 16 or 32");
+  if (lanes < 0 || (lanes > 8 && lanes != 16 && lanes != 32))
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "team code must be 0-8, 16 or 32");
   g_team = lanes;
   return 0;
 }
@@ -1443,9 +1443,10 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   // candidates: (team code, queue order, resident-block cap); team 32 = warp per mode with
   // registers (massless layout), 6 = warp per mode with shared-memory rows, 1/2/3 = thread
   // per mode compiled for 3/4/5 resident blocks per SM (cap 0: that many; 2: two, so that
-  // threads finishing early take the queue's remaining modes)
+  // threads finishing early take the queue's remaining modes), 7 = thread per mode compiled
+  // for 2 resident blocks (more registers per thread, CMB sources only)
   static const int cand[][3] = {{32, 0, 0}, {1, 0, 0}, {1, 2, 0}, {2, 2, 0}, {1, 3, 2},
-                                {1, 2, 2}, {2, 2, 2}, {1, 1, 2}, {6, 0, 0}};
+                                {1, 2, 2}, {2, 2, 2}, {1, 1, 2}, {6, 0, 0}, {7, 2, 0}, {7, 3, 0}};
   const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
   int rc = cambgpu_batch_prepare(p, n);
   if (rc) return rc;
@@ -1460,6 +1461,7 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
     // the shared-memory warp kernel is the latency choice for few modes; on large batches
     // its redundant per-lane scalar work loses to thread per mode several times over
     if (cand[c][0] == 6 && (B.warp_stride > kWarpStrideMax || size_class(B) == 1)) continue;
+    if (cand[c][0] == 7 && B.transfer) continue;  // compiled for CMB sources only
     g_team = cand[c][0];
     g_order = cand[c][1];
     g_blocks_cap = cand[c][2];

@@ -6,12 +6,14 @@
 
 namespace cgdev {
 
+int occ_thread2(bool transfer, int threads);
 int occ_thread3(bool transfer, int threads);
 int occ_thread4(bool transfer, int threads);
 int occ_thread5(bool transfer, int threads);
 int occ_thread6(bool transfer, int threads);
 int occ_thread8(bool transfer, int threads);
 int occ_warp(int team, int threads, int warp_stride);
+cudaError_t launch_thread2(bool, int, int, cudaStream_t, const DevCosmo*, const WorkItem*, int, int*);
 cudaError_t launch_thread3(bool, int, int, cudaStream_t, const DevCosmo*, const WorkItem*, int, int*);
 cudaError_t launch_thread4(bool, int, int, cudaStream_t, const DevCosmo*, const WorkItem*, int, int*);
 cudaError_t launch_thread5(bool, int, int, cudaStream_t, const DevCosmo*, const WorkItem*, int, int*);
@@ -41,8 +43,9 @@ cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, c
   return cudaGetLastError();
 }
 
-// team 1..5 = thread per mode compiled for 3/4/5/6/8 resident blocks of 128 per SM;
-// 6 = warp per mode with shared-memory rows; 8/16/32 = register-resident warp teams
+// team 1..5 = thread per mode compiled for 3/4/5/6/8 resident blocks of 128 per SM, 7 =
+// the same for 2 blocks; 6 = warp per mode with shared-memory rows; 8/16/32 =
+// register-resident warp teams
 int ode_blocks_per_sm(int team, int threads, int warp_stride) {
   switch (team) {
     case 1: return occ_thread3(false, threads);
@@ -50,6 +53,7 @@ int ode_blocks_per_sm(int team, int threads, int warp_stride) {
     case 3: return occ_thread5(false, threads);
     case 4: return occ_thread6(false, threads);
     case 5: return occ_thread8(false, threads);
+    case 7: return occ_thread2(false, threads);
     default: return occ_warp(team, threads, warp_stride);
   }
 }
@@ -57,13 +61,14 @@ int ode_blocks_per_sm(int team, int threads, int warp_stride) {
 cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s, const DevCosmo* cosmos,
                               const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride) {
   // transfer functions are compiled for 3/4/5 resident blocks only: other thread teams use 4
-  if (transfer && team != 1 && team != 3 && team <= 5) team = 2;
+  if (transfer && team != 1 && team != 3 && (team <= 5 || team == 7)) team = 2;
   switch (team) {
     case 1: return launch_thread3(transfer, blocks, threads, s, cosmos, items, nitems, counter);
     case 2: return launch_thread4(transfer, blocks, threads, s, cosmos, items, nitems, counter);
     case 3: return launch_thread5(transfer, blocks, threads, s, cosmos, items, nitems, counter);
     case 4: return launch_thread6(transfer, blocks, threads, s, cosmos, items, nitems, counter);
     case 5: return launch_thread8(transfer, blocks, threads, s, cosmos, items, nitems, counter);
+    case 7: return launch_thread2(transfer, blocks, threads, s, cosmos, items, nitems, counter);
     default: return launch_warp(team, transfer, blocks, threads, s, cosmos, items, nitems, counter, warp_stride);
   }
 }

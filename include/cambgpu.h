@@ -281,7 +281,9 @@ int cambgpu_get_precision(void);
 /* ODE kernel variant: 32/16/8 = lanes per k-mode with the state in registers (massless
  * neutrinos, CMB sources); 6 = one warp per k-mode with the state rows in shared memory
  * (any layout: massive neutrinos, transfer functions); 1/2/3/4/5 = one thread per k-mode
- * compiled for 3/4/5/6/8 resident blocks of 128 per SM; 0 = the autotuned choice. */
+ * compiled for 3/4/5/6/8 resident blocks of 128 per SM; 7 = one thread per k-mode compiled
+ * for 2 resident blocks (CMB sources; transfer-function runs fall back to 2); 0 = the
+ * autotuned choice. */
 int cambgpu_set_ode_team(int lanes_per_mode);
 /* ODE launch shape: queue order (-1 = the autotuned one, else as for the autotuner) and a
  * cap on resident threads per SM in units of 128 (0 = as many as fit; a lower cap leaves
@@ -292,7 +294,7 @@ int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm);
  * 1 = increasing q, 2 = bands of q with the cosmologies of each band ordered by neutrino
  * mass, 3 = decreasing cost measured by the batch's previous run (evaluations x system
  * size; order 2 until a run has recorded it).  best = [team, order, class, cap]; times
- * (optional, >= 9 entries) receives ms per
+ * (optional, >= 11 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch /

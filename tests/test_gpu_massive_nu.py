@@ -45,7 +45,7 @@ def with_team(team, f):
         lib.cambgpu_set_ode_team(0)
 
 
-@pytest.mark.parametrize("team", [0, 6, 2])
+@pytest.mark.parametrize("team", [0, 6, 2, 7])
 def test_sources_parity_006ev(planck, team):
     """Autotuned choice, warp per mode (shared-memory rows), thread per mode."""
     T, src = planck

@@ -104,7 +104,7 @@ def test_batch_of_ragged_cosmologies_matches_oracle():
     assert len(sizes) > 1
 
 
-@pytest.mark.parametrize("team", [32, 16, 8, 6, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("team", [32, 16, 8, 6, 1, 2, 3, 4, 5, 7])
 def test_team_sizes_agree(fid, team):
     T, src, _, _ = fid
     lib = _lib.load()
