@@ -52,11 +52,13 @@ def parse():
                     help="instead of the headline run: N lensed draws (lmax 2500 + 200 margin) through the FP64 "
                          "and the mixed-precision projection, device time per form and the mixed form's C_l "
                          "error against FP64 per l band")
-    ap.add_argument("--kernel-case", choices=["warp1", "thread8", "thread96", "thread128", "thread256"],
+    ap.add_argument("--kernel-case", choices=["warp1", "thread8", "thread96", "thread128", "thread256",
+                                              "thread256r"],
                     help="profiling driver: prepare one fixed case, run the device pipeline 4 times, print the "
                          "last ODE time and exit (warp1: one massless lmax-1000 cosmology, warp per mode; "
                          "thread8 / thread96 / thread128 / thread256: 8 / 96 / 128 / 256 draws of the workload, "
-                         "thread per mode)")
+                         "thread per mode; thread256r: the 256 draws on the variant compiled for two resident "
+                         "blocks per SM)")
     return ap.parse_args()
 
 
@@ -85,9 +87,17 @@ def plain_form_rate(n=3, lmax=2500, seed=1000, mnu_max=0.2):
     return n / t
 
 
-# DRAM bytes (read + write) of one ODE launch of the headline workload, from the ncu
-# capture summarised in profiles/ode_thread_kernel_dram_batch256_lmax2500.md
-ODE_TRAFFIC_BYTES = 1.10e12 + 0.493e12
+# DRAM bytes (read + write) of one ODE launch of the headline workload per thread-per-mode
+# variant (team code), from the ncu captures summarised in
+# profiles/ode_thread_kernel_dram_batch256_lmax2500.md
+ODE_TRAFFIC = {
+    7: (0.8307e12 + 0.4565e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
+                               "(team 7: compiled for 2 resident blocks/SM, queue order 2), "
+                               "profiles/ode_thread_kernel_dram_batch256_lmax2500.md"),
+    1: (1.10e12 + 0.493e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
+                            "(team 1, queue order 2, 2 blocks/SM), "
+                            "profiles/ode_thread_kernel_dram_batch256_lmax2500.md"),
+}
 
 
 def hbm_peak():
@@ -209,6 +219,8 @@ def kernel_case(name):
         ps, team, order, cap = workload(8, 2500, seed=7), 2, -1, 0
     elif name in ("thread96", "thread128"):
         ps, team, order, cap = workload(int(name[6:]), 2500, seed=1000), 1, 2, 2
+    elif name == "thread256r":
+        ps, team, order, cap = workload(256, 2500, seed=1000), 7, 2, 0
     else:
         ps, team, order, cap = workload(256, 2500, seed=1000), 1, 2, 2
     arr = (_lib.CambGpuParams * len(ps))(*ps)
@@ -558,6 +570,8 @@ def main():
     # this workload (mnu 0-0.2 eV, lmax 2500), profiles/ode_thread_kernel_batch32_lmax2500.md
     flops_per_eval = float(os.environ.get("CAMBGPU_FLOPS_PER_EVAL", "1315"))
     achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
+    ode_team = args.team or (tuned["team"] if tuned else 0)
+    traffic, traffic_src = ODE_TRAFFIC.get(ode_team, (None, f"no ncu capture of team {ode_team} on this workload"))
     prec = {0: "FP64 throughout",
             1: "FP64 ODE, source k-spline, C_l integral; FP32 line-of-sight projection with FP64 chunk sums"}
     line = {"metric": METRIC, "value": value,
@@ -583,14 +597,13 @@ def main():
                                      "fetch": host_ms[3]}},
             "gpu_launches": int(launches),
             "roofline": {"bound": "fp64", "kernel": "ode_thread_kernel", "achieved": achieved, "peak": tf.value,
-                         "unit": "TFLOP/s", "frac": achieved / tf.value, "traffic": ODE_TRAFFIC_BYTES,
+                         "unit": "TFLOP/s", "frac": achieved / tf.value, "traffic": traffic,
                          "peak_source": "DFMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64)",
                          "flops_per_eval": flops_per_eval, "evals_per_step": evals_step,
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw "
-                                           "ODE launch (team 1, queue order 2, 2 blocks/SM), "
-                                           "profiles/ode_thread_kernel_dram_batch256_lmax2500.md",
-                         "dram_gbs": ODE_TRAFFIC_BYTES / (ode_ms * 1e-3) / 1e9,
-                         "dram_frac_of_measured_copy": ODE_TRAFFIC_BYTES / (ode_ms * 1e-3) / 1e9 / hbm_peak(),
+                         "traffic_source": traffic_src,
+                         "dram_gbs": traffic / (ode_ms * 1e-3) / 1e9 if traffic else None,
+                         "dram_frac_of_measured_copy":
+                             traffic / (ode_ms * 1e-3) / 1e9 / hbm_peak() if traffic else None,
                          "reading": "stage rows of the resident modes (~250 MB) exceed L2 and stream through DRAM; "
                                     "the kernel is bound by the latency of those local-memory streams"},
             "clocks": clk, "wall_s_timed": wall}
