@@ -92,8 +92,8 @@ def plain_form_rate(n=3, lmax=2500, seed=1000, mnu_max=0.2):
 # profiles/ode_thread_kernel_dram_batch256_lmax2500.md
 ODE_TRAFFIC = {
     7: (0.8307e12 + 0.4565e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
-                               "(team 7: compiled for 2 resident blocks/SM, queue order 2), "
-                               "profiles/ode_thread_kernel_dram_batch256_lmax2500.md"),
+                               "(team 7: compiled for 2 resident blocks/SM, queue order 2, captured with the "
+                               "queue-counter schedule), profiles/ode_thread_kernel_dram_batch256_lmax2500.md"),
     1: (1.10e12 + 0.493e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
                             "(team 1, queue order 2, 2 blocks/SM), "
                             "profiles/ode_thread_kernel_dram_batch256_lmax2500.md"),
@@ -490,12 +490,15 @@ def main():
     tuned = None
     if not args.team and not args.no_autotune:
         best = (C.c_int * 4)()
-        times = np.zeros(11)
+        times = np.zeros(13)
         _lib.check(lib.cambgpu_autotune_ode(arr, B, best, _lib.dptr(times)))
+        sched = [0] * 11 + [1, 1]
+        tried = [i for i in range(13) if times[i] > 0]
         tuned = {"team": best[0], "queue_order": best[1], "blocks_per_sm_cap": best[3],
-                 "candidates": "team,order,blocks-per-SM cap: 32,0,0 1,0,0 1,2,0 2,2,0 1,3,2 1,2,2 2,2,2 1,1,2 6,0,0 "
-                               "7,2,0 7,3,0",
-                 "candidate_ode_ms": [round(x, 2) for x in times[:11]]}
+                 "schedule": "static stride" if sched[min(tried, key=lambda i: times[i])] else "queue counter",
+                 "candidates": "team,order,blocks-per-SM cap,schedule: 32,0,0,0 1,0,0,0 1,2,0,0 2,2,0,0 1,3,2,0 "
+                               "1,2,2,0 2,2,2,0 1,1,2,0 6,0,0,0 7,2,0,0 7,3,0,0 7,2,0,1 7,3,0,1",
+                 "candidate_ode_ms": [round(x, 2) for x in times[:13]]}
     # ---- device-resident pipeline, FP64 form then mixed precision ----
     _lib.check(lib.cambgpu_batch_prepare(arr, B))
 
@@ -572,6 +575,8 @@ def main():
     achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
     ode_team = args.team or (tuned["team"] if tuned else 0)
     traffic, traffic_src = ODE_TRAFFIC.get(ode_team, (None, f"no ncu capture of team {ode_team} on this workload"))
+    if tuned and traffic:
+        traffic_src += f"; the timed launches use the {tuned['schedule']} schedule"
     prec = {0: "FP64 throughout",
             1: "FP64 ODE, source k-spline, C_l integral; FP32 line-of-sight projection with FP64 chunk sums"}
     line = {"metric": METRIC, "value": value,

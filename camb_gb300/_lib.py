@@ -110,6 +110,7 @@ SIGNATURES = {
                                                         _c_double_p, _c_double_p, _c_double_p, _c_int_p]),
     "cambgpu_set_ode_team": (C.c_int, [C.c_int]),
     "cambgpu_set_ode_launch": (C.c_int, [C.c_int, C.c_int]),
+    "cambgpu_set_ode_schedule": (C.c_int, [C.c_int]),
     "cambgpu_prepare_tables": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.POINTER(C.c_void_p), _c_int_p]),
     "cambgpu_get_spectra_prepared": (C.c_int, [C.c_void_p, C.c_int, _c_double_p, _c_double_p, _c_double_p, _c_int_p,
                                                _c_int_p]),

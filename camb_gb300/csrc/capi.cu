@@ -46,13 +46,16 @@ double wall_ms() {
 int g_team = 0;
 int g_precision = 0;  // 0: FP64 throughout; 1: mixed-precision line-of-sight projection
 // autotuned ODE configuration per batch-size class: [0] small (< 24 modes/SM), [1] large
-struct OdeCfg { int team; int order; int cap; };
+// (schedule 0: a static first item per thread, later ones from the atomic queue counter;
+// 1: static stride, thread t takes items t, t + T, t + 2T, ... of the queue order)
+struct OdeCfg { int team; int order; int cap; int sched; };
 // untuned defaults: warp per mode (shared-memory rows) for few modes, where latency
 // decides; thread per mode for large batches, where FP64 throughput does
-OdeCfg g_tuned[2] = {{6, 0, 0}, {1, 2, 2}};
+OdeCfg g_tuned[2] = {{6, 0, 0, 0}, {7, 2, 0, 0}};
 constexpr int kWarpStrideMax = 448;  // the shared-memory warp kernel's largest state row
 int g_order = -1;  // forced queue order (-1: use the tuned one)
 int g_blocks_cap = 0;  // resident ODE blocks per SM (0: as many as fit)
+int g_sched = -1;      // forced ODE schedule (-1: use the tuned one)
 long long g_last_evals = 0;
 long long g_h2d = 0, g_d2h = 0;
 
@@ -775,6 +778,7 @@ int pick_team(const Batch& B) {
 
 int ode_order(const Batch& B) { return g_order >= 0 ? g_order : g_tuned[size_class(B)].order; }
 int ode_cap(const Batch& B) { return g_blocks_cap > 0 ? g_blocks_cap : g_team ? 0 : g_tuned[size_class(B)].cap; }
+int ode_sched(const Batch& B) { return g_sched >= 0 ? g_sched : g_team ? 0 : g_tuned[size_class(B)].sched; }
 
 int run_ode(Batch& B) {
   CUDA_TRY(cudaMemsetAsync(B.d_counter, 0, sizeof(int), g_rt.stream));
@@ -796,7 +800,11 @@ int run_ode(Batch& B) {
   int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
   const WorkItem* queue = order == 3 ? B.d_items_cost : order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
-  CUDA_TRY(launch_ode_kernel(team, blocks, tpb, g_rt.stream, B.d_cosmos, queue, B.nitems, B.d_counter,
+  // static stride: no queue counter (the kernel derives every item from its thread index);
+  // only the tpm kernels (teams 1-7) have that schedule, the register warp kernels (8, 16,
+  // 32) always take their items from the counter
+  int* counter = (ode_sched(B) == 1 && team <= 7) ? nullptr : B.d_counter;
+  CUDA_TRY(launch_ode_kernel(team, blocks, tpb, g_rt.stream, B.d_cosmos, queue, B.nitems, counter,
                              B.transfer, B.warp_stride));
   g_launches++;
   return 0;
@@ -912,6 +920,7 @@ long long run_key(const Batch& B, bool do_ode, bool do_los, bool do_cls) {
   long long k = pick_team(B);
   k = k * 8 + (ode_order(B) + 1);
   k = k * 64 + ode_cap(B);
+  k = k * 2 + ode_sched(B);
   k = k * 4 + g_precision;
   return k * 8 + (do_ode ? 4 : 0) + (do_los ? 2 : 0) + (do_cls ? 1 : 0);
 }
@@ -1424,6 +1433,13 @@ int cambgpu_set_ode_team(int lanes) {
   return 0;
 }
 
+int cambgpu_set_ode_schedule(int schedule) {
+  if (schedule < -1 || schedule > 1)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "schedule must be -1 (tuned), 0 (queue) or 1 (static stride)");
+  g_sched = schedule;
+  return 0;
+}
+
 int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm) {
   if (queue_order < -1 || queue_order > 3 || blocks_per_sm < 0)
     return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "queue order must be -1..3 and blocks per SM >= 0");
@@ -1445,14 +1461,16 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   // per mode compiled for 3/4/5 resident blocks per SM (cap 0: that many; 2: two, so that
   // threads finishing early take the queue's remaining modes), 7 = thread per mode compiled
   // for 2 resident blocks (more registers per thread, CMB sources only)
-  static const int cand[][3] = {{32, 0, 0}, {1, 0, 0}, {1, 2, 0}, {2, 2, 0}, {1, 3, 2},
-                                {1, 2, 2}, {2, 2, 2}, {1, 1, 2}, {6, 0, 0}, {7, 2, 0}, {7, 3, 0}};
+  // 4th column: schedule (0 = queue counter, 1 = static stride)
+  static const int cand[][4] = {{32, 0, 0, 0}, {1, 0, 0, 0}, {1, 2, 0, 0}, {2, 2, 0, 0}, {1, 3, 2, 0},
+                                {1, 2, 2, 0},  {2, 2, 2, 0}, {1, 1, 2, 0}, {6, 0, 0, 0}, {7, 2, 0, 0},
+                                {7, 3, 0, 0},  {7, 2, 0, 1}, {7, 3, 0, 1}};
   const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
   int rc = cambgpu_batch_prepare(p, n);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(g_mu);
   Batch& B = g_res->B;
-  int saved_team = g_team, saved_order = g_order, saved_cap = g_blocks_cap;
+  int saved_team = g_team, saved_order = g_order, saved_cap = g_blocks_cap, saved_sched = g_sched;
   double best_ms = 1e30;
   int bi = 0;
   for (int c = 0; c < nc; ++c) {
@@ -1465,6 +1483,7 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
     g_team = cand[c][0];
     g_order = cand[c][1];
     g_blocks_cap = cand[c][2];
+    g_sched = cand[c][3];
     rc = run_all(B, true, false, false);  // warm-up
     if (rc) break;
     rc = run_all(B, true, false, false);
@@ -1475,8 +1494,9 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   g_team = saved_team;
   g_order = saved_order;
   g_blocks_cap = saved_cap;
+  g_sched = saved_sched;
   if (rc) return rc;
-  g_tuned[size_class(B)] = {cand[bi][0], cand[bi][1], cand[bi][2]};
+  g_tuned[size_class(B)] = {cand[bi][0], cand[bi][1], cand[bi][2], cand[bi][3]};
   if (best) {
     best[0] = cand[bi][0];
     best[1] = cand[bi][1];

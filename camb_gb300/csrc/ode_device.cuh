@@ -1959,7 +1959,9 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
 // The work loop: each thread (W = 1) or warp (W = 32) takes a mode from the queue and
 // advances it one trial step per iteration.  The first item is the thread's (warp's)
 // global index, so each block starts on consecutive queue entries independent of atomic
-// ordering; later items come from the shared counter (past the statically assigned ones).
+// ordering; later items come from the shared counter (past the statically assigned ones),
+// or, when no counter is given, at a static stride of nstatic (items first, first +
+// nstatic, first + 2 nstatic, ...), so that a warp's lanes keep neighbouring queue entries.
 template <bool TR, int W, class WK>
 __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, const WorkItem* __restrict__ items,
                                           int nitems, int* __restrict__ counter, WK& Wk, int first, int nstatic) {
@@ -1968,10 +1970,15 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
   int cosmo = -1, q_ix = 0;
   const bool leader = wlane<W>() == 0;
   R.active = false;
+  int next_static = first;
   for (;;) {
     if (!R.active) {
       int w = first;
-      if (first < 0) {
+      if (counter == nullptr) {
+        w = next_static;
+        if (w >= nitems) break;
+        next_static += nstatic;
+      } else if (first < 0) {
         int t = 0;
         if (leader) t = atomicAdd(counter, 1);
         if constexpr (W > 1) t = __shfl_sync(0xffffffffu, t, 0);

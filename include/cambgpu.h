@@ -289,12 +289,16 @@ int cambgpu_set_ode_team(int lanes_per_mode);
  * cap on resident threads per SM in units of 128 (0 = as many as fit; a lower cap leaves
  * modes in the work queue for threads that finish early). */
 int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm);
+/* ODE schedule (no counterpart in the reference): 0 = each thread's first mode from its
+ * index, later ones from an atomic queue counter; 1 = static stride (thread t of T takes
+ * queue entries t, t + T, t + 2T, ...); -1 = the autotuned choice. */
+int cambgpu_set_ode_schedule(int schedule);
 /* In-library autotuner: times ODE variants, work-queue orders and resident-block caps on
  * n cosmologies and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
  * 1 = increasing q, 2 = bands of q with the cosmologies of each band ordered by neutrino
  * mass, 3 = decreasing cost measured by the batch's previous run (evaluations x system
  * size; order 2 until a run has recorded it).  best = [team, order, class, cap]; times
- * (optional, >= 11 entries) receives ms per
+ * (optional, >= 13 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch /

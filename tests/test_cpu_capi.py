@@ -44,3 +44,6 @@ def test_ode_controls_validate_arguments(lib):
         assert lib.cambgpu_set_ode_team(team) == 0
     assert lib.cambgpu_set_ode_launch(3, 2) == 0
     assert lib.cambgpu_set_ode_team(0) == 0 and lib.cambgpu_set_ode_launch(-1, 0) == 0
+    assert lib.cambgpu_set_ode_schedule(2) == 2 and lib.cambgpu_set_ode_schedule(-2) == 2
+    for sched in (0, 1, -1):
+        assert lib.cambgpu_set_ode_schedule(sched) == 0

@@ -176,27 +176,33 @@ def test_results_stream_matches_blocking_calls():
 
 def test_queue_orders_and_caps_give_identical_results():
     """Every k-mode is integrated independently, so the work-queue order (including the
-    measured-cost order built from the previous run) and the resident-block cap change
-    only the schedule, never a bit of the spectra."""
+    measured-cost order built from the previous run), the resident-block cap and the
+    schedule (queue counter or static stride) change only which thread runs which mode,
+    never a bit of the spectra of one kernel variant."""
     ps = draws(3, seed=5, lmax=500, mnu_max=0.1)
     arr = (_lib.CambGpuParams * len(ps))(*ps)
     lib = _lib.load()
     _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
-    outs = []
+    outs = {}
     try:
-        for team, order, cap in [(1, 0, 0), (1, 2, 2), (1, 3, 2), (1, 3, 1), (1, 1, 0)]:
+        for team, order, cap, sched in [(1, 0, 0, 0), (1, 2, 2, 0), (1, 3, 2, 0), (1, 3, 1, 0), (1, 1, 0, 0),
+                                        (1, 2, 2, 1), (1, 0, 0, 1), (7, 2, 0, 0), (7, 2, 0, 1), (7, 3, 0, 1),
+                                        (6, 0, 0, 0), (6, 0, 0, 1)]:
             _lib.check(lib.cambgpu_set_ode_team(team))
             _lib.check(lib.cambgpu_set_ode_launch(order, cap))
+            _lib.check(lib.cambgpu_set_ode_schedule(sched))
             _lib.check(lib.cambgpu_batch_run(None))
             cls = np.zeros((len(ps), 501, 4))
             _lib.check(lib.cambgpu_batch_fetch(500, _lib.dptr(cls)))
-            outs.append(cls)
+            outs.setdefault(team, []).append(cls)
     finally:
         lib.cambgpu_set_ode_team(0)
         lib.cambgpu_set_ode_launch(-1, 0)
+        lib.cambgpu_set_ode_schedule(-1)
         lib.cambgpu_batch_release()
-    for o in outs[1:]:
-        assert np.array_equal(o, outs[0])
+    for runs in outs.values():
+        for o in runs[1:]:
+            assert np.array_equal(o, runs[0])
 
 
 def test_resident_batch_refuses_after_a_later_staging():
