@@ -88,15 +88,16 @@ def plain_form_rate(n=3, lmax=2500, seed=1000, mnu_max=0.2):
 
 
 # DRAM bytes (read + write) of one ODE launch of the headline workload per thread-per-mode
-# variant (team code), from the ncu captures summarised in
-# profiles/ode_thread_kernel_dram_batch256_lmax2500.md
+# variant (team code): ncu dram__bytes_read.sum + dram__bytes_write.sum of the fourth ODE
+# launch of `bench.py --kernel-case thread256r` (team 7) and `--kernel-case thread256`
+# (team 1), one pass each
 ODE_TRAFFIC = {
     7: (0.8307e12 + 0.4565e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
                                "(team 7: compiled for 2 resident blocks/SM, queue order 2, captured with the "
-                               "queue-counter schedule), profiles/ode_thread_kernel_dram_batch256_lmax2500.md"),
+                               "queue-counter schedule; kernel case thread256r, DRAM summary under profiles/)"),
     1: (1.10e12 + 0.493e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
-                            "(team 1, queue order 2, 2 blocks/SM), "
-                            "profiles/ode_thread_kernel_dram_batch256_lmax2500.md"),
+                            "(team 1, queue order 2, 2 blocks/SM; kernel case thread256, DRAM summary under "
+                            "profiles/)"),
 }
 
 
@@ -570,7 +571,7 @@ def main():
     evals_step = evals
     # FP64 flops per right-hand-side evaluation, stage combinations and error norm
     # included: 2*DFMA + DMUL + DADD thread instructions per evaluation counted by ncu on
-    # this workload (mnu 0-0.2 eV, lmax 2500), profiles/ode_thread_kernel_batch32_lmax2500.md
+    # a 32-draw case of this workload (mnu 0-0.2 eV, lmax 2500)
     flops_per_eval = float(os.environ.get("CAMBGPU_FLOPS_PER_EVAL", "1315"))
     achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
     ode_team = args.team or (tuned["team"] if tuned else 0)
