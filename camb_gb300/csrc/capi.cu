@@ -1104,6 +1104,12 @@ int build_handles(const CambGpuParams* p, int n, std::vector<Handle*>& hs, int* 
 
 }  // namespace
 
+namespace cgdev {
+// the calling thread's error message (cambgpu_last_error), for entry points defined in
+// other translation units; returns code
+int set_last_error(int code, const char* msg) { return set_err(code, msg); }
+}  // namespace cgdev
+
 extern "C" {
 
 void cambgpu_default_params(CambGpuParams* p) {

@@ -11,7 +11,8 @@
 //
 // Limits and sharing rules:
 //   - the scratch is kNoAllocScratchDoubles doubles (16 MiB); a problem whose
-//     5*nk + ntau*nsrc*nk + view words exceed it is rejected with error code 2;
+//     5*nk + ntau*nsrc*nk + view words exceed it is rejected with error code 2 and a
+//     message (cambgpu_last_error) before any device call;
 //   - every GPU that loads the library holds this array until the process exits;
 //   - all calls share the array and it keeps the last call's contents, so calls that
 //     overlap on the GPU (different streams, or host threads racing) corrupt each
@@ -22,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdio>
 #include <cstring>
 
 #include "../../include/cambgpu.h"
@@ -30,6 +32,7 @@
 namespace cgdev {
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
 __global__ void los_flat_kernel(const DevCosmo*);
+int set_last_error(int code, const char* msg);
 }  // namespace cgdev
 
 using namespace cgdev;
@@ -64,30 +67,40 @@ __global__ void noalloc_spline_factors(const double* __restrict__ x, int n, doub
 
 extern "C" int cambgpu_los_flat_noalloc(const CambGpuTables* t, const double* linear_src_dev, double* delta_dev,
                                         void* stream) {
-  if (!t || !linear_src_dev || !delta_dev) return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  if (!t || !linear_src_dev || !delta_dev)
+    return set_last_error(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "los_flat_noalloc: null tables or buffer");
   if (t->nk < 3 || t->ntau < 3 || t->nq < 1 || t->nl < 1 || t->nl > 512 || t->nsrc < 2 || t->nsrc > 3 ||
       t->num_xx < 2)
-    return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CAMBGPU_ERROR_CUDA;
-  if (!g_scratch_addr[dev]) {
-    // one-time set-up on this device (call before any stream capture)
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return CAMBGPU_ERROR_CUDA;
-    if (cudaFuncSetAttribute(los_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) !=
-        cudaSuccess)
-      return CAMBGPU_ERROR_CUDA;
-    g_scratch_addr[dev] = static_cast<double*>(p);
-  }
-  double* base = g_scratch_addr[dev];
-  // scratch layout: [view | spline-factor pointer | spline factors 5*nk | dd_src ntau*nsrc*nk]
+    return set_last_error(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "los_flat_noalloc: grid sizes out of range");
+  // scratch layout: [view | spline-factor pointer | spline factors 5*nk | dd_src ntau*nsrc*nk];
+  // the size check comes before any device call
   const size_t view_words = (sizeof(DevCosmo) + 255) / 256 * 32;
   const size_t ptr_words = 32;
   const size_t spl_words = ((size_t)5 * t->nk + 31) / 32 * 32;
   const size_t dd_words = (size_t)t->ntau * t->nsrc * t->nk;
-  if (view_words + ptr_words + spl_words + dd_words > kNoAllocScratchDoubles)
-    return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  if (view_words + ptr_words + spl_words + dd_words > kNoAllocScratchDoubles) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "los_flat_noalloc: problem needs %zu doubles of scratch (5*nk + ntau*nsrc*nk with nk=%d, "
+                  "ntau=%d, nsrc=%d), above the %zu of the static scratch array",
+                  view_words + ptr_words + spl_words + dd_words, t->nk, t->ntau, t->nsrc, kNoAllocScratchDoubles);
+    return set_last_error(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, msg);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: no current CUDA device");
+  if (!g_scratch_addr[dev]) {
+    // one-time set-up on this device (call before any stream capture)
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+      return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: cudaGetSymbolAddress of the scratch failed");
+    if (cudaFuncSetAttribute(los_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) !=
+        cudaSuccess)
+      return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: cudaFuncSetAttribute failed");
+    g_scratch_addr[dev] = static_cast<double*>(p);
+  }
+  double* base = g_scratch_addr[dev];
   DevCosmo* d_view = reinterpret_cast<DevCosmo*>(base);
   const double** d_splp = reinterpret_cast<const double**>(base + view_words);
   double* d_spl = base + view_words + ptr_words;
@@ -119,19 +132,21 @@ extern "C" int cambgpu_los_flat_noalloc(const CambGpuTables* t, const double* li
   h.LimberBoost = t->LimberBoost;
   // the view and the factor pointer are small pageable copies on the caller's stream;
   // the stream is synchronised before returning so the host structs can go out of scope
-  if (cudaMemcpyAsync(d_view, &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess) return CAMBGPU_ERROR_CUDA;
+  if (cudaMemcpyAsync(d_view, &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: copy of the view failed");
   const double* spl_ptr = d_spl;
   if (cudaMemcpyAsync(d_splp, &spl_ptr, sizeof(spl_ptr), cudaMemcpyHostToDevice, s) != cudaSuccess)
-    return CAMBGPU_ERROR_CUDA;
+    return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: copy of the spline-factor pointer failed");
   noalloc_spline_factors<<<1, 1, 0, s>>>(t->q_evolve, t->nk, d_spl);
   const int rows = t->ntau * t->nsrc;
   source_spline_kernel<<<dim3((rows + 127) / 128, 1), 128, 0, s>>>(d_view, d_splp);
   // the projection leaves l above the last integrated multipole untouched: clear the output
   if (cudaMemsetAsync(delta_dev, 0, (size_t)t->nq * t->nl * t->nsrc * sizeof(double), s) != cudaSuccess)
-    return CAMBGPU_ERROR_CUDA;
+    return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: clearing the output failed");
   const size_t smem = (size_t)t->ntau * (3 + 1 + 1) * 8 + (size_t)t->ntau * 4 + 64;
   los_flat_kernel<<<dim3(t->nq, 1), 256, smem, s>>>(d_view);
-  if (cudaGetLastError() != cudaSuccess) return CAMBGPU_ERROR_CUDA;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return CAMBGPU_ERROR_CUDA;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_last_error(CAMBGPU_ERROR_CUDA, cudaGetErrorString(e));
   return CAMBGPU_OK;
 }

@@ -47,3 +47,19 @@ def test_ode_controls_validate_arguments(lib):
     assert lib.cambgpu_set_ode_schedule(2) == 2 and lib.cambgpu_set_ode_schedule(-2) == 2
     for sched in (0, 1, -1):
         assert lib.cambgpu_set_ode_schedule(sched) == 0
+
+
+def test_noalloc_rejects_oversized_problem_before_any_device_call(lib):
+    """The allocation-free LOS entry point checks the problem against its fixed scratch
+    array first: an oversized problem is refused with code 2 and a message naming the
+    sizes, without touching the device (so this runs without a GPU).  No buffer is read:
+    the pointers only have to be non-null."""
+    T = _lib.Tables(draws(1, seed=5, lmax=300)[0])
+    dv = _lib.CambGpuTables.from_buffer_copy(T.view)
+    dv.nk = 1 << 20
+    buf = np.zeros(8)
+    rc = lib.cambgpu_los_flat_noalloc(C.byref(dv), _lib.dptr(buf), _lib.dptr(buf), None)
+    assert rc == 2
+    msg = lib.cambgpu_last_error().decode()
+    assert "scratch" in msg and str(1 << 20) in msg
+    assert lib.cambgpu_los_flat_noalloc(None, _lib.dptr(buf), _lib.dptr(buf), None) == 2
