@@ -9,6 +9,17 @@ import numpy as np
 from . import _lib
 
 
+def save_cmb_power_array(filename, array, labels, lmin=0):
+    """Writes a zero-based (lmax+1, ncol) C_l array as text, one line per L from lmin: the
+    L column ("%4u"), then each column in "%12.7e", under a "# L <labels>" header line
+    (results.py:62-82, the format the reference's CAMB text outputs use)."""
+    array = np.asarray(array)
+    cols = labels.split() if isinstance(labels, str) else list(labels)
+    ell = np.arange(lmin, array.shape[0], dtype=np.float64)[:, None]
+    header = " L " + " ".join(f"{c:13s}" for c in cols)
+    np.savetxt(filename, np.hstack((ell, array[lmin:])), fmt=["%4u"] + ["%12.7e"] * array.shape[1], header=header)
+
+
 class CAMBdata:
     def __init__(self, params, cls, lensed=None, lens_potential=None, lmax_lensed=0):
         self.Params = params
@@ -74,6 +85,14 @@ class CAMBdata:
         if self.Params.DoLensing:
             return self.get_lensed_scalar_cls(lmax, CMB_unit, raw_cl)
         return self.get_unlensed_scalar_cls(lmax, CMB_unit, raw_cl)
+
+    def save_cmb_power_spectra(self, filename, lmax=None, CMB_unit="muK"):
+        """results.py:459-472: total (lensed when lensing) l(l+1)C_l/2pi, then the lensing
+        potential and its crosses: columns L TT EE BB TE PP PT PE."""
+        lmax = self._lmax_setting(lmax, False)
+        cmb = self.get_total_cls(lmax, CMB_unit=CMB_unit)
+        pot = self.get_lens_potential_cls(lmax, CMB_unit=CMB_unit)
+        save_cmb_power_array(filename, np.hstack((cmb, pot)), "TT EE BB TE PP PT PE")
 
     def get_cmb_power_spectra(self, params=None, lmax=None,
                               spectra=("total", "unlensed_scalar", "unlensed_total", "lensed_scalar", "tensor",
