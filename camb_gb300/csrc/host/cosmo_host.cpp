@@ -824,6 +824,9 @@ static int thermo_init(Cosmology& c, double taumin, std::string& err) {
     c.dotmu[i] = c.xe[i] * c.akthom / a2;
     if (c.tight_tau == 0 && 1 / (tau * c.dotmu[i]) > 0.005) c.tight_tau = tau;
   }
+  c.dotmu_runmin.resize(nthermo);
+  for (int i = 0; i < nthermo; ++i)
+    c.dotmu_runmin[i] = i == 0 ? c.dotmu[0] : std::min(c.dotmu_runmin[i - 1], c.dotmu[i]);
   // optical depth integral from tau0 backwards
   std::vector<double> sdotmu(nthermo), emmu(nthermo);
   {
@@ -1009,10 +1012,21 @@ static void lsamples_init(const Cosmology& c, int lmin, int max_l, std::vector<i
 // GetTauStart and the tight-coupling switch of initial (equations.f90:1940-1950)
 // ------------------------------------------------------------------------
 static double opacity_to_time(const Cosmology& c, double opacity) {
-  // Thermo_OpacityToTime (results.f90:1906-1922)
-  int j = 0;
-  while (j < c.nthermo - 1 && c.dotmu[j] > opacity) ++j;
-  return std::exp(j * c.dlntau) * c.tauminn;
+  // Thermo_OpacityToTime (results.f90:1906-1922): the first table index j < nthermo - 1
+  // with dotmu(j) <= opacity (else nthermo - 1).  The running minimum of dotmu is
+  // non-increasing and first drops to <= opacity at that same index, so bisecting it
+  // gives the scan's answer in O(log nthermo) per k-mode.
+  int lo = 0, hi = c.nthermo - 1;
+  if ((int)c.dotmu_runmin.size() != c.nthermo) {  // tables built without the running minimum
+    while (lo < hi && c.dotmu[lo] > opacity) ++lo;
+    return std::exp(lo * c.dlntau) * c.tauminn;
+  }
+  while (lo < hi) {
+    const int mid = (lo + hi) / 2;
+    if (c.dotmu_runmin[mid] <= opacity) hi = mid;
+    else lo = mid + 1;
+  }
+  return std::exp(lo * c.dlntau) * c.tauminn;
 }
 
 static CambGpuModeSpec mode_setup(const Cosmology& c, double q, bool transfer_only = false) {

@@ -99,6 +99,7 @@ struct Cosmology {
   double z_drag, r_drag0;
   std::vector<double> thermo_horner;  // [nthermo][16]
   std::vector<double> dotmu, ddotmu, dddotmu, ddddotmu, emmu, demmu, cs2, xe, tb, adot;
+  std::vector<double> dotmu_runmin;  // running minimum of dotmu (non-increasing), for opacity_to_time
   Recfast recfast;
   Reion reion;
   // grids
