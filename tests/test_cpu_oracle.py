@@ -70,6 +70,32 @@ def test_oracle_within_reference_accuracy_tolerances():
         assert abs(icl[j, 2] - r[3]) / np.sqrt(r[0] * r[1]) < te_tol, (l, icl[j, 2], r[3])
 
 
+def test_tight_coupling_switch_times_follow_the_opacity_scan():
+    """Every mode's tight-coupling switch time is min(tight_tau, OpacityToTime(q / ep))
+    (equations.f90:1940-1950 with second-order tight coupling), where OpacityToTime
+    (results.f90:1906-1922) takes the first thermal-table index whose opacity is at or
+    below the argument.  The host finds that index by bisection; this restates the scan."""
+    for p in [planck2018(1000), fiducial(2500)]:
+        T = _lib.Tables(p)
+        v = T.view
+        dotmu = np.ctypeslib.as_array(v.dotmu, shape=(v.nthermo,))
+        for m in range(v.nk):
+            ms = v.modes[m]
+            q = ms.q
+            epsw = 100 / v.tau0
+            ep = 1e-2
+            if q > epsw and q > 5 * epsw:
+                ep = 5e-2 / p.AccuracyBoost * 0.65
+            ep *= 2
+            j = 0
+            while j < v.nthermo - 1 and dotmu[j] > q / ep:
+                j += 1
+            # neighbouring indices differ by exp(dlntau) ~ 1 + 5e-4: 1e-14 separates them
+            # while allowing numpy's exp to differ from the C library's by an ulp
+            want = min(v.tight_tau, np.exp(j * v.dlntau) * v.tauminn)
+            assert abs(ms.tight_switch_tau / want - 1) < 1e-14, (m, q, ms.tight_switch_tau, want)
+
+
 def test_scalar_power_known_answer():
     """camb/tests/camb_test.py testPowers: scalar_power(1) = 1.801e-9 for As=2e-9, ns=0.965
     (the reference checks 4 decimal places of the rounded value: relative 1e-4 here)."""
