@@ -52,13 +52,6 @@ def parse():
                     help="instead of the headline run: N lensed draws (lmax 2500 + 200 margin) through the FP64 "
                          "and the mixed-precision projection, device time per form and the mixed form's C_l "
                          "error against FP64 per l band")
-    ap.add_argument("--kernel-case", choices=["warp1", "thread8", "thread96", "thread128", "thread256",
-                                              "thread256r"],
-                    help="profiling driver: prepare one fixed case, run the device pipeline 4 times, print the "
-                         "last ODE time and exit (warp1: one massless lmax-1000 cosmology, warp per mode; "
-                         "thread8 / thread96 / thread128 / thread256: 8 / 96 / 128 / 256 draws of the workload, "
-                         "thread per mode; thread256r: the 256 draws on the variant compiled for two resident "
-                         "blocks per SM)")
     return ap.parse_args()
 
 
@@ -89,7 +82,7 @@ def plain_form_rate(n=3, lmax=2500, seed=1000, mnu_max=0.2):
 
 # DRAM bytes (read + write) of one ODE launch of the headline workload per thread-per-mode
 # variant (team code): ncu dram__bytes_read.sum + dram__bytes_write.sum of the fourth ODE
-# launch of `bench.py --kernel-case thread256r` (team 7) and `--kernel-case thread256`
+# launch of `python -m camb_gb300.kernel_case thread256r` (team 7) and `... thread256`
 # (team 1), one pass each
 ODE_TRAFFIC = {
     7: (0.8307e12 + 0.4565e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
@@ -204,55 +197,10 @@ def lensed_batch(n, lmax=2500, seed=5000, mnu_max=0.2):
             "mixed_vs_fp64_lensed_error_per_l_band": err}
 
 
-def kernel_case(name):
-    """A fixed case for ncu captures: the batch is staged once and the whole device
-    pipeline (ODE, spline, mixed LOS, C_l) runs four times, so `-s 3 -c 1` with a kernel
-    filter captures the fourth launch of that kernel."""
-    from camb_gb300 import _lib
-    lib = _lib.load()
-    if name == "warp1":
-        p = _lib.default_params()
-        p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
-        p.nnu, p.mnu, p.num_massive_neutrinos = 3.046, 0.0, 1
-        p.max_l, p.max_eta_k = 1000, 2500
-        ps, team, order, cap = [p], 6, -1, 0
-    elif name == "thread8":
-        ps, team, order, cap = workload(8, 2500, seed=7), 2, -1, 0
-    elif name in ("thread96", "thread128"):
-        ps, team, order, cap = workload(int(name[6:]), 2500, seed=1000), 1, 2, 2
-    elif name == "thread256r":
-        ps, team, order, cap = workload(256, 2500, seed=1000), 7, 2, 0
-    else:
-        ps, team, order, cap = workload(256, 2500, seed=1000), 1, 2, 2
-    arr = (_lib.CambGpuParams * len(ps))(*ps)
-    _lib.check(lib.cambgpu_set_ode_team(team))
-    _lib.check(lib.cambgpu_set_ode_launch(order, cap))
-    _lib.check(lib.cambgpu_set_precision(1))
-    _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
-    ms = np.zeros(3)
-    for _ in range(4):
-        _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
-    print(json.dumps({"kernel_case": name, "ode_ms": ms[0], "spline_los_ms": ms[1], "cls_ms": ms[2]}))
-    lib.cambgpu_batch_release()
-
-
 def workload(n, lmax, seed, mnu_max=0.2):
-    from camb_gb300 import _lib
-    rng = np.random.default_rng(seed)
-    out = []
-    for _ in range(n):
-        p = _lib.default_params()
-        p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
-        p.nnu = 3.046
-        for name in ["ombh2", "omch2", "H0", "optical_depth", "As", "ns"]:
-            setattr(p, name, getattr(p, name) * (1 + 0.05 * (2 * rng.random() - 1)))
-        if mnu_max > 0:
-            p.mnu = mnu_max * rng.random()
-            p.num_massive_neutrinos = 1
-        p.max_l = lmax
-        p.max_eta_k = 2.5 * lmax
-        out.append(p)
-    return out
+    """The batch's seeded draws (camb_gb300.workload.batch_draws)."""
+    from camb_gb300.workload import batch_draws
+    return batch_draws(n, lmax, seed, mnu_max)
 
 
 class Clocks:
@@ -471,9 +419,6 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
-    if args.kernel_case:
-        kernel_case(args.kernel_case)
-        return
     if args.lensed_batch:
         print(json.dumps(lensed_batch(args.lensed_batch, args.lmax, mnu_max=args.mnu_max)))
         return
@@ -617,7 +562,8 @@ def main():
             "clocks": clk, "wall_s_timed": wall}
     if rank == 0:
         nth = os.cpu_count() or 1
-        cps = workload(args.cpu_sample, args.lmax, seed=2024, mnu_max=args.mnu_max)
+        # the batch's first cpu_sample draws: the same cosmologies the reference arm times
+        cps = workload(args.cpu_sample, args.lmax, seed=1000 + rank, mnu_max=args.mnu_max)
         cpu_reference(cps[:1], nth)
         ref = []
         t = cpu_reference(cps, nth, keep=ref)

@@ -11,20 +11,28 @@
 //
 // Limits and sharing rules:
 //   - the scratch is kNoAllocScratchDoubles doubles (16 MiB); a problem whose
-//     5*nk + ntau*nsrc*nk + view words exceed it is rejected with error code 2 and a
-//     message (cambgpu_last_error) before any device call;
+//     5*nk + ntau*nsrc*nk + view words exceed it, or whose time grid needs more than the
+//     projection kernel's 160 KiB of dynamic shared memory (ntau*44 + 64 bytes, i.e.
+//     ntau above 3722), is rejected with error code 2 and a message
+//     (cambgpu_last_error) before any device call;
+//   - every array in the tables and both buffers must be device (or managed) memory:
+//     a host pointer is rejected with code 2 before anything is launched;
 //   - every GPU that loads the library holds this array until the process exits;
 //   - all calls share the array and it keeps the last call's contents, so calls that
 //     overlap on the GPU (different streams, or host threads racing) corrupt each
 //     other: serialise them;
 //   - the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) and sets the kernel's shared-memory limit; make that
-//     first call before any stream capture.
+//     (cudaGetSymbolAddress) and sets the kernel's shared-memory limit, under a lock,
+//     so two host threads making their first calls together do it once; make that
+//     first call before any stream capture;
+//   - a call returns after the work it queued on `stream` has finished (it
+//     synchronises that stream), so the caller's buffers are complete on return.
 #include <cuda_runtime.h>
 
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "../../include/cambgpu.h"
 #include "device_tables.cuh"
@@ -44,6 +52,18 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles
 
 constexpr int kMaxDevices = 64;
 double* g_scratch_addr[kMaxDevices] = {nullptr};
+std::mutex g_setup_mu;  // guards the one-time per-device set-up below
+constexpr size_t kLosSmemMax = 160 * 1024;  // dynamic shared memory the projection kernel may use
+
+// device (or managed) memory only: the kernels dereference every pointer of the view
+bool on_device(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the (non-sticky) error left by an unknown pointer
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
 
 // spline factors of the k grid (same quantities the host computes for the batched path)
 __global__ void noalloc_spline_factors(const double* __restrict__ x, int n, double* __restrict__ spl) {
@@ -86,21 +106,47 @@ extern "C" int cambgpu_los_flat_noalloc(const CambGpuTables* t, const double* li
                   view_words + ptr_words + spl_words + dd_words, t->nk, t->ntau, t->nsrc, kNoAllocScratchDoubles);
     return set_last_error(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, msg);
   }
+  // the projection stages the time grid in shared memory: sources x3, two weights, an index
+  const size_t smem = (size_t)t->ntau * (3 + 1 + 1) * 8 + (size_t)t->ntau * 4 + 64;
+  if (smem > kLosSmemMax) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "los_flat_noalloc: ntau=%d needs %zu bytes of shared memory (ntau*44 + 64), above the %zu "
+                  "the projection kernel is set up for",
+                  t->ntau, smem, kLosSmemMax);
+    return set_last_error(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, msg);
+  }
+  if (!t->q_evolve || !t->tau_points || !t->tau_dpoints || !t->q_int || !t->ls || !t->bess_x || !t->bessel_horner)
+    return set_last_error(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "los_flat_noalloc: null array in the tables");
+  {
+    const void* ptrs[] = {linear_src_dev, delta_dev, t->q_evolve, t->tau_points, t->tau_dpoints, t->q_int,
+                          t->ls, t->bess_x, t->bessel_horner};
+    const char* names[] = {"linear_src_dev", "delta_dev", "q_evolve", "tau_points", "tau_dpoints", "q_int",
+                           "ls", "bess_x", "bessel_horner"};
+    for (int i = 0; i < 9; ++i)
+      if (!on_device(ptrs[i])) {
+        char msg[160];
+        std::snprintf(msg, sizeof(msg), "los_flat_noalloc: %s is not device memory", names[i]);
+        return set_last_error(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, msg);
+      }
+  }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: no current CUDA device");
+  std::unique_lock<std::mutex> setup_lock(g_setup_mu);
   if (!g_scratch_addr[dev]) {
     // one-time set-up on this device (call before any stream capture)
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
       return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: cudaGetSymbolAddress of the scratch failed");
-    if (cudaFuncSetAttribute(los_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) !=
+    if (cudaFuncSetAttribute(los_flat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLosSmemMax) !=
         cudaSuccess)
       return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: cudaFuncSetAttribute failed");
     g_scratch_addr[dev] = static_cast<double*>(p);
   }
   double* base = g_scratch_addr[dev];
+  setup_lock.unlock();
   DevCosmo* d_view = reinterpret_cast<DevCosmo*>(base);
   const double** d_splp = reinterpret_cast<const double**>(base + view_words);
   double* d_spl = base + view_words + ptr_words;
@@ -143,7 +189,6 @@ extern "C" int cambgpu_los_flat_noalloc(const CambGpuTables* t, const double* li
   // the projection leaves l above the last integrated multipole untouched: clear the output
   if (cudaMemsetAsync(delta_dev, 0, (size_t)t->nq * t->nl * t->nsrc * sizeof(double), s) != cudaSuccess)
     return set_last_error(CAMBGPU_ERROR_CUDA, "los_flat_noalloc: clearing the output failed");
-  const size_t smem = (size_t)t->ntau * (3 + 1 + 1) * 8 + (size_t)t->ntau * 4 + 64;
   los_flat_kernel<<<dim3(t->nq, 1), 256, smem, s>>>(d_view);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

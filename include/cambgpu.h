@@ -187,12 +187,16 @@ int cambgpu_calc_scal_cls(const CambGpuTables* t, const double* delta_p_l_k, dou
  * callers that cannot call cudaMalloc -- code inside a framework that owns all device
  * memory, or a service that must not allocate after start-up.  Every array pointer in
  * `t` (q_evolve, tau_points, tau_dpoints, q_int, ls, bess_x, bessel_horner) and both
- * buffers are DEVICE pointers owned by the caller; the spline scratch lives in a 16 MiB
- * static device array inside the library (problems with 5*nk + ntau*nsrc*nk beyond it
- * are rejected with code 2).  Work is enqueued on `stream` (a cudaStream_t, NULL = the
- * default stream) and the stream is synchronised before returning.  All calls share the
- * scratch: calls that overlap on the GPU race.  The first call on a device sets up the
- * scratch address; make it before any stream capture. */
+ * buffers are DEVICE (or managed) pointers owned by the caller -- a host pointer is
+ * rejected with code 2; the spline scratch lives in a 16 MiB static device array inside
+ * the library.  Problems with 5*nk + ntau*nsrc*nk beyond it, or with ntau above 3722
+ * (the projection stages ntau*44 + 64 bytes of the time grid in at most 160 KiB of
+ * shared memory), are rejected with code 2 and a message before any device call.  Work
+ * is enqueued on `stream` (a cudaStream_t, NULL = the default stream) and the call
+ * blocks until that stream has finished it.  All calls share the scratch: calls that
+ * overlap on the GPU race, so serialise them.  The first call on a device sets up the
+ * scratch address (under a lock, so concurrent first calls do it once); make it before
+ * any stream capture. */
 int cambgpu_los_flat_noalloc(const CambGpuTables* t, const double* linear_src_dev, double* delta_dev, void* stream);
 
 /* ---- whole pipeline (CAMB_GetResults for the scalar flat path) ---- */

@@ -1,7 +1,7 @@
 """Extracts the golden vectors the tests pin the oracle and library against.
 
-Run here, where the reference source tree is mounted (its path is the first
-argument, default /root/reference); writes tests/golden/*.json.  The GPU machine
+Run here, where the reference source tree is mounted (its path is the only
+argument); writes tests/golden/*.json.  The GPU machine
 only reads the JSON files.
 
   template_cls.json  rows of the reference's fortran/HighLExtrapTemplate_lenspotentialCls.dat
@@ -17,7 +17,9 @@ import sys
 
 import numpy as np
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python %s <reference_root>" % os.path.basename(__file__))
+ref = sys.argv[1]
 here = os.path.dirname(os.path.abspath(__file__))
 
 tmpl = np.loadtxt(os.path.join(ref, "fortran", "HighLExtrapTemplate_lenspotentialCls.dat"))

@@ -2,8 +2,7 @@
 lensing (camb/correlations.py lensed_cls, the full-sky Gauss-Legendre method that the
 reference tests against its Fortran curved-sky code, camb_test.py:880-906).
 
-Run here, where the reference source tree is mounted (its path is the first argument,
-default /root/reference).  The input spectra are the oracle's unlensed C_l of the
+Run here, where the reference source tree is mounted (its path is the only argument).  The input spectra are the oracle's unlensed C_l of the
 fiducial lensed cosmology (H0 67.5, ombh2 0.022, omch2 0.122, massless N_eff 3.046,
 tau 0.06, As 2.1e-9, ns 0.965, max_l 2700); writes tests/golden/lensing_pin.npz with
 the inputs, the lensing l range, and the reference's lensed TT EE BB TE.
@@ -16,7 +15,9 @@ import numpy as np
 
 here = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(here, "..", ".."))
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python %s <reference_root>" % os.path.basename(__file__))
+ref = sys.argv[1]
 
 from camb_gb300 import _lib  # noqa: E402
 from oracle import oracle as orc  # noqa: E402

@@ -5,15 +5,18 @@ holding TT, EE, TE, PP, rows 0 and 1 zero.  These are the four columns the refer
 (config.f90:93-116); the library uses them for the templated C_l interpolation
 (results.f90:1745-1824) and the lensing tail extension (lensing.f90:280-336).
 
-Run where the reference tree is mounted: python make_template.py [reference_root]
+Run where the reference tree is mounted: python tests/golden/make_template.py <reference_root>
+(writes camb_gb300/data/highl_template.f64, the product's copy of the table).
 """
 import os
 import sys
 
 import numpy as np
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-here = os.path.dirname(os.path.abspath(__file__))
+if len(sys.argv) != 2:
+    sys.exit("usage: python make_template.py <reference_root>")
+ref = sys.argv[1]
+here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "camb_gb300", "data")
 rows = np.loadtxt(os.path.join(ref, "fortran", "HighLExtrapTemplate_lenspotentialCls.dat"))
 LMAX = 8000
 out = np.zeros((LMAX + 1, 4), dtype="<f8")

@@ -63,3 +63,17 @@ def test_noalloc_rejects_oversized_problem_before_any_device_call(lib):
     msg = lib.cambgpu_last_error().decode()
     assert "scratch" in msg and str(1 << 20) in msg
     assert lib.cambgpu_los_flat_noalloc(None, _lib.dptr(buf), _lib.dptr(buf), None) == 2
+
+
+def test_noalloc_rejects_long_time_grid_before_any_device_call(lib):
+    """A time grid whose shared-memory staging (ntau*44 + 64 bytes) exceeds the projection
+    kernel's 160 KiB is refused with code 2 and a message naming ntau, before any device
+    call (so this runs without a GPU)."""
+    T = _lib.Tables(draws(1, seed=5, lmax=300)[0])
+    dv = _lib.CambGpuTables.from_buffer_copy(T.view)
+    dv.ntau = 4000
+    buf = np.zeros(8)
+    rc = lib.cambgpu_los_flat_noalloc(C.byref(dv), _lib.dptr(buf), _lib.dptr(buf), None)
+    assert rc == 2
+    msg = lib.cambgpu_last_error().decode()
+    assert "ntau=4000" in msg and "shared memory" in msg

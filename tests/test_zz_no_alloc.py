@@ -80,3 +80,26 @@ def test_los_noalloc_rejects_oversized_problem():
     d = torch.zeros(8, dtype=torch.float64, device="cuda")
     rc = lib.cambgpu_los_flat_noalloc(C.byref(dv), C.c_void_p(d.data_ptr()), C.c_void_p(d.data_ptr()), None)
     assert rc == 2
+
+
+def test_los_noalloc_rejects_host_buffers():
+    """Every buffer must be device memory: a host array passed as the sources is refused
+    with code 2 before anything is launched, and the context stays usable."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    lib = _lib.load()
+    T = _lib.Tables(draws(1, seed=5, lmax=300)[0])
+    dv, keep = _device_view(T, torch)
+    host_src = np.zeros((T.view.ntau, T.view.nsrc, T.view.nk))
+    d_out = torch.zeros((T.view.nq, T.view.nl, T.view.nsrc), dtype=torch.float64, device="cuda")
+    rc = lib.cambgpu_los_flat_noalloc(C.byref(dv), _lib.dptr(host_src), C.c_void_p(d_out.data_ptr()), None)
+    assert rc == 2
+    assert "linear_src_dev" in lib.cambgpu_last_error().decode()
+    dv.bess_x = T.view.bess_x  # a host table inside the view
+    d_src = torch.zeros(host_src.shape, dtype=torch.float64, device="cuda")
+    rc = lib.cambgpu_los_flat_noalloc(C.byref(dv), C.c_void_p(d_src.data_ptr()), C.c_void_p(d_out.data_ptr()), None)
+    assert rc == 2
+    assert "bess_x" in lib.cambgpu_last_error().decode()
+    torch.cuda.synchronize()
+    del keep
