@@ -804,6 +804,10 @@ __global__ void __launch_bounds__(128) ode_persistent_kernel(const DevCosmo* __r
 namespace tpm {
 
 constexpr int NV = 448;  // largest packed scalar system handled (mode_init rejects larger ones)
+// Dormand-Prince 5(4) with FSAL needs seven live rows per mode: y, the stage input, and
+// k1..k5; k6 takes k2's row (k2 is dead once the stage-6 input is formed, b2 = e2 = 0) and
+// k7 takes k4's (dead once the fifth-order solution and the error combination are formed).
+constexpr int kRows = 7;
 constexpr int NL = 66;
 constexpr int NUE = 3;
 
@@ -1491,15 +1495,15 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
   }
 }
 
-// The eight stage vectors live in rows of b; the state, trial state and first/last stage
-// rows are named by slot indices so that accepting a step swaps indices, not vectors.
+// The stage vectors live in the seven rows of b; every row is named by a slot index so
+// that accepting a step swaps indices, not vectors.
 struct Work {
-  double b[8][NV];
+  double b[kRows][NV];
 };
 
 // The same rows for a warp's mode, in the warp's slice of shared memory
 struct WorkS {
-  double* b;  // [8][stride]
+  double* b;  // [kRows][stride]
   int stride;
   NuBins* bins;  // [NUE] momentum-bin factors of the current right-hand side
   double* rec;   // [3][NL] the mode's denlk, denlk2, polfack
@@ -1518,7 +1522,7 @@ struct Run {
   double src[13];  // source functions, or the 13 transfer variables without the CMB
   double tau, target, sw_time, h, err, call_hmax;
   double ny;            // min(max|y|, 1) of the current state (valid when ny_valid)
-  int sy, syt, sk1, sk2;  // rows of Work::b holding y, the trial state, k1 and k2 (= k7)
+  int sy, syt, sk1, sk2, sk3, sk4, sk5;  // rows holding y, the trial state and k1..k5 (k6 in sk2, k7 in sk4)
   bool ny_valid;
   long long evals;
   int j, fails, status, sw_kind, sw_eig;
@@ -1574,7 +1578,10 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
   R.sy = 0;
   R.sk1 = 1;
   R.sk2 = 2;
-  R.syt = 7;
+  R.sk3 = 3;
+  R.sk4 = 4;
+  R.sk5 = 5;
+  R.syt = 6;
   R.ny_valid = false;
   double* const Y = row(Wk, R.sy);
   if constexpr (W > 1) {  // the warp's k-scaled recurrence factors (initial(), equations.f90:1911-1916)
@@ -1827,11 +1834,10 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   double* __restrict__ y = row(Wk, R.sy);
   double* __restrict__ yt = row(Wk, R.syt);
   double* __restrict__ k1 = row(Wk, R.sk1);
-  double* __restrict__ k2 = row(Wk, R.sk2);
-  double* __restrict__ k3 = row(Wk, 3);
-  double* __restrict__ k4 = row(Wk, 4);
-  double* __restrict__ k5 = row(Wk, 5);
-  double* __restrict__ k6 = row(Wk, 6);
+  double* __restrict__ k2 = row(Wk, R.sk2);  // also k6
+  double* __restrict__ k3 = row(Wk, R.sk3);  // also the error combination
+  double* __restrict__ k4 = row(Wk, R.sk4);  // also k7
+  double* __restrict__ k5 = row(Wk, R.sk5);
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
@@ -1905,30 +1911,30 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   for (int i = lane; i < n; i += W)
     yt[i] = fma(c65, k5[i], fma(c64, k4[i], fma(c63, k3[i], fma(c62, k2[i], fma(c61, k1[i], y[i])))));
   wsync<W>();
-  derivs1<TR, W>(C, M, x + hs, yt, k6, nullptr, sb, wrec(Wk));
+  derivs1<TR, W>(C, M, x + hs, yt, k2, nullptr, sb, wrec(Wk));  // k6 into k2's row
   wsync<W>();
   // the fifth-order solution, the error combination of k1, k3..k6 (k3 is dead afterwards
   // and holds it) and max|yt| for the next step's hmin, in one pass
   unsigned long long nbt = 0;
 #pragma unroll 4
   for (int i = lane; i < n; i += W) {
-    const double a1 = k1[i], a3 = k3[i], a4 = k4[i], a5 = k5[i], a6 = k6[i];
+    const double a1 = k1[i], a3 = k3[i], a4 = k4[i], a5 = k5[i], a6 = k2[i];
     const double v = fma(cb6, a6, fma(cb5, a5, fma(cb4, a4, fma(cb3, a3, fma(cb1, a1, y[i])))));
     yt[i] = v;
     k3[i] = fma(e6, a6, fma(e5, a5, fma(e4, a4, fma(e3, a3, e1 * a1))));
     nbt = max(nbt, (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL);
   }
   wsync<W>();
-  // stage 7 (FSAL) into k2; at an output time it is the output() evaluation too
+  // stage 7 (FSAL) into k4's row; at an output time it is the output() evaluation too
   const bool want_src = (xt == xend) && !R.target_is_switch;
-  derivs1<TR, W>(C, M, x + hs, yt, k2, want_src ? R.src : nullptr, sb, wrec(Wk));
+  derivs1<TR, W>(C, M, x + hs, yt, k4, want_src ? R.src : nullptr, sb, wrec(Wk));
   wsync<W>();
   R.src_valid = want_src;
   R.evals += 6;
   // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry
   double num = 0, den = 1;
   for (int i = lane; i < n; i += W) {
-    const double ee = fma(e7, k2[i], k3[i]);
+    const double ee = fma(e7, k4[i], k3[i]);
     const double ae = fabs(ee), ay = fabs(y[i]);
     const double sc = ay > 1.0 ? ay : 1.0;
     if (ae * den > num * sc) {
@@ -1944,8 +1950,8 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
     R.sy = R.syt;
     R.syt = t;
     t = R.sk1;
-    R.sk1 = R.sk2;
-    R.sk2 = t;
+    R.sk1 = R.sk4;
+    R.sk4 = t;
     R.ny = __longlong_as_double((long long)wmax_u64<W>(nbt));
     R.fails = 0;
     if (xt == xend) R.fsal = true;
@@ -2063,9 +2069,9 @@ __global__ void __launch_bounds__(128, MINB) ode_thread_kernel(const DevCosmo* _
                    gridDim.x * blockDim.x);
 }
 
-// Warp per mode, one warp per block: the block's dynamic shared memory holds the eight
+// Warp per mode, one warp per block: the block's dynamic shared memory holds the seven
 // state rows of `stride` entries, the recurrence factors and the momentum-bin factors.
-inline size_t warp_smem_bytes(int stride) { return ((size_t)8 * stride + 3 * NL) * sizeof(double) + NUE * sizeof(NuBins); }
+inline size_t warp_smem_bytes(int stride) { return ((size_t)kRows * stride + 3 * NL) * sizeof(double) + NUE * sizeof(NuBins); }
 
 template <bool TR>
 __global__ void __launch_bounds__(32) ode_warp_kernel(const DevCosmo* __restrict__ cosmos,
@@ -2075,7 +2081,7 @@ __global__ void __launch_bounds__(32) ode_warp_kernel(const DevCosmo* __restrict
   WorkS Wk;
   Wk.b = wsm;
   Wk.stride = stride;
-  Wk.rec = wsm + (size_t)8 * stride;
+  Wk.rec = wsm + (size_t)kRows * stride;
   Wk.bins = reinterpret_cast<NuBins*>(Wk.rec + 3 * NL);
   run_modes<TR, 32>(cosmos, items, nitems, counter, Wk, blockIdx.x, gridDim.x);
 }
