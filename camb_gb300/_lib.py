@@ -123,6 +123,7 @@ SIGNATURES = {
     "cambgpu_last_ode_evals": (C.c_longlong, []),
     "cambgpu_last_transfer_bytes": (C.c_int, [C.POINTER(C.c_longlong)]),
     "cambgpu_probe_fp64_tflops": (C.c_int, [_c_double_p]),
+    "cambgpu_probe_fp64_pipe": (C.c_int, [C.c_int, C.c_int, C.c_int, _c_double_p]),
     "cambgpu_kernel_launches": (C.c_longlong, [C.c_int]),
     "cambgpu_last_error": (C.c_char_p, []),
 }

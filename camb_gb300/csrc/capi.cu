@@ -25,6 +25,8 @@ cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s,
                               const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride);
 cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s);
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
+cudaError_t launch_fp64_pipe_probe(int nsm, int warps, int lanes, int chains, int iters, long long* cyc, double* out,
+                                   cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
 __global__ void source_spline_f32_kernel(const DevCosmo*, const double* const*);
 __global__ void los_flat_kernel(const DevCosmo*);
@@ -1535,6 +1537,36 @@ int cambgpu_probe_fp64_tflops(double* tflops) {
   double ms = elapsed(g_rt.ev[4], g_rt.ev[5]);
   cudaFree(d);
   *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  return 0;
+}
+
+int cambgpu_probe_fp64_pipe(int warps_per_sm, int active_lanes, int chains, double* lane_fma_per_sm_cycle) {
+  if (warps_per_sm < 1 || warps_per_sm > 32 || active_lanes < 1 || active_lanes > 32 ||
+      (chains != 1 && chains != 4 && chains != 8) || !lane_fma_per_sm_cycle)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "probe: warps 1-32, lanes 1-32, chains 1, 4 or 8");
+  std::lock_guard<std::mutex> lk(g_mu);
+  int rc = rt_init();
+  if (rc) return rc;
+  const int nsm = g_rt.nsm, iters = 4096;
+  long long* d_cyc = nullptr;
+  double* d_out = nullptr;
+  CUDA_TRY(cudaMalloc(&d_cyc, sizeof(long long) * nsm));
+  CUDA_TRY(cudaMalloc(&d_out, 8));
+  cudaError_t e = launch_fp64_pipe_probe(nsm, warps_per_sm, active_lanes, chains, 64, d_cyc, d_out, g_rt.stream);
+  if (e == cudaSuccess) e = launch_fp64_pipe_probe(nsm, warps_per_sm, active_lanes, chains, iters, d_cyc, d_out,
+                                                   g_rt.stream);
+  std::vector<long long> cyc(nsm);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cyc.data(), d_cyc, sizeof(long long) * nsm, cudaMemcpyDeviceToHost,
+                                            g_rt.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_rt.stream);
+  cudaFree(d_cyc);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return set_err(CAMBGPU_ERROR_CUDA, cudaGetErrorString(e));
+  g_launches += 2;
+  double mean = 0;
+  for (long long c : cyc) mean += (double)c;
+  mean /= nsm;
+  *lane_fma_per_sm_cycle = (double)warps_per_sm * active_lanes * chains * iters / mean;
   return 0;
 }
 

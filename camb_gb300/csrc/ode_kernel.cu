@@ -43,6 +43,50 @@ cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, c
   return cudaGetLastError();
 }
 
+// FP64 issue model: one block per SM (held there by its dynamic shared memory), `lanes`
+// active lanes in each of its warps, NC independent DFMA chains per lane.  Each block
+// records the SM cycles (clock64) of its timed loop.
+template <int NC>
+__global__ void fp64_pipe_probe_kernel(long long* cyc, double* out, int iters, int lanes) {
+  double a[NC];
+#pragma unroll
+  for (int j = 0; j < NC; ++j) a[j] = 1.0 + 1e-7 * (threadIdx.x + j);
+  const double m = 0.999999, c = 1e-9;
+  __syncthreads();
+  const long long t0 = clock64();
+  if ((int)(threadIdx.x & 31) < lanes) {
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int j = 0; j < NC; ++j) a[j] = fma(a[j], m, c);
+    }
+  }
+  __syncthreads();
+  const long long t1 = clock64();
+  double s = 0;
+#pragma unroll
+  for (int j = 0; j < NC; ++j) s += a[j];
+  if (s == 12345.0) out[0] = s;  // keeps the chains live
+  if (threadIdx.x == 0) cyc[blockIdx.x] = t1 - t0;
+}
+
+cudaError_t launch_fp64_pipe_probe(int nsm, int warps, int lanes, int chains, int iters, long long* cyc, double* out,
+                                   cudaStream_t s) {
+  const int smem = 150 * 1024;  // more than half an SM's shared memory: one block per SM
+  const int threads = 32 * warps;
+  cudaError_t e = cudaSuccess;
+  if (chains == 1) {
+    e = cudaFuncSetAttribute(fp64_pipe_probe_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) fp64_pipe_probe_kernel<1><<<nsm, threads, smem, s>>>(cyc, out, iters, lanes);
+  } else if (chains == 4) {
+    e = cudaFuncSetAttribute(fp64_pipe_probe_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) fp64_pipe_probe_kernel<4><<<nsm, threads, smem, s>>>(cyc, out, iters, lanes);
+  } else {
+    e = cudaFuncSetAttribute(fp64_pipe_probe_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) fp64_pipe_probe_kernel<8><<<nsm, threads, smem, s>>>(cyc, out, iters, lanes);
+  }
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
 // team 1..5 = thread per mode compiled for 3/4/5/6/8 resident blocks of 128 per SM, 7 =
 // the same for 2 blocks; 6 = warp per mode with shared-memory rows; 8/16/32 =
 // register-resident warp teams

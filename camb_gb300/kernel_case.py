@@ -17,7 +17,12 @@ that kernel, after three warm launches.  Cases:
   thread256r   the 256 draws, team 7, queue order 2, queue-counter schedule
   thread256s   the 256 draws, team 7, queue order 2, static-stride schedule (the
                configuration the benchmark's autotuner picks)
-  team<T>_<N>  N draws on ODE team code T with its default launch (e.g. team9_32)
+  team<T>_<N>[_o<order>][_s<schedule>][_c<cap>]
+               N draws on ODE team code T, optionally with a queue order, a schedule
+               and a resident-block cap (e.g. team7_256_o2_s1); unset parts keep the
+               tuned defaults
+  fp64pipe     the FP64 issue model (cambgpu_probe_fp64_pipe): lane FMAs per SM cycle for
+               1-16 warps per SM, partially active warps and 1/4/8 independent chains
 """
 import json
 import sys
@@ -28,9 +33,28 @@ from . import _lib
 from .workload import batch_draws
 
 
+def fp64_pipe():
+    """Lane FMAs per SM cycle of the DFMA probe over warps per SM, active lanes, chains."""
+    import ctypes as C
+    lib = _lib.load()
+    rows = []
+    cases = [(w, 32, 8) for w in (1, 2, 3, 4, 6, 8, 16)] + [(1, l, 8) for l in (1, 8, 16)] + \
+            [(4, l, 8) for l in (1, 8, 16)] + [(1, 32, c) for c in (1, 4)] + [(4, 32, c) for c in (1, 4)]
+    for w, l, c in cases:
+        v = C.c_double()
+        _lib.check(lib.cambgpu_probe_fp64_pipe(w, l, c, C.byref(v)))
+        rows.append({"warps_per_sm": w, "active_lanes": l, "chains": c, "lane_fma_per_sm_cycle": round(v.value, 4),
+                     "cycles_per_warp_dfma": round(w * l / v.value, 1)})
+    out = {"kernel_case": "fp64pipe", "rows": rows}
+    print(json.dumps(out))
+    return out
+
+
 def run(name, runs=4):
     lib = _lib.load()
     sched = 0
+    if name == "fp64pipe":
+        return fp64_pipe()
     if name == "warp1":
         p = _lib.default_params()
         p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
@@ -50,8 +74,16 @@ def run(name, runs=4):
     elif name == "thread256":
         ps, team, order, cap = batch_draws(256, 2500, seed=1000), 1, 2, 2
     elif name.startswith("team"):
-        t, n = name[4:].split("_")
-        ps, team, order, cap, sched = batch_draws(int(n), 2500, seed=1000), int(t), -1, 0, -1
+        parts = name[4:].split("_")
+        order, sched, cap = -1, -1, 0
+        for extra in parts[2:]:
+            if extra[0] == "o":
+                order = int(extra[1:])
+            elif extra[0] == "s":
+                sched = int(extra[1:])
+            elif extra[0] == "c":
+                cap = int(extra[1:])
+        ps, team = batch_draws(int(parts[1]), 2500, seed=1000), int(parts[0])
     else:
         raise SystemExit(f"unknown case {name}")
     arr = (_lib.CambGpuParams * len(ps))(*ps)

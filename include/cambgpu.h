@@ -318,6 +318,13 @@ long long cambgpu_last_ode_evals(void);
 int cambgpu_last_transfer_bytes(long long* out2);
 /* Measures the device's FP64 FMA throughput (TFLOP/s) with a DFMA-chain kernel. */
 int cambgpu_probe_fp64_tflops(double* tflops);
+/* The FP64 issue model behind the ODE kernels' design (no counterpart in the reference):
+ * one block per SM with warps_per_sm warps, active_lanes lanes of each warp running
+ * `chains` (1, 4 or 8) independent DFMA chains; returns the lane FMAs retired per SM
+ * cycle (clock64 around the loop, mean over SMs).  On a GB300 a warp issues one DFMA per
+ * 64 cycles whatever its lanes or chains, and an SM saturates near 1.7 lane FMAs per
+ * cycle with four warps. */
+int cambgpu_probe_fp64_pipe(int warps_per_sm, int active_lanes, int chains, double* lane_fma_per_sm_cycle);
 /* Number of kernels the library launched since the counter was reset. */
 long long cambgpu_kernel_launches(int reset);
 /* Message of the calling thread's last error (empty if none). */

@@ -49,6 +49,15 @@ def test_ode_controls_validate_arguments(lib):
         assert lib.cambgpu_set_ode_schedule(sched) == 0
 
 
+def test_fp64_pipe_probe_validates_arguments(lib):
+    import ctypes
+    v = ctypes.c_double()
+    assert lib.cambgpu_probe_fp64_pipe(0, 32, 8, ctypes.byref(v)) == 2
+    assert lib.cambgpu_probe_fp64_pipe(4, 33, 8, ctypes.byref(v)) == 2
+    assert lib.cambgpu_probe_fp64_pipe(4, 32, 3, ctypes.byref(v)) == 2
+    assert lib.cambgpu_probe_fp64_pipe(4, 32, 8, None) == 2
+
+
 def test_noalloc_rejects_oversized_problem_before_any_device_call(lib):
     """The allocation-free LOS entry point checks the problem against its fixed scratch
     array first: an oversized problem is refused with code 2 and a message naming the
