@@ -438,15 +438,16 @@ def main():
     tuned = None
     if not args.team and not args.no_autotune:
         best = (C.c_int * 4)()
-        times = np.zeros(13)
+        times = np.zeros(16)
         _lib.check(lib.cambgpu_autotune_ode(arr, B, best, _lib.dptr(times)))
-        sched = [0] * 11 + [1, 1]
-        tried = [i for i in range(13) if times[i] > 0]
+        sched = [0] * 11 + [1] * 5
+        tried = [i for i in range(16) if times[i] > 0]
         tuned = {"team": best[0], "queue_order": best[1], "blocks_per_sm_cap": best[3],
                  "schedule": "static stride" if sched[min(tried, key=lambda i: times[i])] else "queue counter",
                  "candidates": "team,order,blocks-per-SM cap,schedule: 32,0,0,0 1,0,0,0 1,2,0,0 2,2,0,0 1,3,2,0 "
-                               "1,2,2,0 2,2,2,0 1,1,2,0 6,0,0,0 7,2,0,0 7,3,0,0 7,2,0,1 7,3,0,1",
-                 "candidate_ode_ms": [round(x, 2) for x in times[:13]]}
+                               "1,2,2,0 2,2,2,0 1,1,2,0 6,0,0,0 7,2,0,0 7,3,0,0 7,2,0,1 7,3,0,1 7,4,0,1 "
+                               "1,4,0,1 2,4,0,1",
+                 "candidate_ode_ms": [round(x, 2) for x in times[:16]]}
     # ---- device-resident pipeline, FP64 form then mixed precision ----
     _lib.check(lib.cambgpu_batch_prepare(arr, B))
 

@@ -521,6 +521,11 @@ struct Batch {
   // queue order 3: decreasing measured cost (evaluations x system size) of the last run
   WorkItem* d_items_cost = nullptr;
   std::vector<WorkItem> h_items_cost;
+  // queue order 4: the static-stride queue of a launch of bal_threads threads, balanced by
+  // the last run's measured costs (build_balanced_order); bal_n entries incl. empty slots
+  WorkItem* d_items_bal = nullptr;
+  size_t bal_cap = 0;
+  int bal_threads = 0, bal_n = 0, bal_gen = 0, bal_tried = 0;
   unsigned* d_mode_evals = nullptr;  // [nitems], cosmology-major
   std::vector<size_t> mode_base;     // first mode_evals entry of each cosmology
   bool costs_valid = false, cost_order = false;
@@ -597,6 +602,9 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   for (auto* v : B.views) nitems += v->nk;
   total += ((size_t)n * sizeof(DevCosmo) + 255) + ((size_t)n * 8 + 255) + 4 * (nitems * sizeof(WorkItem) + 255) +
            1024 + ((size_t)n * 4 + 255) + (nitems * 4 + 255);
+  // balanced queue (order 4): the items plus the empty slots of partial rounds
+  const size_t bal_cap = 2 * nitems + 2 * (size_t)g_rt.nsm * 2048;
+  total += (bal_cap * sizeof(WorkItem) + 255);
   rc = g_rt.arena.reserve(total);
   if (rc) return set_err(rc, "device allocation failed");
   B.d_status = g_rt.arena.take<int>(n);
@@ -709,6 +717,8 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   // every mode's evaluations (build_cost_order)
   B.h_items_cost = B.h_items_grp;
   B.d_items_cost = g_rt.arena.take<WorkItem>(items.size());
+  B.d_items_bal = g_rt.arena.take<WorkItem>(bal_cap);
+  B.bal_cap = bal_cap;
   copies.push_back({B.d_items_cost, {B.h_items_cost.data(), items.size() * sizeof(WorkItem)}});
   // single pinned staging buffer for all uploads
   size_t stage = 0;
@@ -782,31 +792,50 @@ int ode_order(const Batch& B) { return g_order >= 0 ? g_order : g_tuned[size_cla
 int ode_cap(const Batch& B) { return g_blocks_cap > 0 ? g_blocks_cap : g_team ? 0 : g_tuned[size_class(B)].cap; }
 int ode_sched(const Batch& B) { return g_sched >= 0 ? g_sched : g_team ? 0 : g_tuned[size_class(B)].sched; }
 
-int run_ode(Batch& B) {
-  CUDA_TRY(cudaMemsetAsync(B.d_counter, 0, sizeof(int), g_rt.stream));
-  CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
-  int team = pick_team(B);
-  int order = ode_order(B);
+// blocks and threads per block of the ODE launch
+void ode_launch_shape(const Batch& B, int team, int& blocks, int& tpb) {
   const int lanes = (team <= 5 || team == 7) ? 1 : team == 6 ? 32 : team;
   // Few modes (a single cosmology): one warp per block, so that the warps spread over the
   // SMs and none shares an SM's FP64 pipe; otherwise blocks of 128.  The shared-memory
   // warp kernel always runs one warp per block.
   const long threads_needed = (long)B.nitems * lanes;
-  const int tpb = (team == 6 || threads_needed < 2L * 128 * g_rt.nsm) ? 32 : 128;
+  tpb = (team == 6 || threads_needed < 2L * 128 * g_rt.nsm) ? 32 : 128;
   int per_sm = std::max(1, ode_blocks_per_sm(team, tpb, B.warp_stride));
   // a cap below the occupancy limit leaves modes in the queue for threads that finish early
   // the cap counts resident threads in units of 128 (a 32-thread-block launch may keep
   // four times as many blocks)
   const int cap = ode_cap(B);
   if (cap > 0) per_sm = std::min(per_sm, cap * (128 / tpb));
-  int blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
+  blocks = (int)std::min<long>((long)g_rt.nsm * per_sm, (threads_needed + tpb - 1) / tpb);
   if (blocks < 1) blocks = 1;
+}
+
+// the balanced queue applies to thread-per-mode launches with the static-stride schedule
+bool balanced_applies(const Batch& B, int team) {
+  return ode_order(B) == 4 && (team <= 5 || team == 7) && ode_sched(B) == 1;
+}
+
+int run_ode(Batch& B) {
+  CUDA_TRY(cudaMemsetAsync(B.d_counter, 0, sizeof(int), g_rt.stream));
+  CUDA_TRY(cudaMemsetAsync(B.d_evals, 0, sizeof(unsigned long long), g_rt.stream));
+  int team = pick_team(B);
+  int order = ode_order(B);
+  int blocks, tpb;
+  ode_launch_shape(B, team, blocks, tpb);
   const WorkItem* queue = order == 3 ? B.d_items_cost : order == 2 ? B.d_items_grp : order == 1 ? B.d_items_rev : B.d_items;
+  int nq = B.nitems;
+  if (order == 4) {
+    queue = B.d_items_grp;  // until a run has measured the costs, or for other schedules
+    if (balanced_applies(B, team) && B.bal_threads == blocks * tpb) {
+      queue = B.d_items_bal;
+      nq = B.bal_n;
+    }
+  }
   // static stride: no queue counter (the kernel derives every item from its thread index);
   // only the tpm kernels (teams 1-7) have that schedule, the register warp kernels (8, 16,
   // 32) always take their items from the counter
   int* counter = (ode_sched(B) == 1 && team <= 7) ? nullptr : B.d_counter;
-  CUDA_TRY(launch_ode_kernel(team, blocks, tpb, g_rt.stream, B.d_cosmos, queue, B.nitems, counter,
+  CUDA_TRY(launch_ode_kernel(team, blocks, tpb, g_rt.stream, B.d_cosmos, queue, nq, counter,
                              B.transfer, B.warp_stride));
   g_launches++;
   return 0;
@@ -902,6 +931,82 @@ int build_cost_order(Batch& B) {
   return 0;
 }
 
+// Queue order 4 for a static-stride launch of T threads (thread t takes entries t, t + T,
+// t + 2T, ...): the q-band order (2) cut into bundles of 32 neighbouring modes -- one warp's
+// lanes, which share hierarchy sizes and switch sequences -- and the bundles dealt to the
+// T/32 warps longest first, each to the warp with the least work so far (LPT), the cost of a
+// bundle being its costliest mode's evaluations x system size in the last run.  Warps are
+// then ranked by their number of bundles so that round k of the stride holds the k-th
+// bundles of the warps that have one; the few slots left over are empty (cosmo = -1).
+int build_balanced_order(Batch& B, int T) {
+  B.bal_tried = T;
+  std::vector<unsigned> ev(B.nitems);
+  CUDA_TRY(cudaMemcpy(ev.data(), B.d_mode_evals, ev.size() * 4, cudaMemcpyDeviceToHost));
+  const int nw = std::max(1, T / 32);
+  const int nb = (B.nitems + 31) / 32;
+  std::vector<double> bcost(nb, 0.0);
+  for (int i = 0; i < B.nitems; ++i) {
+    const WorkItem& w = B.h_items_grp[i];
+    const CambGpuTables& t = *B.views[w.cosmo];
+    const CambGpuModeSpec& ms = t.modes[w.mode];
+    double nv = 4 + (ms.lmaxg + 1) + (ms.lmaxnr + 1) + ms.lmaxgpol - 1;
+    if (t.nu_eig > 0) nv += (ms.lmaxnu + 1) * (1 + t.nu_eig * t.nqmax);
+    bcost[i / 32] = std::max(bcost[i / 32], (double)ev[B.mode_base[w.cosmo] + w.mode] * nv);
+  }
+  std::vector<int> border(nb);
+  for (int b = 0; b < nb; ++b) border[b] = b;
+  std::stable_sort(border.begin(), border.end(), [&](int a, int b) { return bcost[a] > bcost[b]; });
+  std::vector<double> load(nw, 0.0);
+  std::vector<std::vector<int>> wb(nw);
+  // min-heap of (load, warp)
+  std::vector<std::pair<double, int>> heap;
+  for (int w = 0; w < nw; ++w) heap.push_back({0.0, w});
+  auto cmp = [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+    return a.first > b.first || (a.first == b.first && a.second > b.second);
+  };
+  std::make_heap(heap.begin(), heap.end(), cmp);
+  for (int b : border) {
+    std::pop_heap(heap.begin(), heap.end(), cmp);
+    auto top = heap.back();
+    heap.pop_back();
+    wb[top.second].push_back(b);
+    top.first += bcost[b];
+    heap.push_back(top);
+    std::push_heap(heap.begin(), heap.end(), cmp);
+  }
+  std::vector<int> rank(nw);
+  for (int w = 0; w < nw; ++w) rank[w] = w;
+  std::stable_sort(rank.begin(), rank.end(), [&](int a, int b) { return wb[a].size() > wb[b].size(); });
+  const WorkItem empty{-1, 0};
+  std::vector<WorkItem> q;
+  size_t rounds = wb[rank[0]].size();
+  for (size_t k = 0; k < rounds; ++k) {
+    for (int r = 0; r < nw; ++r) {
+      const std::vector<int>& bl = wb[rank[r]];
+      if (k >= bl.size()) break;  // ranked by bundle count: no later warp has round k
+      for (int l = 0; l < 32; ++l) {
+        const int i = bl[k] * 32 + l;
+        q.push_back(i < B.nitems ? B.h_items_grp[i] : empty);
+      }
+    }
+    // threads beyond the ranked warps (T not a multiple of 32) and the rest of the round
+    if (k + 1 < rounds) {
+      size_t full = (size_t)(k + 1) * T;
+      while (q.size() < full) q.push_back(empty);
+    }
+  }
+  B.bal_gen++;
+  if (q.size() > B.bal_cap) {  // too many partial rounds: keep the q-band order
+    B.bal_threads = -1;
+    B.bal_n = 0;
+    return 0;
+  }
+  CUDA_TRY(cudaMemcpy(B.d_items_bal, q.data(), q.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+  B.bal_n = (int)q.size();
+  B.bal_threads = T;
+  return 0;
+}
+
 // under stream capture the stage boundaries are external event records, so that in the
 // graph they stay event-record nodes the host can time and wait on
 int enqueue_all(Batch& B, bool do_ode, bool do_los, bool do_cls, bool capturing) {
@@ -924,6 +1029,7 @@ long long run_key(const Batch& B, bool do_ode, bool do_los, bool do_cls) {
   k = k * 64 + ode_cap(B);
   k = k * 2 + ode_sched(B);
   k = k * 4 + g_precision;
+  k = k * 4096 + (B.bal_gen & 4095);  // each build of the balanced queue is a new graph
   return k * 8 + (do_ode ? 4 : 0) + (do_los ? 2 : 0) + (do_cls ? 1 : 0);
 }
 
@@ -960,6 +1066,15 @@ int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
   if (do_ode && B.costs_valid && !B.cost_order && ode_order(B) == 3) {
     int rc = build_cost_order(B);  // outside any capture: a synchronous copy each way
     if (rc) return rc;
+  }
+  if (do_ode && B.costs_valid) {
+    const int team = pick_team(B);
+    int blocks, tpb;
+    ode_launch_shape(B, team, blocks, tpb);
+    if (balanced_applies(B, team) && B.bal_tried != blocks * tpb) {
+      int rc = build_balanced_order(B, blocks * tpb);  // outside any capture
+      if (rc) return rc;
+    }
   }
   if (B.runs == 0) {
     int rc = enqueue_all(B, do_ode, do_los, do_cls, false);
@@ -1449,8 +1564,8 @@ int cambgpu_set_ode_schedule(int schedule) {
 }
 
 int cambgpu_set_ode_launch(int queue_order, int blocks_per_sm) {
-  if (queue_order < -1 || queue_order > 3 || blocks_per_sm < 0)
-    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "queue order must be -1..3 and blocks per SM >= 0");
+  if (queue_order < -1 || queue_order > 4 || blocks_per_sm < 0)
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "queue order must be -1..4 and blocks per SM >= 0");
   g_order = queue_order;
   g_blocks_cap = blocks_per_sm;
   return 0;
@@ -1472,7 +1587,8 @@ int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times
   // 4th column: schedule (0 = queue counter, 1 = static stride)
   static const int cand[][4] = {{32, 0, 0, 0}, {1, 0, 0, 0}, {1, 2, 0, 0}, {2, 2, 0, 0}, {1, 3, 2, 0},
                                 {1, 2, 2, 0},  {2, 2, 2, 0}, {1, 1, 2, 0}, {6, 0, 0, 0}, {7, 2, 0, 0},
-                                {7, 3, 0, 0},  {7, 2, 0, 1}, {7, 3, 0, 1}};
+                                {7, 3, 0, 0},  {7, 2, 0, 1}, {7, 3, 0, 1}, {7, 4, 0, 1}, {1, 4, 0, 1},
+                                {2, 4, 0, 1}};
   const int nc = (int)(sizeof(cand) / sizeof(cand[0]));
   int rc = cambgpu_batch_prepare(p, n);
   if (rc) return rc;

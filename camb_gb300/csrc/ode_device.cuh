@@ -1993,6 +1993,7 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
       first = -1;
       if (w >= nitems) break;
       const WorkItem it = items[w];
+      if (it.cosmo < 0) continue;  // an empty slot of a balanced queue
       cosmo = it.cosmo;
       q_ix = it.mode;
       mode_init<W>(cosmos[cosmo], q_ix, M, Wk, R);

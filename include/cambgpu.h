@@ -301,8 +301,11 @@ int cambgpu_set_ode_schedule(int schedule);
  * n cosmologies and keeps the fastest for that batch-size class.  Queue orders: 0 = decreasing q,
  * 1 = increasing q, 2 = bands of q with the cosmologies of each band ordered by neutrino
  * mass, 3 = decreasing cost measured by the batch's previous run (evaluations x system
- * size; order 2 until a run has recorded it).  best = [team, order, class, cap]; times
- * (optional, >= 13 entries) receives ms per
+ * size; order 2 until a run has recorded it), 4 = order 2 cut into bundles of 32 modes
+ * dealt to the warps of a static-stride launch by the previous run's costs, longest
+ * first, so that every warp gets the same work (thread-per-mode kernels with the
+ * static-stride schedule; order 2 otherwise or until a run has recorded the costs).
+ * best = [team, order, class, cap]; times (optional, >= 16 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);
 /* Wall-clock split of the last cambgpu_get_spectra_batch / get_results_batch /

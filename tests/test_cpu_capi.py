@@ -38,7 +38,8 @@ def test_prepare_tables_reports_bad_members(lib):
 def test_ode_controls_validate_arguments(lib):
     assert lib.cambgpu_set_ode_team(9) == 2
     assert lib.cambgpu_set_ode_team(-1) == 2
-    assert lib.cambgpu_set_ode_launch(4, 0) == 2
+    assert lib.cambgpu_set_ode_launch(5, 0) == 2
+    assert lib.cambgpu_set_ode_launch(4, 0) == 0
     assert lib.cambgpu_set_ode_launch(2, -1) == 2
     for team in (0, 1, 5, 6, 7, 8, 16, 32):
         assert lib.cambgpu_set_ode_team(team) == 0

@@ -187,7 +187,8 @@ def test_queue_orders_and_caps_give_identical_results():
     try:
         for team, order, cap, sched in [(1, 0, 0, 0), (1, 2, 2, 0), (1, 3, 2, 0), (1, 3, 1, 0), (1, 1, 0, 0),
                                         (1, 2, 2, 1), (1, 0, 0, 1), (7, 2, 0, 0), (7, 2, 0, 1), (7, 3, 0, 1),
-                                        (6, 0, 0, 0), (6, 0, 0, 1)]:
+                                        (6, 0, 0, 0), (6, 0, 0, 1), (7, 4, 0, 1), (1, 4, 0, 1), (1, 4, 3, 1),
+                                        (7, 4, 0, 0)]:
             _lib.check(lib.cambgpu_set_ode_team(team))
             _lib.check(lib.cambgpu_set_ode_launch(order, cap))
             _lib.check(lib.cambgpu_set_ode_schedule(sched))
