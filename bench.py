@@ -142,10 +142,49 @@ def gradient_rate(n=64, lmax=2500, seed=3000, mnu_max=0.2):
     t0 = time.perf_counter()
     cls, g = gradients.cl_gradients(ps)
     t = time.perf_counter() - t0
-    return {"value": n / t, "unit": "gradients/s (dC_l/d 6 parameters, l <= %d, unlensed)" % lmax, "batch": n,
-            "seconds": t, "method": "central differences through the batched pipeline: ombh2, omch2, H0, tau "
-                                    "re-evolved (+-1e-4 relative, 9 cosmologies per gradient in one launch); "
-                                    "As, ns by reweighting the resident transfer functions"}
+    out = {"value": n / t, "unit": "gradients/s (dC_l/d 6 parameters, l <= %d, unlensed)" % lmax, "batch": n,
+           "seconds": t, "method": "central differences through the batched pipeline: ombh2, omch2, H0, tau "
+                                   "re-evolved (+-1e-4 relative, 9 cosmologies per gradient in one launch); "
+                                   "As, ns by reweighting the resident transfer functions"}
+    out.update(gradient_checks(ps[:2], g[:2]))
+    return out
+
+
+def gradient_checks(ps, g):
+    """On the first draws of the gradient batch (outside the timed call): the largest
+    disagreement of the GPU's central differences with the oracle's (same perturbed
+    cosmologies, sampled l, TT/EE/TE, relative to each gradient's peak over l) per
+    parameter, and the finite-difference noise as the disagreement of relative steps 1e-4
+    and 3e-4 (GPU, same statistic; median and largest over l)."""
+    import copy
+    from camb_gb300 import _lib, gradients
+    from oracle import oracle as orc
+    vs_oracle, noise = {}, {}
+    _, g3 = gradients.cl_gradients(ps, rel_step=3e-4)
+    for name in gradients.EVOLVED:
+        j = gradients.PARAMS.index(name)
+        worst, med, mx = 0.0, 0.0, 0.0
+        for i, p in enumerate(ps):
+            v = gradients.get_param(p, name)
+            h = 1e-4 * abs(v)
+            icl = []
+            for sgn in (1.0, -1.0):
+                q = copy.deepcopy(p)
+                gradients.set_param(q, name, v + sgn * h)
+                T = _lib.Tables(q.to_struct())
+                icl.append(orc.cls(T, orc.los(T, orc.evolve_sources(T))))
+            ls = T.ls
+            ref = (icl[0] - icl[1]) / (2 * h)
+            for cg, cr in [(0, 0), (1, 1), (3, 2)]:
+                peak = np.max(np.abs(ref[:, cr]))
+                worst = max(worst, float(np.max(np.abs(g[i, j][ls, cg] - ref[:, cr])) / peak))
+                d = np.abs(g[i, j][ls, cg] - g3[i, j][ls, cg]) / np.max(np.abs(g[i, j][ls, cg]))
+                med, mx = max(med, float(np.median(d))), max(mx, float(d.max()))
+        vs_oracle[name] = worst
+        noise[name] = {"median": med, "max": mx}
+    return {"max_rel_disagreement_vs_oracle_fd": vs_oracle,
+            "fd_noise_step_1e-4_vs_3e-4": noise,
+            "checked_draws": len(ps)}
 
 
 def lensed_batch(n, lmax=2500, seed=5000, mnu_max=0.2):
