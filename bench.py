@@ -80,18 +80,21 @@ def plain_form_rate(n=3, lmax=2500, seed=1000, mnu_max=0.2):
     return n / t
 
 
-# DRAM bytes (read + write) of one ODE launch of the headline workload per thread-per-mode
-# variant (team code): ncu dram__bytes_read.sum + dram__bytes_write.sum of the fourth ODE
-# launch of `python -m camb_gb300.kernel_case thread256r` (team 7) and `... thread256`
-# (team 1), one pass each
+# DRAM bytes (read + write) of one ODE launch of the headline workload per (team code, queue
+# order): ncu dram__bytes_read.sum + dram__bytes_write.sum of the fourth ODE launch of
+# `python -m camb_gb300.kernel_case team7_256_o<order>_s1` (static stride), one pass each
+# (profiles/ode_thread_kernel_dram_batch256_lmax2500.md)
 ODE_TRAFFIC = {
-    7: (0.8307e12 + 0.4565e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
-                               "(team 7: compiled for 2 resident blocks/SM, queue order 2, captured with the "
-                               "queue-counter schedule; kernel case thread256r, DRAM summary under profiles/)"),
-    1: (1.10e12 + 0.493e12, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
-                            "(team 1, queue order 2, 2 blocks/SM; kernel case thread256, DRAM summary under "
-                            "profiles/)"),
+    (7, 4): (916.02e9 + 447.24e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
+                                  "(team 7, balanced queue order 4, static stride; kernel case team7_256_o4_s1)"),
+    (7, 2): (642.02e9 + 383.11e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
+                                  "(team 7, q-band queue order 2, static stride; kernel case team7_256_o2_s1)"),
 }
+# FP64 flops per right-hand-side evaluation (2 DFMA + DMUL + DADD thread instructions,
+# stage combinations, error norm and source output included), ncu on the 32-draw case of
+# this workload (kernel case thread32, profiles/ode_thread_kernel_batch32_lmax2500.md)
+FLOPS_PER_EVAL = 1182
+NOMINAL_FP64_TFLOPS = 152 * 2.07e9 * 4 / 1e12  # SMs x max SM clock x 4 flop per cycle
 
 
 def hbm_peak():
@@ -559,10 +562,12 @@ def main():
     # FP64 flops per right-hand-side evaluation, stage combinations and error norm
     # included: 2*DFMA + DMUL + DADD thread instructions per evaluation counted by ncu on
     # a 32-draw case of this workload (mnu 0-0.2 eV, lmax 2500)
-    flops_per_eval = float(os.environ.get("CAMBGPU_FLOPS_PER_EVAL", "1315"))
+    flops_per_eval = float(FLOPS_PER_EVAL)
     achieved = flops_per_eval * evals_step / (ode_ms * 1e-3) / 1e12
     ode_team = args.team or (tuned["team"] if tuned else 0)
-    traffic, traffic_src = ODE_TRAFFIC.get(ode_team, (None, f"no ncu capture of team {ode_team} on this workload"))
+    ode_order = tuned["queue_order"] if tuned else -1
+    traffic, traffic_src = ODE_TRAFFIC.get((ode_team, ode_order),
+                                           (None, f"no ncu capture of team {ode_team}, order {ode_order}"))
     if tuned and traffic:
         traffic_src += f"; the timed launches use the {tuned['schedule']} schedule"
     prec = {0: "FP64 throughout",
@@ -592,13 +597,18 @@ def main():
             "roofline": {"bound": "fp64", "kernel": "ode_thread_kernel", "achieved": achieved, "peak": tf.value,
                          "unit": "TFLOP/s", "frac": achieved / tf.value, "traffic": traffic,
                          "peak_source": "DFMA-chain probe measured in this run (MEASURED_PEAKS.json has no FP64)",
+                         "frac_of_nominal_fp64": achieved / NOMINAL_FP64_TFLOPS,
+                         "nominal_fp64_tflops": NOMINAL_FP64_TFLOPS,
                          "flops_per_eval": flops_per_eval, "evals_per_step": evals_step,
                          "traffic_source": traffic_src,
                          "dram_gbs": traffic / (ode_ms * 1e-3) / 1e9 if traffic else None,
                          "dram_frac_of_measured_copy":
                              traffic / (ode_ms * 1e-3) / 1e9 / hbm_peak() if traffic else None,
-                         "reading": "stage rows of the resident modes (~250 MB) exceed L2 and stream through DRAM; "
-                                    "the kernel is bound by the latency of those local-memory streams"},
+                         "flops_source": "ncu 2 DFMA + DMUL + DADD thread instructions per evaluation, kernel case "
+                                         "thread32 (profiles/ode_thread_kernel_batch32_lmax2500.md)",
+                         "reading": "the seven stage rows of the resident modes exceed L1 and L2 and stream through "
+                                    "DRAM; a warp issues one FP64 instruction per 64 cycles and two warps per "
+                                    "sub-partition cannot cover that latency (profiles/fp64_issue_model.md)"},
             "clocks": clk, "wall_s_timed": wall}
     if rank == 0:
         nth = os.cpu_count() or 1
