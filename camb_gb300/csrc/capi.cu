@@ -53,7 +53,7 @@ int g_precision = 0;  // 0: FP64 throughout; 1: mixed-precision line-of-sight pr
 struct OdeCfg { int team; int order; int cap; int sched; };
 // untuned defaults: warp per mode (shared-memory rows) for few modes, where latency
 // decides; thread per mode for large batches, where FP64 throughput does
-OdeCfg g_tuned[2] = {{6, 0, 0, 0}, {7, 2, 0, 0}};
+OdeCfg g_tuned[2] = {{6, 0, 0, 0}, {7, 4, 0, 1}};
 constexpr int kWarpStrideMax = 448;  // the shared-memory warp kernel's largest state row
 int g_order = -1;  // forced queue order (-1: use the tuned one)
 int g_blocks_cap = 0;  // resident ODE blocks per SM (0: as many as fit)
