@@ -124,6 +124,8 @@ SIGNATURES = {
     "cambgpu_last_transfer_bytes": (C.c_int, [C.POINTER(C.c_longlong)]),
     "cambgpu_probe_fp64_tflops": (C.c_int, [_c_double_p]),
     "cambgpu_probe_fp64_pipe": (C.c_int, [C.c_int, C.c_int, C.c_int, _c_double_p]),
+    "cambgpu_gemm_bf16x3": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int, C.c_int,
+                                      C.POINTER(C.c_float)]),
     "cambgpu_kernel_launches": (C.c_longlong, [C.c_int]),
     "cambgpu_last_error": (C.c_char_p, []),
 }

@@ -321,6 +321,12 @@ long long cambgpu_last_ode_evals(void);
 int cambgpu_last_transfer_bytes(long long* out2);
 /* Measures the device's FP64 FMA throughput (TFLOP/s) with a DFMA-chain kernel. */
 int cambgpu_probe_fp64_tflops(double* tflops);
+/* Split hi/lo BF16 matrix product on the tensor cores (tcgen05.mma, FP32 accumulation in
+ * tensor memory; no counterpart in the reference, whose projection is FP64 loops):
+ * D[m][n] = sum_k A[m][k] B[n][k] for row-major host buffers A [M][K], B [N][K], D [M][N],
+ * each FP32 operand split into a BF16 pair and D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
+ * The primitive of the shared-grid projection; sizes 1-65536. */
+int cambgpu_gemm_bf16x3(const float* A, const float* B, int M, int N, int K, float* D);
 /* The FP64 issue model behind the ODE kernels' design (no counterpart in the reference):
  * one block per SM with warps_per_sm warps, active_lanes lanes of each warp running
  * `chains` (1, 4 or 8) independent DFMA chains; returns the lane FMAs retired per SM

@@ -1,6 +1,7 @@
 """Host-only entry points of the C ABI on CPU (no device call is made): building a batch's
 host tables ahead of its device run, error codes and per-cosmology status for invalid
 parameters, and the argument checks of the ODE controls."""
+import ctypes
 import ctypes as C
 
 import numpy as np
@@ -57,6 +58,15 @@ def test_fp64_pipe_probe_validates_arguments(lib):
     assert lib.cambgpu_probe_fp64_pipe(4, 33, 8, ctypes.byref(v)) == 2
     assert lib.cambgpu_probe_fp64_pipe(4, 32, 3, ctypes.byref(v)) == 2
     assert lib.cambgpu_probe_fp64_pipe(4, 32, 8, None) == 2
+
+
+def test_gemm_bf16x3_validates_arguments(lib):
+    fp = ctypes.POINTER(ctypes.c_float)
+    a = np.zeros(4, dtype=np.float32)
+    p = a.ctypes.data_as(fp)
+    assert lib.cambgpu_gemm_bf16x3(p, p, 0, 1, 1, p) == 2
+    assert lib.cambgpu_gemm_bf16x3(p, p, 1, 1, 70000, p) == 2
+    assert lib.cambgpu_gemm_bf16x3(None, p, 1, 1, 1, p) == 2
 
 
 def test_noalloc_rejects_oversized_problem_before_any_device_call(lib):
