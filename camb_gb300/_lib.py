@@ -103,6 +103,8 @@ SIGNATURES = {
                                                _c_int_p, _c_double_p, _c_double_p, _c_int_p]),
     "cambgpu_lensing_range": (C.c_int, [C.POINTER(CambGpuTables), _c_int_p]),
     "cambgpu_batch_prepare": (C.c_int, [C.POINTER(CambGpuParams), C.c_int]),
+    "cambgpu_batch_prepare_shared": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, _c_int_p]),
+    "cambgpu_tables_share_grids": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, _c_int_p]),
     "cambgpu_batch_run": (C.c_int, [_c_double_p]),
     "cambgpu_batch_fetch": (C.c_int, [C.c_int, _c_double_p]),
     "cambgpu_batch_release": (None, []),

@@ -17,7 +17,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["ode_thread_a.cu", "ode_thread_b.cu", "ode_thread_c.cu", "ode_thread_d.cu", "ode_thread_e.cu",
               "ode_warp.cu",
-              "ode_kernel.cu", "los_kernel.cu", "cl_lensing.cu", "capi.cu", "noalloc.cu", "tc_gemm.cu"]
+              "ode_kernel.cu", "los_kernel.cu", "cl_lensing.cu", "capi.cu", "noalloc.cu", "tc_gemm.cu", "tc_proj.cu"]
 TEMPLATE = os.path.join(HERE, "data", "highl_template.f64")
 CXX_SOURCES = ["host/cosmo_host.cpp"]
 

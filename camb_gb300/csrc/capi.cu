@@ -25,6 +25,8 @@ cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s,
                               const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride);
 cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s);
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
+cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, const double* chi, const double* dchi,
+                           int nchi, int* err, cudaStream_t s);
 cudaError_t launch_fp64_pipe_probe(int nsm, int warps, int lanes, int chains, int iters, long long* cyc, double* out,
                                    cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
@@ -523,6 +525,12 @@ struct Batch {
   std::vector<WorkItem> h_items_cost;
   // queue order 4: the static-stride queue of a launch of bal_threads threads, balanced by
   // the last run's measured costs (build_balanced_order); bal_n entries incl. empty slots
+  // shared grids (cambgpu_batch_prepare_shared): the comoving-distance nodes every
+  // cosmology's time steps are taken from, for the tensor-core projection (precision 2)
+  bool shared = false;
+  std::vector<double> h_chi, h_dchi;
+  double *d_chi = nullptr, *d_dchi = nullptr;
+  int* d_tc_err = nullptr;
   WorkItem* d_items_bal = nullptr;
   size_t bal_cap = 0;
   int bal_threads = 0, bal_n = 0, bal_gen = 0, bal_tried = 0;
@@ -605,6 +613,7 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   // balanced queue (order 4): the items plus the empty slots of partial rounds
   const size_t bal_cap = 2 * nitems + 2 * (size_t)g_rt.nsm * 2048;
   total += (bal_cap * sizeof(WorkItem) + 255);
+  total += 2 * (B.h_chi.size() * 8 + 255) + 256;  // shared chi nodes and weights, error flag
   rc = g_rt.arena.reserve(total);
   if (rc) return set_err(rc, "device allocation failed");
   B.d_status = g_rt.arena.take<int>(n);
@@ -719,6 +728,13 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   B.d_items_cost = g_rt.arena.take<WorkItem>(items.size());
   B.d_items_bal = g_rt.arena.take<WorkItem>(bal_cap);
   B.bal_cap = bal_cap;
+  B.d_tc_err = g_rt.arena.take<int>(1);
+  if (B.shared) {
+    B.d_chi = g_rt.arena.take<double>(B.h_chi.size());
+    B.d_dchi = g_rt.arena.take<double>(B.h_dchi.size());
+    copies.push_back({B.d_chi, {B.h_chi.data(), B.h_chi.size() * 8}});
+    copies.push_back({B.d_dchi, {B.h_dchi.data(), B.h_dchi.size() * 8}});
+  }
   copies.push_back({B.d_items_cost, {B.h_items_cost.data(), items.size() * sizeof(WorkItem)}});
   // single pinned staging buffer for all uploads
   size_t stage = 0;
@@ -844,6 +860,18 @@ int run_ode(Batch& B) {
 int run_los(Batch& B) {
   int n = (int)B.views.size();
   dim3 g1((B.max_rows + 127) / 128, n);
+  if (g_precision == 2) {
+    // split hi/lo BF16 tensor-core projection of a batch on shared grids, on the FP64
+    // source spline
+    if (!B.shared) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "precision 2 needs a batch on shared grids");
+    source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
+    g_launches++;
+    CUDA_TRY(cudaMemsetAsync(B.d_tc_err, 0, sizeof(int), g_rt.stream));
+    CUDA_TRY(launch_proj_tc(B.d_cosmos, n, B.max_nq, B.views[0]->nsrc, B.d_chi, B.d_dchi, (int)B.h_chi.size(),
+                            B.d_tc_err, g_rt.stream));
+    g_launches++;
+    return 0;
+  }
   // mixed precision: the spline leaves FP32 {source, d2} pairs in dd_src for the FP32 staging
   if (g_precision == 1) source_spline_f32_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
   else source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
@@ -1099,6 +1127,11 @@ int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
     unsigned long long ev = 0;
     CUDA_TRY(cudaMemcpy(&ev, B.d_evals, sizeof(ev), cudaMemcpyDeviceToHost));
     g_last_evals = (long long)ev;
+  }
+  if (do_los && g_precision == 2) {
+    int terr = 0;
+    CUDA_TRY(cudaMemcpy(&terr, B.d_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (terr) return set_err(CAMBGPU_ERROR_CUDA, "tensor-core projection: a completion wait ran out");
   }
   return 0;
 }
@@ -1490,6 +1523,71 @@ int cambgpu_batch_prepare(const CambGpuParams* p, int n) {
   return 0;
 }
 
+// Puts host tables on grids shared by all of them (cg::build_shared_grid): the members'
+// time steps, source k grid, integration q grid and Bessel table are made common, so that
+// the projection of the whole batch at one q is one matrix product.  Host only.
+static int share_grids(const std::vector<Handle*>& hs, cg::SharedGrid& sg) {
+  if (hs.empty()) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "shared grids: empty batch");
+  std::vector<const cg::Cosmology*> cs;
+  const cg::Cosmology& c0 = hs[0]->c;
+  for (auto* h : hs) {
+    if (!h || !h->c.P.want_cls || (h->c.P.want_transfer && !h->c.P.want_cls) || h->c.ls != c0.ls ||
+        h->c.nsrc != c0.nsrc || h->c.P.BesselBoost != c0.P.BesselBoost || h->c.P.AccuracyBoost != c0.P.AccuracyBoost)
+      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS,
+                     "shared grids need CMB runs with one l sampling, one set of sources and one accuracy");
+    cs.push_back(&h->c);
+  }
+  if (c0.ls.size() > 128) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "shared grids: at most 128 sampled l");
+  std::string err;
+  int rc = cg::build_shared_grid(cs, sg, err);
+  if (rc) return set_err(rc, err);
+  if (sg.chi.size() > 4096) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "shared grid: more than 4096 time nodes");
+  double xmax = 0;
+  for (auto* h : hs) xmax = std::max(xmax, h->c.maximum_qeta);
+  std::shared_ptr<const cg::BesselTable> bt;
+  try {
+    bt = cg::get_bessel_table(c0.ls, xmax, c0.P.BesselBoost, c0.P.AccuracyBoost);
+  } catch (const std::exception& e) {
+    return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, e.what());
+  }
+  for (auto* h : hs) {
+    cg::apply_shared_grid(h->c, sg);
+    h->bt = bt;
+    cg::fill_view(h->c, *bt, h->view);
+  }
+  return 0;
+}
+
+int cambgpu_tables_share_grids(void** handles, int n, int* nchi_out) {
+  if (!handles || n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "share_grids: no handles");
+  std::vector<Handle*> hs(n);
+  for (int i = 0; i < n; ++i) hs[i] = static_cast<Handle*>(handles[i]);
+  cg::SharedGrid sg;
+  int rc = share_grids(hs, sg);
+  if (rc) return rc;
+  if (nchi_out) *nchi_out = (int)sg.chi.size();
+  return 0;
+}
+
+int cambgpu_batch_prepare_shared(const CambGpuParams* p, int n, int* nchi_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_res.reset(new Resident());
+  int rc = build_handles(p, n, g_res->handles, nullptr);
+  if (rc) return rc;
+  cg::SharedGrid sg;
+  rc = share_grids(g_res->handles, sg);
+  if (rc) return rc;
+  for (auto* h : g_res->handles) g_res->B.views.push_back(&h->view);
+  g_res->B.shared = true;
+  g_res->B.h_chi = sg.chi;
+  g_res->B.h_dchi = sg.dchi;
+  rc = stage_batch(g_res->B);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+  if (nchi_out) *nchi_out = (int)sg.chi.size();
+  return 0;
+}
+
 int cambgpu_batch_run(double* ms3) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (int rc = resident_check()) return rc;
@@ -1541,7 +1639,7 @@ void cambgpu_batch_release(void) {
 }
 
 int cambgpu_set_precision(int mode) {
-  if (mode != 0 && mode != 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "precision mode must be 0 or 1");
+  if (mode < 0 || mode > 2) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "precision mode must be 0, 1 or 2");
   std::lock_guard<std::mutex> lk(g_mu);
   g_precision = mode;
   return 0;

@@ -1592,6 +1592,78 @@ std::shared_ptr<const BesselTable> get_bessel_table(const std::vector<int>& ls, 
   return tab;
 }
 
+int build_shared_grid(const std::vector<const Cosmology*>& cs, SharedGrid& g, std::string& err) {
+  if (cs.empty()) {
+    err = "shared grid: empty batch";
+    return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  }
+  // k and q grids of the member with the median tau0
+  std::vector<int> order(cs.size());
+  for (size_t i = 0; i < cs.size(); ++i) order[i] = (int)i;
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return cs[a]->tau0 < cs[b]->tau0; });
+  g.grid_member = order[cs.size() / 2];
+  const Cosmology& m = *cs[g.grid_member];
+  g.evolve_q = m.evolve_q.points;
+  g.q_int = m.q_int.points;
+  g.dq_int = m.q_int.dpoints;
+  // chi grid: from chi = 0 (tau0) out to the largest chi of any member's native time
+  // steps, each step the finest native spacing of any member at that chi
+  double chi_end = 0;
+  for (const Cosmology* c : cs) chi_end = std::max(chi_end, c->tau0 - c->timesteps.points.front());
+  auto native_step = [](const Cosmology& c, double chi) {
+    const std::vector<double>& t = c.timesteps.points;
+    const double tau = c.tau0 - chi;
+    if (tau < t.front() || tau > t.back()) return 1e300;
+    size_t i = std::upper_bound(t.begin(), t.end(), tau) - t.begin();
+    if (i == 0) i = 1;
+    if (i >= t.size()) i = t.size() - 1;
+    return t[i] - t[i - 1];
+  };
+  auto min_step = [&](double chi) {
+    double h = 1e300;
+    for (const Cosmology* c : cs) h = std::min(h, native_step(*c, chi));
+    return h;
+  };
+  std::vector<double> up{0.0};
+  while (up.back() < chi_end && up.size() < 1000000) {
+    double h = min_step(up.back());
+    if (!(h < 1e299)) break;
+    h = std::min(h, min_step(up.back() + h));  // do not step over the start of a finer region
+    up.push_back(std::min(up.back() + h, chi_end));
+  }
+  if (up.size() < 4) {
+    err = "shared grid: degenerate time steps";
+    return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  }
+  const size_t n = up.size();
+  g.chi.assign(up.rbegin(), up.rend());  // decreasing chi
+  g.dchi.assign(n, 0.0);
+  g.dchi[0] = (g.chi[0] - g.chi[1]) / 2;
+  for (size_t i = 1; i + 1 < n; ++i) g.dchi[i] = (g.chi[i - 1] - g.chi[i + 1]) / 2;
+  g.dchi[n - 1] = (g.chi[n - 2] - g.chi[n - 1]) / 2;
+  return 0;
+}
+
+int apply_shared_grid(Cosmology& c, const SharedGrid& g) {
+  const double tau_floor = 0.5 * c.timesteps.points.front();
+  int first = 0;
+  while (first < (int)g.chi.size() && c.tau0 - g.chi[first] < tau_floor) ++first;
+  c.timesteps.points.clear();
+  c.timesteps.dpoints.clear();
+  for (size_t i = first; i < g.chi.size(); ++i) {
+    c.timesteps.points.push_back(c.tau0 - g.chi[i]);
+    c.timesteps.dpoints.push_back(g.dchi[i]);
+  }
+  c.timesteps.points.back() = c.tau0;
+  c.evolve_q.points = g.evolve_q;
+  c.evolve_q.dpoints.clear();
+  c.modes.clear();
+  for (double q : c.evolve_q.points) c.modes.push_back(mode_setup(c, q));
+  c.q_int.points = g.q_int;
+  c.q_int.dpoints = g.dq_int;
+  return first;
+}
+
 void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   std::memset(&v, 0, sizeof(v));
   v.grhog = c.grhog; v.grhor = c.grhor; v.grhornomass = c.grhornomass; v.grhoc = c.grhoc;

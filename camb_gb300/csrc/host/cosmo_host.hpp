@@ -125,6 +125,23 @@ struct BesselTable {
 };
 
 int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err);
+
+// Grids shared by a batch of cosmologies (the split-BF16 tensor-core projection needs one
+// Bessel matrix j_l(q chi_n) dchi_n per integration q for every member): one comoving-
+// distance grid chi_n = tau0 - tau_n (node 0 the largest chi, i.e. the earliest time), one
+// source k grid and one integration q grid.  The chi grid follows, at every chi, the finest
+// native time spacing (SetTimeSteps) of any member there, so that each member's
+// recombination and reionization stay as resolved as on its own grid.
+struct SharedGrid {
+  std::vector<double> chi, dchi;  // [nchi], decreasing chi; dchi the quadrature weights
+  std::vector<double> evolve_q, q_int, dq_int;
+  int grid_member = 0;  // the member whose k and q grids are shared
+};
+int build_shared_grid(const std::vector<const Cosmology*>& cs, SharedGrid& g, std::string& err);
+// Replaces a member's time steps (its chi nodes with tau >= taurst / 2), source k grid
+// (with its own mode set-up at each k) and integration q grid by the shared ones; returns
+// the index of the member's first chi node.
+int apply_shared_grid(Cosmology& c, const SharedGrid& g);
 std::shared_ptr<const BesselTable> get_bessel_table(const std::vector<int>& ls, double xmax,
                                                     double bessel_boost, double accuracy_boost);
 void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v);

@@ -1,0 +1,264 @@
+// Flat line-of-sight projection of a batch on shared grids as split hi/lo BF16 products on
+// the fifth-generation tensor cores (DoFlatIntegration, cmbmain.f90:1639-1862, restated as
+// a matrix product).
+//
+// With one comoving-distance grid chi_n for every cosmology of the batch (tau_n = tau0_c -
+// chi_n) and one integration q grid, the projection of source s at wavenumber q is
+//     Delta_s[l][c] = sum_n J_q[l][n] S_q,s[n][c],   J_q[l][n] = j_l(q chi_n) dchi_n,
+// one Bessel matrix per q for the whole batch.  One CTA computes a 128 (sampled l) x 128
+// (cosmologies) tile of one (q, source): it stages 64-deep K tiles of J (from the FP32 Horner
+// table, zero outside each l's integration window) and of S (the source k-spline of each
+// cosmology evaluated at q, zero outside the cosmology's time range and its q*tau < max_etak
+// prefix), split into BF16 pairs, in shared memory; one thread issues the twelve
+// tcgen05.mma per tile into an FP32 accumulator in tensor memory; the epilogue applies the
+// per-cosmology cuts of the FP64 kernel (l above q tau0, the lensed-run integration test),
+// the Limber value of the lensing source, and writes Delta_p_l_k in FP64.
+#include <cuda_runtime.h>
+
+#include "device_tables.cuh"
+#include "tc_gemm.cuh"
+
+namespace cgdev {
+namespace tc {
+
+constexpr int kProjMaxChi = 4096;  // shared chi nodes staged per CTA
+constexpr int kTileBytesP = 128 * kChunk * 2;
+constexpr size_t kProjSmem = 4 * (size_t)kTileBytesP + (size_t)kProjMaxChi * 8 + 2048;
+
+__device__ __forceinline__ int bsearch_lo_d(const double* x, int n, double v) {
+  int lo = 0, hi = n - 1;  // largest i with x[i] <= v, for x increasing
+  while (hi - lo > 1) {
+    const int m = (lo + hi) >> 1;
+    if (x[m] <= v) lo = m;
+    else hi = m;
+  }
+  return lo;
+}
+
+// number of shared nodes with chi_n >= v (chi decreasing)
+__device__ __forceinline__ int count_ge(const double* chi, int n, double v) {
+  int lo = 0, hi = n;  // chi[0..lo) >= v, chi[hi..n) < v
+  while (lo < hi) {
+    const int m = (lo + hi) >> 1;
+    if (chi[m] >= v) lo = m + 1;
+    else hi = m;
+  }
+  return lo;
+}
+
+// the source k-spline of one cosmology at q for time row i (InterpolateSources)
+struct KW {
+  int klo, khi;
+  double a0, b0, a03, b03, ho2o6;
+};
+__device__ __forceinline__ double src_at(const DevCosmo& C, const KW& K, int i, int s) {
+  const size_t b = ((size_t)i * C.nsrc + s) * C.nk;
+  return K.a0 * C.linear_src[b + K.klo] + K.b0 * C.linear_src[b + K.khi] +
+         (K.a03 * C.dd_src[b + K.klo] + K.b03 * C.dd_src[b + K.khi]) * K.ho2o6;
+}
+
+// row i of cosmology C holds a source at q: 1 <= i and the prefix test of source_row_count
+__device__ __forceinline__ bool row_valid(const DevCosmo& C, double q, int i) {
+  if (i < 1 || i >= C.ntau) return false;
+  const double tau = C.tau_points[i];
+  const bool etak_ok = C.want_late_time || q * tau < C.max_etak_scalar;
+  return etak_ok && q * (C.tau0 - tau) > 1e-8;
+}
+
+__global__ void __launch_bounds__(128, 1)
+    proj_tc_kernel(const DevCosmo* __restrict__ cosmos, int ncosmo, const double* __restrict__ chi,
+                   const double* __restrict__ dchi, int nchi, int* __restrict__ err) {
+  extern __shared__ unsigned char tp_smem_raw[];
+  unsigned char* base = tp_smem_raw + ((1024 - (smem_u32(tp_smem_raw) & 1023)) & 1023);
+  unsigned char* a_hi = base;
+  unsigned char* a_lo = base + kTileBytesP;
+  unsigned char* b_hi = base + 2 * kTileBytesP;
+  unsigned char* b_lo = base + 3 * kTileBytesP;
+  int* s_bix = reinterpret_cast<int*>(base + 4 * kTileBytesP);             // [nchi]
+  float* s_a2 = reinterpret_cast<float*>(s_bix + kProjMaxChi);            // [nchi]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(s_a2 + kProjMaxChi);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  __shared__ int s_kbeg, s_kend;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ctile = blockIdx.x, src = blockIdx.y, q_ix = blockIdx.z;
+  const DevCosmo& G = cosmos[0];  // shared grids: q, k, l sampling, Bessel table
+  const double q = G.q_int[q_ix];
+  const int nl = G.nl, nbx = G.num_xx;
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    s_kbeg = nchi;
+    s_kend = 0;
+  }
+  if (warp == 0) tmem_alloc(tslot, 128);
+  __syncthreads();  // s_kbeg / s_kend initialised before the atomics below
+  // Bessel-table interval and Horner variable of every shared node at this q
+  for (int n = tid; n < nchi; n += 128) {
+    const double xx = fabs(q * chi[n]);
+    const int bi = min(bsearch_lo_d(G.bess_x, nbx, xx), nbx - 2);
+    const double xh = G.bess_x[bi + 1], dx = xh - G.bess_x[bi];
+    s_bix[n] = bi;
+    s_a2[n] = (float)((xh - xx) / dx);
+  }
+  // integration window of each sampled l in shared nodes (window_setup in chi): the last
+  // node with chi >= 80 l BessIntBoost / q through the last node with chi >= xlim / q
+  const double bib = G.AccuracyBoost * G.BessIntBoost;
+  int nlo = nchi, nhi = -1;
+  if (tid < nl) {
+    const int l = G.ls[tid];
+    const double xlim = fmax(0.0, l - 4.2 * cbrt((double)l));
+    nlo = count_ge(chi, nchi, 80.0 * l * bib / q) - 1;
+    nhi = count_ge(chi, nchi, xlim / q) - 1;
+    if (nlo < 0) nlo = 0;
+    atomicMin(&s_kbeg, nlo);
+    atomicMax(&s_kend, nhi);
+  }
+  // the k-spline weights of q on the shared source k grid
+  KW K;
+  {
+    const int nk = G.nk;
+    if (q <= G.q_evolve[0]) K.klo = 0;
+    else if (q >= G.q_evolve[nk - 1]) K.klo = nk - 2;
+    else K.klo = bsearch_lo_d(G.q_evolve, nk, q);
+    K.khi = K.klo + 1;
+    const double ho = G.q_evolve[K.khi] - G.q_evolve[K.klo];
+    K.a0 = (G.q_evolve[K.khi] - q) / ho;
+    K.b0 = (q - G.q_evolve[K.klo]) / ho;
+    K.ho2o6 = ho * ho / 6.0;
+    K.a03 = K.a0 * K.a0 * K.a0 - K.a0;
+    K.b03 = K.b0 * K.b0 * K.b0 - K.b0;
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tbase = *tslot;
+  const int c = ctile * 128 + tid;  // this thread's cosmology column
+  const bool has_c = c < ncosmo;
+  const DevCosmo* Cc = has_c ? &cosmos[c] : nullptr;
+  const int c_off = has_c ? nchi - Cc->ntau : 0;  // shared node of the cosmology's row 0
+  const float4* __restrict__ Hrow = tid < nl ? G.bessel_f32 + (size_t)tid * (nbx - 1) : nullptr;
+  constexpr uint32_t idesc = idesc_bf16_f32(128, 128);
+  const int kbeg = (s_kbeg / kChunk) * kChunk, kend = s_kend;
+  uint32_t phase = 0;
+  bool ok = true, any = false;
+  for (int k0 = kbeg; k0 <= kend && ok; k0 += kChunk) {
+    // J: row tid (sampled l), 64 nodes; S: row tid (cosmology), 64 nodes
+#pragma unroll 4
+    for (int k = 0; k < kChunk; ++k) {
+      const int n = k0 + k;
+      float J = 0.0f;
+      if (n < nchi && n >= nlo && n <= nhi) {
+        const float4 h = __ldg(Hrow + s_bix[n]);
+        const float a2 = s_a2[n];
+        J = (h.x + a2 * (h.y + a2 * (h.z + a2 * h.w))) * (float)dchi[n];
+      }
+      float S = 0.0f;
+      if (has_c && n < nchi) {
+        const int i = n - c_off;
+        if (row_valid(*Cc, q, i)) S = (float)src_at(*Cc, K, i, src);
+      }
+      __nv_bfloat16 h, l;
+      const uint32_t off = tile_offset(tid, k);
+      split_bf16(J, h, l);
+      *reinterpret_cast<__nv_bfloat16*>(a_hi + off) = h;
+      *reinterpret_cast<__nv_bfloat16*>(a_lo + off) = l;
+      split_bf16(S, h, l);
+      *reinterpret_cast<__nv_bfloat16*>(b_hi + off) = h;
+      *reinterpret_cast<__nv_bfloat16*>(b_lo + off) = l;
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after_sync();
+#pragma unroll
+      for (int s = 0; s < kChunk / 16; ++s) {
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          const unsigned char* a = p == 2 ? a_lo : a_hi;
+          const unsigned char* b = p == 1 ? b_lo : b_hi;
+          mma_bf16(tbase, smem_desc(smem_u32(a) + s * 256, 128, 1024), smem_desc(smem_u32(b) + s * 256, 128, 1024),
+                   idesc, (any || s > 0 || p > 0) ? 1u : 0u);
+        }
+      }
+      mma_commit(bar);
+    }
+    any = true;
+    const bool done = mbar_wait(bar, phase, 1LL << 26);
+    phase ^= 1;
+    ok = __syncthreads_and(done) != 0;
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+    mbar_wait(bar, phase ^ 1, 1LL << 26);
+  } else {
+    fence_after_sync();
+    // epilogue: thread (warp w, lane) holds sampled l j = 32 w + lane for 32 cosmologies at a time
+    const int j = warp * 32 + lane;
+    const bool has_j = j < nl;
+    const int l = has_j ? G.ls[j] : 0;
+    const double limber_l = 400 * sqrt(G.AccuracyBoost * G.LimberBoost);
+    const double xlim = has_j ? fmax(0.0, l - 4.2 * cbrt((double)l)) : 0.0;
+    // Limber node pair of the lensing source in shared nodes (cmbmain.f90:1821-1832)
+    const double chif = (l + 0.5) / q;
+    const int mlim = count_ge(chi, nchi, chif);  // nodes with chi >= chif
+#pragma unroll 1
+    for (int c0 = 0; c0 < 128; c0 += 32) {
+      float v[32];
+      if (any) tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      else
+        for (int i = 0; i < 32; ++i) v[i] = 0.0f;
+      if (!has_j) continue;
+      for (int i = 0; i < 32; ++i) {
+        const int cc = ctile * 128 + c0 + i;
+        if (cc >= ncosmo) break;
+        const DevCosmo& C = cosmos[cc];
+        const int off = nchi - C.ntau;
+        const double tau0 = C.tau0;
+        int llmax = (int)llrint(q * tau0);
+        if (llmax < 15) llmax = 17;
+        else llmax = (int)llrint(q * (tau0 + 6 * 3.14159265358979323846 / q));
+        double out = v[i];
+        // F_SKIP: above the cut, or the window ends before the cosmology's first source row
+        const bool skip = l > llmax || (off + 1 < nchi && xlim / q > chi[off + 1]);
+        if (skip) out = 0.0;
+        else if (C.nsrc > 2) {
+          const bool doint = q < max(850, l) * 3 * bib / tau0 * 1.2;
+          if (!doint && src < 2) out = 0.0;
+          if (src == 2 && (!doint || l > limber_l)) {
+            double limb = 0.0;
+            // xf = tau0 - (l + 1/2)/q inside (tp[0], tp[ntau-1]): chif below chi[off], above 0
+            if (chif > 0 && chif < chi[off] && mlim >= 1 && mlim < nchi) {
+              const int ia = mlim - 1 - off, ib = mlim - off;  // rows n - 1 and n of the cosmology
+              const double f = (chi[mlim - 1] - chif) / (chi[mlim - 1] - chi[mlim]);
+              const double slo = row_valid(C, q, ia) ? src_at(C, K, ia, 2) : 0.0;
+              const double shi = row_valid(C, q, ib) ? src_at(C, K, ib, 2) : 0.0;
+              limb = (slo * (1 - f) + f * shi) * sqrt(3.14159265358979323846 / 2 / (l + 0.5)) / q;
+            }
+            out = limb;
+          }
+        }
+        C.delta[((size_t)q_ix * nl + j) * C.nsrc + src] = out;
+      }
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tbase, 128);
+}
+
+}  // namespace tc
+
+cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, const double* chi, const double* dchi,
+                           int nchi, int* err, cudaStream_t s) {
+  static const bool attr = [] {
+    cudaFuncSetAttribute(tc::proj_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kProjSmem);
+    cudaGetLastError();
+    return true;
+  }();
+  (void)attr;
+  if (nchi > tc::kProjMaxChi) return cudaErrorInvalidValue;
+  dim3 grid((ncosmo + 127) / 128, nsrc, nq);
+  tc::proj_tc_kernel<<<grid, 128, tc::kProjSmem, s>>>(cosmos, ncosmo, chi, dchi, nchi, err);
+  return cudaGetLastError();
+}
+
+}  // namespace cgdev

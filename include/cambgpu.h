@@ -257,6 +257,18 @@ int cambgpu_lensing_range(const CambGpuTables* t, int* out3);
 /* Builds and uploads n cosmologies; the batch stays resident until released or until
  * another call stages a batch (the arena is shared): the calls below then return 2. */
 int cambgpu_batch_prepare(const CambGpuParams* p, int n);
+/* The same batch on grids shared by all its cosmologies (no counterpart in the reference,
+ * where every cosmology has its own grids): one comoving-distance grid chi_n, each
+ * member's time steps tau_n = tau0 - chi_n (nodes with tau >= taurst/2), following at every
+ * chi the finest native time spacing of any member; the source k grid, integration q grid
+ * and Bessel table of the member with the median tau0.  Needed by the tensor-core
+ * projection (cambgpu_set_precision(2)); the FP64 and mixed forms run on it too, so the
+ * projections compare on the same grids.  CMB runs of one l sampling (at most 128 sampled l)
+ * and one set of sources; nchi_out (optional) receives the number of shared nodes. */
+int cambgpu_batch_prepare_shared(const CambGpuParams* p, int n, int* nchi_out);
+/* The shared grids of cambgpu_batch_prepare_shared applied to n existing table handles of
+ * cambgpu_tables_create (host only; their views change). */
+int cambgpu_tables_share_grids(void** handles, int n, int* nchi_out);
 /* Runs ODE, source spline + LOS, C_l on the resident batch; ms3 = device ms per stage. */
 int cambgpu_batch_run(double* ms3);
 /* C_l of the last run, [n][lmax_out+1][4] as cambgpu_get_results. */
@@ -281,6 +293,11 @@ void cambgpu_batch_release(void);
  * spline itself, the window set-up, the Limber branch, the C_l k-integral, interpolation
  * and lensing stay FP64.  C_l agree with the FP64 form to ~1e-6. */
 int cambgpu_set_precision(int mode);
+/* Mode 2 (no counterpart in the reference): the projection of a batch on shared grids
+ * (cambgpu_batch_prepare_shared) as split hi/lo BF16 products on the tensor cores --
+ * Delta[l][c] = sum_n j_l(q chi_n) dchi_n S_c(q, tau0_c - chi_n) per q and source, one
+ * matrix product for the whole batch, FP32 accumulation in tensor memory, the FP64 kernel's
+ * windows, cuts and Limber values applied around it; other batches return 2. */
 int cambgpu_get_precision(void);
 /* ODE kernel variant: 32/16/8 = lanes per k-mode with the state in registers (massless
  * neutrinos, CMB sources); 6 = one warp per k-mode with the state rows in shared memory

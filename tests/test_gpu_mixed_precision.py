@@ -54,5 +54,5 @@ def test_mixed_precision_transfer_functions():
 
 def test_precision_mode_validation():
     lib = _lib.load()
-    assert lib.cambgpu_set_precision(2) == 2
+    assert lib.cambgpu_set_precision(3) == 2
     assert lib.cambgpu_get_precision() == 0
