@@ -49,9 +49,9 @@ def parse():
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1],
                     help="timed form: 0 FP64 throughout, 1 mixed-precision line-of-sight projection")
     ap.add_argument("--lensed-batch", type=int, default=0,
-                    help="instead of the headline run: N lensed draws (lmax 2500 + 200 margin) through the FP64 "
-                         "and the mixed-precision projection, device time per form and the mixed form's C_l "
-                         "error against FP64 per l band")
+                    help="instead of the headline run: N lensed draws (lmax 2500 + 200 margin) on grids shared by "
+                         "the batch through the FP64, mixed FP32 and tensor-core BF16x3 projections, device time "
+                         "per form and C_l errors per l band (and the shift from each draw's own grids)")
     return ap.parse_args()
 
 
@@ -191,9 +191,13 @@ def gradient_checks(ps, g):
 
 
 def lensed_batch(n, lmax=2500, seed=5000, mnu_max=0.2):
-    """n lensed draws resident on the device: the pipeline once in the FP64 form and once
-    with the mixed-precision projection, lensed TT/EE/BB/TE of both, the mixed form's
-    error against FP64 per l band."""
+    """The batched lensed configuration: n lensed draws (lmax 2500 + 200 margin) resident
+    on the device.  On grids shared by the batch (cambgpu_batch_prepare_shared) the
+    pipeline runs with the FP64 projection, the FP32 (mixed) projection and the split hi/lo
+    BF16 tensor-core projection; each form's device time per stage and the lensed C_l error
+    of the mixed and tensor forms against FP64 per l band are reported.  The same draws on
+    their own grids (cambgpu_batch_prepare, FP64) give the shift that sharing the grids
+    causes, stated separately."""
     from camb_gb300 import _lib
     lib = _lib.load()
     ps = workload(n, lmax, seed=seed, mnu_max=mnu_max)
@@ -202,41 +206,67 @@ def lensed_batch(n, lmax=2500, seed=5000, mnu_max=0.2):
         p.max_l = lmax + 200
         p.max_eta_k = 2.5 * p.max_l
     arr = (_lib.CambGpuParams * n)(*ps)
-    t0 = time.perf_counter()
-    _lib.check(lib.cambgpu_batch_prepare(arr, n))
-    prep = time.perf_counter() - t0
-    out, ms_form = {}, {}
-    for mode in (0, 1):
-        _lib.check(lib.cambgpu_set_precision(mode))
-        ms = np.zeros(3)
-        _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
-        ms_form[mode] = ms.copy()
-        unl = np.zeros((n, lmax + 201, 4))
-        len_ = np.zeros((n, lmax + 201, 4))
+    L = lmax + 200
+
+    def spectra():
+        unl = np.zeros((n, L + 1, 4))
+        len_ = np.zeros((n, L + 1, 4))
+        pot = np.zeros((n, L + 1, 3))
         lml = np.zeros(n, dtype=np.int32)
-        _lib.check(lib.cambgpu_batch_spectra_from_transfer(None, None, None, None, lmax + 200, _lib.dptr(unl),
-                                                           _lib.dptr(len_), None, _lib.iptr(lml)))
-        out[mode] = len_
-    lib.cambgpu_batch_release()
+        _lib.check(lib.cambgpu_batch_spectra_from_transfer(None, None, None, None, L, _lib.dptr(unl), _lib.dptr(len_),
+                                                           _lib.dptr(pot), _lib.iptr(lml)))
+        return len_, pot
+
+    def run_forms(forms, shared):
+        out, ms_form = {}, {}
+        t0 = time.perf_counter()
+        if shared:
+            nchi = C.c_int()
+            _lib.check(lib.cambgpu_batch_prepare_shared(arr, n, C.byref(nchi)))
+        else:
+            _lib.check(lib.cambgpu_batch_prepare(arr, n))
+        prep = time.perf_counter() - t0
+        for mode in forms:
+            _lib.check(lib.cambgpu_set_precision(mode))
+            ms = np.zeros(3)
+            _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))  # warm-up (graph capture on the next)
+            _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
+            ms_form[mode] = ms.copy()
+            out[mode] = spectra()
+        lib.cambgpu_batch_release()
+        return out, ms_form, prep, (nchi.value if shared else None)
+
+    sh, ms_sh, prep_sh, nchi = run_forms((0, 1, 2), True)
+    nat, ms_nat, prep_nat, _ = run_forms((0,), False)
     _lib.check(lib.cambgpu_set_precision(1))
-    ref, got = out[0], out[1]
     bands = [(2, 100), (100, 500), (500, 1000), (1000, 1500), (1500, 2000), (2000, lmax)]
-    err = {}
-    for lo, hi in bands:
-        sl = slice(lo, hi + 1)
-        tt = np.max(np.abs(got[:, sl, 0] / ref[:, sl, 0] - 1))
-        ee = np.max(np.abs(got[:, sl, 1] / ref[:, sl, 1] - 1))
-        bb = np.max(np.abs(got[:, sl, 2] / ref[:, sl, 2] - 1))
-        te = np.max(np.abs(got[:, sl, 3] - ref[:, sl, 3]) / np.sqrt(ref[:, sl, 0] * ref[:, sl, 1]))
-        err[f"{lo}-{hi}"] = {"TT": tt, "EE": ee, "BB": bb, "TE_over_sqrt_TTEE": te}
-    stage = {k: {"ode": v[0], "spline_los": v[1], "cls_interp_lens": v[2]} for k, v in
-             (("fp64", ms_form[0]), ("mixed", ms_form[1]))}
+
+    def band_err(got, ref):
+        err = {}
+        for lo, hi in bands:
+            sl = slice(lo, hi + 1)
+            g, r = got[0][:, sl], ref[0][:, sl]
+            err[f"{lo}-{hi}"] = {"TT": float(np.max(np.abs(g[..., 0] / r[..., 0] - 1))),
+                                 "EE": float(np.max(np.abs(g[..., 1] / r[..., 1] - 1))),
+                                 "BB": float(np.max(np.abs(g[..., 2] / r[..., 2] - 1))),
+                                 "TE_over_sqrt_TTEE": float(np.max(np.abs(g[..., 3] - r[..., 3]) /
+                                                                   np.sqrt(r[..., 0] * r[..., 1]))),
+                                 "PP": float(np.max(np.abs(got[1][:, sl, 0] / ref[1][:, sl, 0] - 1)))}
+        return err
+
+    names = {0: "fp64", 1: "mixed_fp32", 2: "tensor_bf16x3"}
+    stage = {names[k]: {"ode": v[0], "spline_los": v[1], "cls_interp_lens": v[2]} for k, v in ms_sh.items()}
     return {"config": {"workload": f"{n} seeded draws (fiducial LCDM +-5%, mnu 0-{mnu_max:g} eV), lensed "
-                                   f"TT/EE/BB/TE to lmax={lmax} (+200 margin)", "batch": n},
-            "prepare_s": prep, "stage_ms": stage,
-            "cosmologies_per_s_mixed": n / (sum(ms_form[1]) * 1e-3),
-            "cosmologies_per_s_fp64": n / (sum(ms_form[0]) * 1e-3),
-            "mixed_vs_fp64_lensed_error_per_l_band": err}
+                                   f"TT/EE/BB/TE and phi-phi to lmax={lmax} (+200 margin), on grids shared by "
+                                   f"the batch ({nchi} comoving-distance nodes)", "batch": n},
+            "prepare_s": {"shared": prep_sh, "native": prep_nat}, "stage_ms_shared_grids": stage,
+            "stage_ms_native_grids_fp64": {"ode": ms_nat[0][0], "spline_los": ms_nat[0][1],
+                                           "cls_interp_lens": ms_nat[0][2]},
+            "cosmologies_per_s": {names[k]: n / (sum(v) * 1e-3) for k, v in ms_sh.items()},
+            "projection_ms": {names[k]: v[1] for k, v in ms_sh.items()},
+            "tensor_vs_fp64_same_grids_per_l_band": band_err(sh[2], sh[0]),
+            "mixed_vs_fp64_same_grids_per_l_band": band_err(sh[1], sh[0]),
+            "shared_vs_native_grids_fp64_per_l_band": band_err(sh[0], nat[0])}
 
 
 def workload(n, lmax, seed, mnu_max=0.2):

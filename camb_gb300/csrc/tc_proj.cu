@@ -57,12 +57,35 @@ __device__ __forceinline__ double src_at(const DevCosmo& C, const KW& K, int i, 
          (K.a03 * C.dd_src[b + K.klo] + K.b03 * C.dd_src[b + K.khi]) * K.ho2o6;
 }
 
+// the same in FP32 from FP64 table values: the operand is split into BF16 pairs afterwards
+struct KWf {
+  int klo, khi;
+  float a0, b0, a03h, b03h;  // a03, b03 times ho^2/6
+};
+__device__ __forceinline__ float src_at_f(const DevCosmo& C, const KWf& K, int i, int s) {
+  const size_t b = ((size_t)i * C.nsrc + s) * C.nk;
+  const float s0 = (float)__ldg(C.linear_src + b + K.klo), s1 = (float)__ldg(C.linear_src + b + K.khi);
+  const float d0 = (float)__ldg(C.dd_src + b + K.klo), d1 = (float)__ldg(C.dd_src + b + K.khi);
+  return fmaf(K.a0, s0, fmaf(K.b0, s1, fmaf(K.a03h, d0, K.b03h * d1)));
+}
+
 // row i of cosmology C holds a source at q: 1 <= i and the prefix test of source_row_count
 __device__ __forceinline__ bool row_valid(const DevCosmo& C, double q, int i) {
   if (i < 1 || i >= C.ntau) return false;
   const double tau = C.tau_points[i];
   const bool etak_ok = C.want_late_time || q * tau < C.max_etak_scalar;
   return etak_ok && q * (C.tau0 - tau) > 1e-8;
+}
+
+// end of the valid rows [1, end): the prefix test holds on an initial run of rows
+__device__ __forceinline__ int valid_row_end(const DevCosmo& C, double q) {
+  int lo = 1, hi = C.ntau;  // rows below lo pass; the first failing row is in [lo, hi]
+  while (lo < hi) {
+    const int m = (lo + hi) >> 1;
+    if (row_valid(C, q, m)) lo = m + 1;
+    else hi = m;
+  }
+  return lo;
 }
 
 __global__ void __launch_bounds__(128, 1)
@@ -79,6 +102,11 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t* bar = reinterpret_cast<uint64_t*>(s_a2 + kProjMaxChi);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   __shared__ int s_kbeg, s_kend;
+  // per cosmology of the tile: first shared node, valid-row end, l cut, the node of its
+  // second row (window test), lensed integration test for l <= 850, tau0
+  __shared__ int s_off[128], s_rend[128], s_llmax[128];
+  __shared__ double s_chi1[128], s_tau0[128];
+  __shared__ unsigned char s_doint850[128];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ctile = blockIdx.x, src = blockIdx.y, q_ix = blockIdx.z;
   const DevCosmo& G = cosmos[0];  // shared grids: q, k, l sampling, Bessel table
@@ -135,6 +163,27 @@ __global__ void __launch_bounds__(128, 1)
   const bool has_c = c < ncosmo;
   const DevCosmo* Cc = has_c ? &cosmos[c] : nullptr;
   const int c_off = has_c ? nchi - Cc->ntau : 0;  // shared node of the cosmology's row 0
+  const int c_rend = has_c ? valid_row_end(*Cc, q) : 0;
+  KWf Kf;
+  Kf.klo = K.klo;
+  Kf.khi = K.khi;
+  Kf.a0 = (float)K.a0;
+  Kf.b0 = (float)K.b0;
+  Kf.a03h = (float)(K.a03 * K.ho2o6);
+  Kf.b03h = (float)(K.b03 * K.ho2o6);
+  if (has_c) {
+    const double tau0 = Cc->tau0;
+    int llmax = (int)llrint(q * tau0);
+    if (llmax < 15) llmax = 17;
+    else llmax = (int)llrint(q * (tau0 + 6 * 3.14159265358979323846 / q));
+    s_off[tid] = c_off;
+    s_rend[tid] = c_rend;
+    s_llmax[tid] = llmax;
+    s_chi1[tid] = c_off + 1 < nchi ? chi[c_off + 1] : -1.0;
+    s_tau0[tid] = tau0;
+    s_doint850[tid] = q < 850 * 3 * (G.AccuracyBoost * G.BessIntBoost) / tau0 * 1.2;
+  }
+  __syncthreads();  // the per-cosmology arrays, read by the epilogue's threads
   const float4* __restrict__ Hrow = tid < nl ? G.bessel_f32 + (size_t)tid * (nbx - 1) : nullptr;
   constexpr uint32_t idesc = idesc_bf16_f32(128, 128);
   const int kbeg = (s_kbeg / kChunk) * kChunk, kend = s_kend;
@@ -154,7 +203,7 @@ __global__ void __launch_bounds__(128, 1)
       float S = 0.0f;
       if (has_c && n < nchi) {
         const int i = n - c_off;
-        if (row_valid(*Cc, q, i)) S = (float)src_at(*Cc, K, i, src);
+        if (i >= 1 && i < c_rend) S = src_at_f(*Cc, Kf, i, src);
       }
       __nv_bfloat16 h, l;
       const uint32_t off = tile_offset(tid, k);
@@ -207,21 +256,19 @@ __global__ void __launch_bounds__(128, 1)
       else
         for (int i = 0; i < 32; ++i) v[i] = 0.0f;
       if (!has_j) continue;
+      const double xq = xlim / q;
       for (int i = 0; i < 32; ++i) {
-        const int cc = ctile * 128 + c0 + i;
+        const int ct = c0 + i, cc = ctile * 128 + ct;
         if (cc >= ncosmo) break;
         const DevCosmo& C = cosmos[cc];
-        const int off = nchi - C.ntau;
-        const double tau0 = C.tau0;
-        int llmax = (int)llrint(q * tau0);
-        if (llmax < 15) llmax = 17;
-        else llmax = (int)llrint(q * (tau0 + 6 * 3.14159265358979323846 / q));
+        const int off = s_off[ct];
+        const double tau0 = s_tau0[ct];
         double out = v[i];
         // F_SKIP: above the cut, or the window ends before the cosmology's first source row
-        const bool skip = l > llmax || (off + 1 < nchi && xlim / q > chi[off + 1]);
+        const bool skip = l > s_llmax[ct] || (s_chi1[ct] >= 0.0 && xq > s_chi1[ct]);
         if (skip) out = 0.0;
         else if (C.nsrc > 2) {
-          const bool doint = q < max(850, l) * 3 * bib / tau0 * 1.2;
+          const bool doint = l <= 850 ? s_doint850[ct] != 0 : q < max(850, l) * 3 * bib / tau0 * 1.2;
           if (!doint && src < 2) out = 0.0;
           if (src == 2 && (!doint || l > limber_l)) {
             double limb = 0.0;
