@@ -21,6 +21,8 @@ that kernel, after three warm launches.  Cases:
                N draws on ODE team code T, optionally with a queue order, a schedule
                and a resident-block cap (e.g. team7_256_o2_s1); unset parts keep the
                tuned defaults
+  tc<N>        N lensed draws (lmax 2500 + 200) on grids shared by the batch, tensor-core
+               projection (precision 2); fc<N> the same with the FP64 projection
   fp64pipe     the FP64 issue model (cambgpu_probe_fp64_pipe): lane FMAs per SM cycle for
                1-16 warps per SM, partially active warps and 1/4/8 independent chains
 """
@@ -55,6 +57,22 @@ def run(name, runs=4):
     sched = 0
     if name == "fp64pipe":
         return fp64_pipe()
+    if name.startswith(("tc", "fc")):
+        ps = batch_draws(int(name[2:]), 2500, seed=5000)
+        for p in ps:
+            p.do_lensing, p.max_l = 1, 2700
+            p.max_eta_k = 2.5 * 2700
+        arr = (_lib.CambGpuParams * len(ps))(*ps)
+        _lib.check(lib.cambgpu_set_precision(2 if name.startswith("tc") else 0))
+        _lib.check(lib.cambgpu_batch_prepare_shared(arr, len(ps), None))
+        ms = np.zeros(3)
+        for _ in range(runs):
+            _lib.check(lib.cambgpu_batch_run(_lib.dptr(ms)))
+        lib.cambgpu_batch_release()
+        lib.cambgpu_set_precision(1)
+        out = {"kernel_case": name, "ode_ms": ms[0], "spline_los_ms": ms[1], "cls_ms": ms[2]}
+        print(json.dumps(out))
+        return out
     if name == "warp1":
         p = _lib.default_params()
         p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
