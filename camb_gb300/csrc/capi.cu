@@ -1542,7 +1542,9 @@ static int share_grids(const std::vector<Handle*>& hs, cg::SharedGrid& sg) {
   int rc = cg::build_shared_grid(cs, sg, err);
   if (rc) return set_err(rc, err);
   if (sg.chi.size() > 4096) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "shared grid: more than 4096 time nodes");
-  double xmax = 0;
+  // the Bessel table covers every argument q chi of the shared grids: the members with
+  // tau0 above the grid member's see q chi beyond their own q_max tau0
+  double xmax = sg.q_int.back() * sg.chi.front() * 1.0001;
   for (auto* h : hs) xmax = std::max(xmax, h->c.maximum_qeta);
   std::shared_ptr<const cg::BesselTable> bt;
   try {

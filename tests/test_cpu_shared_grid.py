@@ -60,3 +60,19 @@ def test_shared_grid_shift_of_cls_is_the_discretization_error():
         cn = orc.cls(n, orc.los(n, orc.evolve_sources(n)))
         assert np.max(np.abs(cs[:, 0] / cn[:, 0] - 1)) < 2e-3
         assert np.max(np.abs(cs[:, 1] / cn[:, 1] - 1)) < 2e-3
+
+
+def test_shared_grid_extreme_members_lmax2500():
+    """The members with the smallest and largest tau0 of 16 draws at lmax 2500: the shared
+    q grid (from the median member) reaches Bessel arguments q chi beyond the largest
+    member's own q_max tau0, so the shared Bessel table must extend past every member's
+    own; C_l within 2e-3 of each member's native grids at every sampled l."""
+    ps = batch_draws(16, 2500, seed=13)
+    ts, _ = shared_tables(ps)
+    tau0 = np.array([t.view.tau0 for t in ts])
+    for i in (int(np.argmin(tau0)), int(np.argmax(tau0))):
+        t, n = ts[i], _lib.Tables(ps[i])
+        cs = orc.cls(t, orc.los(t, orc.evolve_sources(t)))
+        cn = orc.cls(n, orc.los(n, orc.evolve_sources(n)))
+        assert np.max(np.abs(cs[:, 0] / cn[:, 0] - 1)) < 2e-3
+        assert np.max(np.abs(cs[:, 1] / cn[:, 1] - 1)) < 2e-3
