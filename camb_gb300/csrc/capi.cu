@@ -25,8 +25,8 @@ cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s,
                               const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride);
 cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s);
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
-cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, const double* chi, const double* dchi,
-                           int nchi, int* err, cudaStream_t s);
+cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, int nk, const double* chi,
+                           const float* dchi_f, int nchi, float2* tsrc, int* err, cudaStream_t s);
 cudaError_t launch_fp64_pipe_probe(int nsm, int warps, int lanes, int chains, int iters, long long* cyc, double* out,
                                    cudaStream_t s);
 __global__ void source_spline_kernel(const DevCosmo*, const double* const*);
@@ -529,7 +529,10 @@ struct Batch {
   // cosmology's time steps are taken from, for the tensor-core projection (precision 2)
   bool shared = false;
   std::vector<double> h_chi, h_dchi;
+  std::vector<float> h_dchi_f;
   double *d_chi = nullptr, *d_dchi = nullptr;
+  float* d_dchi_f = nullptr;
+  float2* d_tsrc = nullptr;  // [nk][nsrc][nchi][n] FP32 {source, d2} pairs (tensor-core projection)
   int* d_tc_err = nullptr;
   WorkItem* d_items_bal = nullptr;
   size_t bal_cap = 0;
@@ -614,6 +617,9 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   const size_t bal_cap = 2 * nitems + 2 * (size_t)g_rt.nsm * 2048;
   total += (bal_cap * sizeof(WorkItem) + 255);
   total += 2 * (B.h_chi.size() * 8 + 255) + 256;  // shared chi nodes and weights, error flag
+  if (B.shared)  // FP32 weights, transposed FP32 source pairs
+    total += (B.h_chi.size() * 4 + 255) +
+             ((size_t)B.views[0]->nk * B.views[0]->nsrc * B.h_chi.size() * n * sizeof(float2) + 255);
   rc = g_rt.arena.reserve(total);
   if (rc) return set_err(rc, "device allocation failed");
   B.d_status = g_rt.arena.take<int>(n);
@@ -734,6 +740,10 @@ int stage_batch(Batch& B, int lmax_out = 0) {
     B.d_dchi = g_rt.arena.take<double>(B.h_dchi.size());
     copies.push_back({B.d_chi, {B.h_chi.data(), B.h_chi.size() * 8}});
     copies.push_back({B.d_dchi, {B.h_dchi.data(), B.h_dchi.size() * 8}});
+    B.h_dchi_f.assign(B.h_dchi.begin(), B.h_dchi.end());
+    B.d_dchi_f = g_rt.arena.take<float>(B.h_dchi_f.size());
+    copies.push_back({B.d_dchi_f, {B.h_dchi_f.data(), B.h_dchi_f.size() * 4}});
+    B.d_tsrc = g_rt.arena.take<float2>((size_t)B.views[0]->nk * B.views[0]->nsrc * B.h_chi.size() * n);
   }
   copies.push_back({B.d_items_cost, {B.h_items_cost.data(), items.size() * sizeof(WorkItem)}});
   // single pinned staging buffer for all uploads
@@ -867,9 +877,9 @@ int run_los(Batch& B) {
     source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
     g_launches++;
     CUDA_TRY(cudaMemsetAsync(B.d_tc_err, 0, sizeof(int), g_rt.stream));
-    CUDA_TRY(launch_proj_tc(B.d_cosmos, n, B.max_nq, B.views[0]->nsrc, B.d_chi, B.d_dchi, (int)B.h_chi.size(),
-                            B.d_tc_err, g_rt.stream));
-    g_launches++;
+    CUDA_TRY(launch_proj_tc(B.d_cosmos, n, B.max_nq, B.views[0]->nsrc, B.views[0]->nk, B.d_chi, B.d_dchi_f,
+                            (int)B.h_chi.size(), B.d_tsrc, B.d_tc_err, g_rt.stream));
+    g_launches += 2;
     return 0;
   }
   // mixed precision: the spline leaves FP32 {source, d2} pairs in dd_src for the FP32 staging

@@ -46,27 +46,51 @@ __device__ __forceinline__ int count_ge(const double* chi, int n, double v) {
   return lo;
 }
 
-// the source k-spline of one cosmology at q for time row i (InterpolateSources)
+// the k-spline weights of q on the shared source k grid (InterpolateSources)
 struct KW {
   int klo, khi;
   double a0, b0, a03, b03, ho2o6;
 };
-__device__ __forceinline__ double src_at(const DevCosmo& C, const KW& K, int i, int s) {
-  const size_t b = ((size_t)i * C.nsrc + s) * C.nk;
-  return K.a0 * C.linear_src[b + K.klo] + K.b0 * C.linear_src[b + K.khi] +
-         (K.a03 * C.dd_src[b + K.klo] + K.b03 * C.dd_src[b + K.khi]) * K.ho2o6;
+
+// The batch's sources and their k-spline second derivatives as FP32 pairs, laid out
+// [k][source][shared node][cosmology] so that the 128 cosmologies of a tile read one
+// contiguous kilobyte per (k, source, node); zero where a cosmology has no row.
+__global__ void proj_src_transpose_kernel(const DevCosmo* __restrict__ cosmos, int ncos, int nchi, int nk, int nsrc,
+                                          float2* __restrict__ T) {
+  __shared__ float2 tile[32][33];
+  const int n = blockIdx.z / nsrc, s = blockIdx.z % nsrc;
+  const int k0 = blockIdx.x * 32, c0 = blockIdx.y * 32, tx = threadIdx.x, ty = threadIdx.y;
+  for (int cy = ty; cy < 32; cy += 8) {  // read 32 consecutive k of one cosmology
+    const int c = c0 + cy, k = k0 + tx;
+    float2 v = make_float2(0.0f, 0.0f);
+    if (c < ncos && k < nk) {
+      const DevCosmo& C = cosmos[c];
+      const int i = n - (nchi - C.ntau);
+      if (i >= 0 && i < C.ntau) {
+        const size_t idx = ((size_t)i * nsrc + s) * nk + k;
+        v = make_float2((float)C.linear_src[idx], (float)C.dd_src[idx]);
+      }
+    }
+    tile[cy][tx] = v;
+  }
+  __syncthreads();
+  for (int ky = ty; ky < 32; ky += 8) {  // write 32 consecutive cosmologies of one k
+    const int k = k0 + ky, c = c0 + tx;
+    if (k < nk && c < ncos) T[(((size_t)k * nsrc + s) * nchi + n) * ncos + c] = tile[tx][ky];
+  }
 }
 
-// the same in FP32 from FP64 table values: the operand is split into BF16 pairs afterwards
+// FP32 spline weights of q (the operand is split into BF16 pairs afterwards)
 struct KWf {
   int klo, khi;
   float a0, b0, a03h, b03h;  // a03, b03 times ho^2/6
 };
-__device__ __forceinline__ float src_at_f(const DevCosmo& C, const KWf& K, int i, int s) {
-  const size_t b = ((size_t)i * C.nsrc + s) * C.nk;
-  const float s0 = (float)__ldg(C.linear_src + b + K.klo), s1 = (float)__ldg(C.linear_src + b + K.khi);
-  const float d0 = (float)__ldg(C.dd_src + b + K.klo), d1 = (float)__ldg(C.dd_src + b + K.khi);
-  return fmaf(K.a0, s0, fmaf(K.b0, s1, fmaf(K.a03h, d0, K.b03h * d1)));
+// source s of cosmology c at shared node n, from the transposed pairs
+__device__ __forceinline__ float src_t(const float2* __restrict__ T, int ncos, int nchi, int nsrc, const KWf& K, int s,
+                                       int n, int c) {
+  const float2 p0 = __ldg(T + (((size_t)K.klo * nsrc + s) * nchi + n) * ncos + c);
+  const float2 p1 = __ldg(T + (((size_t)K.khi * nsrc + s) * nchi + n) * ncos + c);
+  return fmaf(K.a0, p0.x, fmaf(K.b0, p1.x, fmaf(K.a03h, p0.y, K.b03h * p1.y)));
 }
 
 // row i of cosmology C holds a source at q: 1 <= i and the prefix test of source_row_count
@@ -90,7 +114,7 @@ __device__ __forceinline__ int valid_row_end(const DevCosmo& C, double q) {
 
 __global__ void __launch_bounds__(128, 1)
     proj_tc_kernel(const DevCosmo* __restrict__ cosmos, int ncosmo, const double* __restrict__ chi,
-                   const double* __restrict__ dchi, int nchi, int* __restrict__ err) {
+                   const float* __restrict__ dchi_f, int nchi, const float2* __restrict__ T, int* __restrict__ err) {
   extern __shared__ unsigned char tp_smem_raw[];
   unsigned char* base = tp_smem_raw + ((1024 - (smem_u32(tp_smem_raw) & 1023)) & 1023);
   unsigned char* a_hi = base;
@@ -111,7 +135,7 @@ __global__ void __launch_bounds__(128, 1)
   const int ctile = blockIdx.x, src = blockIdx.y, q_ix = blockIdx.z;
   const DevCosmo& G = cosmos[0];  // shared grids: q, k, l sampling, Bessel table
   const double q = G.q_int[q_ix];
-  const int nl = G.nl, nbx = G.num_xx;
+  const int nl = G.nl, nbx = G.num_xx, nsrc = G.nsrc;
   if (tid == 0) {
     mbar_init(bar, 1);
     s_kbeg = nchi;
@@ -198,12 +222,12 @@ __global__ void __launch_bounds__(128, 1)
       if (n < nchi && n >= nlo && n <= nhi) {
         const float4 h = __ldg(Hrow + s_bix[n]);
         const float a2 = s_a2[n];
-        J = (h.x + a2 * (h.y + a2 * (h.z + a2 * h.w))) * (float)dchi[n];
+        J = (h.x + a2 * (h.y + a2 * (h.z + a2 * h.w))) * dchi_f[n];
       }
       float S = 0.0f;
       if (has_c && n < nchi) {
         const int i = n - c_off;
-        if (i >= 1 && i < c_rend) S = src_at_f(*Cc, Kf, i, src);
+        if (i >= 1 && i < c_rend) S = src_t(T, ncosmo, nchi, nsrc, Kf, src, n, c);
       }
       __nv_bfloat16 h, l;
       const uint32_t off = tile_offset(tid, k);
@@ -276,8 +300,8 @@ __global__ void __launch_bounds__(128, 1)
             if (chif > 0 && chif < chi[off] && mlim >= 1 && mlim < nchi) {
               const int ia = mlim - 1 - off, ib = mlim - off;  // rows n - 1 and n of the cosmology
               const double f = (chi[mlim - 1] - chif) / (chi[mlim - 1] - chi[mlim]);
-              const double slo = row_valid(C, q, ia) ? src_at(C, K, ia, 2) : 0.0;
-              const double shi = row_valid(C, q, ib) ? src_at(C, K, ib, 2) : 0.0;
+              const double slo = row_valid(C, q, ia) ? (double)src_t(T, ncosmo, nchi, nsrc, Kf, 2, ia + off, cc) : 0.0;
+              const double shi = row_valid(C, q, ib) ? (double)src_t(T, ncosmo, nchi, nsrc, Kf, 2, ib + off, cc) : 0.0;
               limb = (slo * (1 - f) + f * shi) * sqrt(3.14159265358979323846 / 2 / (l + 0.5)) / q;
             }
             out = limb;
@@ -294,8 +318,8 @@ __global__ void __launch_bounds__(128, 1)
 
 }  // namespace tc
 
-cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, const double* chi, const double* dchi,
-                           int nchi, int* err, cudaStream_t s) {
+cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, int nk, const double* chi,
+                           const float* dchi_f, int nchi, float2* tsrc, int* err, cudaStream_t s) {
   static const bool attr = [] {
     cudaFuncSetAttribute(tc::proj_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kProjSmem);
     cudaGetLastError();
@@ -303,8 +327,10 @@ cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc,
   }();
   (void)attr;
   if (nchi > tc::kProjMaxChi) return cudaErrorInvalidValue;
+  dim3 gt((nk + 31) / 32, (ncosmo + 31) / 32, nchi * nsrc);
+  tc::proj_src_transpose_kernel<<<gt, dim3(32, 8), 0, s>>>(cosmos, ncosmo, nchi, nk, nsrc, tsrc);
   dim3 grid((ncosmo + 127) / 128, nsrc, nq);
-  tc::proj_tc_kernel<<<grid, 128, tc::kProjSmem, s>>>(cosmos, ncosmo, chi, dchi, nchi, err);
+  tc::proj_tc_kernel<<<grid, 128, tc::kProjSmem, s>>>(cosmos, ncosmo, chi, dchi_f, nchi, tsrc, err);
   return cudaGetLastError();
 }
 
