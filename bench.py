@@ -650,6 +650,17 @@ def main():
         line["accuracy"] = accuracy_vs_fp64(cps, ref, args.lmax)  # timed form vs the FP64 CPU restatement
         line["single_cosmology_configs"] = single_configs(nth)
         line["gradients"] = gradient_rate()
+        # the batched lensed configuration's projections on grids shared by the batch (the
+        # full 1024-draw case: bench.py --lensed-batch 1024)
+        lb = lensed_batch(256, args.lmax, mnu_max=args.mnu_max)
+        line["shared_grid_projections_lensed_256"] = {
+            "projection_ms": lb["projection_ms"], "cosmologies_per_s": lb["cosmologies_per_s"],
+            "tensor_vs_fp64_same_grids_max": {k: max(b[k] for b in lb["tensor_vs_fp64_same_grids_per_l_band"].values())
+                                               for k in ("TT", "EE", "BB", "TE_over_sqrt_TTEE", "PP")},
+            "shared_vs_native_grids_fp64_max": {k: max(b[k] for b in
+                                                       lb["shared_vs_native_grids_fp64_per_l_band"].values())
+                                                 for k in ("TT", "EE", "BB", "TE_over_sqrt_TTEE", "PP")},
+            "workload": lb["config"]["workload"]}
         plain = plain_form_rate(mnu_max=args.mnu_max)
         line["batched_vs_plain_gpu"] = {
             "plain_fp64_gpu_cosmologies_per_s": plain,
