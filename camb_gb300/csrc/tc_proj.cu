@@ -5,8 +5,8 @@
 // With one comoving-distance grid chi_n for every cosmology of the batch (tau_n = tau0_c -
 // chi_n) and one integration q grid, the projection of source s at wavenumber q is
 //     Delta_s[l][c] = sum_n J_q[l][n] S_q,s[n][c],   J_q[l][n] = j_l(q chi_n) dchi_n,
-// one Bessel matrix per q for the whole batch.  One CTA computes a 128 (sampled l) x 128
-// (cosmologies) tile of one (q, source): it stages 64-deep K tiles of J (from the FP32 Horner
+// one Bessel matrix per q for the whole batch.  One CTA of eight warps computes a 128
+// (sampled l) x 128 (cosmologies) tile of one (q, source): it stages 64-deep K tiles of J (from the FP32 Horner
 // table, zero outside each l's integration window) and of S (the source k-spline of each
 // cosmology evaluated at q, zero outside the cosmology's time range and its q*tau < max_etak
 // prefix), split into BF16 pairs, in shared memory; one thread issues the twelve
@@ -112,7 +112,7 @@ __device__ __forceinline__ int valid_row_end(const DevCosmo& C, double q) {
   return lo;
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
     proj_tc_kernel(const DevCosmo* __restrict__ cosmos, int ncosmo, const double* __restrict__ chi,
                    const float* __restrict__ dchi_f, int nchi, const float2* __restrict__ T, int* __restrict__ err) {
   extern __shared__ unsigned char tp_smem_raw[];
@@ -131,7 +131,11 @@ __global__ void __launch_bounds__(128, 1)
   __shared__ int s_off[128], s_rend[128], s_llmax[128];
   __shared__ double s_chi1[128], s_tau0[128];
   __shared__ unsigned char s_doint850[128];
+  // 256 threads: threads 0-127 stage the J rows (sampled l), 128-255 the S rows
+  // (cosmologies) of each tile; all eight warps read the accumulator back, warp w from
+  // tensor-memory lane quarter w % 4 and column half w / 4
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row = tid & 127, side = tid >> 7;
   const int ctile = blockIdx.x, src = blockIdx.y, q_ix = blockIdx.z;
   const DevCosmo& G = cosmos[0];  // shared grids: q, k, l sampling, Bessel table
   const double q = G.q_int[q_ix];
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(128, 1)
   if (warp == 0) tmem_alloc(tslot, 128);
   __syncthreads();  // s_kbeg / s_kend initialised before the atomics below
   // Bessel-table interval and Horner variable of every shared node at this q
-  for (int n = tid; n < nchi; n += 128) {
+  for (int n = tid; n < nchi; n += 256) {
     const double xx = fabs(q * chi[n]);
     const int bi = min(bsearch_lo_d(G.bess_x, nbx, xx), nbx - 2);
     const double xh = G.bess_x[bi + 1], dx = xh - G.bess_x[bi];
@@ -155,8 +159,8 @@ __global__ void __launch_bounds__(128, 1)
   // node with chi >= 80 l BessIntBoost / q through the last node with chi >= xlim / q
   const double bib = G.AccuracyBoost * G.BessIntBoost;
   int nlo = nchi, nhi = -1;
-  if (tid < nl) {
-    const int l = G.ls[tid];
+  if (side == 0 && row < nl) {
+    const int l = G.ls[row];
     const double xlim = fmax(0.0, l - 4.2 * cbrt((double)l));
     nlo = count_ge(chi, nchi, 80.0 * l * bib / q) - 1;
     nhi = count_ge(chi, nchi, xlim / q) - 1;
@@ -183,8 +187,8 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   fence_after_sync();
   const uint32_t tbase = *tslot;
-  const int c = ctile * 128 + tid;  // this thread's cosmology column
-  const bool has_c = c < ncosmo;
+  const int c = ctile * 128 + row;  // the cosmology column of an S-side thread
+  const bool has_c = side == 1 && c < ncosmo;
   const DevCosmo* Cc = has_c ? &cosmos[c] : nullptr;
   const int c_off = has_c ? nchi - Cc->ntau : 0;  // shared node of the cosmology's row 0
   const int c_rend = has_c ? valid_row_end(*Cc, q) : 0;
@@ -200,43 +204,42 @@ __global__ void __launch_bounds__(128, 1)
     int llmax = (int)llrint(q * tau0);
     if (llmax < 15) llmax = 17;
     else llmax = (int)llrint(q * (tau0 + 6 * 3.14159265358979323846 / q));
-    s_off[tid] = c_off;
-    s_rend[tid] = c_rend;
-    s_llmax[tid] = llmax;
-    s_chi1[tid] = c_off + 1 < nchi ? chi[c_off + 1] : -1.0;
-    s_tau0[tid] = tau0;
-    s_doint850[tid] = q < 850 * 3 * (G.AccuracyBoost * G.BessIntBoost) / tau0 * 1.2;
+    s_off[row] = c_off;
+    s_rend[row] = c_rend;
+    s_llmax[row] = llmax;
+    s_chi1[row] = c_off + 1 < nchi ? chi[c_off + 1] : -1.0;
+    s_tau0[row] = tau0;
+    s_doint850[row] = q < 850 * 3 * (G.AccuracyBoost * G.BessIntBoost) / tau0 * 1.2;
   }
   __syncthreads();  // the per-cosmology arrays, read by the epilogue's threads
-  const float4* __restrict__ Hrow = tid < nl ? G.bessel_f32 + (size_t)tid * (nbx - 1) : nullptr;
+  const float4* __restrict__ Hrow = (side == 0 && row < nl) ? G.bessel_f32 + (size_t)row * (nbx - 1) : nullptr;
   constexpr uint32_t idesc = idesc_bf16_f32(128, 128);
   const int kbeg = (s_kbeg / kChunk) * kChunk, kend = s_kend;
   uint32_t phase = 0;
   bool ok = true, any = false;
   for (int k0 = kbeg; k0 <= kend && ok; k0 += kChunk) {
-    // J: row tid (sampled l), 64 nodes; S: row tid (cosmology), 64 nodes
-#pragma unroll 4
+    // J (side 0): row = sampled l, 64 nodes; S (side 1): row = cosmology, 64 nodes
+    unsigned char* const thi = side == 0 ? a_hi : b_hi;
+    unsigned char* const tlo = side == 0 ? a_lo : b_lo;
+#pragma unroll 8
     for (int k = 0; k < kChunk; ++k) {
       const int n = k0 + k;
-      float J = 0.0f;
-      if (n < nchi && n >= nlo && n <= nhi) {
-        const float4 h = __ldg(Hrow + s_bix[n]);
-        const float a2 = s_a2[n];
-        J = (h.x + a2 * (h.y + a2 * (h.z + a2 * h.w))) * dchi_f[n];
-      }
-      float S = 0.0f;
-      if (has_c && n < nchi) {
+      float v = 0.0f;
+      if (side == 0) {
+        if (n < nchi && n >= nlo && n <= nhi) {
+          const float4 h = __ldg(Hrow + s_bix[n]);
+          const float a2 = s_a2[n];
+          v = (h.x + a2 * (h.y + a2 * (h.z + a2 * h.w))) * dchi_f[n];
+        }
+      } else if (has_c && n < nchi) {
         const int i = n - c_off;
-        if (i >= 1 && i < c_rend) S = src_t(T, ncosmo, nchi, nsrc, Kf, src, n, c);
+        if (i >= 1 && i < c_rend) v = src_t(T, ncosmo, nchi, nsrc, Kf, src, n, c);
       }
       __nv_bfloat16 h, l;
-      const uint32_t off = tile_offset(tid, k);
-      split_bf16(J, h, l);
-      *reinterpret_cast<__nv_bfloat16*>(a_hi + off) = h;
-      *reinterpret_cast<__nv_bfloat16*>(a_lo + off) = l;
-      split_bf16(S, h, l);
-      *reinterpret_cast<__nv_bfloat16*>(b_hi + off) = h;
-      *reinterpret_cast<__nv_bfloat16*>(b_lo + off) = l;
+      const uint32_t off = tile_offset(row, k);
+      split_bf16(v, h, l);
+      *reinterpret_cast<__nv_bfloat16*>(thi + off) = h;
+      *reinterpret_cast<__nv_bfloat16*>(tlo + off) = l;
     }
     fence_proxy_async();
     __syncthreads();
@@ -264,8 +267,9 @@ __global__ void __launch_bounds__(128, 1)
     mbar_wait(bar, phase ^ 1, 1LL << 26);
   } else {
     fence_after_sync();
-    // epilogue: thread (warp w, lane) holds sampled l j = 32 w + lane for 32 cosmologies at a time
-    const int j = warp * 32 + lane;
+    // epilogue: thread (warp w, lane) holds sampled l j = 32 (w % 4) + lane for the 64
+    // cosmology columns of half w / 4, 32 at a time
+    const int j = (warp & 3) * 32 + lane;
     const bool has_j = j < nl;
     const int l = has_j ? G.ls[j] : 0;
     const double limber_l = 400 * sqrt(G.AccuracyBoost * G.LimberBoost);
@@ -274,9 +278,9 @@ __global__ void __launch_bounds__(128, 1)
     const double chif = (l + 0.5) / q;
     const int mlim = count_ge(chi, nchi, chif);  // nodes with chi >= chif
 #pragma unroll 1
-    for (int c0 = 0; c0 < 128; c0 += 32) {
+    for (int c0 = (warp >> 2) * 64; c0 < (warp >> 2) * 64 + 64; c0 += 32) {
       float v[32];
-      if (any) tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (any) tmem_ld32(tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0, v);
       else
         for (int i = 0; i < 32; ++i) v[i] = 0.0f;
       if (!has_j) continue;
@@ -330,7 +334,7 @@ cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc,
   dim3 gt((nk + 31) / 32, (ncosmo + 31) / 32, nchi * nsrc);
   tc::proj_src_transpose_kernel<<<gt, dim3(32, 8), 0, s>>>(cosmos, ncosmo, nchi, nk, nsrc, tsrc);
   dim3 grid((ncosmo + 127) / 128, nsrc, nq);
-  tc::proj_tc_kernel<<<grid, 128, tc::kProjSmem, s>>>(cosmos, ncosmo, chi, dchi_f, nchi, tsrc, err);
+  tc::proj_tc_kernel<<<grid, 256, tc::kProjSmem, s>>>(cosmos, ncosmo, chi, dchi_f, nchi, tsrc, err);
   return cudaGetLastError();
 }
 

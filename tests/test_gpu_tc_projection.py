@@ -83,3 +83,13 @@ def test_lensed_tensor_projection_matches_fp64_on_shared_grids():
         assert rel(g[:, 2], r[:, 2]) < 1e-4
         assert np.max(np.abs(g[:, 3] - r[:, 3]) / np.sqrt(r[:, 0] * r[:, 1])) < 1e-4
         assert rel(pot2[i, 2:2501, 0], pot0[i, 2:2501, 0]) < 1e-4
+
+
+def test_tensor_projection_several_cosmology_tiles():
+    """130 draws: two 128-cosmology tiles, the second nearly empty."""
+    ps = batch_draws(130, 600, seed=23)
+    out, _ = run_shared(ps, (0, 2), 600)
+    ref, got = out[0][0][:, 2:], out[2][0][:, 2:]
+    assert rel(got[..., 0], ref[..., 0]) < 1e-4
+    assert rel(got[..., 1], ref[..., 1]) < 1e-4
+    assert np.max(np.abs(got[..., 3] - ref[..., 3]) / np.sqrt(ref[..., 0] * ref[..., 1])) < 1e-4
