@@ -147,8 +147,8 @@ def gradient_rate(n=64, lmax=2500, seed=3000, mnu_max=0.2):
     t = time.perf_counter() - t0
     out = {"value": n / t, "unit": "gradients/s (dC_l/d 6 parameters, l <= %d, unlensed)" % lmax, "batch": n,
            "seconds": t, "method": "central differences through the batched pipeline: ombh2, omch2, H0, tau "
-                                   "re-evolved (+-1e-4 relative, 9 cosmologies per gradient in one launch); "
-                                   "As, ns by reweighting the resident transfer functions"}
+                                   "re-evolved (+-1e-4 relative, 9 cosmologies per gradient in one launch, FP64 "
+                                   "projection); As, ns by reweighting the resident transfer functions"}
     out.update(gradient_checks(ps[:2], g[:2]))
     return out
 

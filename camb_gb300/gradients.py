@@ -15,6 +15,7 @@ import copy
 
 import numpy as np
 
+from . import _lib
 from .results import _ResidentBatch
 
 PARAMS = ("ombh2", "omch2", "H0", "tau", "As", "ns")
@@ -60,17 +61,28 @@ def fd_members(params_list, rel_step):
     return members, steps
 
 
-def cl_gradients(params_list, rel_step=1e-4, lensed=False):
+def cl_gradients(params_list, rel_step=1e-4, lensed=False, precision=0):
     """C_l and their gradients for a list of CAMBparams.
 
     Returns (cls, grads): cls[n, lmax+1, 4] as CAMBdata.get_unlensed_scalar_cls (or the
     lensed spectra with lensed=True; every input must then have DoLensing) in
     l(l+1)C_l/2pi, columns TT EE BB TE; grads[n, 6, lmax+1, 4] the derivatives with
-    respect to PARAMS in that order."""
+    respect to PARAMS in that order.
+
+    `precision` is the line-of-sight arithmetic of the batch (cambgpu_set_precision;
+    the caller's setting is restored afterwards).  The default is FP64: a difference
+    quotient divides the C_l error by the step, so the mixed form's ~1e-6 relative
+    error would become ~5e-3 of a gradient at rel_step 1e-4."""
     n = len(params_list)
     stride = 1 + 2 * len(EVOLVED)
     members, steps = fd_members(params_list, rel_step)
-    batch = _ResidentBatch(members)
+    lib = _lib.load()
+    prev = lib.cambgpu_get_precision()
+    _lib.check(lib.cambgpu_set_precision(precision))
+    try:
+        batch = _ResidentBatch(members)
+    finally:
+        lib.cambgpu_set_precision(prev)
     col = 1 if lensed else 0
 
     def spectra():

@@ -227,6 +227,47 @@ def get_results_batch(params_list, lmax_out=None):
     return _run(params_list, lmax)
 
 
+_PROJECTIONS = {"fp64": 0, "mixed": 1, "tensor": 2}
+
+
+def get_results_batch_shared(params_list, lmax_out=None, projection="tensor"):
+    """A batch of CMB cosmologies on grids shared by the whole batch
+    (cambgpu_batch_prepare_shared: one comoving-distance grid, one source k grid, one
+    integration q grid and one Bessel table for every member; no counterpart in the
+    reference, where each cosmology has its own grids).  `projection` chooses the
+    arithmetic of the line-of-sight projection: "tensor" (split hi/lo BF16 products on the
+    tensor cores, FP32 accumulation), "mixed" (FP32) or "fp64".  All members share one l
+    sampling and one set of sources; the C_l differ from get_results_batch by the shared
+    grids' resampling (a few 1e-4 at high l), and the tensor and mixed forms from the FP64
+    one on the same grids by ~1e-5.  Returns one CAMBdata per cosmology."""
+    if projection not in _PROJECTIONS:
+        raise _lib.CAMBError(f"projection must be one of {sorted(_PROJECTIONS)}")
+    if any(p.WantTransfer or not p.WantCls for p in params_list):
+        raise _lib.CAMBError("shared grids are for CMB spectra only (WantCls, no WantTransfer)")
+    lib = _lib.load()
+    params = list(params_list)
+    n = len(params)
+    lmax = max(p.max_l for p in params) if lmax_out is None else lmax_out
+    arr = (_lib.CambGpuParams * n)(*[p.to_struct() for p in params])
+    prev = lib.cambgpu_get_precision()
+    _ResidentBatch.generation += 1  # the arena now holds this batch
+    _lib.check(lib.cambgpu_batch_prepare_shared(arr, n, None))
+    try:
+        _lib.check(lib.cambgpu_set_precision(_PROJECTIONS[projection]))
+        _lib.check(lib.cambgpu_batch_run(None))
+        cls = np.zeros((n, lmax + 1, 4))
+        lensed = np.zeros((n, lmax + 1, 4))
+        pot = np.zeros((n, lmax + 1, 3))
+        lml = np.zeros(n, dtype=np.int32)
+        _lib.check(lib.cambgpu_batch_spectra_from_transfer(None, None, None, None, lmax, _lib.dptr(cls),
+                                                           _lib.dptr(lensed), _lib.dptr(pot), _lib.iptr(lml)))
+    finally:
+        lib.cambgpu_set_precision(prev)
+        lib.cambgpu_batch_release()
+    return [CAMBdata(p, cls[i], lensed[i] if p.DoLensing else None, pot[i] if p.DoLensing else None,
+                     int(lml[i])) for i, p in enumerate(params)]
+
+
 class _ResidentBatch:
     """A batch whose tables and transfer functions stay on the device (one at a time:
     staging another batch retires this one)."""

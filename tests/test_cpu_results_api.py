@@ -57,3 +57,13 @@ def test_save_cmb_power_spectra_text_file(data, tmp_path):
     assert np.array_equal(arr[:, 0], np.arange(61))
     np.testing.assert_allclose(arr[:, 1:5], d.get_total_cls(CMB_unit="muK"), rtol=1e-7)
     np.testing.assert_allclose(arr[:, 5:], d.get_lens_potential_cls(60, CMB_unit="muK"), rtol=1e-7)
+
+
+def test_shared_grid_api_checks_its_arguments_before_any_device_call():
+    p = model.set_params(lmax=100)
+    with pytest.raises(model.CAMBError):
+        results.get_results_batch_shared([p], projection="fp16")
+    t = model.set_params(lmax=100)
+    t.WantTransfer = True
+    with pytest.raises(model.CAMBError):
+        results.get_results_batch_shared([t])

@@ -153,3 +153,23 @@ def test_fd_noise_between_relative_steps(box):
                 else:
                     assert np.median(d) < 5e-3, (i, name, c, np.median(d))
                     assert np.quantile(d, 0.9) < 0.15, (i, name, c, np.quantile(d, 0.9))
+
+
+def test_gradients_use_the_fp64_projection_whatever_the_callers_setting(grads):
+    """cl_gradients runs its batch with the FP64 projection by default, so a caller that
+    left the mixed projection set gets the FP64 gradients (the mixed projection would move
+    them by ~1e-3 of their peak), and keeps its setting."""
+    ps, cls, g = grads
+    lib = _lib.load()
+    old = lib.cambgpu_get_precision()
+    _lib.check(lib.cambgpu_set_precision(1))
+    try:
+        cls1, g1 = gradients.cl_gradients(ps)
+        assert lib.cambgpu_get_precision() == 1
+    finally:
+        lib.cambgpu_set_precision(old)
+    np.testing.assert_allclose(cls1, cls, rtol=1e-12, atol=0)
+    for j in range(len(gradients.PARAMS)):
+        for c in (0, 1, 3):
+            peak = np.max(np.abs(g[:, j, 2:, c]))
+            assert np.max(np.abs(g1[:, j, 2:, c] - g[:, j, 2:, c])) < 1e-9 * peak

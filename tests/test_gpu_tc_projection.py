@@ -93,3 +93,24 @@ def test_tensor_projection_several_cosmology_tiles():
     assert rel(got[..., 0], ref[..., 0]) < 1e-4
     assert rel(got[..., 1], ref[..., 1]) < 1e-4
     assert np.max(np.abs(got[..., 3] - ref[..., 3]) / np.sqrt(ref[..., 0] * ref[..., 1])) < 1e-4
+
+
+def test_public_shared_grid_api_tensor_against_fp64_and_native_grids():
+    """get_results_batch_shared (the Python surface) with the tensor projection: lensed TT,
+    EE, BB within 1e-4 of the FP64 projection on the same shared grids, and within 3e-3
+    of get_results_batch on each cosmology's own grids below l = 2000."""
+    import camb_gb300 as cg
+    ps = [cg.set_params(lmax=2000, H0=h, ombh2=b, omch2=c, mnu=m)
+          for h, b, c, m in ((67.5, 0.0224, 0.120, 0.06), (70.0, 0.0220, 0.115, 0.12), (65.0, 0.0228, 0.125, 0.0))]
+    before = _lib.load().cambgpu_get_precision()
+    got = cg.get_results_batch_shared(ps, projection="tensor")
+    ref = cg.get_results_batch_shared(ps, projection="fp64")
+    nat = cg.get_results_batch(ps)
+    for g, r, n in zip(got, ref, nat):
+        gl, rl, nl = (x.get_lensed_scalar_cls(2000, raw_cl=True)[2:] for x in (g, r, n))
+        for c in range(3):
+            assert rel(gl[:, c], rl[:, c]) < 1e-4
+            assert rel(rl[:, c], nl[:, c]) < 3e-3
+        gp, rp = g.get_lens_potential_cls(2000, raw_cl=True)[2:], r.get_lens_potential_cls(2000, raw_cl=True)[2:]
+        assert rel(gp[:, 0], rp[:, 0]) < 1e-4
+    assert _lib.load().cambgpu_get_precision() == before  # the caller's precision is restored
