@@ -374,6 +374,12 @@ class CAMBdataMatter(CAMBdata):
     def get_fsigma8(self):
         return self._mtd.sigma2_vdelta_8 / self._mtd.sigma_8
 
+    def get_matter_power_spectrum(self, minkh=1e-4, maxkh=1.0, npoints=100, var1=None, var2=None, **kwargs):
+        """camb/results.py get_matter_power_spectrum (results.py:1000-1048), linear:
+        kh (npoints values log-spaced from minkh to maxkh), z increasing, PK[z, kh] in
+        (Mpc/h)^3, splined from the transfer functions (matter_power_on_log_grid)."""
+        return _matter_power_spectrum(self.Params, self._mtd.transfer_data, minkh, maxkh, npoints, var1, var2)
+
     def get_linear_matter_power_spectrum(self, var1=None, var2=None, hubble_units=True, k_hunit=True, **kwargs):
         """Transfer_GetUnsplinedPower (results.f90:3472-3513) on the transfer k grid:
         returns k/h (or k), z increasing, PK[z, k]."""
@@ -395,6 +401,87 @@ class CAMBdataMatter(CAMBdata):
             pk *= h ** 3
         z = np.array(self.Params.Transfer.PK_redshifts[::-1], dtype=np.float64)
         return (kh if k_hunit else k), z, pk
+
+
+def _natural_spline_d2(x, y):
+    """Second derivatives of the natural cubic spline through (x, y) (zero at both ends),
+    by the tridiagonal recurrence; y may carry trailing columns."""
+    n = len(x)
+    d2 = np.zeros_like(y)
+    if n < 3:
+        return d2
+    u = np.zeros_like(y)
+    for i in range(1, n - 1):
+        sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1])
+        p = sig * d2[i - 1] + 2.0
+        d2[i] = (sig - 1.0) / p
+        slope = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1])
+        u[i] = (6.0 * slope / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p
+    for i in range(n - 2, -1, -1):
+        d2[i] = d2[i] * d2[i + 1] + u[i]
+    return d2
+
+
+def matter_power_on_log_grid(kh, t1, t2, h, init_power, minkh, dlnkh, npoints):
+    """Transfer_GetMatterPowerD (results.f90:3841-3948), linear: P(k/h) at npoints values
+    spaced by dlnkh in ln(k/h) from minkh, in (Mpc/h)^3, from the transfer functions t1, t2
+    on the transfer grid kh (k/h) of one redshift.  The transfer part T1 T2 k 2pi^2 h^3 is
+    splined in ln(k/h) -- in its logarithm when it has one sign, a natural cubic spline --
+    and extrapolated linearly in ln k past the last node (below the first node the result is
+    the floor exp(-30)); the primordial power multiplies the interpolated value."""
+    kh = np.asarray(kh, dtype=np.float64)
+    x = np.log(kh)
+    mp = np.asarray(t1, dtype=np.float64) * np.asarray(t2, dtype=np.float64) * kh * h * np.pi * 2 * np.pi * h ** 3
+    sign, log_interp = 1.0, True
+    if np.any(mp <= 0):
+        if np.all(mp < 0):
+            sign = -1.0
+        else:
+            log_interp = False
+    if log_interp:
+        mp = np.log(sign * mp)
+    d2 = _natural_spline_d2(x, mp)
+    out = np.empty(npoints)
+    xi = np.log(minkh) + dlnkh * np.arange(npoints)
+    n = len(x)
+    llo, last = 0, npoints
+    for il in range(npoints):
+        if xi[il] < x[0]:
+            out[il] = -30.0
+            continue
+        while llo < n - 1 and xi[il] > x[llo + 1]:
+            llo += 1
+        if llo == n - 1:
+            last = il
+            break
+        ho = x[llo + 1] - x[llo]
+        a0 = (x[llo + 1] - xi[il]) / ho
+        b0 = (xi[il] - x[llo]) / ho
+        out[il] = a0 * mp[llo] + b0 * mp[llo + 1] + ((a0 ** 3 - a0) * d2[llo] + (b0 ** 3 - b0) * d2[llo + 1]) * ho ** 2 / 6
+    for il in range(last, npoints):  # linear extrapolation in the logarithm
+        out[il] = 2 * out[il - 1] - out[il - 2]
+    if log_interp:
+        out = sign * np.exp(np.maximum(-30.0, out))
+    k = np.exp(xi) * h
+    lnrat = np.log(k / init_power.pivot_scalar)
+    return out * init_power.As * np.exp(lnrat * (init_power.ns - 1 + lnrat * (init_power.nrun / 2)))
+
+
+def _matter_power_spectrum(params, td, minkh, maxkh, npoints, var1, var2):
+    if not npoints >= 2:
+        raise _lib.CAMBError("Need at least two points in get_matter_power_spectrum")
+    s1 = 6 if var1 is None else int(var1) - 1
+    s2 = 6 if var2 is None else int(var2) - 1
+    h = params.H0 / 100
+    nz = td.shape[2]
+    dlnkh = (np.log(maxkh) - np.log(minkh)) / (npoints - 1)
+    pk = np.empty((nz, npoints))
+    for zix in range(nz):
+        it = nz - 1 - zix  # increasing z: the transfer times are stored in decreasing z
+        pk[zix] = matter_power_on_log_grid(td[0, :, it], td[s1, :, it], td[s2, :, it], h, params.InitPower, minkh,
+                                           dlnkh, npoints)
+    z = np.array(params.Transfer.PK_redshifts[::-1], dtype=np.float64)
+    return minkh * np.exp(np.arange(npoints) * dlnkh), z, pk
 
 
 def _run_transfer(params_list):

@@ -51,3 +51,37 @@ def test_transfer_with_cmb_is_rejected():
     p.want_cls = 1
     with pytest.raises(_lib.CAMBError):
         _lib.Tables(p)
+
+
+def test_matter_power_known_answers():
+    """get_matter_power_spectrum (the transfer functions splined in ln k,
+    Transfer_GetMatterPowerD) and get_linear_matter_power_spectrum (the transfer grid) on
+    the oracle's transfer functions against the reference's known answers
+    (camb_test.py testPowers, places=2)."""
+    import json
+    import os
+    from camb_gb300 import model, results
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))["matter_power"]
+    cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.07, As=2e-9, ns=0.965)
+    cp.Reion.set_zrei(10)
+    cp.WantCls = False
+    cp.set_matter_power(redshifts=[0.0, 0.17, 3.1], kmax=1.2)
+    T = _lib.Tables(cp.to_struct())
+    tr = orc.evolve_transfer(T)
+    td = np.ascontiguousarray(tr.transpose(2, 1, 0))
+    s8, sv = orc.sigma8(T, tr)
+    r = results.CAMBdataMatter(cp, results.MatterTransferData(td, td[0, :, 0] * cp.H0 / 100, s8, sv))
+    kh, z, pk = r.get_matter_power_spectrum(1e-4, 1, 20)
+    assert list(z) == [0.0, 0.17, 3.1] and pk.shape == (3, 20)
+    np.testing.assert_allclose(kh, np.logspace(-4, 0, 20), rtol=1e-12)
+    kh2, _, pk2 = r.get_linear_matter_power_spectrum()
+    for got, key in [(pk[g["splined"]["index"][0], g["splined"]["index"][1]], "splined"),
+                     (pk2[g["unsplined"]["index"][0], g["unsplined"]["index"][1]], "unsplined")]:
+        want, places = g[key]["value"]
+        assert round(abs(got - want), places) == 0, (key, got, want)
+    # at the transfer grid's own k the spline returns the unsplined values
+    inner = slice(3, len(kh2) - 3)
+    for zi in range(3):
+        for j in range(inner.start, inner.stop, 7):
+            _, _, one = r.get_matter_power_spectrum(kh2[j], kh2[j] * 1.5, 2)
+            np.testing.assert_allclose(one[zi, 0], pk2[zi, j], rtol=1e-5)

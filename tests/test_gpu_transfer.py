@@ -84,6 +84,9 @@ def test_python_surface_sigma8():
     kh, z, pk = r.get_linear_matter_power_spectrum()
     assert list(z) == [0.0, 0.17, 3.1] and pk.shape == (3, len(kh))
     assert np.all(pk > 0) and pk[0].max() > pk[2].max()
+    # the reference's P(k) known answers (camb_test.py testPowers, places=2)
+    _, _, pks = r.get_matter_power_spectrum(1e-4, 1, 20)
+    assert round(abs(pks[-1][-3] - 51.924), 2) == 0 and round(abs(pk[-2][-4] - 56.454), 2) == 0
 
 
 def test_python_surface_cmb_and_matter_power_together():
