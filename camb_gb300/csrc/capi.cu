@@ -537,6 +537,7 @@ struct Batch {
   WorkItem* d_items_bal = nullptr;
   size_t bal_cap = 0;
   int bal_threads = 0, bal_n = 0, bal_gen = 0, bal_tried = 0;
+  bool bal_estimated = false;        // the balanced queue was built from the cost prior
   unsigned* d_mode_evals = nullptr;  // [nitems], cosmology-major
   std::vector<size_t> mode_base;     // first mode_evals entry of each cosmology
   bool costs_valid = false, cost_order = false;
@@ -969,6 +970,76 @@ int build_cost_order(Batch& B) {
   return 0;
 }
 
+// Evaluations per mode as a function of ln q, recorded from the first run of the last batch
+// whose costs were measured, for batches of the same kind (l range, sources, massive
+// neutrinos, transfer functions): a fresh batch's first run then starts on a balanced queue
+// built from these estimates instead of the q-band order.  Any queue holds every mode once,
+// so the estimates change the schedule only, never the results.
+struct CostPrior {
+  long long sig = -1;
+  double lq0 = 0, dlq = 1;
+  std::vector<double> ev;  // mean evaluations per ln q bin (interpolated over empty bins)
+};
+CostPrior g_cost_prior;
+
+long long cost_signature(const Batch& B) {
+  const CambGpuTables& t = *B.views[0];
+  return ((long long)t.max_l * 8 + t.nsrc) * 4 + (B.massive_nu ? 2 : 0) + (B.transfer ? 1 : 0);
+}
+
+int record_cost_prior(Batch& B) {
+  std::vector<unsigned> ev(B.nitems);
+  CUDA_TRY(cudaMemcpy(ev.data(), B.d_mode_evals, ev.size() * 4, cudaMemcpyDeviceToHost));
+  double lo = 1e300, hi = -1e300;
+  for (const WorkItem& w : B.h_items_grp) {
+    const double lq = std::log(B.views[w.cosmo]->modes[w.mode].q);
+    lo = std::min(lo, lq);
+    hi = std::max(hi, lq);
+  }
+  const int nb = 128;
+  CostPrior P;
+  P.sig = cost_signature(B);
+  P.lq0 = lo;
+  P.dlq = std::max(hi - lo, 1e-12) / (nb - 1);
+  std::vector<double> sum(nb, 0.0), cnt(nb, 0.0);
+  for (const WorkItem& w : B.h_items_grp) {
+    const double lq = std::log(B.views[w.cosmo]->modes[w.mode].q);
+    const int b = std::min(nb - 1, std::max(0, (int)std::lround((lq - lo) / P.dlq)));
+    sum[b] += ev[B.mode_base[w.cosmo] + w.mode];
+    cnt[b] += 1;
+  }
+  P.ev.assign(nb, 0.0);
+  int last = -1;
+  for (int b = 0; b < nb; ++b) {
+    if (cnt[b] == 0) continue;
+    P.ev[b] = sum[b] / cnt[b];
+    for (int e = last + 1; e < b; ++e)  // empty bins: linear between filled neighbours
+      P.ev[e] = last < 0 ? P.ev[b] : P.ev[last] + (P.ev[b] - P.ev[last]) * (e - last) / (b - last);
+    last = b;
+  }
+  for (int e = last + 1; e < nb && last >= 0; ++e) P.ev[e] = P.ev[last];
+  g_cost_prior = std::move(P);
+  return 0;
+}
+
+// estimated evaluations of every mode (cosmology-major, as d_mode_evals) from the prior
+std::vector<unsigned> estimated_evals(const Batch& B) {
+  const CostPrior& P = g_cost_prior;
+  std::vector<unsigned> ev(B.nitems, 0);
+  const int nb = (int)P.ev.size();
+  for (const WorkItem& w : B.h_items_grp) {
+    const double x = (std::log(B.views[w.cosmo]->modes[w.mode].q) - P.lq0) / P.dlq;
+    const int b = std::min(nb - 2, std::max(0, (int)std::floor(x)));
+    const double f = std::min(1.0, std::max(0.0, x - b));
+    ev[B.mode_base[w.cosmo] + w.mode] = (unsigned)(P.ev[b] + f * (P.ev[b + 1] - P.ev[b]) + 0.5);
+  }
+  return ev;
+}
+
+bool cost_prior_applies(const Batch& B) {
+  return g_cost_prior.ev.size() >= 2 && g_cost_prior.sig == cost_signature(B);
+}
+
 // Queue order 4 for a static-stride launch of T threads (thread t takes entries t, t + T,
 // t + 2T, ...): the q-band order (2) cut into bundles of 32 neighbouring modes -- one warp's
 // lanes, which share hierarchy sizes and switch sequences -- and the bundles dealt to the
@@ -976,10 +1047,14 @@ int build_cost_order(Batch& B) {
 // bundle being its costliest mode's evaluations x system size in the last run.  Warps are
 // then ranked by their number of bundles so that round k of the stride holds the k-th
 // bundles of the warps that have one; the few slots left over are empty (cosmo = -1).
-int build_balanced_order(Batch& B, int T) {
+// The costs are the last run's measured evaluations, or, before the batch has run, the
+// cost prior's estimates (estimated = true).
+int build_balanced_order(Batch& B, int T, bool estimated = false) {
   B.bal_tried = T;
+  B.bal_estimated = estimated;
   std::vector<unsigned> ev(B.nitems);
-  CUDA_TRY(cudaMemcpy(ev.data(), B.d_mode_evals, ev.size() * 4, cudaMemcpyDeviceToHost));
+  if (estimated) ev = estimated_evals(B);
+  else CUDA_TRY(cudaMemcpy(ev.data(), B.d_mode_evals, ev.size() * 4, cudaMemcpyDeviceToHost));
   const int nw = std::max(1, T / 32);
   const int nb = (B.nitems + 31) / 32;
   std::vector<double> bcost(nb, 0.0);
@@ -1105,12 +1180,16 @@ int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
     int rc = build_cost_order(B);  // outside any capture: a synchronous copy each way
     if (rc) return rc;
   }
-  if (do_ode && B.costs_valid) {
+  if (do_ode) {
     const int team = pick_team(B);
     int blocks, tpb;
     ode_launch_shape(B, team, blocks, tpb);
-    if (balanced_applies(B, team) && B.bal_tried != blocks * tpb) {
-      int rc = build_balanced_order(B, blocks * tpb);  // outside any capture
+    if (balanced_applies(B, team)) {
+      int rc = 0;  // outside any capture
+      if (B.costs_valid && (B.bal_tried != blocks * tpb || B.bal_estimated))
+        rc = build_balanced_order(B, blocks * tpb);
+      else if (!B.costs_valid && B.bal_tried != blocks * tpb && cost_prior_applies(B))
+        rc = build_balanced_order(B, blocks * tpb, true);
       if (rc) return rc;
     }
   }
@@ -1128,7 +1207,11 @@ int run_all(Batch& B, bool do_ode, bool do_los, bool do_cls) {
   }
   B.runs++;
   CUDA_TRY(cudaEventSynchronize(g_rt.ev[3]));
-  if (do_ode) B.costs_valid = true;
+  if (do_ode && !B.costs_valid) {
+    B.costs_valid = true;
+    int rc = record_cost_prior(B);  // the first measured costs of this batch
+    if (rc) return rc;
+  }
   g_timings[0] = elapsed(g_rt.ev[0], g_rt.ev[1]);
   g_timings[1] = 0;
   g_timings[2] = elapsed(g_rt.ev[1], g_rt.ev[2]);

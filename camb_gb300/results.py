@@ -380,6 +380,20 @@ class CAMBdataMatter(CAMBdata):
         (Mpc/h)^3, splined from the transfer functions (matter_power_on_log_grid)."""
         return _matter_power_spectrum(self.Params, self._mtd.transfer_data, minkh, maxkh, npoints, var1, var2)
 
+    def get_matter_power_interpolator(self, nonlinear=True, var1=None, var2=None, hubble_units=True, k_hunit=True,
+                                      return_z_k=False, log_interp=True, extrap_kmax=None, silent=False):
+        """camb/results.py get_matter_power_interpolator: a spline of P(z, k/h) (or of k) through
+        the transfer-grid power at the transfer redshifts -- cubic in ln k, of degree
+        min(nz - 1, 3) in z, of ln(sign P) unless P changes sign; with extrap_kmax, ln P is
+        continued as a power law of the last interval's slope to extrap_kmax.  Evaluate with
+        .P(z, kh) (or call it with (z, ln kh) for the interpolated value itself).  The power
+        is linear: halo-model corrections are not part of this package, and nonlinear=True
+        returns the linear spectrum as the reference does for a model without them."""
+        kh, zs, pk = self.get_linear_matter_power_spectrum(var1, var2, hubble_units)
+        if not k_hunit:
+            kh = kh * self.Params.H0 / 100
+        return MatterPowerInterpolator(zs, kh, pk, log_interp, extrap_kmax, return_z_k)
+
     def get_linear_matter_power_spectrum(self, var1=None, var2=None, hubble_units=True, k_hunit=True, **kwargs):
         """Transfer_GetUnsplinedPower (results.f90:3472-3513) on the transfer k grid:
         returns k/h (or k), z increasing, PK[z, k]."""
@@ -401,6 +415,63 @@ class CAMBdataMatter(CAMBdata):
             pk *= h ** 3
         z = np.array(self.Params.Transfer.PK_redshifts[::-1], dtype=np.float64)
         return (kh if k_hunit else k), z, pk
+
+
+class _PK:
+    """P(z, k) spline built by MatterPowerInterpolator."""
+
+    def __init__(self, zs, logk, vals, islog, sign):
+        from scipy.interpolate import CubicSpline, RectBivariateSpline
+        self.islog, self.logsign = islog, sign
+        self.zmin, self.zmax = float(np.min(zs)), float(np.max(zs))
+        self._zs = np.asarray(zs, dtype=np.float64)
+        if len(zs) > 1:
+            self._s2 = RectBivariateSpline(self._zs, logk, vals, kx=min(len(zs) - 1, 3), ky=min(len(logk) - 1, 3))
+            self._s1 = None
+        else:
+            self._s2 = None
+            self._s1 = CubicSpline(logk, vals[0])
+
+    def __call__(self, z, logk, grid=None):
+        """The interpolated value (ln(sign P) when islog) at (z, ln k)."""
+        if grid is None:
+            grid = not np.isscalar(z) and not np.isscalar(logk)
+        if self._s2 is not None:
+            return self._s2(z, logk, grid=grid)
+        if not np.allclose(z, self._zs[0]):
+            raise _lib.CAMBError(f"P(z,k) requested at z={z}, but only computed for z={self._zs[0]:g}")
+        return self._s1(logk)
+
+    def P(self, z, kh, grid=None):
+        v = self(z, np.log(kh), grid=grid)
+        return self.logsign * np.exp(v) if self.islog else v
+
+
+def MatterPowerInterpolator(zs, kh, pk, log_interp=True, extrap_kmax=None, return_z_k=False):
+    """The spline of get_matter_power_interpolator from P[z, kh] on the transfer grid."""
+    zs = np.asarray(zs, dtype=np.float64)
+    kh = np.asarray(kh, dtype=np.float64)
+    sign = 1.0
+    if log_interp and np.any(pk <= 0):
+        if np.all(pk < 0):
+            sign = -1.0
+        else:
+            log_interp = False
+    vals = np.log(sign * pk) if log_interp else np.array(pk, dtype=np.float64)
+    logk = np.log(kh)
+    kmax = kh[-1]
+    if extrap_kmax and extrap_kmax > kmax:
+        if not log_interp:
+            raise _lib.CAMBError("extrap_kmax needs log interpolation (the power changes sign)")
+        # power law with the last interval's slope, on two nodes: one a tenth of the way back
+        # from extrap_kmax (slope scaled by 0.9) and one at extrap_kmax
+        span = np.log(extrap_kmax) - logk[-1]
+        slope = (vals[:, -1] - vals[:, -2]) / (logk[-1] - logk[-2])
+        vals = np.hstack((vals, (vals[:, -1] + 0.9 * slope * span)[:, None], (vals[:, -1] + slope * span)[:, None]))
+        logk = np.hstack((logk, np.log(extrap_kmax) - 0.1 * span, np.log(extrap_kmax)))
+    res = _PK(zs, logk, vals, log_interp, sign)
+    res.kmin, res.kmax = float(np.min(kh)), float(kmax)
+    return (res, zs, kh) if return_z_k else res
 
 
 def _natural_spline_d2(x, y):

@@ -321,7 +321,11 @@ int cambgpu_set_ode_schedule(int schedule);
  * size; order 2 until a run has recorded it), 4 = order 2 cut into bundles of 32 modes
  * dealt to the warps of a static-stride launch by the previous run's costs, longest
  * first, so that every warp gets the same work (thread-per-mode kernels with the
- * static-stride schedule; order 2 otherwise or until a run has recorded the costs).
+ * static-stride schedule; order 2 otherwise).  Before a batch's first run, order 4 uses
+ * the evaluations per ln q recorded from the first run of the last batch of the same kind
+ * (same lmax, sources, massive neutrinos or not, transfer functions or not), and order 2
+ * when there is none; from the batch's second run its own measured costs.  Queue orders
+ * never change results, only which thread runs which mode.
  * best = [team, order, class, cap]; times (optional, >= 16 entries) receives ms per
  * candidate (0 for candidates that do not apply to the batch). */
 int cambgpu_autotune_ode(const CambGpuParams* p, int n, int* best, double* times);

@@ -85,3 +85,35 @@ def test_matter_power_known_answers():
         for j in range(inner.start, inner.stop, 7):
             _, _, one = r.get_matter_power_spectrum(kh2[j], kh2[j] * 1.5, 2)
             np.testing.assert_allclose(one[zi, 0], pk2[zi, j], rtol=1e-5)
+
+
+def test_matter_power_interpolator():
+    """get_matter_power_interpolator on the oracle's transfer functions: through the
+    transfer-grid power at every node, within 2e-3 of the log-grid spline between nodes at
+    the computed redshifts, monotone growth at intermediate z, a single-redshift run that
+    refuses other z, and the power-law continuation to extrap_kmax."""
+    from camb_gb300 import model, results
+    cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.07, As=2e-9, ns=0.965)
+    cp.Reion.set_zrei(10)
+    cp.WantCls = False
+    cp.set_matter_power(redshifts=[0.0, 0.17, 0.5, 1.0, 3.1], kmax=1.2)
+    T = _lib.Tables(cp.to_struct())
+    tr = orc.evolve_transfer(T)
+    td = np.ascontiguousarray(tr.transpose(2, 1, 0))
+    s8, sv = orc.sigma8(T, tr)
+    r = results.CAMBdataMatter(cp, results.MatterTransferData(td, td[0, :, 0] * cp.H0 / 100, s8, sv))
+    kh, z, pk = r.get_linear_matter_power_spectrum()
+    PK = r.get_matter_power_interpolator(nonlinear=False)
+    np.testing.assert_allclose(PK.P(z, kh), pk, rtol=1e-10)
+    khs, _, pks = r.get_matter_power_spectrum(1e-3, 1.0, 50)
+    np.testing.assert_allclose(PK.P(z, khs), pks, rtol=2e-3)
+    mid = PK.P(np.array([0.3, 0.7]), np.array([0.1]))
+    assert pk[1, np.searchsorted(kh, 0.1)] > mid[0, 0] > mid[1, 0] > pk[3, np.searchsorted(kh, 0.1)] * 0.9
+    ext = r.get_matter_power_interpolator(nonlinear=False, extrap_kmax=10.0)
+    assert ext.kmax == kh[-1] and np.isfinite(ext.P(0.0, 5.0))
+    slope = np.log(pk[0, -1] / pk[0, -2]) / np.log(kh[-1] / kh[-2])
+    np.testing.assert_allclose(np.log(ext.P(0.0, 10.0) / pk[0, -1]) / np.log(10.0 / kh[-1]), slope, rtol=1e-6)
+    one = results.MatterPowerInterpolator([0.5], kh, pk[2:3])
+    np.testing.assert_allclose(one.P(0.5, kh), pk[2], rtol=1e-10)
+    with pytest.raises(_lib.CAMBError):
+        one.P(0.0, 0.1)

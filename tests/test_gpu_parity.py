@@ -206,6 +206,37 @@ def test_queue_orders_and_caps_give_identical_results():
             assert np.array_equal(o, runs[0])
 
 
+def test_first_run_on_the_cost_prior_is_identical():
+    """A fresh batch of a kind that has run before starts on a balanced queue built from the
+    previous batch's evaluations per ln q (the cost prior); like any queue it changes only
+    which thread runs which mode.  The first run of a fresh batch on the prior, its second
+    run on its own measured costs, and a run on the q-band order give the same spectra."""
+    lib = _lib.load()
+    first = draws(3, seed=5, lmax=500, mnu_max=0.1)
+    second = draws(3, seed=6, lmax=500, mnu_max=0.1)
+    outs = []
+    try:
+        _lib.check(lib.cambgpu_set_ode_team(7))
+        _lib.check(lib.cambgpu_set_ode_schedule(1))
+        for ps, order, runs in [(first, 4, 1), (second, 4, 2), (second, 2, 1)]:
+            arr = (_lib.CambGpuParams * len(ps))(*ps)
+            _lib.check(lib.cambgpu_set_ode_launch(order, 0))
+            _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
+            for _ in range(runs):
+                _lib.check(lib.cambgpu_batch_run(None))
+                cls = np.zeros((len(ps), 501, 4))
+                _lib.check(lib.cambgpu_batch_fetch(500, _lib.dptr(cls)))
+                outs.append(cls)
+            lib.cambgpu_batch_release()
+    finally:
+        lib.cambgpu_set_ode_team(0)
+        lib.cambgpu_set_ode_launch(-1, 0)
+        lib.cambgpu_set_ode_schedule(-1)
+        lib.cambgpu_batch_release()
+    assert np.array_equal(outs[1], outs[2]) and np.array_equal(outs[1], outs[3])
+    assert not np.array_equal(outs[0], outs[1])  # different draws
+
+
 def test_resident_batch_refuses_after_a_later_staging():
     """A one-shot call reuses the device arena: the resident batch then reports an error
     instead of computing on overwritten tables, and the library stays usable."""
