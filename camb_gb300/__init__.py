@@ -7,9 +7,9 @@ the reference's camb.get_results / CAMBdata power-spectrum calls.
 """
 from ._lib import CAMBError, Tables, load
 from .model import AccuracyParams, CAMBparams, set_params
-from .results import (CAMBdata, get_results, get_results_batch, get_results_batch_shared, get_results_stream,
-                      get_transfer_functions, get_transfer_functions_batch)
+from .results import (CAMBdata, get_matter_power_interpolator, get_results, get_results_batch,
+                      get_results_batch_shared, get_results_stream, get_transfer_functions, get_transfer_functions_batch)
 
 __all__ = ["CAMBError", "Tables", "load", "AccuracyParams", "CAMBparams", "set_params", "CAMBdata",
-           "get_results", "get_results_batch", "get_results_batch_shared", "get_results_stream", "get_transfer_functions",
+           "get_matter_power_interpolator", "get_results", "get_results_batch", "get_results_batch_shared", "get_results_stream", "get_transfer_functions",
            "get_transfer_functions_batch"]

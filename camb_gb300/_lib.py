@@ -36,7 +36,7 @@ class CambGpuParams(C.Structure):
         ("accurate_polarization", C.c_int), ("accurate_reionization", C.c_int),
         ("LensingBoost", C.c_double),
         ("want_cls", C.c_int), ("want_transfer", C.c_int), ("transfer_high_precision", C.c_int),
-        ("transfer_kmax", C.c_double), ("num_transfer_redshifts", C.c_int), ("transfer_redshifts", C.c_double * 16),
+        ("transfer_kmax", C.c_double), ("num_transfer_redshifts", C.c_int), ("transfer_redshifts", C.c_double * 256),
         ("reion_use_optical_depth", C.c_int), ("reion_redshift", C.c_double),
     ]
 

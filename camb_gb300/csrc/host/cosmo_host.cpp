@@ -1307,8 +1307,8 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
     return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
   }
   if (P.want_transfer) {
-    if (!(P.transfer_kmax > 0) || P.num_transfer_redshifts < 1 || P.num_transfer_redshifts > 16) {
-      err = "transfer kmax and 1-16 redshifts required";
+    if (!(P.transfer_kmax > 0) || P.num_transfer_redshifts < 1 || P.num_transfer_redshifts > 256) {
+      err = "transfer kmax and 1-256 redshifts required";
       return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
     }
     for (int i = 1; i < P.num_transfer_redshifts; ++i)

@@ -135,8 +135,8 @@ class CAMBparams:
             raise CAMBError("non-linear matter power is not part of the GPU path")
         if k_per_logint:
             raise CAMBError("only the optimized transfer k spacing (k_per_logint = 0) is built")
-        if len(redshifts) > 16:
-            raise CAMBError("at most 16 transfer redshifts")
+        if len(redshifts) > 256:
+            raise CAMBError("at most 256 transfer redshifts (max_transfer_redshifts)")
         self.WantTransfer = True
         self.Transfer.high_precision = True
         self.Transfer.kmax = kmax

@@ -330,6 +330,22 @@ class CAMBdataTransfers(CAMBdata):
         self._refresh(self._batch.spectra())
 
 
+def get_matter_power_interpolator(params, zmin=0.0, zmax=10.0, nz_step=100, zs=None, kmax=10.0, nonlinear=True,
+                                  var1=None, var2=None, hubble_units=True, k_hunit=True, return_z_k=False,
+                                  k_per_logint=None, log_interp=True, extrap_kmax=None):
+    """camb.get_matter_power_interpolator: transfer functions of a copy of params at zs
+    (default nz_step redshifts from zmin to zmax, evenly spaced in ln(1 + z - zmin)) to
+    kmax (1/Mpc), then CAMBdataMatter.get_matter_power_interpolator.  Linear power (the
+    reference also switches the non-linear model off here); the CMB is not computed."""
+    pars = copy.deepcopy(params)
+    if zs is None:
+        zs = zmin + np.exp(np.log(zmax - zmin + 1) * np.linspace(0, 1, nz_step)) - 1
+    pars.set_matter_power(redshifts=list(zs), kmax=kmax, k_per_logint=k_per_logint)
+    pars.WantCls = False
+    return get_results(pars).get_matter_power_interpolator(nonlinear, var1, var2, hubble_units, k_hunit, return_z_k,
+                                                           log_interp, extrap_kmax)
+
+
 def get_transfer_functions(params):
     """camb.get_transfer_functions (camb.py:64-79) for the scalar CMB path."""
     return CAMBdataTransfers(_ResidentBatch([params]), 0)

@@ -63,8 +63,8 @@ typedef struct CambGpuParams {
     int want_transfer;           /* 1: transfer functions at transfer_redshifts (with want_cls = 0) */
     int transfer_high_precision; /* Transfer%high_precision (set_matter_power sets it) */
     double transfer_kmax;        /* Transfer%kmax in 1/Mpc */
-    int num_transfer_redshifts;  /* 1..16, in decreasing order as set_matter_power sorts them */
-    double transfer_redshifts[16];
+    int num_transfer_redshifts;  /* 1..256 (max_transfer_redshifts), decreasing, as set_matter_power sorts them */
+    double transfer_redshifts[256];
     int reion_use_optical_depth; /* 1: optical_depth fixes the reionization redshift; 0: reion_redshift does */
     double reion_redshift;
 } CambGpuParams;

@@ -2,6 +2,7 @@
 same inputs, and the reference's sigma8 / f sigma8 known answers through the GPU path.
 Tolerance: each transfer variable within 1e-5 of its peak over k (single-precision
 storage, as the reference), sigma8 within 1e-6 relative of the oracle."""
+import copy
 import ctypes as C
 
 import numpy as np
@@ -102,3 +103,21 @@ def test_python_surface_cmb_and_matter_power_together():
     assert np.array_equal(both.get_unlensed_scalar_cls(800), want_cls)
     assert both.get_sigma8()[0] == results.get_results(tr_only).get_sigma8()[0]
     assert 0.7 < both.get_sigma8()[0] < 0.9
+
+
+def test_top_level_matter_power_interpolator():
+    """camb.get_matter_power_interpolator(params): transfer functions at the default 100
+    redshifts (0-10) to kmax 10 /Mpc on the GPU; at z = 0 the spline agrees with the
+    log-grid power of a single-redshift run within 2e-3, and P falls with z."""
+    import camb_gb300 as camb
+    from camb_gb300 import model
+    cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.06, As=2e-9, ns=0.965, lmax=1000)
+    PK, zs, kh = camb.get_matter_power_interpolator(cp, nonlinear=False, return_z_k=True)
+    assert len(zs) == 100 and zs[0] == 0.0 and abs(zs[-1] - 10.0) < 1e-9
+    one = copy.deepcopy(cp)
+    one.set_matter_power(redshifts=[0.0], kmax=10.0)
+    one.WantCls = False
+    khs, _, pk = camb.get_results(one).get_matter_power_spectrum(1e-3, 5.0, 40)
+    np.testing.assert_allclose(PK.P(0.0, khs), pk[0], rtol=2e-3)
+    p = PK.P(np.array([0.0, 1.0, 5.0]), np.array([0.2]))[:, 0]
+    assert p[0] > p[1] > p[2] > 0
