@@ -8,6 +8,7 @@ last run.  Under ncu, `-k regex:<kernel> -s 3 -c 1` then captures the fourth lau
 that kernel, after three warm launches.  Cases:
 
   warp1        one massless cosmology, lmax 1000, warp per mode (team 6)
+  lens1        one cosmology with mnu 0.06 eV, lensed to lmax 2500 (+200), default kernel
   thread8      8 draws of the lmax-2500 workload, thread per mode (team 2)
   thread32     32 draws, thread per mode compiled for 2 blocks/SM (team 7), queue
                order 2 (q bands), static-stride schedule: the headline ODE
@@ -73,7 +74,13 @@ def run(name, runs=4):
         out = {"kernel_case": name, "ode_ms": ms[0], "spline_los_ms": ms[1], "cls_ms": ms[2]}
         print(json.dumps(out))
         return out
-    if name == "warp1":
+    if name == "lens1":  # one cosmology, mnu 0.06 eV, lensed to lmax 2500 (+200), the default kernel choice
+        p = _lib.default_params()
+        p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
+        p.nnu, p.mnu, p.num_massive_neutrinos = 3.046, 0.06, 1
+        p.do_lensing, p.max_l, p.max_eta_k = 1, 2700, 2.5 * 2700
+        ps, team, order, cap = [p], 0, -1, 0
+    elif name == "warp1":
         p = _lib.default_params()
         p.H0, p.ombh2, p.omch2, p.optical_depth, p.As, p.ns = 67.5, 0.022, 0.122, 0.06, 2.1e-9, 0.965
         p.nnu, p.mnu, p.num_massive_neutrinos = 3.046, 0.0, 1
