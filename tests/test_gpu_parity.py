@@ -257,3 +257,45 @@ def test_resident_batch_refuses_after_a_later_staging():
     _lib.check(lib.cambgpu_batch_prepare(arr, len(ps)))
     _lib.check(lib.cambgpu_batch_run(None))
     lib.cambgpu_batch_release()
+
+
+def test_wide_parameter_box_against_the_oracle():
+    """Twelve cosmologies far outside the benchmark's +-5% box (H0 55-80, ombh2 0.018-0.026,
+    omch2 0.09-0.15, tau 0.03-0.12, ns 0.90-1.02, nrun -0.02-0.02, N_eff 2.5-4, one massive
+    eigenstate of 0-0.5 eV or three degenerate ones), lmax 800, as one batch through
+    cambgpu_get_results_batch (FP64): C_l at the sampled l within 1e-5 of the oracle's, so
+    the switch logic, the hierarchy sizes and the massive-neutrino momentum bins hold
+    outside the draws the other tests use."""
+    rng = np.random.default_rng(77)
+    ps = []
+    for i in range(12):
+        p = fiducial(800)
+        p.H0 = rng.uniform(55, 80)
+        p.ombh2 = rng.uniform(0.018, 0.026)
+        p.omch2 = rng.uniform(0.09, 0.15)
+        p.optical_depth = rng.uniform(0.03, 0.12)
+        p.ns = rng.uniform(0.90, 1.02)
+        p.nrun = rng.uniform(-0.02, 0.02)
+        p.nnu = rng.uniform(2.5, 4.0)
+        if i % 3:
+            p.mnu = rng.uniform(0.0, 0.5)
+            p.num_massive_neutrinos = 3 if i % 3 == 2 else 1
+        ps.append(p)
+    arr = (_lib.CambGpuParams * len(ps))(*ps)
+    lib = _lib.load()
+    old = lib.cambgpu_get_precision()
+    _lib.check(lib.cambgpu_set_precision(0))
+    try:
+        cls = np.zeros((len(ps), 801, 4))
+        st = np.zeros(len(ps), dtype=np.int32)
+        _lib.check(lib.cambgpu_get_results_batch(arr, len(ps), 800, _lib.dptr(cls), _lib.iptr(st)))
+    finally:
+        lib.cambgpu_set_precision(old)
+    assert np.all(st == 0)
+    for i, p in enumerate(ps):
+        T = _lib.Tables(p)
+        icl = orc.cls(T, orc.los(T, orc.evolve_sources(T)))
+        got = cls[i][T.ls]
+        assert np.max(np.abs(got[:, 0] / icl[:, 0] - 1)) < 1e-5, i
+        assert np.max(np.abs(got[:, 1] / icl[:, 1] - 1)) < 1e-5, i
+        assert np.max(np.abs(got[:, 3] - icl[:, 2]) / np.sqrt(icl[:, 0] * icl[:, 1])) < 1e-5, i
