@@ -126,14 +126,17 @@ __global__ void __launch_bounds__(256, 1)
   uint64_t* bar = reinterpret_cast<uint64_t*>(s_a2 + kProjMaxChi);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   __shared__ int s_kbeg, s_kend;
-  // per cosmology of the tile: first shared node, valid-row end, l cut, the node of its
-  // second row (window test), lensed integration test for l <= 850, tau0
-  __shared__ int s_off[128], s_rend[128], s_llmax[128];
+  // per cosmology of the tile: first shared node, l cut, the node of its second row
+  // (window test), lensed integration test for l <= 850, tau0
+  __shared__ int s_off[128], s_llmax[128];
+  __shared__ int s_nlo[128], s_nhi[128];  // integration window of each sampled l, in shared nodes
   __shared__ double s_chi1[128], s_tau0[128];
   __shared__ unsigned char s_doint850[128];
-  // 256 threads: threads 0-127 stage the J rows (sampled l), 128-255 the S rows
-  // (cosmologies) of each tile; all eight warps read the accumulator back, warp w from
-  // tensor-memory lane quarter w % 4 and column half w / 4
+  // 256 threads: warps 0-3 stage the J rows (sampled l; warp w rows 32 w .. 32 w + 31, the
+  // lanes along the nodes, so that a warp's table gathers fall on one row), threads
+  // 128-255 the S rows (cosmologies; one thread per cosmology) of each tile; all eight
+  // warps read the accumulator back, warp w from tensor-memory lane quarter w % 4 and
+  // column half w / 4
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row = tid & 127, side = tid >> 7;
   const int ctile = blockIdx.x, src = blockIdx.y, q_ix = blockIdx.z;
@@ -167,6 +170,10 @@ __global__ void __launch_bounds__(256, 1)
     if (nlo < 0) nlo = 0;
     atomicMin(&s_kbeg, nlo);
     atomicMax(&s_kend, nhi);
+  }
+  if (side == 0) {  // rows past the sampled l keep an empty window
+    s_nlo[row] = nlo;
+    s_nhi[row] = nhi;
   }
   // the k-spline weights of q on the shared source k grid
   KW K;
@@ -205,41 +212,65 @@ __global__ void __launch_bounds__(256, 1)
     if (llmax < 15) llmax = 17;
     else llmax = (int)llrint(q * (tau0 + 6 * 3.14159265358979323846 / q));
     s_off[row] = c_off;
-    s_rend[row] = c_rend;
     s_llmax[row] = llmax;
     s_chi1[row] = c_off + 1 < nchi ? chi[c_off + 1] : -1.0;
     s_tau0[row] = tau0;
     s_doint850[row] = q < 850 * 3 * (G.AccuracyBoost * G.BessIntBoost) / tau0 * 1.2;
   }
   __syncthreads();  // the per-cosmology arrays, read by the epilogue's threads
-  const float4* __restrict__ Hrow = (side == 0 && row < nl) ? G.bessel_f32 + (size_t)row * (nbx - 1) : nullptr;
   constexpr uint32_t idesc = idesc_bf16_f32(128, 128);
   const int kbeg = (s_kbeg / kChunk) * kChunk, kend = s_kend;
   uint32_t phase = 0;
   bool ok = true, any = false;
   for (int k0 = kbeg; k0 <= kend && ok; k0 += kChunk) {
-    // J (side 0): row = sampled l, 64 nodes; S (side 1): row = cosmology, 64 nodes
-    unsigned char* const thi = side == 0 ? a_hi : b_hi;
-    unsigned char* const tlo = side == 0 ? a_lo : b_lo;
-#pragma unroll 8
-    for (int k = 0; k < kChunk; ++k) {
-      const int n = k0 + k;
-      float v = 0.0f;
-      if (side == 0) {
-        if (n < nchi && n >= nlo && n <= nhi) {
-          const float4 h = __ldg(Hrow + s_bix[n]);
-          const float a2 = s_a2[n];
-          v = (h.x + a2 * (h.y + a2 * (h.z + a2 * h.w))) * dchi_f[n];
-        }
-      } else if (has_c && n < nchi) {
-        const int i = n - c_off;
-        if (i >= 1 && i < c_rend) v = src_t(T, ncosmo, nchi, nsrc, Kf, src, n, c);
+    if (side == 0) {
+      // J: warp w fills rows 32 w .. 32 w + 31, each lane two nodes (k = lane, lane + 32);
+      // the nodes' table intervals, Horner variables and weights are the same for every row
+      int nn[2], bix[2];
+      float a2[2], dc[2];
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        nn[hh] = k0 + 32 * hh + lane;
+        const bool in = nn[hh] < nchi;
+        bix[hh] = in ? s_bix[nn[hh]] : 0;
+        a2[hh] = in ? s_a2[nn[hh]] : 0.0f;
+        dc[hh] = in ? dchi_f[nn[hh]] : 0.0f;
       }
-      __nv_bfloat16 h, l;
-      const uint32_t off = tile_offset(row, k);
-      split_bf16(v, h, l);
-      *reinterpret_cast<__nv_bfloat16*>(thi + off) = h;
-      *reinterpret_cast<__nv_bfloat16*>(tlo + off) = l;
+#pragma unroll 4
+      for (int r = 0; r < 32; ++r) {
+        const int jrow = (warp & 3) * 32 + r;
+        const int lo = s_nlo[jrow], hi = s_nhi[jrow];
+        const float4* __restrict__ H = G.bessel_f32 + (size_t)min(jrow, nl - 1) * (nbx - 1);
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          float v = 0.0f;
+          if (nn[hh] < nchi && nn[hh] >= lo && nn[hh] <= hi) {
+            const float4 h = __ldg(H + bix[hh]);
+            v = (h.x + a2[hh] * (h.y + a2[hh] * (h.z + a2[hh] * h.w))) * dc[hh];
+          }
+          __nv_bfloat16 vh, vl;
+          const uint32_t off = tile_offset(jrow, 32 * hh + lane);
+          split_bf16(v, vh, vl);
+          *reinterpret_cast<__nv_bfloat16*>(a_hi + off) = vh;
+          *reinterpret_cast<__nv_bfloat16*>(a_lo + off) = vl;
+        }
+      }
+    } else {
+      // S: row = cosmology, 64 nodes
+#pragma unroll 8
+      for (int k = 0; k < kChunk; ++k) {
+        const int n = k0 + k;
+        float v = 0.0f;
+        if (has_c && n < nchi) {
+          const int i = n - c_off;
+          if (i >= 1 && i < c_rend) v = src_t(T, ncosmo, nchi, nsrc, Kf, src, n, c);
+        }
+        __nv_bfloat16 vh, vl;
+        const uint32_t off = tile_offset(row, k);
+        split_bf16(v, vh, vl);
+        *reinterpret_cast<__nv_bfloat16*>(b_hi + off) = vh;
+        *reinterpret_cast<__nv_bfloat16*>(b_lo + off) = vl;
+      }
     }
     fence_proxy_async();
     __syncthreads();
