@@ -23,7 +23,11 @@
  *   - return 0 on success, else an error code with the meaning of config.f90:66-74
  *     (4 = error_evolution for ODE failures, 9 = allocation, 2 = unsupported params,
  *     5 = reionization, 3 = recombination);  the library never exits the process.
- *   - not thread-safe: one host thread per call, like the reference (cmbmain.f90:7-8).
+ *   - threads: every call that uses the device takes one internal lock, so host threads
+ *     may call concurrently and their device work runs one call at a time; host-table
+ *     building (cambgpu_prepare_tables, cambgpu_tables_create) runs concurrently.  The
+ *     process-wide settings (cambgpu_set_precision / _ode_*) apply to every later call of
+ *     every thread: set them before concurrent use.
  */
 #ifndef CAMBGPU_H
 #define CAMBGPU_H

@@ -299,3 +299,25 @@ def test_wide_parameter_box_against_the_oracle():
         assert np.max(np.abs(got[:, 0] / icl[:, 0] - 1)) < 1e-5, i
         assert np.max(np.abs(got[:, 1] / icl[:, 1] - 1)) < 1e-5, i
         assert np.max(np.abs(got[:, 3] - icl[:, 2]) / np.sqrt(icl[:, 0] * icl[:, 1])) < 1e-5, i
+
+
+def test_concurrent_host_threads_get_the_sequential_results():
+    """Four host threads calling cambgpu_get_spectra_batch at once (each its own batch, two
+    calls each): the host tables build in parallel, the device work serialises on the
+    library's lock, and every thread gets exactly the spectra of a sequential call."""
+    from concurrent.futures import ThreadPoolExecutor
+    lib = _lib.load()
+    batches = [draws(2, seed=400 + i, lmax=600, mnu_max=0.1 * (i % 2)) for i in range(4)]
+
+    def run(ps):
+        arr = (_lib.CambGpuParams * len(ps))(*ps)
+        cls = np.zeros((len(ps), 601, 4))
+        st = np.zeros(len(ps), dtype=np.int32)
+        _lib.check(lib.cambgpu_get_spectra_batch(arr, len(ps), 600, _lib.dptr(cls), None, None, None, _lib.iptr(st)))
+        return cls
+
+    want = [run(ps) for ps in batches]
+    with ThreadPoolExecutor(4) as ex:
+        got = list(ex.map(run, batches + batches))
+    for i, g in enumerate(got):
+        assert np.array_equal(g, want[i % 4]), i
