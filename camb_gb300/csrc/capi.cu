@@ -25,7 +25,7 @@ cudaError_t launch_ode_kernel(int team, int blocks, int threads, cudaStream_t s,
                               const WorkItem* items, int nitems, int* counter, bool transfer, int warp_stride);
 cudaError_t launch_sigma8(const DevCosmo* cosmos, int n, cudaStream_t s);
 cudaError_t launch_fp64_probe(int blocks, int threads, int iters, double* out, cudaStream_t s);
-cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, int nk, const double* chi,
+cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, int nk, int nl, const double* chi,
                            const float* dchi_f, int nchi, float2* tsrc, int* err, cudaStream_t s);
 cudaError_t launch_fp64_pipe_probe(int nsm, int warps, int lanes, int chains, int iters, long long* cyc, double* out,
                                    cudaStream_t s);
@@ -878,7 +878,7 @@ int run_los(Batch& B) {
     source_spline_kernel<<<g1, 128, 0, g_rt.stream>>>(B.d_cosmos, B.d_spl);
     g_launches++;
     CUDA_TRY(cudaMemsetAsync(B.d_tc_err, 0, sizeof(int), g_rt.stream));
-    CUDA_TRY(launch_proj_tc(B.d_cosmos, n, B.max_nq, B.views[0]->nsrc, B.views[0]->nk, B.d_chi, B.d_dchi_f,
+    CUDA_TRY(launch_proj_tc(B.d_cosmos, n, B.max_nq, B.views[0]->nsrc, B.views[0]->nk, B.views[0]->nl, B.d_chi, B.d_dchi_f,
                             (int)B.h_chi.size(), B.d_tsrc, B.d_tc_err, g_rt.stream));
     g_launches += 2;
     return 0;
@@ -1630,7 +1630,6 @@ static int share_grids(const std::vector<Handle*>& hs, cg::SharedGrid& sg) {
                      "shared grids need CMB runs with one l sampling, one set of sources and one accuracy");
     cs.push_back(&h->c);
   }
-  if (c0.ls.size() > 128) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "shared grids: at most 128 sampled l");
   std::string err;
   int rc = cg::build_shared_grid(cs, sg, err);
   if (rc) return set_err(rc, err);

@@ -6,7 +6,8 @@
 // chi_n) and one integration q grid, the projection of source s at wavenumber q is
 //     Delta_s[l][c] = sum_n J_q[l][n] S_q,s[n][c],   J_q[l][n] = j_l(q chi_n) dchi_n,
 // one Bessel matrix per q for the whole batch.  One CTA of eight warps computes a 128
-// (sampled l) x 128 (cosmologies) tile of one (q, source): it stages 64-deep K tiles of J (from the FP32 Horner
+// (sampled l) x 128 (cosmologies) tile of one (q, source), l tiles and cosmology tiles
+// along the grid's x: it stages 64-deep K tiles of J (from the FP32 Horner
 // table, zero outside each l's integration window) and of S (the source k-spline of each
 // cosmology evaluated at q, zero outside the cosmology's time range and its q*tau < max_etak
 // prefix), split into BF16 pairs, in shared memory; one thread issues the twelve
@@ -139,7 +140,10 @@ __global__ void __launch_bounds__(256, 1)
   // column half w / 4
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row = tid & 127, side = tid >> 7;
-  const int ctile = blockIdx.x, src = blockIdx.y, q_ix = blockIdx.z;
+  // blockIdx.x = (tile of 128 sampled l) x (tile of 128 cosmologies)
+  const int ctiles = (ncosmo + 127) / 128;
+  const int ctile = blockIdx.x % ctiles, l0 = (blockIdx.x / ctiles) * 128;
+  const int src = blockIdx.y, q_ix = blockIdx.z;
   const DevCosmo& G = cosmos[0];  // shared grids: q, k, l sampling, Bessel table
   const double q = G.q_int[q_ix];
   const int nl = G.nl, nbx = G.num_xx, nsrc = G.nsrc;
@@ -162,8 +166,8 @@ __global__ void __launch_bounds__(256, 1)
   // node with chi >= 80 l BessIntBoost / q through the last node with chi >= xlim / q
   const double bib = G.AccuracyBoost * G.BessIntBoost;
   int nlo = nchi, nhi = -1;
-  if (side == 0 && row < nl) {
-    const int l = G.ls[row];
+  if (side == 0 && l0 + row < nl) {
+    const int l = G.ls[l0 + row];
     const double xlim = fmax(0.0, l - 4.2 * cbrt((double)l));
     nlo = count_ge(chi, nchi, 80.0 * l * bib / q) - 1;
     nhi = count_ge(chi, nchi, xlim / q) - 1;
@@ -240,7 +244,7 @@ __global__ void __launch_bounds__(256, 1)
       for (int r = 0; r < 32; ++r) {
         const int jrow = (warp & 3) * 32 + r;
         const int lo = s_nlo[jrow], hi = s_nhi[jrow];
-        const float4* __restrict__ H = G.bessel_f32 + (size_t)min(jrow, nl - 1) * (nbx - 1);
+        const float4* __restrict__ H = G.bessel_f32 + (size_t)min(l0 + jrow, nl - 1) * (nbx - 1);
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
           float v = 0.0f;
@@ -298,9 +302,9 @@ __global__ void __launch_bounds__(256, 1)
     mbar_wait(bar, phase ^ 1, 1LL << 26);
   } else {
     fence_after_sync();
-    // epilogue: thread (warp w, lane) holds sampled l j = 32 (w % 4) + lane for the 64
+    // epilogue: thread (warp w, lane) holds sampled l j = l0 + 32 (w % 4) + lane for the 64
     // cosmology columns of half w / 4, 32 at a time
-    const int j = (warp & 3) * 32 + lane;
+    const int j = l0 + (warp & 3) * 32 + lane;
     const bool has_j = j < nl;
     const int l = has_j ? G.ls[j] : 0;
     const double limber_l = 400 * sqrt(G.AccuracyBoost * G.LimberBoost);
@@ -353,7 +357,7 @@ __global__ void __launch_bounds__(256, 1)
 
 }  // namespace tc
 
-cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, int nk, const double* chi,
+cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc, int nk, int nl, const double* chi,
                            const float* dchi_f, int nchi, float2* tsrc, int* err, cudaStream_t s) {
   static const bool attr = [] {
     cudaFuncSetAttribute(tc::proj_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kProjSmem);
@@ -364,7 +368,7 @@ cudaError_t launch_proj_tc(const DevCosmo* cosmos, int ncosmo, int nq, int nsrc,
   if (nchi > tc::kProjMaxChi) return cudaErrorInvalidValue;
   dim3 gt((nk + 31) / 32, (ncosmo + 31) / 32, nchi * nsrc);
   tc::proj_src_transpose_kernel<<<gt, dim3(32, 8), 0, s>>>(cosmos, ncosmo, nchi, nk, nsrc, tsrc);
-  dim3 grid((ncosmo + 127) / 128, nsrc, nq);
+  dim3 grid(((ncosmo + 127) / 128) * ((nl + 127) / 128), nsrc, nq);
   tc::proj_tc_kernel<<<grid, 256, tc::kProjSmem, s>>>(cosmos, ncosmo, chi, dchi_f, nchi, tsrc, err);
   return cudaGetLastError();
 }

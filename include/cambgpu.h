@@ -267,7 +267,7 @@ int cambgpu_batch_prepare(const CambGpuParams* p, int n);
  * chi the finest native time spacing of any member; the source k grid, integration q grid
  * and Bessel table of the member with the median tau0.  Needed by the tensor-core
  * projection (cambgpu_set_precision(2)); the FP64 and mixed forms run on it too, so the
- * projections compare on the same grids.  CMB runs of one l sampling (at most 128 sampled l)
+ * projections compare on the same grids.  CMB runs of one l sampling
  * and one set of sources; nchi_out (optional) receives the number of shared nodes. */
 int cambgpu_batch_prepare_shared(const CambGpuParams* p, int n, int* nchi_out);
 /* The shared grids of cambgpu_batch_prepare_shared applied to n existing table handles of

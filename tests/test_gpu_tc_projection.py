@@ -114,3 +114,20 @@ def test_public_shared_grid_api_tensor_against_fp64_and_native_grids():
         gp, rp = g.get_lens_potential_cls(2000, raw_cl=True)[2:], r.get_lens_potential_cls(2000, raw_cl=True)[2:]
         assert rel(gp[:, 0], rp[:, 0]) < 1e-4
     assert _lib.load().cambgpu_get_precision() == before  # the caller's precision is restored
+
+
+def test_tensor_projection_with_two_l_tiles():
+    """lSampleBoost 2 at lmax 2500 (+200, lensed) samples 155 l, more than one 128-row tile
+    of the tensor-core product: the l tiles run side by side in the grid, and TT, EE, BB
+    and phi-phi stay within 1e-4 of the FP64 projection on the same shared grids."""
+    ps = batch_draws(3, 2500, seed=31)
+    for p in ps:
+        p.do_lensing, p.max_l, p.max_eta_k = 1, 2700, 2.5 * 2700
+        p.lSampleBoost = 2.0
+    out, _ = run_shared(ps, (0, 2), 2700, lensed=True)
+    (_, ref_l, ref_p, lml), (_, got_l, got_p, _) = out[0], out[2]
+    assert _lib.Tables(ps[0]).view.nl > 128
+    L = int(lml.min())
+    for c in range(3):
+        assert rel(got_l[:, 2:L, c], ref_l[:, 2:L, c]) < 1e-4, c
+    assert rel(got_p[:, 2:2501, 0], ref_p[:, 2:2501, 0]) < 1e-4
