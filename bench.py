@@ -401,8 +401,10 @@ def single_configs(nthreads):
     """One cosmology per configuration of the benchmark suite, GPU (C ABI, host buffers)
     against the CPU restatement on the host cores, both with their host tables: the
     plain massless lmax 1000 case; one 0.06 eV neutrino with lensed TT/EE/BB/TE and the
-    lensing potential to lmax 2500; and that cosmology's matter transfer functions to
-    kmax = 10 h/Mpc at z = 0 (computed without the CMB)."""
+    lensing potential to lmax 2500, at max_eta_k = 2.5 (lmax + 200) and at the reference's
+    automatic lens_potential_accuracy 4 (max_eta_k = 72000, linear lensing); and that
+    cosmology's matter transfer functions to kmax = 10 h/Mpc at z = 0 (computed without the
+    CMB)."""
     from camb_gb300 import _lib
     from oracle import oracle as orc
     lib = _lib.load()
@@ -465,8 +467,11 @@ def single_configs(nthreads):
         return (time.perf_counter() - t0) / reps * 1e3, r
 
     out = {}
+    lpa4 = base(2500, True, 0.06)
+    lpa4.max_eta_k = 72000.0  # the reference's automatic lens_potential_accuracy 4 at lmax 2500
     for name, p in [("lmax1000_unlensed_massless", base(1000, False, 0.0)),
-                    ("lmax2500_lensed_mnu0.06", base(2500, True, 0.06))]:
+                    ("lmax2500_lensed_mnu0.06", base(2500, True, 0.06)),
+                    ("lmax2500_lensed_mnu0.06_max_eta_k72000", lpa4)]:
         g, _ = timed(gpu_cmb, p)
         c, _ = timed(cpu_cmb, p, reps=1)
         out[name] = {"gpu_ms": g, "cpu_ms": c, "cpu_threads": nthreads}

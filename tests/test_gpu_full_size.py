@@ -80,3 +80,21 @@ def test_transfer_kmax10():
     peak = np.max(np.abs(ref), axis=1, keepdims=True)
     assert np.max(np.abs(got - ref) / np.where(peak > 0, peak, 1)) < 1e-5
     assert abs(s8[0] / rs8[0] - 1) < 1e-9
+
+
+def test_lensed_massive_lmax2500_lens_potential_accuracy_4():
+    """The same cosmology at the reference's automatic lens_potential_accuracy for lmax 2500
+    (4: max_eta_k = 72000, so source modes to k ~ 5 /Mpc and Bessel arguments to 72000;
+    linear lensing): sources of the highest-k modes and the C_l against the oracle."""
+    p = fiducial(2500, lensing=True, mnu=0.06, num_massive_neutrinos=1)
+    p.max_eta_k = 72000.0
+    T, allc, lensed = oracle_spectra(p)
+    assert T.view.nk > 250 and T.view.num_xx > 100000
+    src = orc.evolve_sources(T)
+    g = T.evolve_sources_gpu()
+    assert rel_peak(g[..., -40:], src[..., -40:], axis=0) < 1e-6  # the 40 highest-k modes
+    unl, lens, pot, lml = gpu_spectra([p], p.max_l)
+    n = lensed.shape[0] - 1
+    assert lml[0] == n
+    check4(unl[0], as_tebt(allc), 2, p.max_l, bb=False)
+    check4(lens[0], lensed, 2, n)
