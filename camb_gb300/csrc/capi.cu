@@ -810,6 +810,8 @@ int pick_team(const Batch& B) {
   // the register-resident warp kernels (8/16/32 lanes) evolve the massless-neutrino CMB
   // layout only; the shared-memory warp kernel (6) any layout up to kWarpStrideMax entries
   if ((B.massive_nu || B.transfer) && t >= 8) t = 6;
+  // the register warp kernels hold at most 128 packed variables (higher lAccuracyBoost)
+  if (t >= 8 && B.warp_stride > 128) t = 6;
   if (B.transfer && t > 3 && t != 6) t = 2;
   if (t == 6 && B.warp_stride > kWarpStrideMax) t = 2;
   return t;

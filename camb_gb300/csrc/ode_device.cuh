@@ -808,7 +808,7 @@ constexpr int NV = 448;  // largest packed scalar system handled (mode_init reje
 // k1..k5; k6 takes k2's row (k2 is dead once the stage-6 input is formed, b2 = e2 = 0) and
 // k7 takes k4's (dead once the fifth-order solution and the error combination are formed).
 constexpr int kRows = 7;
-constexpr int NL = 66;
+constexpr int NL = 256;  // multipoles of any hierarchy: l < 256 (lAccuracyBoost up to ~3.9)
 constexpr int NUE = 3;
 
 // l-only factors of the multipole recurrences (initial(), equations.f90:1911-1916):
@@ -1570,7 +1570,7 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
   R.active = true;
   R.status = 0;
   const int lm = max(max(M.lmaxg, M.lmaxgpol), max(M.lmaxnr, M.lmaxnu));
-  if (M.nvar > row_cap(Wk) || lm >= NL || M.lmaxgpol >= 20 || C.nu_eig > NUE || C.nqmax > NQ) {
+  if (M.nvar > row_cap(Wk) || lm >= NL || C.nu_eig > NUE || C.nqmax > NQ) {
     R.active = false;
     R.status = CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
     return;

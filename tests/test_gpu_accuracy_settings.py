@@ -18,6 +18,7 @@ pytestmark = pytest.mark.gpu
 SETTINGS = {
     "AccuracyBoost 2": dict(AccuracyBoost=2.0),
     "lAccuracyBoost 2, lSampleBoost 2": dict(lAccuracyBoost=2.0, lSampleBoost=2.0),
+    "lAccuracyBoost 3 (photon hierarchy to l = 192)": dict(lAccuracyBoost=3.0),
     "k and time sampling boosts 1.5": dict(SourcekAccuracyBoost=1.5, IntkAccuracyBoost=1.5, TimeStepBoost=1.5),
     "tolerance, switch, Bessel, Limber boosts": dict(IntTolBoost=2.0, TimeSwitchBoost=1.5, BessIntBoost=1.5,
                                                      LimberBoost=1.5),
@@ -52,3 +53,28 @@ def test_setting_against_the_oracle(name):
     ell = np.arange(2, p.max_l + 1, dtype=np.float64)
     pp = allc[2:, 3] * ((ell + 1) / ell) ** 2 / (2 * np.pi)  # the output's (L(L+1))^2 C_L/2pi
     assert np.max(np.abs(pot[0][2:, 0] / pp - 1)) < 1e-5
+
+
+def test_raised_l_accuracy_on_the_thread_per_mode_kernel():
+    """A batch at lAccuracyBoost 1.5 (photon hierarchies to l = 96) on the thread-per-mode
+    kernel of large batches (team 7, static stride): C_l of three members against the
+    oracle within 1e-5."""
+    from tests.cosmologies import draws
+    ps = draws(6, seed=55, lmax=1000, mnu_max=0.1)
+    for p in ps:
+        p.lAccuracyBoost = 1.5
+    lib = _lib.load()
+    _lib.check(lib.cambgpu_set_ode_team(7))
+    _lib.check(lib.cambgpu_set_ode_schedule(1))
+    try:
+        unl, _, _, _ = gpu_spectra(ps, 1000)
+    finally:
+        lib.cambgpu_set_ode_team(0)
+        lib.cambgpu_set_ode_schedule(-1)
+    for i in (0, 2, 5):
+        T = _lib.Tables(ps[i])
+        icl = orc.cls(T, orc.los(T, orc.evolve_sources(T)))
+        got = unl[i][T.ls]
+        assert np.max(np.abs(got[:, 0] / icl[:, 0] - 1)) < 1e-5
+        assert np.max(np.abs(got[:, 1] / icl[:, 1] - 1)) < 1e-5
+        assert np.max(np.abs(got[:, 3] - icl[:, 2]) / np.sqrt(icl[:, 0] * icl[:, 1])) < 1e-5
