@@ -116,6 +116,28 @@ class CAMBparams:
             self.Reion.optical_depth = tau
         return self
 
+    def set_accuracy(self, AccuracyBoost=1.0, lSampleBoost=1.0, lAccuracyBoost=1.0, DoLateRadTruncation=True,
+                     min_l_logl_sampling=None):
+        """model.py set_accuracy: the overall accuracy knobs (Accuracy.AccuracyBoost,
+        lSampleBoost, lAccuracyBoost).  The late radiation truncation is always on in this
+        path and the log-l sampling threshold keeps its default."""
+        if not DoLateRadTruncation:
+            raise CAMBError("DoLateRadTruncation = False is not part of the GPU path")
+        if min_l_logl_sampling:
+            raise CAMBError("min_l_logl_sampling is not part of the GPU path")
+        self.Accuracy.AccuracyBoost = AccuracyBoost
+        self.Accuracy.lSampleBoost = lSampleBoost
+        self.Accuracy.lAccuracyBoost = lAccuracyBoost
+        return self
+
+    def set_dark_energy(self, w=-1.0, cs2=1.0, wa=0, use_tabulated_w=False, wde_a_array=None, wde_w_array=None,
+                        dark_energy_model="fluid"):
+        """model.py set_dark_energy: only the cosmological constant (w = -1, wa = 0) is part
+        of this path, the reference's default; any other equation of state raises."""
+        if w != -1.0 or wa != 0 or use_tabulated_w or dark_energy_model not in ("fluid", "ppf"):
+            raise CAMBError("only a cosmological constant (w = -1, wa = 0) is part of the GPU path")
+        return self
+
     def set_for_lmax(self, lmax, max_eta_k=None, lens_potential_accuracy=0, lens_output_margin=200,
                      k_eta_fac=2.5, lens_k_eta_reference=18000.0):
         """model.py:1018-1063 (the non-linear lensing switch is out of scope)."""
@@ -187,9 +209,27 @@ def set_params(cp=None, lmax=None, H0=None, ombh2=0.022, omch2=0.12, omk=0.0, mn
     cp.InitPower.set_params(As=As, ns=ns, nrun=nrun, pivot_scalar=pivot_scalar)
     if lmax is not None:
         cp.set_for_lmax(lmax, max_eta_k=max_eta_k, lens_potential_accuracy=lens_potential_accuracy)
+    # the remaining keywords as camb.set_params routes them (camb.py:200-238): the accuracy
+    # and dark-energy setters, then attributes (dotted names reach sub-objects), and an
+    # error for a name that is none of these
+    de = {k: kwargs.pop(k) for k in ("w", "wa", "cs2", "use_tabulated_w", "wde_a_array", "wde_w_array",
+                                     "dark_energy_model") if k in kwargs}
+    if de:
+        cp.set_dark_energy(**de)
+    acc = {k: kwargs.pop(k) for k in ("AccuracyBoost", "lSampleBoost", "lAccuracyBoost", "DoLateRadTruncation",
+                                      "min_l_logl_sampling") if k in kwargs}
+    if acc:
+        cp.set_accuracy(**{**dict(AccuracyBoost=cp.Accuracy.AccuracyBoost, lSampleBoost=cp.Accuracy.lSampleBoost,
+                                  lAccuracyBoost=cp.Accuracy.lAccuracyBoost), **acc})
     for k, v in kwargs.items():
-        if hasattr(cp.Accuracy, k):
-            setattr(cp.Accuracy, k, v)
-        else:
-            setattr(cp, k, v)
+        obj, name = cp, k
+        if "." in k:
+            *path, name = k.split(".")
+            for part in path:
+                obj = getattr(obj, part)
+        elif hasattr(cp.Accuracy, k):
+            obj = cp.Accuracy
+        if not hasattr(obj, name):
+            raise CAMBError(f"Unrecognized parameter: {k}")
+        setattr(obj, name, v)
     return cp

@@ -67,3 +67,32 @@ def test_shared_grid_api_checks_its_arguments_before_any_device_call():
     t.WantTransfer = True
     with pytest.raises(model.CAMBError):
         results.get_results_batch_shared([t])
+
+
+def test_set_accuracy_and_dark_energy_follow_the_reference():
+    """set_accuracy sets the three overall knobs (model.py set_accuracy); set_dark_energy()
+    with its defaults is accepted (the reference's cosmological constant) and any other
+    equation of state raises, as do the accuracy options this path does not build."""
+    p = model.set_params(lmax=100)
+    assert p.set_accuracy(AccuracyBoost=2, lSampleBoost=1.5, lAccuracyBoost=3) is p
+    assert (p.Accuracy.AccuracyBoost, p.Accuracy.lSampleBoost, p.Accuracy.lAccuracyBoost) == (2, 1.5, 3)
+    s = p.to_struct()
+    assert (s.AccuracyBoost, s.lSampleBoost, s.lAccuracyBoost) == (2, 1.5, 3)
+    assert p.set_dark_energy() is p
+    for bad in (dict(w=-0.9), dict(wa=0.1), dict(use_tabulated_w=True)):
+        with pytest.raises(model.CAMBError):
+            p.set_dark_energy(**bad)
+    with pytest.raises(model.CAMBError):
+        p.set_accuracy(DoLateRadTruncation=False)
+
+
+def test_set_params_routes_keywords_like_the_reference():
+    """camb.set_params routing (camb.py:200-238): accuracy and dark-energy keywords go to
+    their setters, dotted names reach sub-objects, and an unknown name raises instead of
+    being stored and ignored."""
+    p = model.set_params(lmax=100, AccuracyBoost=1.5, w=-1.0, **{"Accuracy.IntTolBoost": 2.0})
+    assert p.Accuracy.AccuracyBoost == 1.5 and p.Accuracy.IntTolBoost == 2.0
+    with pytest.raises(model.CAMBError):
+        model.set_params(lmax=100, w=-0.9)
+    with pytest.raises(model.CAMBError):
+        model.set_params(lmax=100, not_a_parameter=1)
