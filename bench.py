@@ -152,7 +152,22 @@ def gradient_rate(n=64, lmax=2500, seed=3000, mnu_max=0.2):
                                    "re-evolved (+-1e-4 relative, 9 cosmologies per gradient in one launch, FP64 "
                                    "projection); As, ns by reweighting the resident transfer functions"}
     out.update(gradient_checks(ps[:2], g[:2]))
+    out["cpu"] = cpu_gradient_rate(ps[:4])
     return out
+
+
+def cpu_gradient_rate(ps):
+    """The same central differences on the host cores: each gradient's 9 members (the
+    draw and +-1e-4 in ombh2, omch2, H0, tau) through the CPU restatement, one cosmology
+    per thread, host tables included (As and ns come from reweighting and cost nothing)."""
+    from camb_gb300 import gradients
+    members, _ = gradients.fd_members(ps, 1e-4)
+    nth = os.cpu_count() or 1
+    structs = [m.to_struct() for m in members]
+    cpu_reference_batch(structs[:nth], nth)
+    t = cpu_reference_batch(structs, nth)
+    return {"value": len(ps) / t, "unit": "gradients/s", "cores": nth,
+            "sample": f"{len(ps)} gradients ({len(structs)} cosmologies), one cosmology per thread"}
 
 
 def gradient_checks(ps, g):
@@ -258,6 +273,13 @@ def lensed_batch(n, lmax=2500, seed=5000, mnu_max=0.2):
 
     names = {0: "fp64", 1: "mixed_fp32", 2: "tensor_bf16x3"}
     stage = {names[k]: {"ode": v[0], "spline_los": v[1], "cls_interp_lens": v[2]} for k, v in ms_sh.items()}
+    # the CPU restatement on the first draws, each on its own grids, one cosmology per thread
+    nth = os.cpu_count() or 1
+    sample = ps[:2 * nth]
+    t_cpu = cpu_reference_batch(sample, nth, lensed=True)
+    cpu = {"value": len(sample) / t_cpu, "unit": "cosmologies/s", "cores": nth,
+           "sample": f"the batch's first {len(sample)} draws on their own grids, one cosmology per thread, host "
+                     f"tables + ODE + LOS + C_l + interpolation + lensing"}
     return {"config": {"workload": f"{n} seeded draws (fiducial LCDM +-5%, mnu 0-{mnu_max:g} eV), lensed "
                                    f"TT/EE/BB/TE and phi-phi to lmax={lmax} (+200 margin), on grids shared by "
                                    f"the batch ({nchi} comoving-distance nodes)", "batch": n},
@@ -265,6 +287,7 @@ def lensed_batch(n, lmax=2500, seed=5000, mnu_max=0.2):
             "stage_ms_native_grids_fp64": {"ode": ms_nat[0][0], "spline_los": ms_nat[0][1],
                                            "cls_interp_lens": ms_nat[0][2]},
             "cosmologies_per_s": {names[k]: n / (sum(v) * 1e-3) for k, v in ms_sh.items()},
+            "cpu_baseline": cpu,
             "projection_ms": {names[k]: v[1] for k, v in ms_sh.items()},
             "tensor_vs_fp64_same_grids_per_l_band": band_err(sh[2], sh[0]),
             "mixed_vs_fp64_same_grids_per_l_band": band_err(sh[1], sh[0]),
@@ -334,10 +357,11 @@ def cpu_reference(params, nthreads, keep=None):
     return time.perf_counter() - t0
 
 
-def cpu_reference_batch(params, nthreads):
+def cpu_reference_batch(params, nthreads, lensed=False):
     """The same CPU path with the cosmologies spread over the host threads, each
     cosmology on one thread (the batch-parallel form, beside the reference's own
-    OpenMP-over-k parallelism of cpu_reference).  The ctypes calls release the GIL."""
+    OpenMP-over-k parallelism of cpu_reference).  The ctypes calls release the GIL.  With
+    lensed=True also the interpolation to every l and the lensing of the C_l."""
     from concurrent.futures import ThreadPoolExecutor
     from camb_gb300 import _lib
     from oracle import oracle as orc
@@ -345,7 +369,10 @@ def cpu_reference_batch(params, nthreads):
 
     def one(p):
         T = _lib.Tables(p)
-        orc.cls(T, orc.los(T, orc.evolve_sources(T, 1), 1))
+        icl = orc.cls(T, orc.los(T, orc.evolve_sources(T, 1), 1))
+        if lensed:
+            allc = orc.interpolate_cls(T.ls, icl, T.view.cl_template_scale)
+            orc.lens_cls(allc[:, :4], T.ls, p.max_l, lens_accuracy_boost=T.view.lens_accuracy_boost)
 
     t0 = time.perf_counter()
     with ThreadPoolExecutor(nthreads) as ex:
@@ -697,6 +724,7 @@ def main():
         lb = lensed_batch(256, args.lmax, mnu_max=args.mnu_max)
         line["shared_grid_projections_lensed_256"] = {
             "projection_ms": lb["projection_ms"], "cosmologies_per_s": lb["cosmologies_per_s"],
+            "cpu_baseline": lb["cpu_baseline"],
             "tensor_vs_fp64_same_grids_max": {k: max(b[k] for b in lb["tensor_vs_fp64_same_grids_per_l_band"].values())
                                                for k in ("TT", "EE", "BB", "TE_over_sqrt_TTEE", "PP")},
             "shared_vs_native_grids_fp64_max": {k: max(b[k] for b in
