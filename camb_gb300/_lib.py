@@ -38,6 +38,7 @@ class CambGpuParams(C.Structure):
         ("want_cls", C.c_int), ("want_transfer", C.c_int), ("transfer_high_precision", C.c_int),
         ("transfer_kmax", C.c_double), ("num_transfer_redshifts", C.c_int), ("transfer_redshifts", C.c_double * 256),
         ("reion_use_optical_depth", C.c_int), ("reion_redshift", C.c_double),
+        ("recfast_no_rosenbrock", C.c_int),
     ]
 
 

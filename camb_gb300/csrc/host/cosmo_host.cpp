@@ -380,8 +380,10 @@ static void escape_prob(double tau, double& p) {
   else p = (1 - std::exp(-tau)) / tau;
 }
 
-// ION right-hand side in redshift: y = (x_H, x_He, a*T_mat)
-static void recfast_rhs(const RecfastCtx& ctx, double z, const double* y, double* f) {
+// ION right-hand side in redshift: y = (x_H, x_He, a*T_mat).  full_h: the full Peebles
+// hydrogen equation at every x_H (the smooth system of the Rosenbrock phase), instead of
+// the Saha hold above x_H = 0.99 and the Saha-rate derivative above 0.985.
+static void recfast_rhs(const RecfastCtx& ctx, double z, const double* y, double* f, bool full_h = false) {
   using namespace rf;
   const Recfast& R = *ctx.r;
   double x_H = y[0], x_He = y[1];
@@ -458,8 +460,8 @@ static void recfast_rhs(const RecfastCtx& ctx, double z, const double* y, double
   double timeH = 2.0 / (3.0 * R.HO * ainv * std::sqrt(ainv));
   double RupE = Rup * std::exp(-CL * inv_Tmat);
   double A_H = x * x_H * n * Rdown - RupE * (1.0 - x_H);
-  if (x_H > 0.99) f[0] = 0;
-  else if (x_H > 0.985) f[0] = A_H / denH;
+  if (!full_h && x_H > 0.99) f[0] = 0;
+  else if (!full_h && x_H > 0.985) f[0] = A_H / denH;
   else {
     double B_H = 1.0 + Kf * Lambda * n * (1.0 - x_H);
     double C_H = 1.0 / R.fu + Kf * Lambda * n * (1.0 - x_H) / R.fu + Kf * Rup * n * (1.0 - x_H);
@@ -572,6 +574,151 @@ static int dp45_host(F&& fcn, int n, double& x, double* y, double xend, DP45Host
   return -1;
 }
 
+// The stiff early phase of hydrogen recombination (TRecfast_init with use_rosenbrock,
+// recfast.f90:739-760): from the end of the helium Saha phase until x_H falls to 0.976 the
+// full smooth H/He/T_m system is integrated with ROS2, the two-stage L-stable Rosenbrock
+// method of Verwer, Spee, Blom and Hundsdorfer (1999; gamma = 1 + 1/sqrt 2), embedded
+// error (k1 + k2)/(2 gamma), with the step control of RecfastRosenbrockAdvance
+// (:1072-1155) and RecfastROS2Step (:1031-1070).  The Jacobian is formed by central
+// differences of the right-hand side (the reference differentiates it analytically).
+namespace ros2 {
+const double gamma = 1.0 + 1.0 / std::sqrt(2.0);
+const double a21 = 1.0 / gamma, c21 = -2.0 / gamma, m1 = 3.0 / (2.0 * gamma), m2 = 1.0 / (2.0 * gamma);
+const double safety = 0.9, min_scale = 0.2, max_scale = 2.5;
+const double ion_scale_floor = 1e-3;  // ionization fractions on a smaller absolute scale than a*T_m
+const double tol = 3e-4, handoff_xH = 0.976;
+const int max_steps = 4096;
+
+// LU with partial pivoting of a 3x3 matrix, in place; false when singular
+bool lu3(double a[3][3], int piv[3]) {
+  for (int k = 0; k < 3; ++k) {
+    int p = k;
+    for (int i = k + 1; i < 3; ++i)
+      if (std::fabs(a[i][k]) > std::fabs(a[p][k])) p = i;
+    piv[k] = p;
+    if (!(std::fabs(a[p][k]) > 0) || !std::isfinite(a[p][k])) return false;
+    if (p != k)
+      for (int j = 0; j < 3; ++j) std::swap(a[k][j], a[p][j]);
+    for (int i = k + 1; i < 3; ++i) {
+      a[i][k] /= a[k][k];
+      for (int j = k + 1; j < 3; ++j) a[i][j] -= a[i][k] * a[k][j];
+    }
+  }
+  return true;
+}
+
+void lu3_solve(const double a[3][3], const int piv[3], const double* b, double* x) {
+  double y[3] = {b[0], b[1], b[2]};
+  for (int k = 0; k < 3; ++k) {
+    std::swap(y[k], y[piv[k]]);
+    for (int i = k + 1; i < 3; ++i) y[i] -= a[i][k] * y[k];
+  }
+  for (int k = 2; k >= 0; --k) {
+    double t = y[k];
+    for (int j = k + 1; j < 3; ++j) t -= a[k][j] * x[j];
+    x[k] = t / a[k][k];
+  }
+}
+
+bool state_ok(const double* y) {
+  for (int i = 0; i < 3; ++i)
+    if (!std::isfinite(y[i])) return false;
+  return std::min(y[0], y[1]) >= -1e-8 && y[2] > 0;
+}
+
+// f, the Jacobian d f / d y and the one-sided z derivative f_t of the full system at (z, y)
+void derivs(const RecfastCtx& ctx, double z, const double* y, double h, double* f, double J[3][3], double* f_t) {
+  recfast_rhs(ctx, z, y, f, true);
+  for (int j = 0; j < 3; ++j) {
+    const double d = 1e-7 * std::max(std::fabs(y[j]), j < 2 ? 1e-6 : 1.0);
+    double yp[3] = {y[0], y[1], y[2]}, ym[3] = {y[0], y[1], y[2]}, fp[3], fm[3];
+    yp[j] += d;
+    ym[j] -= d;
+    recfast_rhs(ctx, z, yp, fp, true);
+    recfast_rhs(ctx, z, ym, fm, true);
+    for (int i = 0; i < 3; ++i) J[i][j] = (fp[i] - fm[i]) / (2 * d);
+  }
+  // EvaluateRecfastODETimeDerivative (recfast.f90:1002-1029)
+  double dz = std::min(0.05, std::max(1e-4, 1e-5 * std::max(1.0, std::fabs(z))));
+  if (std::fabs(h) > 0) dz = std::max(std::min(dz, 0.5 * std::fabs(h)), 1e-8 * std::max(1.0, std::fabs(z)));
+  double zp = std::max(rf::zfinal, std::min(rf::zinitial, z + std::copysign(dz, h)));
+  if (zp == z) zp = std::max(rf::zfinal, std::min(rf::zinitial, z - std::copysign(dz, h)));
+  if (zp != z) {
+    double fz[3];
+    recfast_rhs(ctx, zp, y, fz, true);
+    for (int i = 0; i < 3; ++i) f_t[i] = (fz[i] - f[i]) / (zp - z);
+  } else {
+    f_t[0] = f_t[1] = f_t[2] = 0;
+  }
+}
+
+bool step(const RecfastCtx& ctx, double z, const double* y, double h, const double* f, const double* f_t,
+          const double J[3][3], double* yout, double* yerr) {
+  double m[3][3];
+  int piv[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) m[i][j] = (i == j ? 1.0 : 0.0) - gamma * h * J[i][j];
+  if (!lu3(m, piv)) return false;
+  const double gh = gamma * h, gh2 = gh * gh;
+  double rhs[3], k1[3], k2[3], ys[3], fs[3];
+  for (int i = 0; i < 3; ++i) rhs[i] = gh * f[i] + gh2 * f_t[i];
+  lu3_solve(m, piv, rhs, k1);
+  for (int i = 0; i < 3; ++i) ys[i] = y[i] + a21 * k1[i];
+  recfast_rhs(ctx, z + h, ys, fs, true);
+  for (int i = 0; i < 3; ++i) rhs[i] = gh * fs[i] + gamma * c21 * k1[i] - gh2 * f_t[i];
+  lu3_solve(m, piv, rhs, k2);
+  for (int i = 0; i < 3; ++i) {
+    yout[i] = y[i] + m1 * k1[i] + m2 * k2[i];
+    yerr[i] = (k1[i] + k2[i]) / (2 * gamma);
+    if (!std::isfinite(yerr[i])) return false;
+  }
+  return state_ok(yout);
+}
+
+bool advance(const RecfastCtx& ctx, double zstart, double* y, double zend, double tol) {
+  if (zend == zstart) return true;
+  const double dir = zend > zstart ? 1.0 : -1.0;
+  double z = zstart, h = zend - zstart;
+  const double min_step = std::max(std::fabs(h) * 1e-8, 1e-10);
+  double f[3], f_t[3], J[3][3];
+  bool need = true;
+  for (int attempt = 0; attempt < max_steps; ++attempt) {
+    if (dir * (zend - z) <= 0) return true;
+    if (dir * (zend - (z + h)) < 0) h = zend - z;
+    if (need) {  // f, J and f_t depend on (z, y) only: reused across retries
+      derivs(ctx, z, y, h, f, J, f_t);
+      need = false;
+    }
+    double yt[3], ye[3], err = 0;
+    bool ok = step(ctx, z, y, h, f, f_t, J, yt, ye);
+    if (ok) {
+      for (int i = 0; i < 3; ++i) {
+        const double sc = i < 2 ? std::max({ion_scale_floor, std::fabs(y[i]), std::fabs(yt[i])})
+                                : std::max({1.0, std::fabs(y[i]), std::fabs(yt[i])});
+        err = std::max(err, std::fabs(ye[i]) / sc);
+      }
+      if (!std::isfinite(err)) ok = false;
+    }
+    if (ok && err <= tol) {
+      for (int i = 0; i < 3; ++i) y[i] = yt[i];
+      y[0] = std::max(y[0], 0.0);
+      y[1] = std::max(y[1], 0.0);
+      z += h;
+      need = true;
+      if (dir * (zend - z) <= 0) return true;
+      double fac = err == 0 ? max_scale : std::min(max_scale, std::max(min_scale, safety * std::sqrt(tol / err)));
+      h = dir * std::min(std::fabs(h) * fac, std::fabs(zend - z));
+    } else {
+      double fac = ok ? std::min(0.9, std::max(min_scale, safety * std::sqrt(tol / std::max(err, 1e-300))))
+                      : min_scale;
+      h *= fac;
+      if (std::fabs(h) < min_step) return false;
+    }
+  }
+  return false;
+}
+}  // namespace ros2
+
 static void regular_spline_horner(const std::vector<double>& y, const std::vector<double>& d2, double h,
                                   std::vector<double>& hc) {
   int n = (int)y.size();
@@ -636,10 +783,12 @@ static int recfast_init(Cosmology& c, std::string& err) {
   DP45Host s;
   s.tol = 3e-6 / P.IntTolBoost;
   s.hmax = 20;
+  bool handed_off = P.recfast_no_rosenbrock != 0;  // the Rosenbrock phase has handed back to Dormand-Prince
   for (int i = 1; i <= R.nz; ++i) {
     double zstart = zinitial - (i - 1) * R.delta_z, zend = zinitial - i * R.delta_z;
     double z = zend, ainv = 1 + z, x0;
     double z_scale = R.Tnow / K::COBE_CMBTemp * ainv - 1;
+    if (!handed_off && y[0] <= ros2::handoff_xH) handed_off = true;
     if (z_scale > 8000) {
       x0 = 1 + 2 * R.fHe;
       y[0] = 1; y[1] = 1; y[2] = R.Tnow;
@@ -655,6 +804,33 @@ static int recfast_init(Cosmology& c, std::string& err) {
       double xHe0 = 0.5 * (std::sqrt((rhs - 1) * (rhs - 1) + 4 * (1 + R.fHe) * rhs) - (rhs - 1));
       x0 = xHe0;
       y[0] = 1; y[1] = (x0 - 1) / R.fHe; y[2] = R.Tnow;
+    } else if (!handed_off) {
+      double ys[3] = {y[0], y[1], y[2]};
+      if (!ros2::advance(ctx, zstart, y, zend, ros2::tol / P.IntTolBoost)) {
+        err = "RECFAST Rosenbrock integration failed";
+        return CAMBGPU_ERROR_RECOMBINATION;
+      }
+      if (y[0] <= ros2::handoff_xH) {
+        // hand off at the interval's start: redo the crossing interval with Dormand-Prince
+        y[0] = ys[0]; y[1] = ys[1]; y[2] = ys[2];
+        handed_off = true;
+        double zz = zstart;
+        if (y[0] > 0.99) {
+          double rhs = std::exp(1.5 * std::log(CR * R.Tnow / ainv) - CB1 / (R.Tnow * ainv)) / R.NNow;
+          double xH0 = 0.5 * (std::sqrt(rhs * rhs + 4 * rhs) - rhs);
+          int ind = dp45_host(fcn, 3, zz, y, zend, s);
+          if (ind < 0) { err = "RECFAST integration failed"; return CAMBGPU_ERROR_RECOMBINATION; }
+          y[0] = xH0;
+          x0 = y[0] + R.fHe * y[1];
+          s.fsal_valid = false;
+        } else {
+          int ind = dp45_host(fcn, 3, zz, y, zend, s);
+          if (ind < 0) { err = "RECFAST integration failed"; return CAMBGPU_ERROR_RECOMBINATION; }
+          x0 = y[0] + R.fHe * y[1];
+        }
+      } else {
+        x0 = y[0] + R.fHe * y[1];
+      }
     } else if (y[0] > 0.99) {
       double rhs = std::exp(1.5 * std::log(CR * R.Tnow / ainv) - CB1 / (R.Tnow * ainv)) / R.NNow;
       double xH0 = 0.5 * (std::sqrt(rhs * rhs + 4 * rhs) - rhs);

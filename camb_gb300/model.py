@@ -61,6 +61,15 @@ class TanhReionization:
         return self
 
 
+class Recfast:
+    """CAMBparams%Recomb (recombination.py Recfast): the cosmorec fudge set is built in;
+    use_rosenbrock integrates the stiff early phase with the Rosenbrock method
+    (recfast.f90:739-760), as the reference does by default."""
+
+    def __init__(self):
+        self.use_rosenbrock = True
+
+
 class TransferParams:
     """CAMBparams%Transfer (model.f90:160-175): matter transfer function settings."""
 
@@ -88,6 +97,7 @@ class CAMBparams:
         self.WantCls, self.WantScalars = True, True
         self.InitPower = InitialPowerLaw()
         self.Reion = TanhReionization()
+        self.Recomb = Recfast()
         self.Accuracy = AccuracyParams()
         for k, v in kwargs.items():
             setattr(self, k, v)
@@ -195,6 +205,7 @@ class CAMBparams:
             s.transfer_redshifts[i] = z
         s.reion_use_optical_depth = 1 if self.Reion.use_optical_depth else 0
         s.reion_redshift = self.Reion.redshift
+        s.recfast_no_rosenbrock = 0 if self.Recomb.use_rosenbrock else 1
         return s
 
 

@@ -71,6 +71,8 @@ typedef struct CambGpuParams {
     double transfer_redshifts[256];
     int reion_use_optical_depth; /* 1: optical_depth fixes the reionization redshift; 0: reion_redshift does */
     double reion_redshift;
+    int recfast_no_rosenbrock;   /* 1: Recfast%use_rosenbrock = F (Dormand-Prince with the Saha hold
+                                    throughout); 0 (default): the Rosenbrock phase until x_H = 0.976 */
 } CambGpuParams;
 
 /* Per-k-mode setup: the hierarchy sizes of GetNumEqns (equations.f90:860-1070)

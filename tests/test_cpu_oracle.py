@@ -190,3 +190,32 @@ def test_small_lmax_modes_start_inside_thermal_tables():
             assert min(starts) >= T.view.tauminn
             src = orc.evolve_sources(T, 2)
             assert np.all(np.isfinite(src))
+
+
+def test_recfast_rosenbrock_phase_against_dormand_prince():
+    """RECFAST's stiff early phase as the reference integrates it by default (ROS2
+    Rosenbrock on the full hydrogen system until x_H = 0.976, then Dormand-Prince,
+    recfast.f90:739-760) against the form without it (Recfast%use_rosenbrock = F: the Saha
+    hold above x_H = 0.99 and Dormand-Prince throughout).  Measured: x_e differs by up to
+    ~6e-4 around the helium and early hydrogen recombination (z ~ 1550-2000) and by
+    < 1e-6 below z = 1400; the oracle C_l by < 1e-4."""
+    import copy as _copy
+    from tests.cosmologies import fiducial
+    p = fiducial(2000)
+    q = _copy.copy(p)
+    q.recfast_no_rosenbrock = 1
+    lib = _lib.load()
+    z = np.linspace(200, 3000, 1401)
+    xe = {}
+    cl = {}
+    for tag, par in (("ros", p), ("dp", q)):
+        T = _lib.Tables(par)
+        x = np.zeros_like(z)
+        _lib.check(lib.cambgpu_recfast_xe(T.handle, _lib.dptr(z), len(z), _lib.dptr(x)))
+        xe[tag] = x
+        cl[tag] = orc.cls(T, orc.los(T, orc.evolve_sources(T)))
+    d = np.abs(xe["ros"] / xe["dp"] - 1)
+    assert 1e-5 < d.max() < 2e-3
+    assert d[z < 1400].max() < 1e-6
+    for c in (0, 1):
+        assert np.max(np.abs(cl["ros"][:, c] / cl["dp"][:, c] - 1)) < 1e-4
