@@ -359,7 +359,7 @@ struct Upload {
   std::vector<double> spl;  // [5][nk]
   std::vector<double> inv_q;  // 1/nu_q
   std::vector<double> inv_tgrid;  // 1/tau_j of the thermal log grid
-  std::vector<double> lfac;       // [2][nl] per sampled l: x_lim, sqrt(pi/2/(l+1/2))
+  std::vector<double> lfac;       // [3][nl] per sampled l: x_lim, sqrt(pi/2/(l+1/2)), doint threshold
   DevCosmo d;
 };
 
@@ -452,14 +452,18 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.nl = t.nl;
   // l-only factors of the projection windows and the Limber value (DoFlatIntegration,
   // cmbmain.f90:1702-1716, 1821-1832), for the mixed-precision projection
-  u.lfac.resize(2 * (size_t)t.nl);
+  u.lfac.resize(3 * (size_t)t.nl);
+  const double bib = t.AccuracyBoost * t.BessIntBoost;
   for (int j = 0; j < t.nl; ++j) {
     const double l = t.ls[j];
     u.lfac[j] = std::fmax(0.0, l - 4.2 * std::cbrt(l));
     u.lfac[t.nl + j] = std::sqrt(3.14159265358979323846 / 2 / (l + 0.5));
+    // the lensed-run integration test's threshold on q, as the kernel's FP64 form forms it
+    u.lfac[2 * (size_t)t.nl + j] = std::max(850, t.ls[j]) * 3 * bib / t.tau0 * 1.2;
   }
   d.l_xlim = (const double*)put(u.lfac.data(), u.lfac.size() * 8);
   d.l_limb = d.l_xlim + t.nl;
+  d.l_doint = d.l_xlim + 2 * (size_t)t.nl;
   d.max_l = t.max_l;
   d.cl_template_scale = t.cl_template_scale;
   d.lensed = nullptr;

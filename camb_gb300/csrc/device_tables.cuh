@@ -68,6 +68,7 @@ struct DevCosmo {
   int nl;
   const double* l_xlim;  // [nl] max(0, l - 4.2 l^(1/3))
   const double* l_limb;  // [nl] sqrt(pi / (2 l + 1))
+  const double* l_doint;  // [nl] max(850, l) 3 BessIntBoost / tau0 1.2 (lensed-run integration test)
   // Bessel table
   const double* bess_x;
   const double* bessel_horner;  // [nl][num_xx-1][4]

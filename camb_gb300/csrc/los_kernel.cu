@@ -189,7 +189,7 @@ __device__ __forceinline__ void window_setup(const DevCosmo& C, double q, int so
       if (tmax < tp[1]) flag = F_SKIP;
       else {
         bool doint = true;
-        if (nsrc > 2) doint = q < max(850, l) * 3 * BessIntBoost / tau0 * 1.2;
+        if (nsrc > 2) doint = q < (FAST ? C.l_doint[j] : max(850, l) * 3 * BessIntBoost / tau0 * 1.2);
         if (doint) {
           flag |= F_INT;
           ns = time_index_of(tp, ntau, tmin);
@@ -223,6 +223,10 @@ struct KInterp {
   double a0, b0, a03, b03, ho2o6;
 };
 
+// the same for every thread of a CTA (one q): thread 0 computes it, the others read it
+// from shared memory (saves the bisection and divisions on the FP64 pipe of every warp)
+__device__ __forceinline__ KInterp k_interp_shared(const DevCosmo& C, double q, KInterp* s_K);
+
 __device__ __forceinline__ KInterp k_interp(const DevCosmo& C, double q) {
   const int nk = C.nk;
   KInterp K;
@@ -237,6 +241,12 @@ __device__ __forceinline__ KInterp k_interp(const DevCosmo& C, double q) {
   K.a03 = K.a0 * K.a0 * K.a0 - K.a0;
   K.b03 = K.b0 * K.b0 * K.b0 - K.b0;
   return K;
+}
+
+__device__ __forceinline__ KInterp k_interp_shared(const DevCosmo& C, double q, KInterp* s_K) {
+  if (threadIdx.x == 0) *s_K = k_interp(C, q);
+  __syncthreads();
+  return *s_K;
 }
 
 // One CTA per integration wavenumber q, FP64 throughout (the plain form): the interpolated
@@ -254,7 +264,8 @@ __device__ __forceinline__ void los_flat_body(const DevCosmo& C, int q_ix, doubl
   const double q = C.q_int[q_ix];
   const double tau0 = C.tau0;
   load_segments(C, S);
-  const KInterp K = k_interp(C, q);
+  __shared__ KInterp s_K;
+  const KInterp K = k_interp_shared(C, q, &s_K);
   const int cnt = source_row_count(C, q, &s_cnt);  // synchronises (segments visible after)
   const int source_steps = max(2, 1 + cnt);        // 1-based count of rows filled (row 1 is zero)
   const int nbx = C.num_xx;
@@ -365,7 +376,8 @@ __device__ __forceinline__ void los_mixed_body(const DevCosmo& C, int q_ix, floa
   const double q = C.q_int[q_ix];
   const double tau0 = C.tau0;
   load_segments(C, S);
-  const KInterp K = k_interp(C, q);
+  __shared__ KInterp s_K;
+  const KInterp K = k_interp_shared(C, q, &s_K);
   const float a0 = (float)K.a0, b0 = (float)K.b0, a3 = (float)(K.a03 * K.ho2o6), b3 = (float)(K.b03 * K.ho2o6);
   const int cnt = source_row_count(C, q, &s_cnt);
   const int source_steps = max(2, 1 + cnt);
