@@ -92,6 +92,7 @@ SIGNATURES = {
     "cambgpu_tables_destroy": (None, [C.c_void_p]),
     "cambgpu_tables_derived": (C.c_int, [C.c_void_p, _c_double_p]),
     "cambgpu_recfast_xe": (C.c_int, [C.c_void_p, _c_double_p, C.c_int, _c_double_p]),
+    "cambgpu_conformal_time": (C.c_int, [C.c_void_p, _c_double_p, C.c_int, _c_double_p]),
     "cambgpu_evolve_scalar_sources": (C.c_int, [C.POINTER(CambGpuTables), _c_double_p]),
     "cambgpu_los_flat": (C.c_int, [C.POINTER(CambGpuTables), _c_double_p, _c_double_p]),
     "cambgpu_calc_scal_cls": (C.c_int, [C.POINTER(CambGpuTables), _c_double_p, _c_double_p]),
@@ -216,6 +217,13 @@ class Tables:
         z = np.ascontiguousarray(z, dtype=np.float64)
         out = np.zeros_like(z)
         check(self._lib.cambgpu_recfast_xe(self.handle, dptr(z), len(z), dptr(out)))
+        return out
+
+    def conformal_time(self, z):
+        """Conformal time from the big bang to redshift z in Mpc (CAMBdata.conformal_time)."""
+        z = np.ascontiguousarray(np.atleast_1d(z), dtype=np.float64)
+        out = np.zeros_like(z)
+        check(self._lib.cambgpu_conformal_time(self.handle, dptr(z), len(z), dptr(out)))
         return out
 
     def array(self, name, n):

@@ -177,6 +177,10 @@ void cambgpu_tables_destroy(void* handle);
  * zre (reionization mid redshift), x_e(z) at the requested redshifts. */
 int cambgpu_tables_derived(void* handle, double* out8);
 int cambgpu_recfast_xe(void* handle, const double* z, int n, double* xe);
+/* Conformal time from the big bang to each redshift z[i], in Mpc: CAMBdata_TimeOfz
+ * (results.f90:673-681, DeltaTime(0, 1/(1+z)) at its default tolerance), which
+ * camb.CAMBdata.conformal_time (camb/results.py:1779) calls. */
+int cambgpu_conformal_time(void* handle, const double* z, int n, double* eta);
 
 /* ---- hot path on the GPU (host buffers in and out) ---- */
 /* (1) cmbmain.f90:205-209: LinearSrc laid out [ntau][nsrc][nk] (k fastest, as the

@@ -219,3 +219,30 @@ def test_recfast_rosenbrock_phase_against_dormand_prince():
     assert d[z < 1400].max() < 1e-6
     for c in (0, 1):
         assert np.max(np.abs(cl["ros"][:, c] / cl["dp"][:, c] - 1)) < 1e-4
+
+
+def test_background_known_answers():
+    """camb_test.py testBackground: for H0 68.5, ombh2 0.022, omch2 0.122, YHe 0.2453,
+    mnu 0.07 (one eigenstate, N_eff 3.044), the reionization redshift that gives
+    tau = 0.06, the conformal time at z = 11.5 and the sound horizon at the drag epoch
+    (each to two places).  These tie the host
+    background integration (massive neutrinos included) and the reionization model to the
+    reference itself, not to the restatement, which shares the host tables."""
+    ka = json.load(open(os.path.join(HERE, "golden", "known_answers.json")))["background"]
+    c = ka["cosmology"]
+    p = CAMBparams()
+    p.set_cosmology(H0=c["H0"], ombh2=c["ombh2"], omch2=c["omch2"], YHe=c["YHe"], mnu=c["mnu"], omk=c["omk"],
+                    tau=c["tau"])
+    p.set_for_lmax(1000)
+    T = _lib.Tables(p.to_struct())
+    zre, places = ka["zre_from_tau"]
+    assert abs(T.derived()["zre"] - zre) < 0.5 * 10.0 ** -places
+    eta, places = ka["conformal_time_z11.5"]
+    t0, t115 = T.conformal_time([0.0, 11.5])
+    assert abs(t115 - eta) < 0.5 * 10.0 ** -places
+    assert t0 == pytest.approx(T.view.tau0, rel=1e-12)
+    # sound horizon at the drag epoch: the library keeps it as the l-sampling template
+    # scale, 0.010392206684501 / (r_drag / DMt0) (lSamples_init, results.f90:1517-1520)
+    d = T.derived()
+    rdrag, places = ka["rdrag"]
+    assert abs(0.010392206684501 * d["DMt0"] / d["scale"] - rdrag) < 0.5 * 10.0 ** -places
