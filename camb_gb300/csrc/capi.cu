@@ -78,8 +78,10 @@ int set_err(int code, const std::string& msg) {
 struct Arena {
   char* base = nullptr;
   size_t cap = 0, used = 0;
+  bool overflow = false;  // a take() past cap: the caller fails before any device use
   int reserve(size_t bytes) {
     used = 0;
+    overflow = false;
     if (bytes <= cap) return 0;
     if (base) cudaFree(base);
     base = nullptr;
@@ -92,6 +94,10 @@ struct Arena {
   template <class T>
   T* take(size_t n) {
     size_t bytes = (n * sizeof(T) + 255) & ~size_t(255);
+    if (used + bytes > cap) {
+      overflow = true;
+      return reinterpret_cast<T*>(base);
+    }
     T* p = reinterpret_cast<T*>(base + used);
     used += bytes;
     return p;
@@ -360,6 +366,8 @@ struct Upload {
   std::vector<double> inv_q;  // 1/nu_q
   std::vector<double> inv_tgrid;  // 1/tau_j of the thermal log grid
   std::vector<double> lfac;       // [3][nl] per sampled l: x_lim, sqrt(pi/2/(l+1/2)), doint threshold
+  std::vector<double> tdist;      // [ntau] tau0 - tau_i
+  std::vector<float> tdpf;        // [ntau] dtau_i in FP32
   DevCosmo d;
 };
 
@@ -370,7 +378,8 @@ size_t bytes_for(const CambGpuTables& t) {
   s += 2 * r((size_t)t.ntau * 8) + r((size_t)t.nk * sizeof(CambGpuModeSpec)) + r((size_t)t.nk * 8);
   s += 2 * r((size_t)t.ntau * t.nsrc * t.nk * 8);
   s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
-  s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256) + r((size_t)t.nl * 16);
+  s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256) + r((size_t)t.nl * 24);
+  s += r((size_t)t.ntau * 8) + r((size_t)t.ntau * 4);  // tau0 - tau_i, FP32 dtau_i
   s += 3 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
   s += r((size_t)(t.max_l + 1) * 6 * 8) + r((size_t)(t.max_l + 1) * 4 * 8);  // all-l C_l, lensed C_l
   if (t.transfer_only)
@@ -441,6 +450,16 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.tau_points = (const double*)put(t.tau_points, (size_t)t.ntau * 8);
   d.tau_dpoints = (const double*)put(t.tau_dpoints, (size_t)t.ntau * 8);
   d.ntau = t.ntau;
+  // per time step of the mixed projection's staging: the distance to today and the step
+  // width in FP32, formed here once instead of in every CTA
+  u.tdist.resize(t.ntau);
+  u.tdpf.resize(t.ntau);
+  for (int i = 0; i < t.ntau; ++i) {
+    u.tdist[i] = t.tau0 - t.tau_points[i];
+    u.tdpf[i] = (float)t.tau_dpoints[i];
+  }
+  d.tau_dist = (const double*)put(u.tdist.data(), (size_t)t.ntau * 8);
+  d.tau_dpf = (const float*)put(u.tdpf.data(), (size_t)t.ntau * 4);
   d.modes = (const CambGpuModeSpec*)put(t.modes, (size_t)t.nk * sizeof(CambGpuModeSpec));
   d.q_evolve = (const double*)put(t.q_evolve, (size_t)t.nk * 8);
   d.nk = t.nk;
@@ -751,6 +770,7 @@ int stage_batch(Batch& B, int lmax_out = 0) {
     B.d_tsrc = g_rt.arena.take<float2>((size_t)B.views[0]->nk * B.views[0]->nsrc * B.h_chi.size() * n);
   }
   copies.push_back({B.d_items_cost, {B.h_items_cost.data(), items.size() * sizeof(WorkItem)}});
+  if (g_rt.arena.overflow) return set_err(CAMBGPU_ERROR_ALLOCATION, "device arena sized below its uses (internal)");
   // single pinned staging buffer for all uploads
   size_t stage = 0;
   for (auto& cp : copies) stage += (cp.second.second + 255) & ~size_t(255);
@@ -1410,6 +1430,13 @@ int cambgpu_recfast_xe(void* handle, const double* z, int n, double* xe) {
   if (!handle) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "null handle");
   const cg::Cosmology& c = static_cast<Handle*>(handle)->c;
   for (int i = 0; i < n; ++i) xe[i] = c.recfast.x_e(1 / (1 + z[i]));
+  return 0;
+}
+
+int cambgpu_conformal_time(void* handle, const double* z, int n, double* eta) {
+  if (!handle) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "null handle");
+  const cg::Cosmology& c = static_cast<Handle*>(handle)->c;
+  for (int i = 0; i < n; ++i) eta[i] = c.time_of_z(z[i]);
   return 0;
 }
 

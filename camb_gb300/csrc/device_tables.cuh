@@ -37,6 +37,8 @@ struct DevCosmo {
   // time grid
   const double* tau_points;
   const double* tau_dpoints;
+  const double* tau_dist;  // [ntau] tau0 - tau_i (mixed projection staging)
+  const float* tau_dpf;     // [ntau] dtau_i in FP32 (mixed projection staging)
   int ntau;
   // source k grid
   const CambGpuModeSpec* modes;

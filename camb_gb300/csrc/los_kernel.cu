@@ -374,7 +374,6 @@ __device__ __forceinline__ void los_mixed_body(const DevCosmo& C, int q_ix, floa
   __shared__ int s_cnt;
   __shared__ SegShared S;
   const double q = C.q_int[q_ix];
-  const double tau0 = C.tau0;
   load_segments(C, S);
   __shared__ KInterp s_K;
   const KInterp K = k_interp_shared(C, q, &s_K);
@@ -384,13 +383,13 @@ __device__ __forceinline__ void los_mixed_body(const DevCosmo& C, int q_ix, floa
   const int nbx = C.num_xx;
   const float2* __restrict__ LD = reinterpret_cast<const float2*>(C.dd_src);
   for (int i = threadIdx.x; i < source_steps; i += blockDim.x) {
-    const double xx = fabs(q * (tau0 - C.tau_points[i]));
+    const double xx = fabs(q * C.tau_dist[i]);
     int bi;
     if (C.nseg > 0) bi = bess_interval_estimate(S.x0, S.ih, S.i0, S.n, C.nseg, nbx, (float)xx);
     else bi = bsearch_lo(C.bess_x, nbx, xx);
     s_bix[i] = bi;
     s_wf[i] = (float)(ldgd(C.bess_x + bi + 1) - xx) * __ldg(C.bess_inv_dxf + bi);
-    const float dt = (float)C.tau_dpoints[i];
+    const float dt = __ldg(C.tau_dpf + i);
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
       float v = 0.f;
