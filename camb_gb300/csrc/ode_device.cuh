@@ -1931,18 +1931,28 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   wsync<W>();
   R.src_valid = want_src;
   R.evals += 6;
-  // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry
+  // mixed error norm max |e_i| / max(1, |y_i|) without a division per entry.  Where
+  // |y_i| <= 1 the quotient is |e_i| itself, and non-negative doubles order as their bit
+  // patterns, so those entries take an integer maximum off the FP64 pipe; only entries
+  // with |y_i| > 1 compare cross-multiplied quotients.
+  constexpr unsigned long long kAbs = 0x7fffffffffffffffULL, kOne = 0x3ff0000000000000ULL;
+  unsigned long long m1 = 0;
   double num = 0, den = 1;
   for (int i = lane; i < n; i += W) {
     const double ee = fma(e7, k4[i], k3[i]);
-    const double ae = fabs(ee), ay = fabs(y[i]);
-    const double sc = ay > 1.0 ? ay : 1.0;
-    if (ae * den > num * sc) {
-      num = ae;
-      den = sc;
+    const unsigned long long be = (unsigned long long)__double_as_longlong(ee) & kAbs;
+    const unsigned long long by = (unsigned long long)__double_as_longlong(y[i]) & kAbs;
+    if (by <= kOne) {
+      m1 = max(m1, be);
+    } else {
+      const double ae = __longlong_as_double((long long)be), ay = __longlong_as_double((long long)by);
+      if (ae * den > num * ay) {
+        num = ae;
+        den = ay;
+      }
     }
   }
-  R.err = wmax<W>(num / den) * R.h;
+  R.err = fmax(__longlong_as_double((long long)wmax_u64<W>(m1)), wmax<W>(num / den)) * R.h;
   if (R.err <= tol) {
     R.tau = xt;
     // accept: the trial state and k7 become y and k1 by swapping rows
