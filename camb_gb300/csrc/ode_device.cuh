@@ -808,6 +808,18 @@ constexpr int NV = 448;  // largest packed scalar system handled (mode_init reje
 // k1..k5; k6 takes k2's row (k2 is dead once the stage-6 input is formed, b2 = e2 = 0) and
 // k7 takes k4's (dead once the fifth-order solution and the error combination are formed).
 constexpr int kRows = 7;
+// Unroll of the multipole sweeps of the right-hand side and of the stage combinations.
+// Measured on the 256-draw lmax-2500 batch (team 7, balanced queue): unrolled groups keep
+// more row loads in flight, but the rows miss L1 and L2 and the wider bursts lose --
+// 4 / 4 took 1266 ms, 8 / 4 1332, 8 / 8 1448, 2 / 4 1237, 2 / 1 1202 (stage / sweep).
+#ifndef CG_RHS_UNROLL
+#define CG_RHS_UNROLL 1
+#endif
+#ifndef CG_STAGE_UNROLL
+#define CG_STAGE_UNROLL 2
+#endif
+constexpr int kRhsUnroll = CG_RHS_UNROLL;
+constexpr int kStageUnroll = CG_STAGE_UNROLL;
 constexpr int NL = 256;  // multipoles of any hierarchy: l < 256 (lAccuracyBoost up to ~3.9)
 constexpr int NUE = 3;
 
@@ -1263,7 +1275,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
       if constexpr (W == 1) {
         // one read of each entry: the neighbours travel in registers
         double ym = pig, y0 = g3v;
-#pragma unroll 4
+#pragma unroll kRhsUnroll
         for (int l = 3; l < lg; ++l) {
           const double yp = y[g + l + 1];
           dy[g + l] = k * (__ldg(ra + l) * ym - __ldg(rb + l) * yp) - opac * y0;
@@ -1275,7 +1287,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
         dy[pol + 2] = -opac * (E2 - polter) - k * (1.0 / 3.0) * p3v;
         ym = E2;
         y0 = p3v;
-#pragma unroll 4
+#pragma unroll kRhsUnroll
         for (int l = 3; l < lp; ++l) {
           const double yp = y[pol + l + 1];
           dy[pol + l] = -opac * y0 + k * (__ldg(ra + l) * ym - __ldg(rp + l) * yp);
@@ -1309,7 +1321,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
       const int ln = M.lmaxnr;
       if constexpr (W == 1) {
         double ym = pir, y0 = n3v;
-#pragma unroll 4
+#pragma unroll kRhsUnroll
         for (int l = 3; l < ln; ++l) {
           const double yp = y[r + l + 1];
           dy[r + l] = k * (__ldg(ra + l) * ym - __ldg(rb + l) * yp);
@@ -1348,7 +1360,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
           const double y3v = y[ind + 3];
           dy[ind + 2] = vk * (0.4 * y1v - 0.6 * y3v) + k * 8.0 / 15.0 * sigma;
           double ym = y2v, yc = y3v;
-#pragma unroll 4
+#pragma unroll kRhsUnroll
           for (int l = 3; l < lt; ++l) {
             const double yp = y[ind + l + 1];
             dy[ind + l] = vk * (__ldg(ra + l) * ym - __ldg(rb + l) * yp);
@@ -1387,7 +1399,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
     if constexpr (W == 1) {
       double pm = y[p0], pc = y[p0 + 1], rm = y[r], rc = y[r + 1];
       dy[p0] = k * a2 * qr - k * pc;
-#pragma unroll 4
+#pragma unroll kRhsUnroll
       for (int l = 1; l < lp; ++l) {
         const double rpv = y[r + l + 1], pp = y[p0 + l + 1];
         const double al = __ldg(ra + l), bl = __ldg(rb + l);
@@ -1493,6 +1505,24 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
     if (C.nsrc > 2 && tau > C.tau_maxvis && ang > 0.1)
       src[2] = -2 * phi * (tau - C.tau_maxvis) / ((C.tau0 - C.tau_maxvis) * ang);
   }
+}
+
+#ifndef CG_RHS_CALL
+#define CG_RHS_CALL 1
+#endif
+// The right-hand side as one out-of-line function for the thread-per-mode kernels (a
+// trial step evaluates it at eight call sites; inlined, each is a copy of the whole
+// body): half the code, 0.8 % faster at 256 draws (1212 against 1222 ms)
+template <bool TR, int W, class YV>
+__device__ __noinline__ void derivs1_call(const DevCosmo& C, St& M, double tau, const YV y, double* __restrict__ dy,
+                                          double* src, NuBins* sbins, const double* wrec) {
+  derivs1<TR, W>(C, M, tau, y, dy, src, sbins, wrec);
+}
+template <bool TR, int W, class YV>
+__device__ __forceinline__ void rhs(const DevCosmo& C, St& M, double tau, const YV y, double* __restrict__ dy,
+                                    double* src, NuBins* sbins, const double* wrec) {
+  if constexpr (W == 1 && CG_RHS_CALL != 0) derivs1_call<TR, W>(C, M, tau, y, dy, src, sbins, wrec);
+  else derivs1<TR, W>(C, M, tau, y, dy, src, sbins, wrec);
 }
 
 // The stage vectors live in the seven rows of b; every row is named by a slot index so
@@ -1841,7 +1871,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   if (R.need_f) {
     if (R.fsal) R.fsal = false;
     else {
-      derivs1<TR, W>(C, M, R.tau, y, k1, nullptr, sb, wrec(Wk));
+      rhs<TR, W>(C, M, R.tau, y, k1, nullptr, sb, wrec(Wk));
       wsync<W>();
       R.evals++;
     }
@@ -1887,36 +1917,36 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   const double c51 = hs * a51, c52 = hs * a52, c53 = hs * a53, c54 = hs * a54;
   const double c61 = hs * a61, c62 = hs * a62, c63 = hs * a63, c64 = hs * a64, c65 = hs * a65;
   const double cb1 = hs * b1, cb3 = hs * b3, cb4 = hs * b4, cb5 = hs * b5, cb6 = hs * b6;
-#pragma unroll 4
+#pragma unroll kStageUnroll
   for (int i = lane; i < n; i += W) yt[i] = fma(c21, k1[i], y[i]);
   wsync<W>();
-  derivs1<TR, W>(C, M, x + hs / 5.0, yt, k2, nullptr, sb, wrec(Wk));
+  rhs<TR, W>(C, M, x + hs / 5.0, yt, k2, nullptr, sb, wrec(Wk));
   wsync<W>();
-#pragma unroll 4
+#pragma unroll kStageUnroll
   for (int i = lane; i < n; i += W) yt[i] = fma(c32, k2[i], fma(c31, k1[i], y[i]));
   wsync<W>();
-  derivs1<TR, W>(C, M, x + hs * (3.0 / 10.0), yt, k3, nullptr, sb, wrec(Wk));
+  rhs<TR, W>(C, M, x + hs * (3.0 / 10.0), yt, k3, nullptr, sb, wrec(Wk));
   wsync<W>();
-#pragma unroll 4
+#pragma unroll kStageUnroll
   for (int i = lane; i < n; i += W) yt[i] = fma(c43, k3[i], fma(c42, k2[i], fma(c41, k1[i], y[i])));
   wsync<W>();
-  derivs1<TR, W>(C, M, x + hs * (4.0 / 5.0), yt, k4, nullptr, sb, wrec(Wk));
+  rhs<TR, W>(C, M, x + hs * (4.0 / 5.0), yt, k4, nullptr, sb, wrec(Wk));
   wsync<W>();
-#pragma unroll 4
+#pragma unroll kStageUnroll
   for (int i = lane; i < n; i += W) yt[i] = fma(c54, k4[i], fma(c53, k3[i], fma(c52, k2[i], fma(c51, k1[i], y[i]))));
   wsync<W>();
-  derivs1<TR, W>(C, M, x + hs * (8.0 / 9.0), yt, k5, nullptr, sb, wrec(Wk));
+  rhs<TR, W>(C, M, x + hs * (8.0 / 9.0), yt, k5, nullptr, sb, wrec(Wk));
   wsync<W>();
-#pragma unroll 4
+#pragma unroll kStageUnroll
   for (int i = lane; i < n; i += W)
     yt[i] = fma(c65, k5[i], fma(c64, k4[i], fma(c63, k3[i], fma(c62, k2[i], fma(c61, k1[i], y[i])))));
   wsync<W>();
-  derivs1<TR, W>(C, M, x + hs, yt, k2, nullptr, sb, wrec(Wk));  // k6 into k2's row
+  rhs<TR, W>(C, M, x + hs, yt, k2, nullptr, sb, wrec(Wk));  // k6 into k2's row
   wsync<W>();
   // the fifth-order solution, the error combination of k1, k3..k6 (k3 is dead afterwards
   // and holds it) and max|yt| for the next step's hmin, in one pass
   unsigned long long nbt = 0;
-#pragma unroll 4
+#pragma unroll kStageUnroll
   for (int i = lane; i < n; i += W) {
     const double a1 = k1[i], a3 = k3[i], a4 = k4[i], a5 = k5[i], a6 = k2[i];
     const double v = fma(cb6, a6, fma(cb5, a5, fma(cb4, a4, fma(cb3, a3, fma(cb1, a1, y[i])))));
@@ -1927,7 +1957,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   wsync<W>();
   // stage 7 (FSAL) into k4's row; at an output time it is the output() evaluation too
   const bool want_src = (xt == xend) && !R.target_is_switch;
-  derivs1<TR, W>(C, M, x + hs, yt, k4, want_src ? R.src : nullptr, sb, wrec(Wk));
+  rhs<TR, W>(C, M, x + hs, yt, k4, want_src ? R.src : nullptr, sb, wrec(Wk));
   wsync<W>();
   R.src_valid = want_src;
   R.evals += 6;
@@ -2034,7 +2064,7 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
         apply_switch<W>(C, M, Wk, R);
       } else {
         if (!R.src_valid) {
-          derivs1<TR, W>(C, M, R.tau, row(Wk, R.sy), row(Wk, R.syt), R.src, sbins(Wk), wrec(Wk));
+          rhs<TR, W>(C, M, R.tau, row(Wk, R.sy), row(Wk, R.syt), R.src, sbins(Wk), wrec(Wk));
           wsync<W>();
         }
         R.evals++;  // the output() evaluation of the reference
