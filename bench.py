@@ -87,15 +87,13 @@ def plain_form_rate(n=3, lmax=2500, seed=1000, mnu_max=0.2):
 # `python -m camb_gb300.kernel_case team7_256_o<order>_s1` (static stride), one pass each
 # (profiles/ode_thread_kernel_dram_batch256_lmax2500.md)
 ODE_TRAFFIC = {
-    (7, 4): (916.02e9 + 447.24e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
+    (7, 4): (911.95e9 + 442.84e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
                                   "(team 7, balanced queue order 4, static stride; kernel case team7_256_o4_s1)"),
-    (7, 2): (642.02e9 + 383.11e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 256-draw ODE launch "
-                                  "(team 7, q-band queue order 2, static stride; kernel case team7_256_o2_s1)"),
 }
 # FP64 flops per right-hand-side evaluation (2 DFMA + DMUL + DADD thread instructions,
 # stage combinations, error norm and source output included), ncu on the 32-draw case of
 # this workload (kernel case thread32, profiles/ode_thread_kernel_batch32_lmax2500.md)
-FLOPS_PER_EVAL = 1182
+FLOPS_PER_EVAL = 1165
 NOMINAL_FP64_TFLOPS = 152 * 2.07e9 * 4 / 1e12  # SMs x max SM clock x 4 flop per cycle
 
 
