@@ -1525,10 +1525,21 @@ __device__ __forceinline__ void rhs(const DevCosmo& C, St& M, double tau, const 
   else derivs1<TR, W>(C, M, tau, y, dy, src, sbins, wrec);
 }
 
+// Pitch of the rows in a thread's local memory.  Rows packed at the mode's own system size
+// (7 x ~85 entries together) ran 11 % slower at 256 draws than rows NV entries apart
+// (1319 against 1189 ms): the six rows a stage combination reads at one entry then fall
+// on neighbouring addresses instead of spreading over the memory partitions.  Among
+// pitches of 448, 456, 480 and 512 entries, 456 ran fastest (1180 against 1191 ms).
+#ifndef CG_ROW_PITCH
+#define CG_ROW_PITCH 456
+#endif
+constexpr int kRowPitch = CG_ROW_PITCH;
+static_assert(kRowPitch >= NV, "a row holds the largest packed system");
+
 // The stage vectors live in the seven rows of b; every row is named by a slot index so
 // that accepting a step swaps indices, not vectors.
 struct Work {
-  double b[kRows][NV];
+  double b[kRows][kRowPitch];
 };
 
 // The same rows for a warp's mode, in the warp's slice of shared memory
@@ -1543,6 +1554,7 @@ __device__ __forceinline__ double* row(const WorkS& w, int s) { return w.b + (si
 __device__ __forceinline__ NuBins* sbins(Work&) { return nullptr; }
 __device__ __forceinline__ NuBins* sbins(const WorkS& w) { return w.bins; }
 __device__ __forceinline__ int row_cap(const Work&) { return NV; }
+
 __device__ __forceinline__ int row_cap(const WorkS& w) { return w.stride; }
 __device__ __forceinline__ const double* wrec(const Work&) { return nullptr; }
 __device__ __forceinline__ const double* wrec(const WorkS& w) { return w.rec; }
@@ -1766,6 +1778,11 @@ __device__ __forceinline__ void swap_rows(Run& R, double*& Y, double*& YT) {
   YT = p;
 }
 
+// A new layout larger than the mode's largest packed system (which sizes its rows): not
+// expected, since setup_indices bounds every layout of the mode at its start; the mode
+// ends with an evolution error instead of writing past its rows.
+__device__ __forceinline__ void layout_overflow(Run& R) { R.status = CAMBGPU_ERROR_EVOLUTION; }
+
 template <int W, class WK>
 __device__ void apply_switch(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   const double noSwitch = C.tau0 + 1;
@@ -1778,6 +1795,7 @@ __device__ void apply_switch(const DevCosmo& C, St& M, WK& Wk, Run& R) {
     N.tc = false;
     N.tight_off = noSwitch;
     setup_indices(C, N, false);
+    if (N.n > N.nvar) return layout_overflow(R);
     copy_vars<W>(C, M, N, Y, YT);
     M = N;
     swap_rows(R, Y, YT);
@@ -1801,6 +1819,7 @@ __device__ void apply_switch(const DevCosmo& C, St& M, WK& Wk, Run& R) {
     const double a2 = a * a;
     N.approx[e] = true;
     setup_indices(C, N, false);
+    if (N.n > N.nvar) return layout_overflow(R);
     copy_vars<W>(C, M, N, Y, YT);
     double rhonu, pnu, clxnu, qnu, dpnu, pinu;
     nuf::rho_P(a * C.nu_masses[e], rhonu, pnu);
@@ -1845,6 +1864,7 @@ __device__ void apply_switch(const DevCosmo& C, St& M, WK& Wk, Run& R) {
       N.nophot = true;
     }
     setup_indices(C, N, false);
+    if (N.n > N.nvar) return layout_overflow(R);
     copy_vars<W>(C, M, N, Y, YT);
     M = N;
     swap_rows(R, Y, YT);
@@ -2084,6 +2104,10 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
       }
       int guard = 0;
       for (;;) {
+        if (R.status) {  // a switch that could not be applied
+          more = false;
+          break;
+        }
         more = next_target<TR>(C, M, R);
         if (!more || !(R.target_is_switch && R.target == R.tau) || ++guard > 16) break;
         apply_switch<W>(C, M, Wk, R);  // switches due at the current time
