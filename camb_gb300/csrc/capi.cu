@@ -362,6 +362,7 @@ int device_lens_geom(const HostLensGeom& h, LensGeomDev& G) {
 // per-cosmology upload plan
 struct Upload {
   const CambGpuTables* t;
+  const std::vector<double>* pre_tgrid = nullptr;  // inv_tgrid formed with the host tables, if any
   std::vector<double> spl;  // [5][nk]
   std::vector<double> inv_q;  // 1/nu_q
   std::vector<double> inv_tgrid;  // 1/tau_j of the thermal log grid
@@ -386,6 +387,12 @@ size_t bytes_for(const CambGpuTables& t) {
     s += r((size_t)t.num_transfer_times * 8) + r((size_t)t.num_transfer_times * t.nk * 13 * 4) +
          r((size_t)t.num_transfer_times * 16);
   return s;
+}
+
+// 1/tau_j on the thermal log grid tau_j = tauminn exp(j dlntau), j = 0..nthermo
+void thermal_inverse_grid(int nthermo, double tauminn, double dlntau, std::vector<double>& out) {
+  out.resize((size_t)nthermo + 1);
+  for (int j = 0; j <= nthermo; ++j) out[j] = 1.0 / (tauminn * std::exp(j * dlntau));
 }
 
 void spline_factors(const CambGpuTables& t, std::vector<double>& spl) {
@@ -441,9 +448,12 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.nthermo = t.nthermo;
   d.tauminn = t.tauminn; d.inv_tauminn = 1.0 / t.tauminn; d.dlntau = t.dlntau; d.dlntau_inv = t.dlntau_inv;
   d.dlntau_inv_log2 = (float)(0.69314718055994530942 * t.dlntau_inv);
-  u.inv_tgrid.resize((size_t)t.nthermo + 1);
-  for (int j = 0; j <= t.nthermo; ++j) u.inv_tgrid[j] = 1.0 / (t.tauminn * std::exp(j * t.dlntau));
-  d.inv_tgrid = (const double*)put(u.inv_tgrid.data(), u.inv_tgrid.size() * 8);
+  if (u.pre_tgrid && u.pre_tgrid->size() == (size_t)t.nthermo + 1) {
+    d.inv_tgrid = (const double*)put(u.pre_tgrid->data(), u.pre_tgrid->size() * 8);
+  } else {
+    thermal_inverse_grid(t.nthermo, t.tauminn, t.dlntau, u.inv_tgrid);
+    d.inv_tgrid = (const double*)put(u.inv_tgrid.data(), u.inv_tgrid.size() * 8);
+  }
   int e = t.nthermo - 1;
   d.cs2_end = t.cs2[e]; d.dotmu_end = t.dotmu[e]; d.ddotmu_end = t.ddotmu[e]; d.dddotmu_end = t.dddotmu[e];
   d.emmu_end = t.emmu[e];
@@ -535,6 +545,7 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
 // A batch resident on the device
 struct Batch {
   std::vector<const CambGpuTables*> views;
+  std::vector<const std::vector<double>*> tgrid;  // per view: inv_tgrid built with its tables, or empty
   std::vector<Upload> ups;
   DevCosmo* d_cosmos = nullptr;
   const double** d_spl = nullptr;
@@ -656,6 +667,7 @@ int stage_batch(Batch& B, int lmax_out = 0) {
   B.ups.resize(n);
   for (int c = 0; c < n; ++c) {
     B.ups[c].t = B.views[c];
+    B.ups[c].pre_tgrid = c < (int)B.tgrid.size() ? B.tgrid[c] : nullptr;
     rc = upload(B.ups[c], B.d_status + c, copies);
     if (rc) return rc;
     B.ups[c].d.evals = B.d_evals;
@@ -1271,7 +1283,14 @@ struct Handle {
   cg::Cosmology c;
   std::shared_ptr<const cg::BesselTable> bt;
   CambGpuTables view;
+  std::vector<double> inv_tgrid;  // 1/tau_j of the thermal log grid, formed with the tables
 };
+
+// a handle's tables (and the thermal inverse grid built with them) into a batch
+void add_handle(Batch& B, Handle* h) {
+  B.views.push_back(&h->view);
+  B.tgrid.push_back(&h->inv_tgrid);
+}
 
 int make_handle(const CambGpuParams* p, Handle*& h) {
   h = new Handle();
@@ -1337,6 +1356,9 @@ int build_handles(const CambGpuParams* p, int n, std::vector<Handle*>& hs, int* 
           err = e.what();
         }
         if (rc) { delete h; h = nullptr; }
+        // the per-step thermal inverse grid of the upload, formed here on the building
+        // thread (in a stream of batches, while the device runs the previous batch)
+        else thermal_inverse_grid(h->c.nthermo, h->c.tauminn, h->c.dlntau, h->inv_tgrid);
         hs[i] = h;
         rcs[i] = rc;
         errs[i] = err;
@@ -1520,7 +1542,7 @@ int cambgpu_get_spectra_prepared(const CambGpuPrepared* t, int lmax_out, double*
   int rc = 0;
   const double t1 = wall_ms();
   Batch B;
-  for (auto* h : t->hs) B.views.push_back(&h->view);
+  for (auto* h : t->hs) add_handle(B, h);
   rc = stage_batch(B, lmax_out);
   if (rc) return rc;
   if (B.transfer) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "want_cls = 0: use cambgpu_get_transfer_batch");
@@ -1578,7 +1600,7 @@ int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float*
   for (auto* h : hs)
     if (transfer && h->view.nk > nq_max) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "nq_max too small");
   Batch B;
-  for (auto* h : hs) B.views.push_back(&h->view);
+  for (auto* h : hs) add_handle(B, h);
   rc = stage_batch(B);
   if (rc) return rc;
   rc = run_all(B, true, false, false);
@@ -1642,7 +1664,7 @@ int cambgpu_batch_prepare(const CambGpuParams* p, int n) {
   g_res.reset(new Resident());
   int rc = build_handles(p, n, g_res->handles, nullptr);
   if (rc) return rc;
-  for (auto* h : g_res->handles) g_res->B.views.push_back(&h->view);
+  for (auto* h : g_res->handles) add_handle(g_res->B, h);
   rc = stage_batch(g_res->B);
   if (rc) return rc;
   CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
@@ -1704,7 +1726,7 @@ int cambgpu_batch_prepare_shared(const CambGpuParams* p, int n, int* nchi_out) {
   cg::SharedGrid sg;
   rc = share_grids(g_res->handles, sg);
   if (rc) return rc;
-  for (auto* h : g_res->handles) g_res->B.views.push_back(&h->view);
+  for (auto* h : g_res->handles) add_handle(g_res->B, h);
   g_res->B.shared = true;
   g_res->B.h_chi = sg.chi;
   g_res->B.h_dchi = sg.dchi;
