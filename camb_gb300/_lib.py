@@ -81,6 +81,8 @@ class CambGpuTables(C.Structure):
         ("transfer_only", C.c_int), ("num_transfer_times", C.c_int), ("transfer_times", _c_double_p),
         ("hubble_h", C.c_double), ("want_cls", C.c_int), ("transfer_high_precision", C.c_int),
         ("late_phot_switch_boost_min", C.c_double),
+        ("src_keep_tau", C.c_double),
+        ("transfer_source_modes", C.c_int),
     ]
 
 
@@ -89,6 +91,7 @@ SIGNATURES = {
     "cambgpu_default_params": (None, [C.POINTER(CambGpuParams)]),
     "cambgpu_tables_create": (C.c_int, [C.POINTER(CambGpuParams), C.POINTER(C.c_void_p)]),
     "cambgpu_tables_view": (C.c_int, [C.c_void_p, C.POINTER(CambGpuTables)]),
+    "cambgpu_tables_transfer_view": (C.c_int, [C.c_void_p, C.POINTER(CambGpuTables)]),
     "cambgpu_tables_destroy": (None, [C.c_void_p]),
     "cambgpu_tables_derived": (C.c_int, [C.c_void_p, _c_double_p]),
     "cambgpu_recfast_xe": (C.c_int, [C.c_void_p, _c_double_p, C.c_int, _c_double_p]),
@@ -195,6 +198,12 @@ class Tables:
         self.handle = h
         self.view = CambGpuTables()
         check(self._lib.cambgpu_tables_view(h, C.byref(self.view)))
+
+    def transfer_view(self):
+        """The transfer-function half of a run that wants the CMB and transfer functions."""
+        v = CambGpuTables()
+        check(self._lib.cambgpu_tables_transfer_view(self.handle, C.byref(v)))
+        return v
 
     def close(self):
         if self.handle:

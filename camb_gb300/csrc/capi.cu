@@ -535,6 +535,8 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   }
   d.bess_x = bx;
   d.num_xx = t.num_xx;
+  d.src_keep_tau = t.src_keep_tau;
+  d.tr_src_modes = t.transfer_source_modes;
   d.nsrc = t.nsrc; d.want_late_time = t.want_late_time; d.max_etak_scalar = t.max_etak_scalar; d.tol1 = t.tol1;
   d.AccuracyBoost = t.AccuracyBoost; d.IntTolBoost = t.IntTolBoost; d.TimeSwitchBoost = t.TimeSwitchBoost;
   d.BessIntBoost = t.BessIntBoost; d.LimberBoost = t.LimberBoost;
@@ -1284,12 +1286,21 @@ struct Handle {
   std::shared_ptr<const cg::BesselTable> bt;
   CambGpuTables view;
   std::vector<double> inv_tgrid;  // 1/tau_j of the thermal log grid, formed with the tables
+  bool combined = false;          // wants the CMB and transfer functions: tview is the latter
+  CambGpuTables tview;
 };
 
-// a handle's tables (and the thermal inverse grid built with them) into a batch
-void add_handle(Batch& B, Handle* h) {
-  B.views.push_back(&h->view);
+// a handle's tables (and the thermal inverse grid built with them) into a batch; its
+// transfer-function half for a transfer batch of a run that wants the CMB too
+void add_handle(Batch& B, Handle* h, bool transfer_half = false) {
+  B.views.push_back(transfer_half && h->combined ? &h->tview : &h->view);
   B.tgrid.push_back(&h->inv_tgrid);
+}
+
+// the transfer-function half of a run that wants the CMB and transfer functions
+void fill_transfer_half(Handle* h, const CambGpuParams& p) {
+  h->combined = p.want_transfer && p.want_cls;
+  if (h->combined) cg::fill_transfer_view(h->c, h->tview);
 }
 
 int make_handle(const CambGpuParams* p, Handle*& h) {
@@ -1316,6 +1327,7 @@ int make_handle(const CambGpuParams* p, Handle*& h) {
       return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, e.what());
     }
     cg::fill_view(h->c, *h->bt, h->view);
+    fill_transfer_half(h, *p);
   } else {
     static const cg::BesselTable empty;  // transfer functions need no Bessel table
     cg::fill_view(h->c, empty, h->view);
@@ -1388,6 +1400,7 @@ int build_handles(const CambGpuParams* p, int n, std::vector<Handle*>& hs, int* 
       continue;
     }
     cg::fill_view(hs[i]->c, *hs[i]->bt, hs[i]->view);
+    fill_transfer_half(hs[i], p[i]);
   }
   return worst;
 }
@@ -1435,6 +1448,14 @@ int cambgpu_tables_create(const CambGpuParams* p, void** handle) {
 int cambgpu_tables_view(void* handle, CambGpuTables* view) {
   if (!handle) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "null handle");
   *view = static_cast<Handle*>(handle)->view;
+  return 0;
+}
+
+int cambgpu_tables_transfer_view(void* handle, CambGpuTables* view) {
+  if (!handle) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "null handle");
+  const Handle* h = static_cast<Handle*>(handle);
+  if (!h->combined) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "not a run that wants the CMB and transfers");
+  *view = h->tview;
   return 0;
 }
 
@@ -1588,8 +1609,7 @@ int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float*
   std::lock_guard<std::mutex> lk(g_mu);
   if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
   for (int c = 0; c < n; ++c) {
-    if (!p[c].want_transfer || p[c].want_cls)
-      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "transfer batches need want_transfer = 1 and want_cls = 0");
+    if (!p[c].want_transfer) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "transfer batches need want_transfer = 1");
     if (p[c].num_transfer_redshifts != p[0].num_transfer_redshifts)
       return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "every cosmology of a transfer batch needs the same redshift count");
   }
@@ -1597,10 +1617,12 @@ int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float*
   int rc = build_handles(p, n, hs, status);
   struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
   if (rc) return rc;
+  // a run that wants the CMB too contributes its transfer-function half
+  auto half = [](const Handle* h) -> const CambGpuTables& { return h->combined ? h->tview : h->view; };
   for (auto* h : hs)
-    if (transfer && h->view.nk > nq_max) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "nq_max too small");
+    if (transfer && half(h).nk > nq_max) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "nq_max too small");
   Batch B;
-  for (auto* h : hs) add_handle(B, h);
+  for (auto* h : hs) add_handle(B, h, true);
   rc = stage_batch(B);
   if (rc) return rc;
   rc = run_all(B, true, false, false);
@@ -1612,7 +1634,7 @@ int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float*
   const int nz = p[0].num_transfer_redshifts;
   std::vector<double> s8(2 * (size_t)nz);
   for (int c = 0; c < n; ++c) {
-    const CambGpuTables& v = hs[c]->view;
+    const CambGpuTables& v = half(hs[c]);
     if (nq) nq[c] = v.nk;
     if (transfer) {
       for (int z = 0; z < v.num_transfer_times; ++z) {

@@ -85,6 +85,8 @@ struct DevCosmo {
   int num_xx;
   // settings
   int nsrc, want_late_time;
+  double src_keep_tau;  // source modes keep evolving until tau passes it (runs with transfers)
+  int tr_src_modes;     // transfer path: leading modes that also stop at the source times
   double max_etak_scalar, tol1, AccuracyBoost, IntTolBoost, TimeSwitchBoost, BessIntBoost, LimberBoost;
   double As, ns, nrun, pivot_scalar, Alens;
 };

@@ -1478,10 +1478,6 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
   c.max_etak_scalar = initAccuracyBoost * std::max(1700.0, c.maximum_qeta) / 20;
   if (c.maximum_qeta < 3500 && P.AccuracyBoost < 2) c.max_etak_scalar *= 1.5;
   const bool transfer_only = P.want_transfer && !P.want_cls;
-  if (P.want_transfer && P.want_cls) {
-    err = "transfer functions are computed without the CMB (set want_cls = 0)";
-    return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
-  }
   if (P.want_transfer) {
     if (!(P.transfer_kmax > 0) || P.num_transfer_redshifts < 1 || P.num_transfer_redshifts > 256) {
       err = "transfer kmax and 1-256 redshifts required";
@@ -1537,6 +1533,9 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
     else dlnk0 = 5.0 / 10 / SAB;
     if (P.accurate_reionization) dlnk0 /= 2;
     if (c.reion.on && P.accurate_polarization && P.accurate_reionization) dlnk0 = std::min(dlnk0, 0.075);
+    // highPrecisionTransferSources: a run that wants high-precision transfer functions with
+    // the CMB reuses this grid for them, at least 20 points per e-fold (k_per_logint = 0)
+    if (P.want_cls && transfer_hp(P)) dlnk0 = std::min(dlnk0, 1.0 / 20);
     double dkn1 = 0.6 / c.taurst / SAB;
     double dkn2 = 0.9 / c.taurst / SAB / 1.2;
     double q_switch = 2 * 6.3 / c.taurst;
@@ -1585,9 +1584,14 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
     c.q_int.get_array(true);
   }
   c.tol1 = 1e-4 / std::exp(P.AccuracyBoost * P.IntTolBoost - 1);
+  // CalcScalarSources and GetTransfer alike: high-precision transfers tighten the
+  // tolerance of every mode, the CMB source modes of a run with transfers included
+  // (cmbmain.f90:1018-1021, 1180-1181)
+  if (transfer_hp(P)) c.tol1 /= 100;
   c.modes.clear();
-  if (transfer_only) {
-    if (transfer_hp(P)) c.tol1 /= 100;  // CalcScalarSources / GetTransfer
+  c.tr_q.clear();
+  c.tr_modes.clear();
+  if (P.want_transfer) {
     // transfer times: cumulative DeltaTime over the decreasing redshifts (TimeOfzArr,
     // results.f90:683-711)
     c.transfer_times.assign(P.num_transfer_redshifts, 0.0);
@@ -1630,9 +1634,24 @@ int build_cosmology(const CambGpuParams& p, Cosmology& c, std::string& err) {
       dlog_highk = nq / std::log(kmax * 1.05 / last);
       for (int i = 1; i <= nq; ++i) qt.push_back(last * std::exp(i / dlog_highk));
     }
-    for (double q : qt) c.modes.push_back(mode_setup(c, q, true));
+  }
+  if (transfer_only) {
+    for (double q : c.q_trans) c.modes.push_back(mode_setup(c, q, true));
   } else {
     for (double q : c.evolve_q.points) c.modes.push_back(mode_setup(c, q));
+    if (P.want_transfer) {
+      // InitTransfer with WantCls (cmbmain.f90:681-699): the source modes carry the
+      // transfer outputs up to the source grid's last point, the transfer grid's points
+      // beyond it (TransferOut, cmbmain.f90:1136-1165) are transfer-only modes
+      const double top = c.evolve_q.points.back() + 1e-4;
+      c.tr_q = c.evolve_q.points;
+      c.tr_modes = c.modes;
+      for (double q : c.q_trans)
+        if (q > top) {
+          c.tr_q.push_back(q);
+          c.tr_modes.push_back(mode_setup(c, q, true));
+        }
+    }
   }
   return 0;
 }
@@ -1869,6 +1888,10 @@ void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   v.transfer_only = transfer_only ? 1 : 0;
   v.num_transfer_times = transfer_only ? (int)c.transfer_times.size() : 0;
   v.transfer_times = transfer_only ? c.transfer_times.data() : nullptr;
+  // with transfer functions wanted too, the source modes keep evolving (and storing their
+  // sources) at late times until the last transfer time (CalcScalarSources,
+  // cmbmain.f90:1032-1035)
+  v.src_keep_tau = (!transfer_only && c.P.want_transfer) ? c.transfer_times.back() : -1.0;
   v.hubble_h = c.P.H0 / 100;
   v.want_cls = c.P.want_cls;
   v.transfer_high_precision = transfer_hp(c.P) ? 1 : 0;
@@ -1892,6 +1915,19 @@ void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v) {
   // template_shift_scale_tol (results.f90:49, 1517-1520)
   v.cl_template_scale = std::fabs(c.scale - 1.0) > 0.01 ? c.scale : 1.0;
   v.lens_accuracy_boost = c.P.AccuracyBoost * (c.P.LensingBoost > 0 ? c.P.LensingBoost : 1.0);
+}
+
+void fill_transfer_view(const Cosmology& c, CambGpuTables& v) {
+  static const BesselTable empty;
+  fill_view(c, empty, v);
+  v.nk = (int)c.tr_q.size();
+  v.q_evolve = c.tr_q.data();
+  v.modes = c.tr_modes.data();
+  v.transfer_only = 1;  // the device's transfer-function path, WantCls still set (want_cls)
+  v.num_transfer_times = (int)c.transfer_times.size();
+  v.transfer_times = c.transfer_times.data();
+  v.src_keep_tau = -1.0;
+  v.transfer_source_modes = c.evolve_q.npoints();
 }
 
 

@@ -107,6 +107,11 @@ struct Cosmology {
   std::vector<int> ls;
   std::vector<CambGpuModeSpec> modes;       // per k mode: the source grid, or q_trans without the CMB
   std::vector<double> q_trans, transfer_times;  // transfer k grid and times (transfer functions only)
+  // a run that wants the CMB and transfer functions (InitTransfer with WantCls,
+  // cmbmain.f90:681-699): the source grid followed by the transfer grid's points above it,
+  // with the source modes' own set-up and the others' transfer-only set-up
+  std::vector<double> tr_q;
+  std::vector<CambGpuModeSpec> tr_modes;
   int nsrc;
   double tol1;
 
@@ -145,5 +150,7 @@ int apply_shared_grid(Cosmology& c, const SharedGrid& g);
 std::shared_ptr<const BesselTable> get_bessel_table(const std::vector<int>& ls, double xmax,
                                                     double bessel_boost, double accuracy_boost);
 void fill_view(const Cosmology& c, const BesselTable& b, CambGpuTables& v);
+// the transfer-function half of a run that wants the CMB too (view of tr_q / tr_modes)
+void fill_transfer_view(const Cosmology& c, CambGpuTables& v);
 
 }  // namespace cg

@@ -1569,6 +1569,11 @@ struct Run {
   long long evals;
   int j, fails, status, sw_kind, sw_eig;
   bool active, target_is_switch, need_f, first, fsal, reset, src_valid;
+  // transfer path, a source mode of a run that also wants the CMB: it stops at the source
+  // times as well (no output there), in CalcScalarSources' order; st 0: transfer times
+  // before the second source time, 1: next stop the source time js, 2: at source time jj
+  bool stops, tgt_out;
+  int st, js, jj;
 };
 
 enum { SW_TC = 1, SW_KTAU, SW_NU_MASSLESS, SW_NU_NONREL, SW_NU_MASSIVE, SW_NONU, SW_NOPHOT };
@@ -1675,6 +1680,11 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
   wsync<W>();
   R.tau = tau;
   R.j = C.transfer_only ? 0 : 1;
+  R.stops = C.transfer_only && q_ix < C.tr_src_modes;
+  R.tgt_out = true;
+  R.st = 0;
+  R.js = 1;
+  R.jj = 0;
   R.h = R.err = 0;
   R.fails = 0;
   R.fsal = false;
@@ -1693,16 +1703,80 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
 // Picks the next integration target with the switch logic of EvolveScal
 // (equations.f90:261-331) and records which switch the target is.  Returns false
 // when the mode is finished.
+// The next stop of a source mode on the transfer path of a run that also wants the CMB,
+// CalcScalarSources with WantTransfer (cmbmain.f90:1020-1070): the transfer times before the
+// second source time, then every source time, each followed by the transfer times inside
+// its interval (or within 1e-5 of it, or any left at the last source time -- the reference's
+// `goto 101`).  A pure function of the stop state (settling states that consume nothing);
+// run_modes advances the state when a stop is reached.  false: no stop left.
+__device__ __forceinline__ bool stop_target(const DevCosmo& C, Run& R, double& tgt) {
+  const double* P = C.tau_points;
+  const double* TT = C.transfer_times;
+  const int ntau = C.ntau;
+  for (int guard = 0; guard < 4; ++guard) {
+    if (R.st == 0) {
+      if (P[1] > TT[R.j]) {
+        tgt = TT[R.j];
+        R.tgt_out = true;
+        return true;
+      }
+      R.st = 1;
+      R.js = 1;
+    }
+    if (R.st == 1) {
+      if (R.js >= ntau) return false;
+      tgt = P[R.js];
+      R.tgt_out = false;
+      return true;
+    }
+    const int jj = R.jj;  // st 2
+    if (jj < ntau - 1 && P[jj] < TT[R.j] && P[jj + 1] > TT[R.j]) {
+      tgt = TT[R.j];
+      R.tgt_out = true;
+      return true;
+    }
+    if (fabs(R.tau - TT[R.j]) < 1e-5 || jj == ntau - 1) {
+      tgt = R.tau;  // output at the current state
+      R.tgt_out = true;
+      return true;
+    }
+    R.st = 1;
+    R.js = jj + 1;
+  }
+  return false;
+}
+
+// run_modes' step after a stop of that kind is reached (the transfer output, if any, done)
+__device__ __forceinline__ void stop_reached(const DevCosmo& C, Run& R) {
+  if (R.st == 1) {  // a source time: the transfer checks after it
+    R.st = 2;
+    R.jj = R.js;
+    return;
+  }
+  if (R.st == 2) {  // a transfer output after source time jj: again, or on to the next source time
+    const int jj = R.jj;
+    if (!(jj < C.ntau - 1 && R.j < C.n_tt && C.tau_points[jj + 1] > C.transfer_times[R.j])) {
+      R.st = 1;
+      R.js = jj + 1;
+    }
+  }
+}
+
 template <bool TR>
 __device__ bool next_target(const DevCosmo& C, St& M, Run& R) {
   double tauend;
   if constexpr (TR) {  // GetTransfer: the transfer times in turn
     if (R.j >= C.n_tt) return false;
     tauend = C.transfer_times[R.j];
+    R.tgt_out = true;
+    if (R.stops && !stop_target(C, R, tauend)) return false;
   } else {
     if (R.j >= C.ntau) return false;
     tauend = C.tau_points[R.j];
-    if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time) return false;
+    // CalcScalarSources' late-time cut; a run with transfer functions keeps the mode going
+    // until the last transfer time (cmbmain.f90:1032-1035)
+    if (M.q * tauend > C.max_etak_scalar && tauend > C.taurend && !C.want_late_time && R.tau > C.src_keep_tau)
+      return false;
   }
   const double noSwitch = C.tau0 + 1;
   const double smallTime = fmin(R.tau, M.ik) / 100;
@@ -1976,7 +2050,7 @@ __device__ int trial_step(const DevCosmo& C, St& M, WK& Wk, Run& R) {
   }
   wsync<W>();
   // stage 7 (FSAL) into k4's row; at an output time it is the output() evaluation too
-  const bool want_src = (xt == xend) && !R.target_is_switch;
+  const bool want_src = (xt == xend) && !R.target_is_switch && R.tgt_out;
   rhs<TR, W>(C, M, x + hs, yt, k4, want_src ? R.src : nullptr, sb, wrec(Wk));
   wsync<W>();
   R.src_valid = want_src;
@@ -2082,6 +2156,8 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
       bool more = true;
       if (R.target_is_switch) {
         apply_switch<W>(C, M, Wk, R);
+      } else if (TR && !R.tgt_out) {  // a source-time stop of the transfer path: no output
+        stop_reached(C, R);
       } else {
         if (!R.src_valid) {
           rhs<TR, W>(C, M, R.tau, row(Wk, R.sy), row(Wk, R.syt), R.src, sbins(Wk), wrec(Wk));
@@ -2101,6 +2177,7 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
           }
         }
         R.j++;
+        if (TR && R.stops) stop_reached(C, R);
       }
       int guard = 0;
       for (;;) {

@@ -184,21 +184,16 @@ def get_results_stream(batches, lmax_out=None):
                     pass
 
 
-def _split(p):
-    """(CMB-only copy, transfer-only copy) of a CAMBparams asking for both."""
-    cmb, tr = copy.deepcopy(p), copy.deepcopy(p)
-    cmb.WantTransfer = False
-    tr.WantCls = False
-    return cmb, tr
-
-
 def _run_both(params_list, lmax_out):
-    """WantCls and WantTransfer together: the CMB spectra and the matter transfer
-    functions as two batches (each as with the other request off), merged into one
-    CAMBdataMatter per cosmology."""
-    cmbs, trs = zip(*[_split(p) for p in params_list])
-    cmb_out = _run(list(cmbs), lmax_out)
-    tr_out = _run_transfer(list(trs))
+    """WantCls and WantTransfer together (CalcScalarSources with WantTransfer, then
+    TransferOut): the library runs the request in two halves from the same host tables --
+    the CMB half (source modes at the run's tolerance, /100 for high-precision transfers,
+    kept evolving to the last transfer time) and the transfer half (the source k grid
+    followed by the transfer grid beyond it, the source modes stopping at every source time
+    as the reference's single evolution does) -- merged into one CAMBdataMatter per
+    cosmology."""
+    cmb_out = _run(params_list, lmax_out)
+    tr_out = _run_transfer(params_list)
     out = []
     for p, c, t in zip(params_list, cmb_out, tr_out):
         r = CAMBdataMatter(p, t.get_matter_transfer_data())

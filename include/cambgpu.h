@@ -161,6 +161,14 @@ typedef struct CambGpuTables {
     int want_cls;
     int transfer_high_precision;       /* Transfer%high_precision with transfers requested */
     double late_phot_switch_boost_min; /* 2 for high-precision transfers (equations.f90:318-320), else 0 */
+    /* A run that wants the CMB and transfer functions keeps evolving its source modes, and
+     * storing their sources, at late times until tau passes this time, the last transfer
+     * time (CalcScalarSources, cmbmain.f90:1032-1035); -1 otherwise. */
+    double src_keep_tau;
+    /* The transfer half of such a run: its first transfer_source_modes modes are the source
+     * grid's, which stop at every source time as well, in CalcScalarSources' order
+     * (cmbmain.f90:1020-1070); 0 otherwise. */
+    int transfer_source_modes;
 } CambGpuTables;
 
 /* Fills p with the reference's defaults (model.f90:36-209, Python set_params). */
@@ -172,6 +180,11 @@ void cambgpu_default_params(CambGpuParams* p);
  * SetkValuesForInt (cmbmain.f90:1267-1349) and InitSpherBessels (bessels.f90:64-112). */
 int cambgpu_tables_create(const CambGpuParams* p, void** handle);
 int cambgpu_tables_view(void* handle, CambGpuTables* view);
+/* The transfer-function half of a handle whose parameters want the CMB and transfer
+ * functions (want_cls = want_transfer = 1): the source k grid followed by the transfer
+ * grid's points above it (InitTransfer with WantCls, cmbmain.f90:681-699), transfer_only
+ * set for the device's transfer path; code 2 for any other handle. */
+int cambgpu_tables_transfer_view(void* handle, CambGpuTables* view);
 void cambgpu_tables_destroy(void* handle);
 /* Background quantities for checks: tau0, DMt0, taurst, taurend, tau_maxvis,
  * zre (reionization mid redshift), x_e(z) at the requested redshifts. */

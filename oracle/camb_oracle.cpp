@@ -1108,7 +1108,7 @@ void calc_scalar_sources(const Ctx& C, int q_ix, double* LinearSrc, ModeStats& s
   double sources[8];
   for (int j = 2; j <= T->ntau; ++j) {
     double tauend = T->tau_points[j - 1];
-    if (EV.q * tauend > T->max_etak_scalar && tauend > T->taurend && !T->want_late_time) {
+    if (EV.q * tauend > T->max_etak_scalar && tauend > T->taurend && !T->want_late_time && tau > T->src_keep_tau) {
       for (int s_ = 0; s_ < nsrc; ++s_) LinearSrc[((size_t)(j - 1) * nsrc + s_) * nk + q_ix] = 0;
     } else {
       if (!evolve_scal(C, EV, tau, y, tauend, tol1, ind, s, w, st)) return;
@@ -1117,6 +1117,86 @@ void calc_scalar_sources(const Ctx& C, int q_ix, double* LinearSrc, ModeStats& s
       derivs(C, EV, EV.ScalEqsToPropagate, tau, y.data(), yprime.data());
       EV.OutputSources = nullptr;
       for (int s_ = 0; s_ < nsrc; ++s_) LinearSrc[((size_t)(j - 1) * nsrc + s_) * nk + q_ix] = sources[s_];
+    }
+  }
+}
+
+// outtransf (equations.f90:2256-2271) at the current state: the 13 transfer variables in
+// single precision, the entries after k/h divided by k^2 after the float store
+static void store_transfer(const Ctx& C, EvolutionVars& EV, double tau, std::vector<double>& y, float* o) {
+  double O[13];
+  std::vector<double> yprime(EV.nvar + 2, 0.0);
+  EV.OutputTransfer = O;
+  derivs(C, EV, EV.ScalEqsToPropagate, tau, y.data(), yprime.data());
+  EV.OutputTransfer = nullptr;
+  o[0] = (float)O[0];
+  for (int v = 1; v < 13; ++v) {
+    float f = (float)O[v];
+    o[v] = (float)(f / EV.k2_buf);
+  }
+}
+
+// CalcScalarSources with WantTransfer (cmbmain.f90:998-1074), the reference's form of a run
+// that wants the CMB and transfer functions: the source mode also stops at every transfer
+// time (before the second source time, or inside the source interval that contains it) and
+// stores the transfer variables there as TransferData(:, q_ix, itf) of the transfer half
+// `Ttr` (its first nk entries are the source grid); it keeps evolving at late times until
+// the last transfer time.
+void calc_sources_and_transfers(const Ctx& C, const CambGpuTables* Ttr, int q_ix, double* LinearSrc, float* tr,
+                                ModeStats& st) {
+  const CambGpuTables* T = C.T;
+  C_ = &C;
+  EvolutionVars EV{};
+  EV.q = T->q_evolve[q_ix];
+  EV.q2 = EV.q * EV.q;
+  EV.OutputSources = nullptr;
+  EV.OutputTransfer = nullptr;
+  double taustart = tau_start(T, EV.q);
+  const CambGpuModeSpec& ms = T->modes[q_ix];
+  get_num_eqns(C, EV, ms);
+  setup_indices(EV, true);
+  for (int i = 0; i < T->nu_eig; ++i) EV.MassiveNuApproxTime[i] = ms.nu_approx_time[i];
+  std::vector<double> w[10];
+  for (int j = 1; j <= 9; ++j) w[j].assign(EV.nvar + 2, 0.0);
+  std::vector<double> y(EV.nvar + 2, 0.0);
+  initial(C, EV, y, taustart);
+  double tau = taustart;
+  int ind = 1;
+  RKSettings s;
+  const double tol1 = T->tol1;
+  const int nsrc = T->nsrc, nk = T->nk, ntau = T->ntau;
+  const int ntr = Ttr->num_transfer_times, trk = Ttr->nk;
+  const double* TT = Ttr->transfer_times;
+  auto out_tr = [&](int itf) { store_transfer(C, EV, tau, y, tr + ((size_t)itf * trk + q_ix) * 13); };
+  int itf = 0;
+  while (itf < ntr && T->tau_points[1] > TT[itf]) {
+    if (!evolve_scal(C, EV, tau, y, TT[itf], tol1, ind, s, w, st)) return;
+    out_tr(itf);
+    ++itf;
+  }
+  double sources[8];
+  for (int j = 2; j <= ntau; ++j) {  // the reference's 1-based time index
+    const double tauend = T->tau_points[j - 1];
+    if (EV.q * tauend > T->max_etak_scalar && tauend > T->taurend && !T->want_late_time && tau > TT[ntr - 1]) {
+      for (int s_ = 0; s_ < nsrc; ++s_) LinearSrc[((size_t)(j - 1) * nsrc + s_) * nk + q_ix] = 0;
+      continue;
+    }
+    if (!evolve_scal(C, EV, tau, y, tauend, tol1, ind, s, w, st)) return;
+    std::vector<double> yprime(EV.nvar + 2, 0.0);
+    EV.OutputSources = sources;
+    derivs(C, EV, EV.ScalEqsToPropagate, tau, y.data(), yprime.data());
+    EV.OutputSources = nullptr;
+    for (int s_ = 0; s_ < nsrc; ++s_) LinearSrc[((size_t)(j - 1) * nsrc + s_) * nk + q_ix] = sources[s_];
+    bool again = true;  // the reference's `goto 101`
+    while (again && itf < ntr) {
+      again = false;
+      if (j < ntau && tauend < TT[itf] && T->tau_points[j] > TT[itf])
+        if (!evolve_scal(C, EV, tau, y, TT[itf], tol1, ind, s, w, st)) return;
+      if (std::fabs(tau - TT[itf]) < 1e-5 || j == ntau) {
+        out_tr(itf);
+        ++itf;
+        if (j < ntau && itf < ntr && T->tau_points[j] > TT[itf]) again = true;
+      }
     }
   }
 }
@@ -1235,6 +1315,33 @@ int oracle_evolve_transfer(const CambGpuTables* T, float* out, int nthreads, lon
     ModeStats st;
     calc_transfer(C, i, out, st);
     if (evals) evals[i] = st.evals;
+    if (st.status) {
+#pragma omp critical
+      status = st.status;
+    }
+  }
+  return status;
+}
+
+// A run that wants the CMB and transfer functions, as the reference computes it: the
+// source modes of `Tcmb` by CalcScalarSources with the transfer stops, the transfer
+// half's modes above the source grid by TransferOut (cmbmain.f90:182-221).
+// LinearSrc: [ntau][nsrc][Tcmb->nk]; tr: [num_transfer_times][Ttr->nk][13].
+int oracle_evolve_combined(const CambGpuTables* Tcmb, const CambGpuTables* Ttr, double* LinearSrc, float* tr,
+                           int nthreads) {
+  if (Tcmb->transfer_only || !Ttr->transfer_only || Ttr->num_transfer_times < 1 || Ttr->nk < Tcmb->nk)
+    return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  Ctx C, Ct;
+  init_ctx(C, Tcmb);
+  init_ctx(Ct, Ttr);
+  int status = 0;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  const int nsrc_k = Tcmb->nk, ntot = Ttr->nk;
+#pragma omp parallel for schedule(dynamic)
+  for (int i = ntot - 1; i >= 0; --i) {
+    ModeStats st;
+    if (i < nsrc_k) calc_sources_and_transfers(C, Ttr, i, LinearSrc, tr, st);
+    else calc_transfer(Ct, i, tr, st);
     if (st.status) {
 #pragma omp critical
       status = st.status;

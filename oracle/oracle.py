@@ -42,8 +42,13 @@ def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _view(tables):
+    """A Tables handle's view, or a CambGpuTables view itself (the transfer half)."""
+    return tables.view if hasattr(tables, "view") else tables
+
+
 def evolve_sources(tables, nthreads=0, k_range=None, with_evals=False):
-    v = tables.view
+    v = _view(tables)
     out = np.zeros((v.ntau, v.nsrc, v.nk))
     evals = np.zeros(v.nk, dtype=np.int64)
     lo, hi = k_range if k_range else (0, v.nk)
@@ -118,7 +123,7 @@ def lens_cls(all_cls, ls, max_l, lmin=2, lens_output_margin=200, lens_accuracy_b
 
 def evolve_transfer(tables, nthreads=0, with_evals=False):
     """GetTransfer for every transfer k: [ntimes][nk][13] float32 (TransferData order)."""
-    v = tables.view
+    v = _view(tables)
     lib = load()
     lib.oracle_evolve_transfer.restype = C.c_int
     lib.oracle_evolve_transfer.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_long)]
@@ -131,9 +136,27 @@ def evolve_transfer(tables, nthreads=0, with_evals=False):
     return (out, evals) if with_evals else out
 
 
+def evolve_combined(tables, nthreads=0):
+    """The reference's run that wants the CMB and transfer functions (CalcScalarSources with
+    the transfer stops, then TransferOut above the source grid): (LinearSrc [ntau][nsrc][nk]
+    of the CMB view, TransferData [ntimes][nk_transfer][13] of the transfer half)."""
+    v, t = tables.view, tables.transfer_view()
+    lib = load()
+    lib.oracle_evolve_combined.restype = C.c_int
+    lib.oracle_evolve_combined.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_float),
+                                           C.c_int]
+    src = np.zeros((v.ntau, v.nsrc, v.nk))
+    tr = np.zeros((t.num_transfer_times, t.nk, 13), dtype=np.float32)
+    rc = lib.oracle_evolve_combined(C.addressof(v), C.addressof(t), _dp(src), tr.ctypes.data_as(C.POINTER(C.c_float)),
+                                    nthreads)
+    if rc:
+        raise RuntimeError(f"oracle combined evolution failed: {rc}")
+    return src, tr
+
+
 def sigma8(tables, tr):
     """Transfer_Get_sigmas at R = 8 Mpc/h: (sigma8, sigma2_vdelta_8) per transfer time."""
-    v = tables.view
+    v = _view(tables)
     lib = load()
     lib.oracle_sigma8.restype = None
     lib.oracle_sigma8.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double),

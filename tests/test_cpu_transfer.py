@@ -46,11 +46,69 @@ def test_transfer_grid_and_outputs(run):
     assert s8[0] < s8[1] < s8[2]
 
 
-def test_transfer_with_cmb_is_rejected():
-    p, _ = sigma8_known_answer()
+def combined_known_answer():
+    """The testPowers cosmology as the reference runs it there: the CMB on (lmax 2500,
+    max_eta_k 5000) with high-precision transfer functions at z = 3.1, 0.17, 0."""
+    p, g = sigma8_known_answer()
     p.want_cls = 1
+    p.max_l, p.max_eta_k = 2500, 5000
+    return p, g
+
+
+@pytest.fixture(scope="module")
+def combined():
+    p, g = combined_known_answer()
+    T = _lib.Tables(p)
+    src, tr = orc.evolve_combined(T)
+    return T, src, tr, g
+
+
+def test_cmb_with_transfers_tables(combined):
+    """A run that wants the CMB and transfer functions: the CMB half carries the /100
+    tolerance and the 20-per-e-fold source grid of high-precision transfers
+    (cmbmain.f90:875-893, 1018-1021) and keeps its modes to the last transfer time; the
+    transfer half is the source grid followed by the transfer grid above it (InitTransfer with
+    WantCls, cmbmain.f90:681-699), its source modes flagged to stop at the source times."""
+    T, _, _, _ = combined
+    v, t = T.view, T.transfer_view()
+    p0, _ = combined_known_answer()
+    p0.want_transfer = 0
+    T0 = _lib.Tables(p0)
+    assert v.tol1 == pytest.approx(T0.view.tol1 / 100) and v.nk > T0.view.nk
+    q = T.q_evolve
+    qt = np.ctypeslib.as_array(t.q_evolve, shape=(t.nk,))
+    assert t.transfer_only == 1 and t.want_cls == 1 and t.transfer_source_modes == v.nk
+    assert np.array_equal(qt[: v.nk], q) and np.all(qt[v.nk:] > q[-1] + 1e-4) and np.all(np.diff(qt) > 0)
+    assert v.src_keep_tau == t.transfer_times[t.num_transfer_times - 1]
+    assert T0.view.src_keep_tau == -1 and T0.view.transfer_source_modes == 0
     with pytest.raises(_lib.CAMBError):
-        _lib.Tables(p)
+        T0.transfer_view()
+
+
+def test_cmb_with_transfers_known_answers(combined):
+    """testPowers is this run: the exact restatement of it (the source modes stopping at the
+    transfer times inside CalcScalarSources, TransferOut above the source grid) meets the
+    sigma8 and f sigma8 known answers to places=3 (and within 1e-4)."""
+    T, _, tr, g = combined
+    s8, sv = orc.sigma8(T.transfer_view(), tr)
+    fs8 = sv / s8
+    for got, key in [(s8[0], "s8_z3.1"), (s8[2], "s8_z0"), (fs8[0], "fs8_z3.1"), (fs8[2], "fs8_z0")]:
+        want, places = g[key]
+        assert round(abs(got - want), places) == 0, (key, got, want)
+        assert abs(got - want) < 1e-4, (key, got, want)
+
+
+def test_cmb_half_matches_the_single_evolution(combined):
+    """The library's CMB half evolves the source modes without the transfer stops.  At the
+    high-precision tolerance its sources differ from the reference's single evolution by
+    under 1e-9 of each mode's peak (measured 4.8e-11) and the C_l by under 1e-10."""
+    T, src, _, _ = combined
+    src_h = orc.evolve_sources(T)
+    peak = np.abs(src).max(axis=(0, 1), keepdims=True)
+    assert np.max(np.abs(src_h - src) / np.maximum(peak, 1e-300)) < 1e-9
+    cl = orc.cls(T, orc.los(T, src))
+    cl_h = orc.cls(T, orc.los(T, src_h))
+    assert np.max(np.abs(cl_h[:, :2] / cl[:, :2] - 1)) < 1e-10
 
 
 def test_matter_power_known_answers():

@@ -90,18 +90,60 @@ def test_python_surface_sigma8():
     assert round(abs(pks[-1][-3] - 51.924), 2) == 0 and round(abs(pk[-2][-4] - 56.454), 2) == 0
 
 
+def combined_known_answer():
+    """testPowers as the reference runs it: the CMB on (lmax 2500, max_eta_k 5000) with
+    high-precision transfer functions at z = 3.1, 0.17, 0."""
+    p, g = sigma8_known_answer()
+    p.want_cls = 1
+    p.max_l, p.max_eta_k = 2500, 5000
+    return p, g
+
+
+def test_cmb_with_transfers_match_the_oracle():
+    """A run that wants the CMB and transfer functions.  Transfer half on the GPU (the source
+    grid plus the transfer grid above it; source modes stopping at every source time)
+    against the oracle's single evolution of the whole run (CalcScalarSources with the
+    transfer stops, TransferOut above): each variable within 1e-5 of its peak over k,
+    sigma8 within 1e-6, and the known answers.  CMB half on the GPU (source modes at the
+    /100 tolerance, kept to the last transfer time, no transfer stops) against the oracle's
+    same form on the same tables: sources within 1e-6 of their peak."""
+    p, g = combined_known_answer()
+    T = _lib.Tables(p)
+    t = T.transfer_view()
+    src, ref = orc.evolve_combined(T)
+    rs8, rsv = orc.sigma8(t, ref)
+    tr, nq, s8, sv = gpu_transfer([p])
+    assert nq[0] == t.nk and t.transfer_source_modes == T.view.nk
+    got = tr[0, :, : nq[0]]
+    peak = np.max(np.abs(ref), axis=1, keepdims=True)
+    assert np.max(np.abs(got - ref) / np.where(peak > 0, peak, 1)) < 1e-5
+    assert np.max(np.abs(s8[0] / rs8 - 1)) < 1e-6
+    assert np.max(np.abs(sv[0] / rsv - 1)) < 1e-6
+    fs8 = sv[0] / s8[0]
+    for got_v, key in [(s8[0][0], "s8_z3.1"), (s8[0][2], "s8_z0"), (fs8[0], "fs8_z3.1"), (fs8[2], "fs8_z0")]:
+        want, places = g[key]
+        assert round(abs(got_v - want), places) == 0, (key, got_v, want)
+    gs = T.evolve_sources_gpu()
+    cpu = orc.evolve_sources(T)  # the same form: no transfer stops
+    num = np.max(np.abs(gs - cpu), axis=0)
+    den = np.max(np.abs(cpu), axis=0)
+    m = den > 0
+    assert np.max(num[m] / den[m]) < 1e-6
+
+
 def test_python_surface_cmb_and_matter_power_together():
     """set_matter_power with the CMB on (the reference's usual call): one result object
-    carries both; each part equals the run that asks for it alone."""
+    carries both halves of the run, each equal to its C-ABI call on the same parameters
+    (C_l through cambgpu_get_spectra_batch, sigma8 through cambgpu_get_transfer_batch)."""
     from camb_gb300 import model, results
     cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.06, As=2.1e-9, ns=0.965, lmax=800,
                           DoLensing=False)
     cp.set_matter_power(redshifts=[0.0], kmax=1.0)
     both = results.get_results(cp)
-    cmb_only, tr_only = results._split(cp)
-    want_cls = results.get_results(cmb_only).get_unlensed_scalar_cls(800)
+    want_cls = results._run([cp], 800)[0].get_unlensed_scalar_cls(800)
     assert np.array_equal(both.get_unlensed_scalar_cls(800), want_cls)
-    assert both.get_sigma8()[0] == results.get_results(tr_only).get_sigma8()[0]
+    _, _, s8, _ = gpu_transfer([cp.to_struct()])
+    assert both.get_sigma8()[0] == s8[0][0]
     assert 0.7 < both.get_sigma8()[0] < 0.9
 
 
