@@ -171,7 +171,10 @@ def get_results_stream(batches, lmax_out=None):
                     fut = ex.submit(_prepare, nxt)
                 try:
                     lmax = max(p.max_l for p in cur) if lmax_out is None else lmax_out
-                    out = _run_prepared(handle, cur, lmax)
+                    if any(p.WantTransfer for p in cur):  # transfer functions: the batch path
+                        out = get_results_batch(cur, lmax)
+                    else:
+                        out = _run_prepared(handle, cur, lmax)
                 finally:
                     lib.cambgpu_free_prepared(handle)
                 yield out
