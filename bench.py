@@ -106,8 +106,8 @@ def hbm_peak():
 
 
 def stream_steps(lib, arr, n, steps, lmax, cls, st):
-    """steps batches through the C ABI, the host tables of batch k+1 built on a host thread
-    while batch k is staged, run and read back."""
+    """steps batches through the C ABI, the host tables of batch k+1 built (and those of
+    batch k released) on a host thread while batch k is staged, run and read back."""
     from concurrent.futures import ThreadPoolExecutor
     from camb_gb300 import _lib
 
@@ -126,7 +126,7 @@ def stream_steps(lib, arr, n, steps, lmax, cls, st):
             try:
                 _lib.check(lib.cambgpu_get_spectra_prepared(h, lmax, _lib.dptr(cls), None, None, None, _lib.iptr(st)))
             finally:
-                lib.cambgpu_free_prepared(h)
+                ex.submit(lib.cambgpu_free_prepared, h)  # released on the host thread too
 
 
 def gradient_rate(n=64, lmax=2500, seed=3000, mnu_max=0.2):

@@ -152,8 +152,8 @@ def _prepare(params_list):
 
 def get_results_stream(batches, lmax_out=None):
     """get_results_batch over a sequence of batches, pipelined: while the device runs one
-    batch, a host thread builds the next batch's tables (cambgpu_prepare_tables).  Yields
-    each batch's list of CAMBdata in order."""
+    batch, a host thread builds the next batch's tables (cambgpu_prepare_tables) and
+    releases the previous batch's.  Yields each batch's list of CAMBdata in order."""
     from concurrent.futures import ThreadPoolExecutor
     lib = _lib.load()
     it = iter(batches)
@@ -176,7 +176,7 @@ def get_results_stream(batches, lmax_out=None):
                     else:
                         out = _run_prepared(handle, cur, lmax)
                 finally:
-                    lib.cambgpu_free_prepared(handle)
+                    ex.submit(lib.cambgpu_free_prepared, handle)  # released on the host thread
                 yield out
                 cur = nxt
         finally:
