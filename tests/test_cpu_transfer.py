@@ -145,6 +145,32 @@ def test_matter_power_known_answers():
             np.testing.assert_allclose(one[zi, 0], pk2[zi, j], rtol=1e-5)
 
 
+def test_matter_power_known_answers_with_the_cmb_on():
+    """The same P(k) known answers from the run testPowers actually makes (the CMB on, lmax
+    2500): the exact restatement of that single evolution, on its transfer grid (the 20
+    per e-fold source grid followed by the transfer grid above it)."""
+    import json
+    import os
+    from camb_gb300 import model, results
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))["matter_power"]
+    cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.07, As=2e-9, ns=0.965, lmax=2500,
+                          DoLensing=False)
+    cp.Reion.set_zrei(10)
+    cp.set_matter_power(redshifts=[0.0, 0.17, 3.1], kmax=1.2)
+    T = _lib.Tables(cp.to_struct())
+    t = T.transfer_view()
+    _, tr = orc.evolve_combined(T)
+    td = np.ascontiguousarray(tr.transpose(2, 1, 0))
+    s8, sv = orc.sigma8(t, tr)
+    r = results.CAMBdataMatter(cp, results.MatterTransferData(td, td[0, :, 0] * cp.H0 / 100, s8, sv))
+    _, _, pk = r.get_matter_power_spectrum(1e-4, 1, 20)
+    _, _, pk2 = r.get_linear_matter_power_spectrum()
+    for got, key in [(pk[g["splined"]["index"][0], g["splined"]["index"][1]], "splined"),
+                     (pk2[g["unsplined"]["index"][0], g["unsplined"]["index"][1]], "unsplined")]:
+        want, places = g[key]["value"]
+        assert round(abs(got - want), places) == 0, (key, got, want)
+
+
 def test_matter_power_interpolator():
     """get_matter_power_interpolator on the oracle's transfer functions: through the
     transfer-grid power at every node, within 2e-3 of the log-grid spline between nodes at
