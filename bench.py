@@ -427,9 +427,9 @@ def single_configs(nthreads):
     against the CPU restatement on the host cores, both with their host tables: the
     plain massless lmax 1000 case; one 0.06 eV neutrino with lensed TT/EE/BB/TE and the
     lensing potential to lmax 2500, at max_eta_k = 2.5 (lmax + 200) and at the reference's
-    automatic lens_potential_accuracy 4 (max_eta_k = 72000, linear lensing); and that
+    automatic lens_potential_accuracy 4 (max_eta_k = 72000, linear lensing); that
     cosmology's matter transfer functions to kmax = 10 h/Mpc at z = 0 (computed without the
-    CMB)."""
+    CMB); and a run that wants the CMB and high-precision transfer functions together."""
     from camb_gb300 import _lib
     from oracle import oracle as orc
     lib = _lib.load()
@@ -505,6 +505,40 @@ def single_configs(nthreads):
     c, s8c = timed(cpu_tr, p, reps=1)
     out["transfer_kmax10h_mnu0.06_z0"] = {"gpu_ms": g, "cpu_ms": c, "cpu_threads": nthreads, "sigma8_gpu": s8g,
                                            "sigma8_cpu": s8c}
+
+    # the CMB and high-precision transfer functions in one run (set_matter_power with the CMB
+    # on: z = 3.1, 0.17, 0 to k = 1.2 /Mpc, testPowers' run): the GPU's two halves through
+    # the C ABI against the CPU restatement of the reference's single evolution
+    def both_params():
+        p = base(2500, False, 0.07)
+        p.want_transfer, p.transfer_high_precision, p.transfer_kmax = 1, 1, 1.2
+        p.num_transfer_redshifts = 3
+        for i, z in enumerate((3.1, 0.17, 0.0)):
+            p.transfer_redshifts[i] = z
+        return p
+
+    def gpu_both(p):
+        gpu_cmb(p)
+        tr = np.zeros((1, 3, 1024, 13), dtype=np.float32)
+        nq = (C.c_int * 1)()
+        s8 = np.zeros(3)
+        sv = np.zeros(3)
+        st = (C.c_int * 1)()
+        _lib.check(lib.cambgpu_get_transfer_batch(C.byref(p), 1, 1024, tr.ctypes.data_as(C.POINTER(C.c_float)), nq,
+                                                  _lib.dptr(s8), _lib.dptr(sv), st))
+        return s8[2]
+
+    def cpu_both(p):
+        T = _lib.Tables(p)
+        src, tr = orc.evolve_combined(T, nthreads)
+        orc.interpolate_cls(T.ls, orc.cls(T, orc.los(T, src, nthreads)), T.view.cl_template_scale)
+        return orc.sigma8(T.transfer_view(), tr)[0][2]
+
+    p = both_params()
+    g, s8g = timed(gpu_both, p)
+    c, s8c = timed(cpu_both, p, reps=1)
+    out["lmax2500_mnu0.07_with_transfers_3z_kmax1.2"] = {"gpu_ms": g, "cpu_ms": c, "cpu_threads": nthreads,
+                                                         "sigma8_z0_gpu": s8g, "sigma8_z0_cpu": s8c}
     return out
 
 
