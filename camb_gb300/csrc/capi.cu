@@ -469,6 +469,28 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
     u.tdpf[i] = (float)t.tau_dpoints[i];
   }
   d.tau_dist = (const double*)put(u.tdist.data(), (size_t)t.ntau * 8);
+  // the time grid's runs of uniform spacing (SetTimeSteps adds a few uniform ranges), for the
+  // mixed projection's window ends
+  {
+    const double* x = t.tau_points;
+    int k = 0;
+    d.ntseg = 0;
+    while (k < t.ntau - 1) {
+      const double h = x[k + 1] - x[k];
+      int e = k + 1;
+      while (e < t.ntau - 1 && std::fabs((x[e + 1] - x[e]) - h) <= 1e-6 * h) ++e;
+      if (d.ntseg == cgdev::kTimeSegMax) {
+        d.ntseg = 0;
+        break;
+      }
+      d.tseg_x0[d.ntseg] = x[k];
+      d.tseg_inv_h[d.ntseg] = (e - k) / (x[e] - x[k]);
+      d.tseg_i0[d.ntseg] = k;
+      d.tseg_n[d.ntseg] = e - k;
+      ++d.ntseg;
+      k = e;
+    }
+  }
   d.tau_dpf = (const float*)put(u.tdpf.data(), (size_t)t.ntau * 4);
   d.modes = (const CambGpuModeSpec*)put(t.modes, (size_t)t.nk * sizeof(CambGpuModeSpec));
   d.q_evolve = (const double*)put(t.q_evolve, (size_t)t.nk * 8);

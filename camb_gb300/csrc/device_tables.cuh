@@ -10,6 +10,7 @@
 namespace cgdev {
 
 constexpr int kBessSegMax = 8;
+constexpr int kTimeSegMax = 8;
 
 struct DevCosmo {
   // background
@@ -82,6 +83,10 @@ struct DevCosmo {
   double seg_inv_h[kBessSegMax];
   int seg_i0[kBessSegMax];      // grid index of the first point
   int seg_n[kBessSegMax];       // intervals in the run
+  // the source time grid as runs of uniform spacing (ntseg = 0: more than kTimeSegMax)
+  int ntseg;
+  double tseg_x0[kTimeSegMax], tseg_inv_h[kTimeSegMax];
+  int tseg_i0[kTimeSegMax], tseg_n[kTimeSegMax];
   int num_xx;
   // settings
   int nsrc, want_late_time;

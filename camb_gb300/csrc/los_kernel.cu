@@ -132,6 +132,27 @@ __device__ int source_row_count(const DevCosmo& C, double q, int* s_cnt) {
   return *s_cnt;
 }
 
+// time_index_of from the time grid's runs of uniform spacing: an FP32 estimate of the
+// interval, then FP64 comparisons against the grid points settle the exact answer (the
+// largest i with tau_i <= v, as the bisection finds it), falling back to the bisection if
+// the estimate is more than four intervals off
+__device__ __forceinline__ int time_index_runs(const DevCosmo& C, const double* __restrict__ tp, double v) {
+  const int n = C.ntau;
+  if (C.ntseg == 0) return time_index_of(tp, n, v);
+  if (v < tp[0]) return 0;
+  if (v >= tp[n - 1]) return n;
+  const float vf = (float)v;
+  int r = 0;
+  for (int t = 1; t < C.ntseg; ++t) r = vf >= (float)C.tseg_x0[t] ? t : r;
+  int i = (int)((vf - (float)C.tseg_x0[r]) * (float)C.tseg_inv_h[r]);
+  i = C.tseg_i0[r] + min(max(i, 0), C.tseg_n[r] - 1);
+  i = min(max(i, 0), n - 2);
+  for (int g = 0; g < 4 && tp[i] > v; ++g) --i;       // tp[0] <= v: stops at 0 at the latest
+  for (int g = 0; g < 4 && tp[i + 1] <= v; ++g) ++i;  // tp[n-1] > v: stops at n-2 at the latest
+  if (tp[i] > v || tp[i + 1] <= v) return time_index_of(tp, n, v);
+  return i + 1;
+}
+
 // Interval of x in the Bessel x grid from its runs of uniform spacing, in FP32: the exact
 // interval or a neighbour of it.
 __device__ __forceinline__ int bess_interval_estimate(const float* s_x0, const float* s_ih, const int* s_i0,
@@ -192,15 +213,15 @@ __device__ __forceinline__ void window_setup(const DevCosmo& C, double q, int so
         if (nsrc > 2) doint = q < (FAST ? C.l_doint[j] : max(850, l) * 3 * BessIntBoost / tau0 * 1.2);
         if (doint) {
           flag |= F_INT;
-          ns = time_index_of(tp, ntau, tmin);
-          ne = min(source_steps, time_index_of(tp, ntau, tmax));
+          ns = FAST ? time_index_runs(C, tp, tmin) : time_index_of(tp, ntau, tmin);
+          ne = min(source_steps, FAST ? time_index_runs(C, tp, tmax) : time_index_of(tp, ntau, tmax));
         }
         if (nsrc > 2 && (!doint || l > limber_l)) {
           // Limber approximation for the lensing potential (cmbmain.f90:1821-1832)
           flag |= F_LIMBER;
           double xf = FAST ? tau0 - (l + 0.5) * inv_q : tau0 - (l + 0.5) / q;
           if (xf < tp[ntau - 1] && xf > tp[0]) {
-            int n = time_index_of(tp, ntau, xf);  // 1-based
+            int n = FAST ? time_index_runs(C, tp, xf) : time_index_of(tp, ntau, xf);  // 1-based
             double f = (xf - tp[n - 1]) / (tp[n] - tp[n - 1]);
             double s_lo = (n - 1 < source_steps) ? (double)s_raw3[n - 1] : 0.0;
             double s_hi = (n < source_steps) ? (double)s_raw3[n] : 0.0;
