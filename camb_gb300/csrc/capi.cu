@@ -34,6 +34,7 @@ __global__ void source_spline_f32_kernel(const DevCosmo*, const double* const*);
 __global__ void los_flat_kernel(const DevCosmo*);
 __global__ void los_flat_mixed_kernel(const DevCosmo*);
 __global__ void scal_cls_kernel(const DevCosmo*);
+__global__ void pk_weight_kernel(const DevCosmo*);
 }  // namespace cgdev
 
 using namespace cgdev;
@@ -381,6 +382,7 @@ size_t bytes_for(const CambGpuTables& t) {
   s += r((size_t)t.nq * t.nl * t.nsrc * 8) + r((size_t)t.nl * 6 * 8);
   s += 2 * r((size_t)t.nq * 8) + r((size_t)t.nl * 4) + r(5 * (size_t)t.nk * 8) + r(256) + r((size_t)t.nl * 24);
   s += r((size_t)t.ntau * 8) + r((size_t)t.ntau * 4);  // tau0 - tau_i, FP32 dtau_i
+  s += r((size_t)t.nq * 8);                            // C_l k-integral weights
   s += 3 * r((size_t)t.nqmax * 8) + r((size_t)t.nu_eig * t.nqmax * 8);  // neutrino momenta, weights, switch times
   s += r((size_t)(t.max_l + 1) * 6 * 8) + r((size_t)(t.max_l + 1) * 4 * 8);  // all-l C_l, lensed C_l
   if (t.transfer_only)
@@ -550,6 +552,7 @@ int upload(Upload& u, int* status_dev, std::vector<std::pair<void*, std::pair<co
   d.dd_src = g_rt.arena.take<double>((size_t)t.ntau * t.nsrc * t.nk);
   d.delta = g_rt.arena.take<double>((size_t)t.nq * t.nl * t.nsrc);
   d.icl = g_rt.arena.take<double>((size_t)t.nl * 6);
+  d.pk_w = g_rt.arena.take<double>((size_t)t.nq);
   d.all_cl = g_rt.arena.take<double>((size_t)(t.max_l + 1) * 6);
   if (t.transfer_only) {
     d.transfer_out = g_rt.arena.take<float>((size_t)t.num_transfer_times * t.nk * 13);
@@ -965,6 +968,10 @@ int run_los(Batch& B) {
 
 int run_cls(Batch& B) {
   int n = (int)B.views.size();
+  // the primordial-power weights once per (cosmology, q), then the k-integral per sampled l
+  pk_weight_kernel<<<dim3((B.max_nq + 255) / 256, n), 256, 0, g_rt.stream>>>(B.d_cosmos);
+  g_launches++;
+  CUDA_TRY(cudaGetLastError());
   dim3 g(B.max_nl, n);
   scal_cls_kernel<<<g, 256, 0, g_rt.stream>>>(B.d_cosmos);
   g_launches++;

@@ -67,6 +67,7 @@ struct DevCosmo {
   const double* q_int;
   const double* dq_int;
   int nq;
+  double* pk_w;  // [nq] A_s P(q) dq/q of the current primordial power (the C_l k-integral weights)
   const int* ls;
   int nl;
   const double* l_xlim;  // [nl] max(0, l - 4.2 l^(1/3))

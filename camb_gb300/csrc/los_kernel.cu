@@ -12,6 +12,7 @@
 //   los_flat_mixed_kernel the same projection with the staged sources, Bessel weights,
 //                         table and products in FP32 and compensated FP32 sums
 //                         (mixed precision).
+//   pk_weight_kernel      the primordial-power weights A_s P(q) dq/q, once per (cosmology, q).
 //   scal_cls_kernel       CalcScalCls (cmbmain.f90:3179-3343): one CTA per sampled l,
 //                         block reduction over q of P(k) Delta_X Delta_Y dlnk.
 #include <cuda_runtime.h>
@@ -533,6 +534,20 @@ __global__ void __launch_bounds__(LOS_THREADS) los_flat_mixed_kernel(const DevCo
 
 constexpr int CLS_THREADS = 256;
 
+// CalcScalCls' weight of integration wavenumber q: A_s P(q) dlnq (the primordial power of
+// InitialPower.f90:121-144 times dq/q), the same for every sampled l, so formed once per
+// (cosmology, q) instead of once per (l, q)
+__global__ void pk_weight_kernel(const DevCosmo* __restrict__ cosmos) {
+  const DevCosmo& C = cosmos[blockIdx.y];
+  for (int q_ix = blockIdx.x * blockDim.x + threadIdx.x; q_ix < C.nq; q_ix += gridDim.x * blockDim.x) {
+    const double k = C.q_int[q_ix];
+    const double dlnk = C.dq_int[q_ix] / k;
+    const double lnrat = log(k / C.pivot_scalar);
+    const double ap = C.As * exp(lnrat * (C.ns - 1 + lnrat * (C.nrun / 2)));
+    C.pk_w[q_ix] = ap * dlnk;
+  }
+}
+
 __global__ void __launch_bounds__(CLS_THREADS) scal_cls_kernel(const DevCosmo* __restrict__ cosmos) {
   const DevCosmo& C = cosmos[blockIdx.y];
   const int j = blockIdx.x;
@@ -540,12 +555,8 @@ __global__ void __launch_bounds__(CLS_THREADS) scal_cls_kernel(const DevCosmo* _
   const int nsrc = C.nsrc, nl = C.nl;
   double c[6] = {0, 0, 0, 0, 0, 0};
   for (int q_ix = threadIdx.x; q_ix < C.nq; q_ix += blockDim.x) {
-    double k = C.q_int[q_ix];
-    double dlnk = C.dq_int[q_ix] / k;
-    double lnrat = log(k / C.pivot_scalar);
-    double ap = C.As * exp(lnrat * (C.ns - 1 + lnrat * (C.nrun / 2)));
     const double* D = C.delta + ((size_t)q_ix * nl + j) * nsrc;
-    double w = ap * dlnk;
+    const double w = C.pk_w[q_ix];
     double d0 = D[0], d1 = D[1];
     c[0] += w * d0 * d0;
     c[1] += w * d1 * d1;
