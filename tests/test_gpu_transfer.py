@@ -131,6 +131,30 @@ def test_cmb_with_transfers_match_the_oracle():
     assert np.max(num[m] / den[m]) < 1e-6
 
 
+def test_cmb_with_transfers_batch_of_masses():
+    """Three such runs in one transfer launch (each cosmology its own source grid, so its
+    own number of modes that stop at the source times), each against the oracle's single
+    evolution of its run."""
+    ps = []
+    for m in (0.0, 0.06, 0.2):
+        p, _ = combined_known_answer()
+        p.mnu = m
+        p.max_l, p.max_eta_k = 1200, 3000
+        ps.append(p)
+    tr, nq, s8, _ = gpu_transfer(ps)
+    for i, p in enumerate(ps):
+        T = _lib.Tables(p)
+        t = T.transfer_view()
+        _, ref = orc.evolve_combined(T)
+        assert nq[i] == t.nk
+        got = tr[i, :, : nq[i]]
+        peak = np.max(np.abs(ref), axis=1, keepdims=True)
+        assert np.max(np.abs(got - ref) / np.where(peak > 0, peak, 1)) < 1e-5
+        rs8, _ = orc.sigma8(t, ref)
+        assert np.max(np.abs(s8[i] / rs8 - 1)) < 1e-6
+    assert s8[0][2] > s8[1][2] > s8[2][2]
+
+
 def test_python_surface_cmb_and_matter_power_together():
     """set_matter_power with the CMB on (the reference's usual call): one result object
     carries both halves of the run, each equal to its C-ABI call on the same parameters
