@@ -1708,7 +1708,8 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
 // second source time, then every source time, each followed by the transfer times inside
 // its interval (or within 1e-5 of it, or any left at the last source time -- the reference's
 // `goto 101`).  A pure function of the stop state (settling states that consume nothing);
-// run_modes advances the state when a stop is reached.  false: no stop left.
+// run_modes advances the state when a stop is reached.  false: no stop left (or, with an
+// evolution error in R.status, a state that did not settle).
 __device__ __forceinline__ bool stop_target(const DevCosmo& C, Run& R, double& tgt) {
   const double* P = C.tau_points;
   const double* TT = C.transfer_times;
@@ -1743,6 +1744,7 @@ __device__ __forceinline__ bool stop_target(const DevCosmo& C, Run& R, double& t
     R.st = 1;
     R.js = jj + 1;
   }
+  R.status = CAMBGPU_ERROR_EVOLUTION;  // not settled in four passes: not expected
   return false;
 }
 
@@ -2137,7 +2139,10 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
       }
       if (!next_target<TR>(cosmos[cosmo], M, R)) {
         R.active = false;
-        if (leader) atomicAdd(cosmos[cosmo].evals, (unsigned long long)R.evals);
+        if (leader) {
+          if (R.status) atomicExch(cosmos[cosmo].status, R.status);
+          atomicAdd(cosmos[cosmo].evals, (unsigned long long)R.evals);
+        }
         continue;
       }
     }
