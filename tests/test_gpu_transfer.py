@@ -131,6 +131,32 @@ def test_cmb_with_transfers_match_the_oracle():
     assert np.max(num[m] / den[m]) < 1e-6
 
 
+def test_cmb_with_transfers_ending_before_today():
+    """Transfer redshifts 3.1 and 1 only: the CMB half's modes keep evolving to z = 1 and
+    then take the late-time cut (src_keep_tau below tau0), the transfer half's source modes
+    stop at the source times up to z = 1; both against the oracle on the same tables
+    (sources within 1e-6 of their peak; transfers within 1e-5 of theirs)."""
+    p, _ = combined_known_answer()
+    p.num_transfer_redshifts = 2
+    p.transfer_redshifts[0], p.transfer_redshifts[1] = 3.1, 1.0
+    p.max_l, p.max_eta_k = 1500, 3750
+    T = _lib.Tables(p)
+    t = T.transfer_view()
+    assert T.view.src_keep_tau < 0.9 * T.view.tau0
+    _, ref = orc.evolve_combined(T)
+    tr, nq, _, _ = gpu_transfer([p])
+    got = tr[0, :, : nq[0]]
+    peak = np.max(np.abs(ref), axis=1, keepdims=True)
+    assert nq[0] == t.nk
+    assert np.max(np.abs(got - ref) / np.where(peak > 0, peak, 1)) < 1e-5
+    cpu = orc.evolve_sources(T)
+    gs = T.evolve_sources_gpu()
+    num = np.max(np.abs(gs - cpu), axis=0)
+    den = np.max(np.abs(cpu), axis=0)
+    m = den > 0
+    assert np.max(num[m] / den[m]) < 1e-6
+
+
 def test_cmb_with_transfers_batch_of_masses():
     """Three such runs in one transfer launch (each cosmology its own source grid, so its
     own number of modes that stop at the source times), each against the oracle's single
