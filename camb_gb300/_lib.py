@@ -106,6 +106,10 @@ SIGNATURES = {
                                               _c_double_p, _c_int_p, _c_int_p]),
     "cambgpu_get_transfer_batch": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, C.POINTER(C.c_float),
                                                _c_int_p, _c_double_p, _c_double_p, _c_int_p]),
+    "cambgpu_get_results_with_transfers": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, C.c_int, _c_double_p,
+                                                       _c_double_p, _c_double_p, _c_int_p, C.c_int,
+                                                       C.POINTER(C.c_float), _c_int_p, _c_double_p, _c_double_p,
+                                                       _c_int_p]),
     "cambgpu_lensing_range": (C.c_int, [C.POINTER(CambGpuTables), _c_int_p]),
     "cambgpu_batch_prepare": (C.c_int, [C.POINTER(CambGpuParams), C.c_int]),
     "cambgpu_batch_prepare_shared": (C.c_int, [C.POINTER(CambGpuParams), C.c_int, _c_int_p]),

@@ -1326,6 +1326,34 @@ void add_handle(Batch& B, Handle* h, bool transfer_half = false) {
   B.tgrid.push_back(&h->inv_tgrid);
 }
 
+// transfer functions and sigma8 of a transfer batch staged from hs (each its transfer half
+// when it wants the CMB too) into the caller's arrays; synchronises the stream
+int fetch_transfers(Batch& B, const std::vector<Handle*>& hs, int nz, int nq_max, float* transfer, int* nq,
+                    double* sigma8, double* sigma2_vdelta_8) {
+  std::vector<double> s8(2 * (size_t)nz);
+  for (size_t c = 0; c < hs.size(); ++c) {
+    const CambGpuTables& v = hs[c]->combined ? hs[c]->tview : hs[c]->view;
+    if (nq) nq[c] = v.nk;
+    if (transfer) {
+      for (int z = 0; z < v.num_transfer_times; ++z) {
+        float* dst = transfer + (((size_t)c * nz + z) * nq_max) * 13;
+        CUDA_TRY(cudaMemcpyAsync(dst, B.ups[c].d.transfer_out + (size_t)z * v.nk * 13, (size_t)v.nk * 13 * 4,
+                                 cudaMemcpyDeviceToHost, g_rt.stream));
+      }
+    }
+    if (sigma8 || sigma2_vdelta_8) {
+      CUDA_TRY(cudaMemcpyAsync(s8.data(), B.ups[c].d.sigma8, s8.size() * 8, cudaMemcpyDeviceToHost, g_rt.stream));
+      CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+      for (int z = 0; z < nz; ++z) {
+        if (sigma8) sigma8[c * nz + z] = s8[2 * z];
+        if (sigma2_vdelta_8) sigma2_vdelta_8[c * nz + z] = s8[2 * z + 1];
+      }
+    }
+  }
+  CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
+  return 0;
+}
+
 // the transfer-function half of a run that wants the CMB and transfer functions
 void fill_transfer_half(Handle* h, const CambGpuParams& p) {
   h->combined = p.want_transfer && p.want_cls;
@@ -1660,29 +1688,75 @@ int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float*
   g_launches++;
   rc = check_status(B, status);
   if (rc) return rc;
-  const int nz = p[0].num_transfer_redshifts;
-  std::vector<double> s8(2 * (size_t)nz);
+  return fetch_transfers(B, hs, p[0].num_transfer_redshifts, nq_max, transfer, nq, sigma8, sigma2_vdelta_8);
+}
+
+int cambgpu_get_results_with_transfers(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
+                                       double* lens_potential, int* lmax_lensed, int nq_max, float* transfer, int* nq,
+                                       double* sigma8, double* sigma2_vdelta_8, int* status) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (n < 1) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "empty batch");
+  if (lmax_out < 0 || lmax_out > 8000) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "lmax_out out of range");
   for (int c = 0; c < n; ++c) {
-    const CambGpuTables& v = half(hs[c]);
-    if (nq) nq[c] = v.nk;
-    if (transfer) {
-      for (int z = 0; z < v.num_transfer_times; ++z) {
-        float* dst = transfer + (((size_t)c * nz + z) * nq_max) * 13;
-        CUDA_TRY(cudaMemcpyAsync(dst, B.ups[c].d.transfer_out + (size_t)z * v.nk * 13, (size_t)v.nk * 13 * 4,
-                                 cudaMemcpyDeviceToHost, g_rt.stream));
-      }
-    }
-    if (sigma8 || sigma2_vdelta_8) {
-      CUDA_TRY(cudaMemcpyAsync(s8.data(), B.ups[c].d.sigma8, s8.size() * 8, cudaMemcpyDeviceToHost, g_rt.stream));
-      CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
-      for (int z = 0; z < nz; ++z) {
-        if (sigma8) sigma8[(size_t)c * nz + z] = s8[2 * z];
-        if (sigma2_vdelta_8) sigma2_vdelta_8[(size_t)c * nz + z] = s8[2 * z + 1];
-      }
-    }
+    if (!p[c].want_transfer || !p[c].want_cls)
+      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "this call needs want_cls = want_transfer = 1");
+    if (p[c].num_transfer_redshifts != p[0].num_transfer_redshifts)
+      return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "every cosmology of a transfer batch needs the same redshift count");
   }
-  CUDA_TRY(cudaStreamSynchronize(g_rt.stream));
-  return 0;
+  std::vector<Handle*> hs;
+  int rc = build_handles(p, n, hs, status);
+  struct Guard { std::vector<Handle*>& h; ~Guard() { for (auto* x : h) delete x; } } guard{hs};
+  if (rc) return rc;
+  for (auto* h : hs)
+    if (transfer && h->tview.nk > nq_max) return set_err(CAMBGPU_ERROR_UNSUPPORTED_PARAMS, "nq_max too small");
+  // the CMB sources, stored by the transfer half's launch and read by the CMB half: outside
+  // the arena, which the CMB half stages again
+  std::vector<size_t> off(n + 1, 0);
+  for (int c = 0; c < n; ++c)
+    off[c + 1] = off[c] + (size_t)hs[c]->view.ntau * hs[c]->view.nsrc * hs[c]->view.nk;
+  struct DevBuf { double* p = nullptr; ~DevBuf() { if (p) cudaFree(p); } } src;
+  rc = rt_init();
+  if (rc) return rc;
+  CUDA_TRY(cudaMalloc(&src.p, off[n] * 8));
+  CUDA_TRY(cudaMemsetAsync(src.p, 0, off[n] * 8, g_rt.stream));
+  {
+    // transfer half: the source modes evolved once, CMB sources at the source times and
+    // transfer variables at the transfer times; the transfer grid's modes above them
+    Batch B;
+    for (auto* h : hs) add_handle(B, h, true);
+    rc = stage_batch(B);
+    if (rc) return rc;
+    std::vector<DevCosmo> hc(n);
+    for (int c = 0; c < n; ++c) {
+      B.ups[c].d.src_out = src.p + off[c];
+      B.ups[c].d.src_nk = hs[c]->view.nk;
+      hc[c] = B.ups[c].d;
+    }
+    CUDA_TRY(cudaMemcpyAsync(B.d_cosmos, hc.data(), (size_t)n * sizeof(DevCosmo), cudaMemcpyHostToDevice, g_rt.stream));
+    rc = run_all(B, true, false, false);
+    if (rc) return rc;
+    CUDA_TRY(launch_sigma8(B.d_cosmos, n, g_rt.stream));
+    g_launches++;
+    rc = check_status(B, status);
+    if (rc) return rc;
+    rc = fetch_transfers(B, hs, p[0].num_transfer_redshifts, nq_max, transfer, nq, sigma8, sigma2_vdelta_8);
+    if (rc) return rc;
+  }
+  // CMB half: the sources copied in, then spline, projection, C_l, interpolation, lensing
+  Batch B;
+  for (auto* h : hs) add_handle(B, h);
+  rc = stage_batch(B, lmax_out);
+  if (rc) return rc;
+  for (int c = 0; c < n; ++c)
+    CUDA_TRY(cudaMemcpyAsync(B.ups[c].d.linear_src, src.p + off[c], (off[c + 1] - off[c]) * 8, cudaMemcpyDeviceToDevice,
+                             g_rt.stream));
+  rc = run_all(B, false, true, true);
+  if (rc) return rc;
+  rc = check_status(B, status);
+  if (rc) return rc;
+  if (lmax_lensed)
+    for (int c = 0; c < n; ++c) lmax_lensed[c] = B.ups[c].d.lensed ? B.ups[c].d.lmax_lensed : 0;
+  return fetch_spectra(B, lmax_out, unlensed, lensed, lens_potential);
 }
 
 int cambgpu_lensing_range(const CambGpuTables* t, int* out3) {

@@ -93,6 +93,8 @@ struct DevCosmo {
   int nsrc, want_late_time;
   double src_keep_tau;  // source modes keep evolving until tau passes it (runs with transfers)
   int tr_src_modes;     // transfer path: leading modes that also stop at the source times
+  double* src_out;      // and store their CMB sources there ([ntau][nsrc][src_nk]), or null
+  int src_nk;
   double max_etak_scalar, tol1, AccuracyBoost, IntTolBoost, TimeSwitchBoost, BessIntBoost, LimberBoost;
   double As, ns, nrun, pivot_scalar, Alens;
 };

@@ -951,6 +951,7 @@ struct St {
   bool tc, hk, nonu, nophot, has_nu_rel;
   bool approx[NUE], nonrel[NUE];
   double approx_time[NUE], G11[NUE], G30[NUE], lboost[NUE];
+  bool out_src;  // transfer path: the output evaluation forms the CMB sources, not outtransf's
 };
 
 // SetupScalarArrayIndices (equations.f90:585-701): the propagated variables are packed
@@ -1465,7 +1466,7 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
     const double gpres = gpres_noDE - grhov_t;
     const double diff_rhopi = pidot_sum - (4 * dgpi + dgpi_diff) * adotoa;
     const double phi = -((dgrho + 3 * dgq * adotoa * ik) + dgpi) / (2 * M.k2);
-    if constexpr (TR) {  // outtransf's variables (equations.f90:2832-2845), src holds 13
+    if (TR && !M.out_src) {  // outtransf's variables (equations.f90:2832-2845), src holds 13
       src[0] = k / C.hubble_h;
       src[1] = clxc;
       src[2] = clxb;
@@ -1600,6 +1601,7 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
   M.poltruncfac = (double)M.lmaxgpol / max(1, M.lmaxgpol - 2);
   M.kptf = M.k * M.poltruncfac;
   M.pig = M.pigdot = 0;
+  M.out_src = false;
   M.tight_off = ms.tight_switch_tau;
   M.tc = true;
   M.hk = M.nonu = M.nophot = false;
@@ -1710,42 +1712,50 @@ __device__ void mode_init(const DevCosmo& C, int q_ix, St& M, WK& Wk, Run& R) {
 // `goto 101`).  A pure function of the stop state (settling states that consume nothing);
 // run_modes advances the state when a stop is reached.  false: no stop left (or, with an
 // evolution error in R.status, a state that did not settle).
-__device__ __forceinline__ bool stop_target(const DevCosmo& C, Run& R, double& tgt) {
+__device__ __forceinline__ bool stop_target(const DevCosmo& C, St& M, Run& R, double& tgt) {
   const double* P = C.tau_points;
   const double* TT = C.transfer_times;
-  const int ntau = C.ntau;
-  for (int guard = 0; guard < 4; ++guard) {
-    if (R.st == 0) {
-      if (P[1] > TT[R.j]) {
-        tgt = TT[R.j];
-        R.tgt_out = true;
-        return true;
-      }
-      R.st = 1;
-      R.js = 1;
-    }
-    if (R.st == 1) {
-      if (R.js >= ntau) return false;
-      tgt = P[R.js];
-      R.tgt_out = false;
-      return true;
-    }
-    const int jj = R.jj;  // st 2
-    if (jj < ntau - 1 && P[jj] < TT[R.j] && P[jj + 1] > TT[R.j]) {
+  const int ntau = C.ntau, ntt = C.n_tt;
+  const bool tr_left = R.j < ntt;
+  if (!tr_left && !C.src_out) return false;  // nothing left to store
+  if (R.st == 0) {
+    if (tr_left && P[1] > TT[R.j]) {
       tgt = TT[R.j];
       R.tgt_out = true;
+      M.out_src = false;
       return true;
     }
-    if (fabs(R.tau - TT[R.j]) < 1e-5 || jj == ntau - 1) {
-      tgt = R.tau;  // output at the current state
-      R.tgt_out = true;
-      return true;
+    R.st = 1;
+    R.js = 1;
+  }
+  if (R.st == 2) {
+    const int jj = R.jj;
+    if (tr_left) {
+      if (jj < ntau - 1 && P[jj] < TT[R.j] && P[jj + 1] > TT[R.j]) {
+        tgt = TT[R.j];
+        R.tgt_out = true;
+        M.out_src = false;
+        return true;
+      }
+      if (fabs(R.tau - TT[R.j]) < 1e-5 || jj == ntau - 1) {
+        tgt = R.tau;  // output at the current state
+        R.tgt_out = true;
+        M.out_src = false;
+        return true;
+      }
     }
     R.st = 1;
     R.js = jj + 1;
   }
-  R.status = CAMBGPU_ERROR_EVOLUTION;  // not settled in four passes: not expected
-  return false;
+  if (R.js >= ntau) return false;
+  // past the last transfer time the reference's late-time cut ends the mode's sources
+  if (!tr_left && M.q * P[R.js] > C.max_etak_scalar && P[R.js] > C.taurend && !C.want_late_time &&
+      R.tau > TT[ntt - 1])
+    return false;
+  tgt = P[R.js];
+  R.tgt_out = C.src_out != nullptr;  // the CMB sources of a single launch of both halves
+  M.out_src = true;
+  return true;
 }
 
 // run_modes' step after a stop of that kind is reached (the transfer output, if any, done)
@@ -1768,10 +1778,12 @@ template <bool TR>
 __device__ bool next_target(const DevCosmo& C, St& M, Run& R) {
   double tauend;
   if constexpr (TR) {  // GetTransfer: the transfer times in turn
-    if (R.j >= C.n_tt) return false;
-    tauend = C.transfer_times[R.j];
-    R.tgt_out = true;
-    if (R.stops && !stop_target(C, R, tauend)) return false;
+    if (R.stops) {
+      if (!stop_target(C, M, R, tauend)) return false;
+    } else {
+      if (R.j >= C.n_tt) return false;
+      tauend = C.transfer_times[R.j];
+    }
   } else {
     if (R.j >= C.ntau) return false;
     tauend = C.tau_points[R.j];
@@ -2164,6 +2176,7 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
       } else if (TR && !R.tgt_out) {  // a source-time stop of the transfer path: no output
         stop_reached(C, R);
       } else {
+        const bool out_src = TR && M.out_src;  // the CMB sources at a source-time stop
         if (!R.src_valid) {
           rhs<TR, W>(C, M, R.tau, row(Wk, R.sy), row(Wk, R.syt), R.src, sbins(Wk), wrec(Wk));
           wsync<W>();
@@ -2171,7 +2184,10 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
         R.evals++;  // the output() evaluation of the reference
         const int nk = C.nk;
         if (leader) {
-          if constexpr (TR) {
+          if (out_src) {
+            const int nsrc = C.nsrc;
+            for (int s = 0; s < nsrc; ++s) C.src_out[((size_t)R.js * nsrc + s) * C.src_nk + q_ix] = R.src[s];
+          } else if constexpr (TR) {
             // TransferData is single precision: store, then divide the stored value by k^2
             float* o = C.transfer_out + ((size_t)R.j * nk + q_ix) * 13;
             o[0] = (float)R.src[0];
@@ -2181,8 +2197,13 @@ __device__ __forceinline__ void run_modes(const DevCosmo* __restrict__ cosmos, c
             for (int s = 0; s < nsrc; ++s) C.linear_src[((size_t)R.j * nsrc + s) * nk + q_ix] = R.src[s];
           }
         }
-        R.j++;
-        if (TR && R.stops) stop_reached(C, R);
+        R.src_valid = false;  // consumed (the next stop may be at the same time)
+        if (out_src) {
+          stop_reached(C, R);
+        } else {
+          R.j++;
+          if (TR && R.stops) stop_reached(C, R);
+        }
       }
       int guard = 0;
       for (;;) {

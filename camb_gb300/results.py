@@ -188,19 +188,41 @@ def get_results_stream(batches, lmax_out=None):
 
 
 def _run_both(params_list, lmax_out):
-    """WantCls and WantTransfer together (CalcScalarSources with WantTransfer, then
-    TransferOut): the library runs the request in two halves from the same host tables --
-    the CMB half (source modes at the run's tolerance, /100 for high-precision transfers,
-    kept evolving to the last transfer time) and the transfer half (the source k grid
-    followed by the transfer grid beyond it, the source modes stopping at every source time
-    as the reference's single evolution does) -- merged into one CAMBdataMatter per
+    """WantCls and WantTransfer together, as the reference's single evolution
+    (cambgpu_get_results_with_transfers: one transfer-path launch stores each source
+    mode's CMB sources at the source times and its transfer variables at the transfer
+    times; the projection and C_l follow on those sources), one CAMBdataMatter per
     cosmology."""
-    cmb_out = _run(params_list, lmax_out)
-    tr_out = _run_transfer(params_list)
+    lib = _lib.load()
+    n = len(params_list)
+    nz = params_list[0].Transfer.PK_num_redshifts
+    if any(p.Transfer.PK_num_redshifts != nz for p in params_list):
+        raise _lib.CAMBError("a transfer batch needs the same number of redshifts")
+    arr = (_lib.CambGpuParams * n)(*[p.to_struct() for p in params_list])
+    cls = np.zeros((n, lmax_out + 1, 4))
+    lens = any(p.DoLensing for p in params_list)
+    lensed = np.zeros((n, lmax_out + 1, 4)) if lens else None
+    pot = np.zeros((n, lmax_out + 1, 3)) if lens else None
+    lml = np.zeros(n, dtype=np.int32)
+    nq_max = 4096
+    tr = np.zeros((n, nz, nq_max, 13), dtype=np.float32)
+    nq = np.zeros(n, dtype=np.int32)
+    s8 = np.zeros((n, nz))
+    sv = np.zeros((n, nz))
+    st = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.cambgpu_get_results_with_transfers(
+        arr, n, lmax_out, _lib.dptr(cls), _lib.dptr(lensed) if lens else None, _lib.dptr(pot) if lens else None,
+        _lib.iptr(lml), nq_max, tr.ctypes.data_as(C.POINTER(C.c_float)), _lib.iptr(nq), _lib.dptr(s8),
+        _lib.dptr(sv), _lib.iptr(st)))
     out = []
-    for p, c, t in zip(params_list, cmb_out, tr_out):
-        r = CAMBdataMatter(p, t.get_matter_transfer_data())
-        r._cls, r._lensed, r._pot, r._lmax_lensed = c._cls, c._lensed, c._pot, c._lmax_lensed
+    for i, p in enumerate(params_list):
+        td = np.ascontiguousarray(tr[i, :, : nq[i], :].transpose(2, 1, 0))  # [13, nq, nz]
+        q = td[0, :, 0].astype(np.float64) * p.H0 / 100
+        r = CAMBdataMatter(p, MatterTransferData(td, q, s8[i], sv[i]))
+        r._cls = cls[i]
+        r._lensed = lensed[i] if lens and p.DoLensing else None
+        r._pot = pot[i] if lens and p.DoLensing else None
+        r._lmax_lensed = int(lml[i])
         out.append(r)
     return out
 

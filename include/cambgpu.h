@@ -271,6 +271,18 @@ void cambgpu_free_prepared(CambGpuPrepared* t);
 int cambgpu_get_transfer_batch(const CambGpuParams* p, int n, int nq_max, float* transfer, int* nq, double* sigma8,
                                double* sigma2_vdelta_8, int* status);
 
+/* A run that wants the CMB and transfer functions (want_cls = want_transfer = 1 for every
+ * cosmology), in the reference's single evolution: one transfer-path launch evolves each
+ * source mode once, storing its CMB sources at the source times and its transfer
+ * variables at the transfer times (CalcScalarSources with WantTransfer,
+ * cmbmain.f90:1020-1070), and the transfer grid's modes above the source grid
+ * (TransferOut, cmbmain.f90:1136-1165); the projection, C_l, interpolation and lensing then
+ * run on those sources.  Outputs as cambgpu_get_spectra_batch and
+ * cambgpu_get_transfer_batch. */
+int cambgpu_get_results_with_transfers(const CambGpuParams* p, int n, int lmax_out, double* unlensed, double* lensed,
+                                       double* lens_potential, int* lmax_lensed, int nq_max, float* transfer, int* nq,
+                                       double* sigma8, double* sigma2_vdelta_8, int* status);
+
 /* Lensing l range of a cosmology's tables: out3 = {lmax of the lensing sums
  * (LensingExtrapLmax, lensing.f90:161-177), lmax_lensed (InitLensedClArrays,
  * lensing.f90:230-247), number of theta points}. */

@@ -131,6 +131,55 @@ def test_cmb_with_transfers_match_the_oracle():
     assert np.max(num[m] / den[m]) < 1e-6
 
 
+def both_in_one_launch(ps, lmax, nq_max=2048):
+    lib = _lib.load()
+    n = len(ps)
+    nz = ps[0].num_transfer_redshifts
+    arr = (_lib.CambGpuParams * n)(*ps)
+    cls = np.zeros((n, lmax + 1, 4))
+    tr = np.zeros((n, nz, nq_max, 13), dtype=np.float32)
+    nq = np.zeros(n, dtype=np.int32)
+    s8 = np.zeros((n, nz))
+    sv = np.zeros((n, nz))
+    st = np.zeros(n, dtype=np.int32)
+    lml = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.cambgpu_get_results_with_transfers(arr, n, lmax, _lib.dptr(cls), None, None, _lib.iptr(lml), nq_max,
+                                                      tr.ctypes.data_as(C.POINTER(C.c_float)), _lib.iptr(nq),
+                                                      _lib.dptr(s8), _lib.dptr(sv), _lib.iptr(st)))
+    assert not st.any()
+    return cls, tr, nq, s8, sv
+
+
+@pytest.mark.parametrize("zs", [(3.1, 0.17, 0.0), (3.1, 1.0)])
+def test_single_launch_is_the_single_evolution(zs):
+    """cambgpu_get_results_with_transfers: one transfer-path launch stores the source modes'
+    CMB sources at the source times and their transfer variables at the transfer times.
+    Against the oracle's single evolution of the run: transfer variables within 1e-5 of
+    their peak, sigma8 within 1e-6, and the C_l of its sources (the FP64 projection) within
+    1e-5 at the sampled l -- also when the last transfer time is before today (the source
+    modes then keep storing sources to the late-time cut)."""
+    p, _ = combined_known_answer()
+    p.num_transfer_redshifts = len(zs)
+    for i, z in enumerate(zs):
+        p.transfer_redshifts[i] = z
+    p.max_l, p.max_eta_k = 1500, 3750
+    T = _lib.Tables(p)
+    t = T.transfer_view()
+    src, ref = orc.evolve_combined(T)
+    icl = orc.cls(T, orc.los(T, src))
+    rs8, _ = orc.sigma8(t, ref)
+    cls, tr, nq, s8, _ = both_in_one_launch([p], 1500)
+    assert nq[0] == t.nk
+    got = tr[0, :, : nq[0]]
+    peak = np.max(np.abs(ref), axis=1, keepdims=True)
+    assert np.max(np.abs(got - ref) / np.where(peak > 0, peak, 1)) < 1e-5
+    assert np.max(np.abs(s8[0] / rs8 - 1)) < 1e-6
+    g = cls[0][T.ls]
+    assert np.max(np.abs(g[:, 0] / icl[:, 0] - 1)) < 1e-5
+    assert np.max(np.abs(g[:, 1] / icl[:, 1] - 1)) < 1e-5
+    assert np.max(np.abs(g[:, 3] - icl[:, 2]) / np.sqrt(icl[:, 0] * icl[:, 1])) < 1e-5
+
+
 def test_cmb_with_transfers_ending_before_today():
     """Transfer redshifts 3.1 and 1 only: the CMB half's modes keep evolving to z = 1 and
     then take the late-time cut (src_keep_tau below tau0), the transfer half's source modes
@@ -182,18 +231,22 @@ def test_cmb_with_transfers_batch_of_masses():
 
 
 def test_python_surface_cmb_and_matter_power_together():
-    """set_matter_power with the CMB on (the reference's usual call): one result object
-    carries both halves of the run, each equal to its C-ABI call on the same parameters
-    (C_l through cambgpu_get_spectra_batch, sigma8 through cambgpu_get_transfer_batch)."""
+    """set_matter_power with the CMB on (the reference's usual call): one result object with
+    the C_l and the transfer functions of the single launch, equal to that C-ABI call on
+    the same parameters; the two-call form (CMB half without the transfer stops) agrees to
+    1e-7 in the C_l and exactly in sigma8."""
     from camb_gb300 import model, results
     cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.06, As=2.1e-9, ns=0.965, lmax=800,
                           DoLensing=False)
     cp.set_matter_power(redshifts=[0.0], kmax=1.0)
     both = results.get_results(cp)
-    want_cls = results._run([cp], 800)[0].get_unlensed_scalar_cls(800)
-    assert np.array_equal(both.get_unlensed_scalar_cls(800), want_cls)
-    _, _, s8, _ = gpu_transfer([cp.to_struct()])
-    assert both.get_sigma8()[0] == s8[0][0]
+    cls, _, _, s8, _ = both_in_one_launch([cp.to_struct()], 800)
+    assert np.array_equal(both._cls, cls[0]) and both.get_sigma8()[0] == s8[0][0]
+    two = results._run([cp], 800)[0].get_unlensed_scalar_cls(800)
+    one = both.get_unlensed_scalar_cls(800)
+    assert np.max(np.abs(one[2:, :2] / two[2:, :2] - 1)) < 1e-7
+    _, _, s8t, _ = gpu_transfer([cp.to_struct()])
+    assert both.get_sigma8()[0] == s8t[0][0]
     assert 0.7 < both.get_sigma8()[0] < 0.9
 
 
