@@ -507,7 +507,7 @@ def single_configs(nthreads):
                                            "sigma8_cpu": s8c}
 
     # the CMB and high-precision transfer functions in one run (set_matter_power with the CMB
-    # on: z = 3.1, 0.17, 0 to k = 1.2 /Mpc, testPowers' run): the GPU's two halves through
+    # on: z = 3.1, 0.17, 0 to k = 1.2 /Mpc, testPowers' run): the GPU's single launch through
     # the C ABI against the CPU restatement of the reference's single evolution
     def both_params():
         p = base(2500, False, 0.07)
@@ -518,14 +518,17 @@ def single_configs(nthreads):
         return p
 
     def gpu_both(p):
-        gpu_cmb(p)
+        n = p.max_l + 1
+        unl = np.zeros((n, 4))
         tr = np.zeros((1, 3, 1024, 13), dtype=np.float32)
         nq = (C.c_int * 1)()
         s8 = np.zeros(3)
         sv = np.zeros(3)
         st = (C.c_int * 1)()
-        _lib.check(lib.cambgpu_get_transfer_batch(C.byref(p), 1, 1024, tr.ctypes.data_as(C.POINTER(C.c_float)), nq,
-                                                  _lib.dptr(s8), _lib.dptr(sv), st))
+        lml = (C.c_int * 1)()
+        _lib.check(lib.cambgpu_get_results_with_transfers(C.byref(p), 1, p.max_l, _lib.dptr(unl), None, None, lml, 1024,
+                                                          tr.ctypes.data_as(C.POINTER(C.c_float)), nq, _lib.dptr(s8),
+                                                          _lib.dptr(sv), st))
         return s8[2]
 
     def cpu_both(p):
