@@ -1308,7 +1308,9 @@ int oracle_evolve_transfer(const CambGpuTables* T, float* out, int nthreads, lon
   Ctx C;
   init_ctx(C, T);
   int nk = T->nk, status = 0;
-  if (!T->transfer_only) return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
+  // the transfer half of a run with the CMB has source modes that also stop at the source
+  // times: oracle_evolve_combined restates that run
+  if (!T->transfer_only || T->transfer_source_modes > 0) return CAMBGPU_ERROR_UNSUPPORTED_PARAMS;
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic)
   for (int i = nk - 1; i >= 0; --i) {
