@@ -97,3 +97,25 @@ def test_noalloc_rejects_long_time_grid_before_any_device_call(lib):
     assert rc == 2
     msg = lib.cambgpu_last_error().decode()
     assert "ntau=4000" in msg and "shared memory" in msg
+
+
+def test_results_with_transfers_validates_before_any_device_call(lib):
+    """cambgpu_get_results_with_transfers wants the CMB and transfer functions in every member
+    and one redshift count across the batch; anything else is code 2 with a message,
+    before any device call."""
+    p = fiducial(300)
+    p.want_transfer, p.num_transfer_redshifts = 1, 1
+    p.transfer_redshifts[0] = 0.0
+    q = fiducial(300)  # CMB only
+    for ps in ([p, q], [q]):
+        arr = (_lib.CambGpuParams * len(ps))(*ps)
+        st = np.zeros(len(ps), dtype=np.int32)
+        rc = lib.cambgpu_get_results_with_transfers(arr, len(ps), 300, None, None, None, None, 16, None, None, None,
+                                                    None, _lib.iptr(st))
+        assert rc == 2 and b"want_cls = want_transfer = 1" in lib.cambgpu_last_error()
+    r = fiducial(300)
+    r.want_transfer, r.num_transfer_redshifts = 1, 2
+    r.transfer_redshifts[0], r.transfer_redshifts[1] = 1.0, 0.0
+    arr = (_lib.CambGpuParams * 2)(p, r)
+    rc = lib.cambgpu_get_results_with_transfers(arr, 2, 300, None, None, None, None, 16, None, None, None, None, None)
+    assert rc == 2 and b"same redshift count" in lib.cambgpu_last_error()
