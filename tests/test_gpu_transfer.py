@@ -180,6 +180,23 @@ def test_single_launch_is_the_single_evolution(zs):
     assert np.max(np.abs(g[:, 3] - icl[:, 2]) / np.sqrt(icl[:, 0] * icl[:, 1])) < 1e-5
 
 
+def test_single_launch_lensed():
+    """The single launch with lensing on: the lensed C_l and the lensing potential of the
+    CMB half match the two-call form (whose CMB half lacks only the transfer stops) to
+    1e-6, and sigma8 is the transfer call's."""
+    from camb_gb300 import model, results
+    cp = model.set_params(H0=67.5, ombh2=0.022, omch2=0.122, mnu=0.06, As=2.1e-9, ns=0.965, lmax=1000)
+    cp.set_matter_power(redshifts=[0.5, 0.0], kmax=1.0)
+    one = results.get_results(cp)
+    two = results._run([cp], 1000)[0]
+    a, b = one.get_lensed_scalar_cls(1000)[2:], two.get_lensed_scalar_cls(1000)[2:]
+    assert np.max(np.abs(a[:, :2] / b[:, :2] - 1)) < 1e-6
+    pa, pb = one.get_lens_potential_cls(1000)[2:, 0], two.get_lens_potential_cls(1000)[2:, 0]
+    assert np.max(np.abs(pa / pb - 1)) < 1e-6
+    _, _, s8, _ = gpu_transfer([cp.to_struct()])
+    assert np.array_equal(one.get_sigma8(), s8[0])
+
+
 def test_cmb_with_transfers_ending_before_today():
     """Transfer redshifts 3.1 and 1 only: the CMB half's modes keep evolving to z = 1 and
     then take the late-time cut (src_keep_tau below tau0), the transfer half's source modes
