@@ -1511,6 +1511,11 @@ __device__ __forceinline__ void derivs1(const DevCosmo& C, St& M, double tau, co
 #ifndef CG_RHS_CALL
 #define CG_RHS_CALL 1
 #endif
+// (the warp-per-mode kernels keep it inline: out of line they ran 176 against 172 ms on one
+// lensed lmax-2500 cosmology and 65 against 58 ms on one lmax-1000 cosmology)
+#ifndef CG_RHS_CALL_WARP
+#define CG_RHS_CALL_WARP 0
+#endif
 // The right-hand side as one out-of-line function for the thread-per-mode kernels (a
 // trial step evaluates it at eight call sites; inlined, each is a copy of the whole
 // body): half the code, 0.8 % faster at 256 draws (1212 against 1222 ms)
@@ -1522,7 +1527,7 @@ __device__ __noinline__ void derivs1_call(const DevCosmo& C, St& M, double tau, 
 template <bool TR, int W, class YV>
 __device__ __forceinline__ void rhs(const DevCosmo& C, St& M, double tau, const YV y, double* __restrict__ dy,
                                     double* src, NuBins* sbins, const double* wrec) {
-  if constexpr (W == 1 && CG_RHS_CALL != 0) derivs1_call<TR, W>(C, M, tau, y, dy, src, sbins, wrec);
+  if constexpr ((W == 1 || CG_RHS_CALL_WARP != 0) && CG_RHS_CALL != 0) derivs1_call<TR, W>(C, M, tau, y, dy, src, sbins, wrec);
   else derivs1<TR, W>(C, M, tau, y, dy, src, sbins, wrec);
 }
 
